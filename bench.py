@@ -1,0 +1,374 @@
+"""Benchmark: queries/s of the C^2graph traversal path on one GB300 (and GTEPS).
+
+Workload (default): the scale-22 R-MAT graph of the single-query / batched
+configurations (4,194,304 vertices, edge factor 16, a/b/c/d = 0.57/0.19/0.19/0.05,
+seed 2, int32 weights in [1,1000], flist = out-normalised uniform(0,1)), pruned by
+this library's purn-sssp / purn-ppr (byte-identical to the reference tools).  The
+query mix is the batched configuration's: 256 SSSP + 256 PPR sources, half uniform
+over vertices with out-edges, half from the top 1% out-degree vertices (selection
+seed 2024).  A step runs a slice of that mix (--sssp-per-step + --ppr-per-step
+queries, rotating through the 512 sources) through the per-query GPU path:
+  SSSP: sssp-purn on sssp/ with the source's own record as seeds (EXACT mode), int32
+        distances (bit-exact against the oracle in tests/);
+  PPR:  ppr-purn on ppr/ (alpha 0.15, rmax 1e-7, FP32; L1 <= 1e-6 vs the FP64 oracle
+        in tests/).
+value = queries per second with the graph and outputs resident in HBM (CUDA events on
+the stream the kernels run on); e2e = the same through the C ABI with host output
+buffers (device->host copy of every result inside the timed region).  The graph
+(~1.6 GB of CSR) is larger than L2, so no flush is needed between steps.
+
+--impl reference times the reference's CPU implementation of the path (the oracle's
+restatement of the reference CPU Bellman-Ford / BSP push, all host threads, one query
+per thread) on a bounded sample of the same query mix.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(REPO, "c-2graph_gb300")
+for p in (REPO, PKG):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+METRIC = "queries/s batched vs per-query (SSSP exact, PPR L1<=1e-6) & GTEPS, 1xGB300"
+ALPHA, RMAX = 0.15, 1e-7
+
+
+def env_rank():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), \
+        int(os.environ.get("LOCAL_RANK", "0"))
+
+
+def measured_peak():
+    p = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            j = json.load(f)
+        return float(j["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi sampling during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in self.lines:
+            parts = [x.strip() for x in l.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def make_dataset(d, scale, ef, seed):
+    import c2g
+
+    t0 = time.time()
+    c2g.rmat_write(d, scale, ef, seed, 1, 1000)
+    t1 = time.time()
+    c2g.prune_sssp(d)
+    c2g.prune_ppr(d)
+    return t1 - t0, time.time() - t1
+
+
+def pick_sources(vlist, n_each, seed=2024):
+    """Config-3 selection: half uniform over vertices with out-edges, half from the top
+    1% out-degree vertices."""
+    deg = np.diff(vlist)
+    rng = np.random.default_rng(seed)
+    cand = np.flatnonzero(deg > 0)
+    top = np.argsort(-deg, kind="stable")[:max(1, len(deg) // 100)]
+    top = top[deg[top] > 0]
+    half = n_each // 2
+    out = np.concatenate([rng.choice(cand, n_each - half, replace=False), rng.choice(top, half, replace=False)])
+    return out.astype(np.int32)
+
+
+def run_reference(args, rank, world):
+    """CPU arm: the reference's CPU implementation (oracle restatement), all threads."""
+    if rank != 0:
+        return
+    import c2g
+    import oracle
+
+    threads = os.cpu_count() or 1
+    with tempfile.TemporaryDirectory(dir=args.workdir) as d:
+        c2g.rmat_write(d, args.scale, args.edge_factor, args.seed, 1, 1000)
+        o = oracle.load_dataset(d, "origin")
+        ssrc = pick_sources(o["vlist"], 256)
+        psrc = pick_sources(o["vlist"], 256, seed=2025)
+        ns, npq = min(args.cpu_sample, 256), min(args.cpu_sample, 256)
+        times, q_total = [], 0
+        for step in range(args.warmup + args.steps):
+            k = (step * ns) % 256
+            t0 = time.time()
+            oracle.batch("sssp", o["vlist"], o["elist"], o["wlist"], None, np.roll(ssrc, -k)[:ns], threads=threads)
+            oracle.batch("ppr", o["vlist"], o["elist"], None, o["flist"], np.roll(psrc, -k)[:npq], alpha=ALPHA,
+                         rmax=RMAX, threads=threads)
+            dt = time.time() - t0
+            if step >= args.warmup:
+                times.append(dt)
+                q_total += ns + npq
+    v = q_total / sum(times)
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "queries/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * float(np.mean(times)),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32+f32",
+            "data": "synthetic R-MAT (seeded), no public dataset",
+            "config": {"workload": "rmat-s%d-ef%d query mix 50%% SSSP / 50%% PPR" % (args.scale, args.edge_factor),
+                       "graph": "origin (reference CPU Bellman-Ford runs unpruned)", "alpha": ALPHA, "rmax": RMAX},
+            "cpu_baseline": {"value": v, "unit": "queries/s", "cores": threads, "kind": "port",
+                             "sample": "%d SSSP + %d PPR queries per step, one per thread" % (ns, npq)},
+            "e2e": {"value": v, "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, rank, world, local_rank):
+    import torch
+
+    import c2g
+
+    dev = local_rank
+    torch.cuda.set_device(dev)
+    dist_on = world > 1
+    if dist_on:
+        import torch.distributed as tdist
+
+        tdist.init_process_group("nccl", device_id=torch.device("cuda", dev))
+    work = tempfile.mkdtemp(dir=args.workdir)
+    gen_s, prune_s = make_dataset(work, args.scale, args.edge_factor, args.seed)
+    so = {"vlist": c2g.read_array(os.path.join(work, "sssp", "vlist.bin"))}
+    po = {"vlist": c2g.read_array(os.path.join(work, "ppr", "vlist.bin"))}
+    V = len(so["vlist"]) - 1
+    ssrc = pick_sources(so["vlist"], 256, seed=2024 + rank)
+    psrc = pick_sources(po["vlist"], 256, seed=2025 + rank)
+
+    gs = c2g.Graph.load(work, "sssp", device=dev)
+    gp = c2g.Graph.load(work, "ppr", device=dev)
+    stream = torch.cuda.Stream(device=dev)
+    gs.set_stream(stream.cuda_stream)
+    gp.set_stream(stream.cuda_stream)
+    gs.sssp_config(delta=args.delta, tile=args.tile)
+    prm = gp.ppr_params(alpha=ALPHA, rmax=RMAX, seeded=1, max_iter=500)
+    dist_d = torch.empty(V, dtype=torch.int32, device=dev)
+    pr_d = torch.empty(V, dtype=torch.float32, device=dev)
+    res_d = torch.empty(V, dtype=torch.float32, device=dev)
+    dist_h = torch.empty(V, dtype=torch.int32).pin_memory().numpy()
+    nS, nP = args.sssp_per_step, args.ppr_per_step
+
+    def step(i, host):
+        ks = [(i * nS + j) % 256 for j in range(nS)]
+        kp = [(i * nP + j) % 256 for j in range(nP)]
+        acc = {"sssp_ms": 0.0, "ppr_ms": 0.0, "sssp_bytes": 0.0, "ppr_bytes": 0.0, "sssp_edges": 0,
+               "ppr_edges": 0, "sssp_iters": 0, "ppr_iters": 0}
+        for k in ks:
+            s = int(ssrc[k])
+            if host:
+                _, st = gs.sssp(s, seeds=True, mode=c2g.SEEDS_EXACT, out=dist_h)
+            else:
+                _, st = gs.sssp(s, seeds=True, mode=c2g.SEEDS_EXACT, out_ptr=dist_d.data_ptr())
+            acc["sssp_ms"] += st.device_ms
+            acc["sssp_bytes"] += st.alg_bytes
+            acc["sssp_edges"] += st.edges_relaxed
+            acc["sssp_iters"] += st.iterations
+        for k in kp:
+            s = int(psrc[k])
+            if host:
+                _, _, st = gp.ppr(s, prm)
+            else:
+                _, _, st = gp.ppr(s, prm, pr_ptr=pr_d.data_ptr(), res_ptr=res_d.data_ptr())
+            acc["ppr_ms"] += st.device_ms
+            acc["ppr_bytes"] += st.alg_bytes
+            acc["ppr_edges"] += st.edges_relaxed
+            acc["ppr_iters"] += st.iterations
+        return acc
+
+    def barrier():
+        torch.cuda.synchronize(dev)
+        if dist_on:
+            tdist.barrier()
+        torch.cuda.synchronize(dev)
+
+    def timed(host):
+        for i in range(args.warmup):
+            step(i, host)
+        barrier()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        tot = None
+        e0.record(stream)
+        t0 = time.time()
+        for i in range(args.steps):
+            a = step(args.warmup + i, host)
+            tot = a if tot is None else {k: tot[k] + a[k] for k in tot}
+        e1.record(stream)
+        barrier()
+        wall = time.time() - t0
+        ms = e0.elapsed_time(e1)
+        if dist_on:
+            t = torch.tensor([ms], device=dev)
+            tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms, wall, tot
+
+    with ClockSampler(dev) as clk:
+        ms_dev, wall_dev, tot = timed(False)
+    ms_e2e, wall_e2e, _ = timed(True)
+    q_step = nS + nP
+    q_all = q_step * args.steps * world
+    value = q_all / (ms_dev / 1000.0)
+    e2e = q_all / (ms_e2e / 1000.0)
+
+    # Graph500-style TEPS on one sample query: out-edges of reached vertices / time.
+    s0 = int(ssrc[0])
+    d0, st0 = gs.sssp(s0, seeds=True, mode=c2g.SEEDS_EXACT)
+    reached_edges = int(np.diff(so["vlist"])[d0 != c2g.INF_DIST].sum())
+    gteps_sample = reached_edges / (st0.device_ms / 1000.0) / 1e9
+
+    dominant = "sssp" if tot["sssp_ms"] >= tot["ppr_ms"] else "ppr"
+    peak, peak_kind = measured_peak()
+    achieved = tot[dominant + "_bytes"] / (tot[dominant + "_ms"] / 1000.0) / 1e9
+    kernel_name = "sssp_persistent" if dominant == "sssp" else "ppr_persistent"
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        import oracle  # CPU-baseline leg only
+
+        threads = 1
+        t0 = time.time()
+        o = oracle.load_dataset(work, "origin")
+        k = args.cpu_sample
+        oracle.batch("sssp", o["vlist"], o["elist"], o["wlist"], None, ssrc[:k], threads=threads)
+        oracle.batch("ppr", o["vlist"], o["elist"], None, o["flist"], psrc[:k], alpha=ALPHA, rmax=RMAX,
+                     threads=threads)
+        dt = time.time() - t0
+        cpu = {"value": 2 * k / dt, "unit": "queries/s", "cores": threads, "kind": "port",
+               "sample": "%d SSSP (Bellman-Ford, origin/) + %d PPR (FP32 BSP push) queries on one core" % (k, k)}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "queries/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_dev / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "int32 (SSSP) + f32 (PPR)",
+            "data": "synthetic R-MAT (seeded); no public dataset",
+            "config": {"workload": "rmat-s%d-ef%d pruned, per-query GPU path, %d SSSP + %d PPR per step"
+                                   % (args.scale, args.edge_factor, nS, nP),
+                       "path": "per-query", "vertices": V, "edges_sssp": int(so["vlist"][-1]),
+                       "edges_ppr": int(po["vlist"][-1]), "alpha": ALPHA, "rmax": RMAX, "delta": args.delta,
+                       "tile": args.tile, "l2": "graph larger than L2 (no flush needed)",
+                       "parallelism": "replicas (query-sharded)" if world > 1 else "single GPU"},
+            "e2e": {"value": e2e, "unit": "queries/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 4 * V * q_step + 4 * V * nP},
+            "gpu_launches": 2 * q_step * args.steps,
+            "roofline": {"bound": "hbm", "kernel": kernel_name, "achieved": achieved, "peak": peak,
+                         "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak, "traffic": None},
+            "cpu_baseline": cpu,
+            "clocks": clk.summary(),
+            "detail": {
+                "sssp_ms_per_query": tot["sssp_ms"] / (nS * args.steps),
+                "ppr_ms_per_query": tot["ppr_ms"] / (nP * args.steps),
+                "sssp_gteps_relaxed": tot["sssp_edges"] / (tot["sssp_ms"] / 1000.0) / 1e9,
+                "ppr_gteps_pushed": tot["ppr_edges"] / (tot["ppr_ms"] / 1000.0) / 1e9,
+                "sssp_gteps_graph500_sample": gteps_sample,
+                "sssp_rounds_per_query": tot["sssp_iters"] / (nS * args.steps),
+                "ppr_rounds_per_query": tot["ppr_iters"] / (nP * args.steps),
+                "sssp_alg_gbs": tot["sssp_bytes"] / (tot["sssp_ms"] / 1000.0) / 1e9,
+                "ppr_alg_gbs": tot["ppr_bytes"] / (tot["ppr_ms"] / 1000.0) / 1e9,
+                "kernel_share_sssp": tot["sssp_ms"] / (tot["sssp_ms"] + tot["ppr_ms"]),
+                "gen_s": gen_s, "prune_s": prune_s, "wall_s_device_run": wall_dev, "wall_s_e2e_run": wall_e2e,
+            },
+        }
+        print(json.dumps(line), flush=True)
+    gs.close()
+    gp.close()
+    if dist_on:
+        tdist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--scale", type=int, default=22)
+    ap.add_argument("--edge-factor", type=int, default=16)
+    ap.add_argument("--seed", type=int, default=2)
+    ap.add_argument("--sssp-per-step", type=int, default=16)
+    ap.add_argument("--ppr-per-step", type=int, default=16)
+    ap.add_argument("--delta", type=int, default=0)
+    ap.add_argument("--tile", type=int, default=256)
+    ap.add_argument("--cpu-sample", type=int, default=2)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workdir", default=None)
+    args = ap.parse_args()
+    rank, world, local_rank = env_rank()
+    import __graft_entry__
+
+    if rank == 0:
+        __graft_entry__.build()
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        if world > 1 and rank != 0:
+            # wait for rank 0's build
+            for _ in range(600):
+                if os.path.exists(os.path.join(PKG, "lib", "libc2graph.so")):
+                    break
+                time.sleep(1)
+        run_ours(args, rank, world, local_rank)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,237 @@
+"""Python host binding of the C^2graph GB300 library (ctypes over include/c2graph.h).
+
+The library is the product; this module only marshals arguments.  It mirrors the
+reference's programs: ``Graph.load(dir, "origin"|"sssp"|"ppr")`` reads the reference's
+binary dataset layout, ``Graph.sssp`` / ``Graph.ppr`` run the sssp-base / sssp-purn /
+ppr-base / ppr-purn traversals, ``prune_sssp`` / ``prune_ppr`` are purn-sssp /
+purn-ppr, and ``rmat_write`` writes a synthetic origin/ dataset.
+
+Importing never compiles anything; ``build()`` (the package's build.py) does.  A
+missing library raises ``LibraryMissing``: there is no fallback implementation.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+PKG_DIR = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+LIB_PATH = os.path.join(PKG_DIR, "lib", "libc2graph.so")
+BIN_DIR = os.path.join(PKG_DIR, "bin")
+INCLUDE = os.path.join(os.path.dirname(PKG_DIR), "include", "c2graph.h")
+
+INF_DIST = 1999999999
+
+OK = 0
+ERR_ARG, ERR_IO, ERR_FORMAT, ERR_CUDA, ERR_OOM = -1, -2, -3, -4, -5
+ERR_RANGE, ERR_TIMEOUT, ERR_OVERFLOW, ERR_UNSUPPORTED, ERR_NODEVICE = -6, -7, -8, -9, -10
+FLAG_BARRIER_TIMEOUT, FLAG_ITER_CAP, FLAG_QUEUE_OVERFLOW, FLAG_BOUNDS = 0x1, 0x2, 0x4, 0x8
+
+VARIANTS = {"origin": 0, "sssp": 1, "ppr": 2}
+SEEDS_COMPAT, SEEDS_EXACT = 0, 1
+
+
+class LibraryMissing(RuntimeError):
+    pass
+
+
+class C2GError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("c2graph error %d: %s" % (code, msg))
+        self.code = code
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [("source", ctypes.c_int32), ("iterations", ctypes.c_int32),
+                ("vertices_popped", ctypes.c_int64), ("edges_relaxed", ctypes.c_int64),
+                ("touched", ctypes.c_int64), ("n_seeds", ctypes.c_int64),
+                ("alg_bytes", ctypes.c_double), ("device_ms", ctypes.c_float),
+                ("status_flags", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
+
+
+class PprParams(ctypes.Structure):
+    _fields_ = [("alpha", ctypes.c_float), ("rmax", ctypes.c_float), ("r0", ctypes.c_float),
+                ("pr0", ctypes.c_float), ("max_iter", ctypes.c_int32), ("seeded", ctypes.c_int32)]
+
+
+_lib = None
+
+_P = ctypes.c_void_p
+_I32P = ctypes.POINTER(ctypes.c_int32)
+_F32P = ctypes.POINTER(ctypes.c_float)
+
+# name -> (restype, argtypes); every symbol include/c2graph.h declares.
+SIGNATURES = {
+    "c2g_abi_version": (ctypes.c_int, []),
+    "c2g_last_error": (ctypes.c_char_p, []),
+    "c2g_device_count": (ctypes.c_int, [_I32P]),
+    "c2g_graph_load": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, ctypes.POINTER(_P)]),
+    "c2g_graph_create": (ctypes.c_int, [ctypes.c_int, ctypes.c_int32, ctypes.c_int64, _P, _P, _P, _P,
+                                        ctypes.POINTER(_P)]),
+    "c2g_graph_set_records": (ctypes.c_int, [_P, ctypes.c_int32, _P, _P, _P, ctypes.c_int, _P]),
+    "c2g_graph_free": (None, [_P]),
+    "c2g_graph_info": (ctypes.c_int, [_P, _I32P, ctypes.POINTER(ctypes.c_int64), _I32P]),
+    "c2g_graph_set_stream": (ctypes.c_int, [_P, _P]),
+    "c2g_sssp_resolve_source": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int, ctypes.c_int, _I32P]),
+    "c2g_sssp": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int, ctypes.c_int, _P, ctypes.c_int,
+                                ctypes.POINTER(Stats)]),
+    "c2g_sssp_set_config": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32]),
+    "c2g_ppr": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.POINTER(PprParams), _P, _P, ctypes.c_int,
+                               ctypes.POINTER(Stats)]),
+    "c2g_ppr_default_params": (ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(PprParams)]),
+    "c2g_rmat_write": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, ctypes.c_uint64,
+                                      ctypes.c_int32, ctypes.c_int32, ctypes.c_double, ctypes.c_double,
+                                      ctypes.c_double]),
+    "c2g_prune_sssp": (ctypes.c_int, [ctypes.c_char_p]),
+    "c2g_prune_ppr": (ctypes.c_int, [ctypes.c_char_p]),
+}
+
+
+def lib():
+    """Load libc2graph.so (raises LibraryMissing when it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.isfile(LIB_PATH):
+            raise LibraryMissing("libc2graph.so not built: run __graft_entry__.build() "
+                                 "(expected at %s)" % LIB_PATH)
+        L = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _check(rc):
+    if rc != OK:
+        msg = lib().c2g_last_error()
+        raise C2GError(rc, msg.decode() if msg else "")
+    return rc
+
+
+def _ptr(a):
+    return ctypes.c_void_p(a.ctypes.data) if a is not None else None
+
+
+def device_count():
+    n = ctypes.c_int32(0)
+    _check(lib().c2g_device_count(ctypes.byref(n)))
+    return n.value
+
+
+def rmat_write(dir, scale, edge_factor, seed, wmin=1, wmax=100, a=0.57, b=0.19, c=0.19):
+    _check(lib().c2g_rmat_write(os.fsencode(dir), scale, edge_factor, seed, wmin, wmax, a, b, c))
+
+
+def prune_sssp(dir):
+    _check(lib().c2g_prune_sssp(os.fsencode(dir)))
+
+
+def prune_ppr(dir):
+    _check(lib().c2g_prune_ppr(os.fsencode(dir)))
+
+
+def read_array(path, dtype=np.int32):
+    """Read a reference binary array (raw 4-byte elements, no header)."""
+    return np.fromfile(path, dtype=dtype)
+
+
+class Graph:
+    """A device-resident graph handle."""
+
+    def __init__(self, handle):
+        self._h = handle
+        V = ctypes.c_int32()
+        E = ctypes.c_int64()
+        R = ctypes.c_int32()
+        _check(lib().c2g_graph_info(self._h, ctypes.byref(V), ctypes.byref(E), ctypes.byref(R)))
+        self.V, self.E, self.R = V.value, E.value, R.value
+
+    @classmethod
+    def load(cls, dir, variant="origin", device=0):
+        h = ctypes.c_void_p()
+        _check(lib().c2g_graph_load(os.fsencode(dir), VARIANTS[variant], device, ctypes.byref(h)))
+        return cls(h)
+
+    @classmethod
+    def create(cls, vlist, elist, wlist=None, flist=None, device=0):
+        vlist = np.ascontiguousarray(vlist, dtype=np.int32)
+        elist = np.ascontiguousarray(elist, dtype=np.int32)
+        wlist = None if wlist is None else np.ascontiguousarray(wlist, dtype=np.int32)
+        flist = None if flist is None else np.ascontiguousarray(flist, dtype=np.float32)
+        h = ctypes.c_void_p()
+        _check(lib().c2g_graph_create(device, len(vlist) - 1, len(elist), _ptr(vlist), _ptr(elist),
+                                      _ptr(wlist), _ptr(flist), ctypes.byref(h)))
+        return cls(h)
+
+    def set_records(self, hvlist, helist, hwlist, record_vertex=None):
+        hvlist = np.ascontiguousarray(hvlist, dtype=np.int32)
+        helist = np.ascontiguousarray(helist, dtype=np.int32)
+        is_float = np.asarray(hwlist).dtype.kind == "f"
+        hwlist = np.ascontiguousarray(hwlist, dtype=np.float32 if is_float else np.int32)
+        rv = None if record_vertex is None else np.ascontiguousarray(record_vertex, dtype=np.int32)
+        _check(lib().c2g_graph_set_records(self._h, len(hvlist) - 1, _ptr(hvlist), _ptr(helist),
+                                           _ptr(hwlist), int(is_float), _ptr(rv)))
+        self.R = len(hvlist) - 1
+
+    def close(self):
+        if self._h:
+            lib().c2g_graph_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def set_stream(self, stream_ptr):
+        _check(lib().c2g_graph_set_stream(self._h, ctypes.c_void_p(stream_ptr)))
+
+    def sssp_config(self, delta=0, tile=256, max_iter=1 << 20):
+        _check(lib().c2g_sssp_set_config(self._h, delta, tile, max_iter))
+
+    def resolve_source(self, source, pruned=False, mode=SEEDS_COMPAT):
+        out = ctypes.c_int32()
+        _check(lib().c2g_sssp_resolve_source(self._h, source, int(pruned), mode, ctypes.byref(out)))
+        return out.value
+
+    def sssp(self, source, seeds=False, mode=SEEDS_COMPAT, out=None, out_ptr=None):
+        """Distances as an int32 numpy array (or into device memory at out_ptr)."""
+        st = Stats()
+        if out_ptr is not None:
+            _check(lib().c2g_sssp(self._h, source, int(seeds), mode, ctypes.c_void_p(out_ptr), 1,
+                                  ctypes.byref(st)))
+            return None, st
+        dist = out if out is not None else np.empty(self.V, dtype=np.int32)
+        _check(lib().c2g_sssp(self._h, source, int(seeds), mode, _ptr(dist), 0, ctypes.byref(st)))
+        return dist, st
+
+    def ppr_params(self, adsorption=False, **kw):
+        p = PprParams()
+        _check(lib().c2g_ppr_default_params(self._h, int(adsorption), ctypes.byref(p)))
+        for k, v in kw.items():
+            setattr(p, k, v)
+        return p
+
+    def ppr(self, source, params=None, pr_ptr=None, res_ptr=None, **kw):
+        """(pr, res, stats) as float32 numpy arrays (or into device memory)."""
+        p = params if params is not None else self.ppr_params(**kw)
+        st = Stats()
+        if pr_ptr is not None:
+            _check(lib().c2g_ppr(self._h, source, ctypes.byref(p), ctypes.c_void_p(pr_ptr),
+                                 ctypes.c_void_p(res_ptr) if res_ptr else None, 1, ctypes.byref(st)))
+            return None, None, st
+        pr = np.empty(self.V, dtype=np.float32)
+        res = np.empty(self.V, dtype=np.float32)
+        _check(lib().c2g_ppr(self._h, source, ctypes.byref(p), _ptr(pr), _ptr(res), 0, ctypes.byref(st)))
+        return pr, res, st

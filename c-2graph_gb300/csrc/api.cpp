@@ -1,0 +1,430 @@
+// C ABI entry points (include/c2graph.h): graph loading, source rules, seed selection
+// and result/statistics copy-out around the traversal launches.
+#include <cuda_runtime.h>
+
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/c2graph.h"
+#include "host_io.h"
+#include "internal.h"
+
+namespace c2g {
+
+int build_adj(c2g_graph* g, const int32_t* col, const int32_t* w, int2** out);
+
+static const int kNoSidecar = -2;
+
+static void graph_release(c2g_graph* g) {
+    if (!g) return;
+    int prev = 0;
+    cudaGetDevice(&prev);
+    cudaSetDevice(g->device);
+    sssp_free(g);
+    ppr_free(g);
+    void* ptrs[] = {g->row, g->adj_w, g->adj_f, g->hv, g->he, g->hw, g->rec_of_vertex};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    if (g->ev0) cudaEventDestroy(g->ev0);
+    if (g->ev1) cudaEventDestroy(g->ev1);
+    if (g->own_stream && g->stream) cudaStreamDestroy(g->stream);
+    cudaSetDevice(prev);
+    delete g;
+}
+
+// RAII guard that makes the graph's device current for the duration of a call.
+struct DeviceScope {
+    int prev = -1;
+    explicit DeviceScope(int dev) {
+        if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+        cudaSetDevice(dev);
+    }
+    ~DeviceScope() {
+        if (prev >= 0) cudaSetDevice(prev);
+    }
+};
+
+static int graph_new(int device, c2g_graph** out) {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+        cudaGetLastError();
+        return fail(C2G_ERR_NODEVICE, "no CUDA device available");
+    }
+    if (device < 0 || device >= n) return fail(C2G_ERR_ARG, "device %d out of range [0,%d)", device, n);
+    c2g_graph* g = new c2g_graph();
+    g->device = device;
+    cudaError_t e = cudaSetDevice(device);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&g->num_sms, cudaDevAttrMultiProcessorCount, device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) g->own_stream = true;
+    if (e == cudaSuccess) e = cudaEventCreate(&g->ev0);
+    if (e == cudaSuccess) e = cudaEventCreate(&g->ev1);
+    if (e != cudaSuccess) {
+        graph_release(g);
+        return fail(C2G_ERR_CUDA, "graph init: %s", cudaGetErrorString(e));
+    }
+    *out = g;
+    return C2G_OK;
+}
+
+static int graph_fill(c2g_graph* g, const std::vector<int32_t>& vlist, const int32_t* elist, int64_t E,
+                      const int32_t* wlist, const float* flist) {
+    g->V = (int32_t)vlist.size() - 1;
+    g->E = E;
+    g->h_row = vlist;
+    C2G_CUDA(cudaMalloc(&g->row, sizeof(int32_t) * vlist.size()));
+    C2G_CUDA(cudaMemcpy(g->row, vlist.data(), sizeof(int32_t) * vlist.size(), cudaMemcpyHostToDevice));
+    int rc;
+    if (wlist && (rc = build_adj(g, elist, wlist, &g->adj_w))) return rc;
+    if (flist && (rc = build_adj(g, elist, reinterpret_cast<const int32_t*>(flist), &g->adj_f))) return rc;
+    return C2G_OK;
+}
+
+static int records_fill(c2g_graph* g, int32_t R, const int32_t* hv, const int32_t* he, const void* hw, bool hw_float,
+                        const int32_t* rec_vertex) {
+    if (R < 0 || !hv) return fail(C2G_ERR_ARG, "records: bad count or NULL hvlist");
+    if (hv[0] != 0) return fail(C2G_ERR_FORMAT, "hvlist[0] = %d, expected 0", hv[0]);
+    for (int32_t r = 0; r < R; ++r)
+        if (hv[r + 1] < hv[r]) return fail(C2G_ERR_FORMAT, "hvlist not monotone at %d", r);
+    const int64_t H = hv[R];
+    if (H > 0 && (!he || !hw)) return fail(C2G_ERR_ARG, "records: NULL helist/hwlist");
+    for (int64_t k = 0; k < H; ++k)
+        if (he[k] < 0 || he[k] >= g->V)
+            return fail(C2G_ERR_FORMAT, "helist[%lld] = %d out of range", (long long)k, he[k]);
+    for (void* p : {(void*)g->hv, (void*)g->he, (void*)g->hw, (void*)g->rec_of_vertex})
+        if (p) cudaFree(p);
+    g->hv = g->he = g->hw = g->rec_of_vertex = nullptr;
+    g->R = R;
+    g->H = H;
+    g->hw_float = hw_float;
+    g->h_hv.assign(hv, hv + R + 1);
+    C2G_CUDA(cudaMalloc(&g->hv, sizeof(int32_t) * (R + 1)));
+    C2G_CUDA(cudaMemcpy(g->hv, hv, sizeof(int32_t) * (R + 1), cudaMemcpyHostToDevice));
+    C2G_CUDA(cudaMalloc(&g->he, sizeof(int32_t) * (H ? H : 1)));
+    C2G_CUDA(cudaMalloc(&g->hw, sizeof(int32_t) * (H ? H : 1)));
+    if (H) {
+        C2G_CUDA(cudaMemcpy(g->he, he, sizeof(int32_t) * H, cudaMemcpyHostToDevice));
+        C2G_CUDA(cudaMemcpy(g->hw, hw, sizeof(int32_t) * H, cudaMemcpyHostToDevice));
+    }
+    g->h_rec_of_vertex.clear();
+    if (rec_vertex) {
+        g->h_rec_of_vertex.assign((size_t)g->V, -1);
+        for (int32_t r = 0; r < R; ++r) {
+            const int32_t v = rec_vertex[r];
+            if (v < 0 || v >= g->V) return fail(C2G_ERR_FORMAT, "hvmap[%d] = %d out of range", r, v);
+            g->h_rec_of_vertex[v] = r;
+        }
+    }
+    return C2G_OK;
+}
+
+static int stats_fill(c2g_graph* g, const TraversalCtl* dctl, int32_t source, float ms, bool ppr, c2g_stats* st) {
+    TraversalCtl ctl;
+    C2G_CUDA(cudaMemcpyAsync(&ctl, dctl, sizeof(ctl), cudaMemcpyDeviceToHost, g->stream));
+    C2G_CUDA(cudaStreamSynchronize(g->stream));
+    if (ctl.flags & (C2G_FLAG_BARRIER_TIMEOUT | C2G_FLAG_QUEUE_OVERFLOW | C2G_FLAG_BOUNDS)) {
+        // The launch ended early: force the stamp arrays to be reset by the next launch.
+        StampState reset{1 << 30, 1 << 30, {0, 0}};
+        StampState* dst = ppr ? g->ppr.st : g->sssp.st;
+        cudaMemcpy(dst, &reset, sizeof(reset), cudaMemcpyHostToDevice);
+    }
+    if (st) {
+        std::memset(st, 0, sizeof(*st));
+        st->source = source;
+        st->iterations = ctl.iterations;
+        st->vertices_popped = ctl.popped;
+        st->edges_relaxed = ctl.relaxed;
+        st->touched = ctl.touched;
+        st->n_seeds = ctl.seeds;
+        st->device_ms = ms;
+        st->status_flags = ctl.flags;
+        const double V = (double)g->V;
+        // Byte model: SSSP 4V + 16 per popped vertex + 12 per relaxed edge;
+        // push 12V + 20 per popped vertex + 12 per pushed edge.
+        st->alg_bytes = ppr ? 12.0 * V + 20.0 * (double)ctl.popped + 12.0 * (double)ctl.relaxed
+                            : 4.0 * V + 16.0 * (double)ctl.popped + 12.0 * (double)ctl.relaxed;
+    }
+    if (ctl.flags & C2G_FLAG_BARRIER_TIMEOUT) return fail(C2G_ERR_TIMEOUT, "grid barrier wait ran out");
+    if (ctl.flags & C2G_FLAG_QUEUE_OVERFLOW) return fail(C2G_ERR_OVERFLOW, "frontier queue overflow");
+    if (ctl.flags & C2G_FLAG_BOUNDS) return fail(C2G_ERR_OVERFLOW, "device index check failed");
+    return C2G_OK;
+}
+
+static bool is_device_ptr(const void* p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+// Seeds of `source` in the record arrays under `mode`; n = -1 when unavailable.
+static int record_range(const c2g_graph* g, int32_t source, int mode, int32_t* first, int32_t* n) {
+    *first = 0;
+    *n = 0;
+    if (g->R < 0) return fail(C2G_ERR_UNSUPPORTED, "graph has no pruned records (hvlist)");
+    int32_t r;
+    if (mode == C2G_SEEDS_COMPAT) {
+        // The reference reads hvlist[source] and hvlist[source+1]; beyond the record count
+        // that read is out of bounds, reported here as a range error.
+        if (source + 1 > g->R)
+            return fail(C2G_ERR_RANGE, "COMPAT seeds: source %d >= record count %d", source, g->R);
+        r = source;
+    } else if (mode == C2G_SEEDS_EXACT) {
+        if (g->h_rec_of_vertex.empty())
+            return fail(C2G_ERR_UNSUPPORTED, "EXACT seeds need the record->vertex sidecar (hvmap.bin)");
+        r = g->h_rec_of_vertex[source];
+        if (r < 0) return C2G_OK;
+    } else {
+        return fail(C2G_ERR_ARG, "bad seed mode %d", mode);
+    }
+    *first = g->h_hv[r];
+    *n = g->h_hv[r + 1] - g->h_hv[r];
+    return C2G_OK;
+}
+
+}  // namespace c2g
+
+using namespace c2g;
+
+extern "C" {
+
+int c2g_abi_version(void) { return C2G_ABI_VERSION; }
+const char* c2g_last_error(void) { return c2g::last_error(); }
+
+int c2g_device_count(int* count) {
+    if (!count) return fail(C2G_ERR_ARG, "count is NULL");
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) {
+        cudaGetLastError();
+        n = 0;
+    }
+    *count = n;
+    return C2G_OK;
+}
+
+int c2g_graph_create(int device, int32_t V, int64_t E, const int32_t* vlist, const int32_t* elist,
+                     const int32_t* wlist, const float* flist, c2g_graph** out) {
+    if (!out || !vlist || (E > 0 && !elist)) return fail(C2G_ERR_ARG, "graph_create: NULL argument");
+    if (V < 0 || E < 0 || E >= (int64_t(1) << 31)) return fail(C2G_ERR_ARG, "graph_create: bad sizes");
+    if (!wlist && !flist) return fail(C2G_ERR_ARG, "graph_create: need wlist or flist");
+    *out = nullptr;
+    std::vector<int32_t> vl(vlist, vlist + V + 1);
+    std::vector<int32_t> el(elist, elist + E);
+    int rc = check_csr(vl, el);
+    if (rc) return rc;
+    c2g_graph* g = nullptr;
+    if ((rc = graph_new(device, &g))) return rc;
+    DeviceScope ds(device);
+    if ((rc = graph_fill(g, vl, elist, E, wlist, flist))) {
+        graph_release(g);
+        return rc;
+    }
+    g->variant = C2G_GRAPH_ORIGIN;
+    *out = g;
+    return C2G_OK;
+}
+
+int c2g_graph_load(const char* dir, int variant, int device, c2g_graph** out) {
+    if (!dir || !out) return fail(C2G_ERR_ARG, "graph_load: NULL argument");
+    *out = nullptr;
+    const std::string base(dir);
+    std::string sub;
+    switch (variant) {
+        case C2G_GRAPH_ORIGIN: sub = "/origin/"; break;
+        case C2G_GRAPH_SSSP: sub = "/sssp/"; break;
+        case C2G_GRAPH_PPR: sub = "/ppr/"; break;
+        default: return fail(C2G_ERR_ARG, "bad graph variant %d", variant);
+    }
+    const std::string d = base + sub;
+    std::vector<int32_t> vlist, elist, wlist, hv, he, hwi, hvmap;
+    std::vector<float> flist, hwf;
+    int rc;
+    if ((rc = read_array4(d + "vlist.bin", vlist))) return rc;
+    if ((rc = read_array4(d + "elist.bin", elist))) return rc;
+    const int32_t* wp = nullptr;
+    const float* fp = nullptr;
+    if (variant == C2G_GRAPH_ORIGIN) {
+        const bool hw = file_exists(d + "wlist.bin"), hf = file_exists(d + "flist.bin");
+        if (!hw && !hf) return fail(C2G_ERR_IO, "file:%swlist.bin not exist.", d.c_str());
+        if (hw && (rc = read_array4(d + "wlist.bin", wlist))) return rc;
+        if (hf && (rc = read_array4(d + "flist.bin", flist))) return rc;
+        if (hw) wp = wlist.data();
+        if (hf) fp = flist.data();
+    } else if (variant == C2G_GRAPH_SSSP) {
+        if ((rc = read_array4(d + "wlist.bin", wlist))) return rc;
+        wp = wlist.data();
+        if ((rc = read_array4(d + "hvlist.bin", hv))) return rc;
+        if ((rc = read_array4(d + "helist.bin", he))) return rc;
+        if ((rc = read_array4(d + "hwlist.bin", hwi))) return rc;
+        if (file_exists(d + "hvmap.bin") && (rc = read_array4(d + "hvmap.bin", hvmap))) return rc;
+    } else {
+        if ((rc = read_array4(d + "wlist.bin", flist))) return rc;
+        fp = flist.data();
+        if ((rc = read_array4(d + "hvlist.bin", hv))) return rc;
+        if ((rc = read_array4(d + "helist.bin", he))) return rc;
+        if ((rc = read_array4(d + "hwlist.bin", hwf))) return rc;
+    }
+    if ((rc = check_csr(vlist, elist))) return rc;
+    if ((wp && wlist.size() < elist.size()) || (fp && flist.size() < elist.size()))
+        return fail(C2G_ERR_FORMAT, "weight file shorter than elist in %s", d.c_str());
+    if (variant != C2G_GRAPH_ORIGIN) {
+        if (hv.empty()) return fail(C2G_ERR_FORMAT, "%shvlist.bin is empty", d.c_str());
+        const int64_t H = hv.back();
+        const size_t hwn = variant == C2G_GRAPH_SSSP ? hwi.size() : hwf.size();
+        if (H < 0 || (int64_t)he.size() < H || (int64_t)hwn < H)
+            return fail(C2G_ERR_FORMAT, "record arrays shorter than hvlist[R] = %lld", (long long)H);
+        if (!hvmap.empty() && hvmap.size() != hv.size() - 1)
+            return fail(C2G_ERR_FORMAT, "hvmap.bin has %zu entries for %zu records", hvmap.size(), hv.size() - 1);
+    }
+    c2g_graph* g = nullptr;
+    if ((rc = graph_new(device, &g))) return rc;
+    DeviceScope ds(device);
+    if ((rc = graph_fill(g, vlist, elist.data(), (int64_t)elist.size(), wp, fp))) {
+        graph_release(g);
+        return rc;
+    }
+    g->variant = variant;
+    if (variant != C2G_GRAPH_ORIGIN) {
+        const void* hw = variant == C2G_GRAPH_SSSP ? (const void*)hwi.data() : (const void*)hwf.data();
+        rc = records_fill(g, (int32_t)hv.size() - 1, hv.data(), he.data(), hw, variant == C2G_GRAPH_PPR,
+                          hvmap.empty() ? nullptr : hvmap.data());
+        if (rc) {
+            graph_release(g);
+            return rc;
+        }
+    }
+    *out = g;
+    return C2G_OK;
+}
+
+int c2g_graph_set_records(c2g_graph* g, int32_t R, const int32_t* hvlist, const int32_t* helist,
+                          const void* hwlist, int hw_is_float, const int32_t* record_vertex) {
+    if (!g) return fail(C2G_ERR_ARG, "graph is NULL");
+    std::lock_guard<std::mutex> lk(g->mu);
+    DeviceScope ds(g->device);
+    return records_fill(g, R, hvlist, helist, hwlist, hw_is_float != 0, record_vertex);
+}
+
+void c2g_graph_free(c2g_graph* g) { graph_release(g); }
+
+int c2g_graph_info(const c2g_graph* g, int32_t* V, int64_t* E, int32_t* R) {
+    if (!g) return fail(C2G_ERR_ARG, "graph is NULL");
+    if (V) *V = g->V;
+    if (E) *E = g->E;
+    if (R) *R = g->R;
+    return C2G_OK;
+}
+
+int c2g_graph_set_stream(c2g_graph* g, void* stream) {
+    if (!g) return fail(C2G_ERR_ARG, "graph is NULL");
+    std::lock_guard<std::mutex> lk(g->mu);
+    DeviceScope ds(g->device);
+    if (g->own_stream && g->stream) cudaStreamDestroy(g->stream);
+    g->own_stream = false;
+    g->stream = (cudaStream_t)stream;
+    return C2G_OK;
+}
+
+int c2g_sssp_set_config(c2g_graph* g, int32_t delta, int32_t tile, int32_t max_iter) {
+    if (!g) return fail(C2G_ERR_ARG, "graph is NULL");
+    int lt = 0;
+    while ((1 << lt) < tile) ++lt;
+    if (tile < 32 || tile > 4096 || (1 << lt) != tile) return fail(C2G_ERR_ARG, "tile %d not a power of two in [32,4096]", tile);
+    if (max_iter < 1) return fail(C2G_ERR_ARG, "max_iter must be >= 1");
+    std::lock_guard<std::mutex> lk(g->mu);
+    g->sssp_cfg.delta = delta > 0 ? delta : 0;
+    g->sssp_cfg.log_tile = lt;
+    g->sssp_cfg.max_iter = max_iter;
+    return C2G_OK;
+}
+
+int c2g_sssp_resolve_source(const c2g_graph* g, int32_t source, int pruned, int mode, int32_t* adjusted) {
+    if (!g || !adjusted) return fail(C2G_ERR_ARG, "NULL argument");
+    for (int32_t s = source;; ++s) {
+        if (s < 0 || s >= g->V) return fail(C2G_ERR_RANGE, "no eligible source at or after %d (V = %d)", source, g->V);
+        if (g->h_row[s + 1] - g->h_row[s] < 1) continue;
+        if (pruned) {
+            int32_t first, n;
+            int rc = record_range(g, s, mode, &first, &n);
+            if (rc) return rc;
+            if (n > 1000) continue;
+        }
+        *adjusted = s;
+        return C2G_OK;
+    }
+}
+
+int c2g_sssp(c2g_graph* g, int32_t source, int use_seeds, int seed_mode, int32_t* dist, int dist_on_device,
+             c2g_stats* stats) {
+    if (!g || !dist) return fail(C2G_ERR_ARG, "NULL argument");
+    if (source < 0 || source >= g->V) return fail(C2G_ERR_RANGE, "source %d out of range [0,%d)", source, g->V);
+    std::lock_guard<std::mutex> lk(g->mu);
+    DeviceScope ds(g->device);
+    int32_t first = 0, n = 0;
+    int rc;
+    if (use_seeds && (rc = record_range(g, source, seed_mode, &first, &n))) return rc;
+    if (dist_on_device && !is_device_ptr(dist)) return fail(C2G_ERR_ARG, "dist is not a device pointer");
+    float ms = 0.f;
+    rc = sssp_launch(g, source, n ? g->he + first : nullptr, n ? g->hw + first : nullptr, n,
+                     dist_on_device ? dist : nullptr, &ms);
+    if (rc) return rc;
+    if (!dist_on_device)
+        C2G_CUDA(cudaMemcpyAsync(dist, g->sssp.dist, sizeof(int32_t) * (size_t)g->V, cudaMemcpyDeviceToHost, g->stream));
+    return stats_fill(g, g->sssp.ctl, source, ms, false, stats);
+}
+
+int c2g_ppr_default_params(const c2g_graph* g, int adsorption, c2g_ppr_params* out) {
+    if (!g || !out) return fail(C2G_ERR_ARG, "NULL argument");
+    if (!adsorption) {
+        out->alpha = 0.2f;                                  // src/ppr/purn/Main.cu:66
+        out->rmax = 0.001f / (float)((int64_t)g->V + 1);    // :67
+        out->r0 = 1.0f;
+        out->pr0 = 0.2f;
+        out->max_iter = 500;                                // :224
+        out->seeded = g->variant == C2G_GRAPH_PPR ? 1 : 0;
+    } else {
+        out->alpha = 0.2f;                                  // src/adsorption/w-base/Main.cu:63
+        out->rmax = 1.0f / (float)(g->V > 0 ? g->V : 1);    // :64
+        out->r0 = 10.0f;                                    // :149
+        out->pr0 = 8.0f;                                    // :152, 0.8 * 10
+        out->max_iter = 2000;                               // :186
+        out->seeded = 0;
+    }
+    return C2G_OK;
+}
+
+int c2g_ppr(c2g_graph* g, int32_t source, const c2g_ppr_params* params, float* pr, float* res, int on_device,
+            c2g_stats* stats) {
+    if (!g || !params || !pr) return fail(C2G_ERR_ARG, "NULL argument");
+    if (source < 0 || source >= g->V) return fail(C2G_ERR_RANGE, "source %d out of range [0,%d)", source, g->V);
+    if (!(params->alpha > 0.f && params->alpha <= 1.f)) return fail(C2G_ERR_ARG, "alpha must be in (0,1]");
+    if (!(params->rmax >= 0.f)) return fail(C2G_ERR_ARG, "rmax must be >= 0");
+    if (params->max_iter < 1) return fail(C2G_ERR_ARG, "max_iter must be >= 1");
+    std::lock_guard<std::mutex> lk(g->mu);
+    DeviceScope ds(g->device);
+    int32_t first = 0, n = 0;
+    if (params->seeded) {
+        if (g->R < 0 || !g->hw_float) return fail(C2G_ERR_UNSUPPORTED, "seeded push needs ppr/ records");
+        if (g->R != g->V) return fail(C2G_ERR_FORMAT, "ppr/ hvlist has %d records for %d vertices", g->R, g->V);
+        first = g->h_hv[source];
+        n = g->h_hv[source + 1] - first;
+    }
+    if (on_device && (!is_device_ptr(pr) || (res && !is_device_ptr(res))))
+        return fail(C2G_ERR_ARG, "pr/res are not device pointers");
+    float ms = 0.f;
+    int rc = ppr_launch(g, source, *params, n ? g->he + first : nullptr,
+                        n ? reinterpret_cast<const float*>(g->hw + first) : nullptr, n, on_device ? pr : nullptr,
+                        on_device ? res : nullptr, &ms);
+    if (rc) return rc;
+    if (!on_device) {
+        C2G_CUDA(cudaMemcpyAsync(pr, g->ppr.pr, sizeof(float) * (size_t)g->V, cudaMemcpyDeviceToHost, g->stream));
+        if (res)
+            C2G_CUDA(cudaMemcpyAsync(res, g->ppr.res, sizeof(float) * (size_t)g->V, cudaMemcpyDeviceToHost, g->stream));
+    }
+    return stats_fill(g, g->ppr.ctl, source, ms, true, stats);
+}
+
+}  // extern "C"

@@ -1,0 +1,175 @@
+// Device building blocks shared by the traversal kernels (sm_103a):
+//   * a bounded grid barrier for persistent cooperative launches,
+//   * L2-coherent loads for data other CTAs write during a launch,
+//   * the warp-aggregated frontier append that also writes the edge-tile markers.
+//
+// The reference synchronises its 20 persistent CTAs with unbounded spins on volatile
+// counters (src/sssp/purn/Main.cu:173-189,336-347,379-383) and compacts the frontier
+// with a full-V BlockScan sweep every round (src/sssp/purn/Main.cu:350-377).  Here the
+// launch is cooperative (co-residency guaranteed), every wait has a time limit after
+// which the kernel records C2G_FLAG_BARRIER_TIMEOUT and returns, and the next frontier
+// is appended sparsely as vertices improve.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/c2graph.h"
+
+namespace c2g {
+
+constexpr unsigned kFull = 0xffffffffu;
+constexpr int kInfDist = 1999999999;  // unreachable distance, src/sssp/base/Main.cu:121
+
+struct GridBarrier {
+    unsigned count;
+    unsigned gen;
+};
+
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release_u32(unsigned* p, unsigned v) {
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ unsigned atom_add_acq_rel_u32(unsigned* p, unsigned v) {
+    unsigned old;
+    asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+    return old;
+}
+__device__ __forceinline__ unsigned long long globaltimer_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// L2-coherent loads (bypass L1): for arrays written by other CTAs in the same launch.
+__device__ __forceinline__ int ldcg(const int* p) { return __ldcg(p); }
+__device__ __forceinline__ unsigned ldcg(const unsigned* p) { return __ldcg(p); }
+__device__ __forceinline__ float ldcg(const float* p) { return __ldcg(p); }
+__device__ __forceinline__ int2 ldcg(const int2* p) { return __ldcg(p); }
+__device__ __forceinline__ unsigned long long ldcg(const unsigned long long* p) { return __ldcg(p); }
+
+// Grid barrier with a time limit.  Every CTA of a cooperative launch calls it; it
+// returns false (and all later calls return false) once any CTA has given up, so the
+// caller returns and the launch ends with C2G_FLAG_BARRIER_TIMEOUT recorded.
+__device__ __forceinline__ bool grid_sync(GridBarrier* b, int* flags, unsigned long long limit_ns) {
+    __shared__ int s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int ok = 1;
+        const unsigned g = ld_acquire_u32(&b->gen);
+        const unsigned arrived = atom_add_acq_rel_u32(&b->count, 1u);
+        if (arrived == gridDim.x - 1) {
+            b->count = 0;
+            st_release_u32(&b->gen, g + 1);
+        } else {
+            const unsigned long long t0 = globaltimer_ns();
+            unsigned spins = 0;
+            while (ld_acquire_u32(&b->gen) == g) {
+                if (++spins > 32) __nanosleep(64);
+                if ((spins & 255u) == 0) {
+                    if (ld_acquire_u32(reinterpret_cast<unsigned*>(flags)) & C2G_FLAG_BARRIER_TIMEOUT) {
+                        ok = 0;
+                        break;
+                    }
+                    if (globaltimer_ns() - t0 > limit_ns) {
+                        atomicOr(flags, C2G_FLAG_BARRIER_TIMEOUT);
+                        ok = 0;
+                        break;
+                    }
+                }
+            }
+        }
+        if (ok && (ld_acquire_u32(reinterpret_cast<unsigned*>(flags)) & C2G_FLAG_BARRIER_TIMEOUT)) ok = 0;
+        s_ok = ok;
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+// Destination of a frontier append.  Entries are (vertex, base) where base is the
+// exclusive prefix of the out-degrees of all entries before it, obtained from one
+// 64-bit atomic on ctr = (count << 32) | edge_total, so the frontier's edges form one
+// contiguous index range [0, T).  mark[t] receives the entry that owns edge t*TILE,
+// which lets a warp start expanding any edge tile without a search.
+struct FrontierOut {
+    int2* q;                  // entries (vertex, base)
+    float* val;               // optional per-entry value (PPR residual)
+    int* mark;                // tile -> owning entry
+    unsigned long long* ctr;  // packed counter
+    unsigned cap;             // entry capacity
+    unsigned mark_cap;        // marker capacity
+    int log_tile;             // log2(edges per tile)
+    int* flags;
+};
+
+// Warp-collective: every lane calls it; lanes with `want` append (v, deg, val).
+// deg must be > 0 for appended entries.
+__device__ __forceinline__ void frontier_push(const FrontierOut& out, bool want, int v, int deg, float val) {
+    const int lane = threadIdx.x & 31;
+    const unsigned m = __ballot_sync(kFull, want);
+    if (m == 0) return;
+    const int d = want ? deg : 0;
+    int incl = d;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(kFull, incl, o);
+        if (lane >= o) incl += t;
+    }
+    const unsigned total = (unsigned)__shfl_sync(kFull, incl, 31);
+    const int leader = __ffs(m) - 1;
+    unsigned long long old = 0;
+    if (lane == leader)
+        old = atomicAdd(out.ctr, ((unsigned long long)__popc(m) << 32) | (unsigned long long)total);
+    old = __shfl_sync(kFull, old, leader);
+    if (want) {
+        const unsigned slot = (unsigned)(old >> 32) + (unsigned)__popc(m & ((1u << lane) - 1u));
+        const unsigned base = (unsigned)old + (unsigned)(incl - d);
+        if (slot < out.cap) {
+            out.q[slot] = make_int2(v, (int)base);
+            if (out.val) out.val[slot] = val;
+            const unsigned tile = 1u << out.log_tile;
+            unsigned t0 = (base + tile - 1) >> out.log_tile;
+            const unsigned t1 = (base + (unsigned)deg - 1) >> out.log_tile;
+            for (unsigned t = t0; t <= t1 && t < out.mark_cap; ++t) out.mark[t] = (int)slot;
+        } else {
+            atomicOr(out.flags, C2G_FLAG_QUEUE_OVERFLOW);
+        }
+    }
+}
+
+// Warp-collective count-only append of vertex ids.
+__device__ __forceinline__ void list_push(int* list, unsigned* ctr, unsigned cap, int* flags, bool want, int v) {
+    const int lane = threadIdx.x & 31;
+    const unsigned m = __ballot_sync(kFull, want);
+    if (m == 0) return;
+    const int leader = __ffs(m) - 1;
+    unsigned old = 0;
+    if (lane == leader) old = atomicAdd(ctr, (unsigned)__popc(m));
+    old = __shfl_sync(kFull, old, leader);
+    if (want) {
+        const unsigned slot = old + (unsigned)__popc(m & ((1u << lane) - 1u));
+        if (slot < cap)
+            list[slot] = v;
+        else
+            atomicOr(flags, C2G_FLAG_QUEUE_OVERFLOW);
+    }
+}
+
+// Owner lookup inside a batch of 32 frontier entries held one per lane: the largest
+// lane k with base_k <= e (bases strictly increase across valid lanes; invalid lanes
+// hold INT_MAX).
+__device__ __forceinline__ int owner_lane(unsigned base, unsigned e) {
+    int k = 0;
+#pragma unroll
+    for (int s = 16; s >= 1; s >>= 1) {
+        const unsigned b = (unsigned)__shfl_sync(kFull, (int)base, k + s);
+        if (b <= e) k += s;
+    }
+    return k;
+}
+
+}  // namespace c2g

@@ -1,0 +1,46 @@
+// Device ingest of a CSR graph: the reference copies vlist/elist/wlist to separate
+// device arrays through an extra host copy (src/sssp/purn/DeviceMemory.cuh:48-67,
+// vec_to_arr by value).  Here the raw arrays go host->device once and a kernel
+// interleaves (target, weight) into one 8-byte record per edge, so the traversal
+// kernels read each edge with a single coalesced load.
+#include "internal.h"
+
+namespace c2g {
+
+__global__ void interleave_kernel(const int* __restrict__ col, const int* __restrict__ w, int2* __restrict__ adj,
+                                  long long E) {
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < E; e += stride)
+        adj[e] = make_int2(__ldg(col + e), __ldg(w + e));
+}
+
+// Build adj[E] on the device from host arrays col[E] and w[E] (w holds int32 weights
+// or float bits).  Uses two temporary device arrays.
+int build_adj(c2g_graph* g, const int32_t* col, const int32_t* w, int2** out) {
+    const size_t E = (size_t)g->E;
+    int2* adj = nullptr;
+    int *dcol = nullptr, *dw = nullptr;
+    C2G_CUDA(cudaMalloc(&adj, sizeof(int2) * (E ? E : 1)));
+    *out = adj;
+    if (E == 0) return C2G_OK;
+    C2G_CUDA(cudaMalloc(&dcol, sizeof(int) * E));
+    cudaError_t e = cudaMalloc(&dw, sizeof(int) * E);
+    if (e != cudaSuccess) {
+        cudaFree(dcol);
+        C2G_CUDA(e);
+    }
+    e = cudaMemcpyAsync(dcol, col, sizeof(int) * E, cudaMemcpyHostToDevice, g->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dw, w, sizeof(int) * E, cudaMemcpyHostToDevice, g->stream);
+    if (e == cudaSuccess) {
+        const int blocks = g->num_sms * 4;
+        interleave_kernel<<<blocks, 256, 0, g->stream>>>(dcol, dw, adj, (long long)E);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+    cudaFree(dcol);
+    cudaFree(dw);
+    C2G_CUDA(e);
+    return C2G_OK;
+}
+
+}  // namespace c2g

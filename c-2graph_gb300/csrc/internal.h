@@ -1,0 +1,140 @@
+// Internal host-side types of the C^2graph GB300 library (not part of the ABI).
+//
+// Device layout of a graph (HBM):
+//   row   int32[V+1]        CSR row pointer (reference vlist)
+//   adj_w int2[E]           (target, int32 weight) interleaved: one 8-byte load per edge
+//   adj_f int2[E]           (target, float weight bits) for the push kernels
+//   hv/he/hw                pruned records (reference hvlist/helist/hwlist)
+//   rec_of_vertex int32[V]  vertex -> record index (from the hvmap sidecar), -1 if none
+// Per-query workspaces are allocated on first use and kept for the handle's lifetime.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <mutex>
+#include <vector>
+
+#include "../../include/c2graph.h"
+#include "host_io.h"
+
+namespace c2g {
+
+#define C2G_CUDA(call)                                                                       \
+    do {                                                                                     \
+        cudaError_t e_ = (call);                                                             \
+        if (e_ != cudaSuccess)                                                               \
+            return ::c2g::fail(e_ == cudaErrorMemoryAllocation ? C2G_ERR_OOM : C2G_ERR_CUDA, \
+                               "%s in %s at line %d", cudaGetErrorString(e_), __FILE__,      \
+                               __LINE__);                                                    \
+    } while (0)
+
+// Control block of one persistent traversal launch; zeroed before every launch.
+struct TraversalCtl {
+    unsigned long long qctr[3];  // frontier counters per round slot: (count<<32)|edges
+    unsigned tilectr[3];         // dynamic tile scheduler per round slot
+    unsigned listctr[3];         // PPR touched-list counters per round slot
+    unsigned farctr[3];          // SSSP far piles (rotating: current, target, free)
+    int farmin[3];
+    unsigned bar_count, bar_gen;  // GridBarrier
+    int flags;                    // C2G_FLAG_*
+    int iterations;
+    long long popped, relaxed, touched, seeds;
+    int pad[4];
+};
+
+// Stamps survive across launches; the kernel advances the bases itself.
+struct StampState {
+    int stamp_base;
+    int epoch_base;
+    int pad[2];
+};
+
+struct SsspWork {
+    int* dist = nullptr;
+    int* stamp = nullptr;
+    int* farstamp = nullptr;
+    int2* q[2] = {nullptr, nullptr};
+    int* mark[2] = {nullptr, nullptr};
+    int* far = nullptr;  // three far piles of V ids each
+    TraversalCtl* ctl = nullptr;
+    StampState* st = nullptr;
+    unsigned mark_cap = 0;
+    int log_tile = -1;
+};
+
+struct PprWork {
+    float* pr = nullptr;
+    float* res = nullptr;
+    float* msg = nullptr;
+    int* stamp = nullptr;
+    int2* q[2] = {nullptr, nullptr};
+    float* qval[2] = {nullptr, nullptr};
+    int* mark[2] = {nullptr, nullptr};
+    int* touched = nullptr;
+    TraversalCtl* ctl = nullptr;
+    StampState* st = nullptr;
+    unsigned mark_cap = 0;
+    int log_tile = -1;
+};
+
+struct SsspConfig {
+    int delta = 0;       // <= 0: no near/far split
+    int log_tile = 8;    // 256 edges per warp tile
+    int max_iter = 1 << 20;
+};
+
+struct PprConfig {
+    int log_tile = 8;
+};
+
+struct LaunchGeom {
+    int blocks = 0;
+    int threads = 512;
+};
+
+}  // namespace c2g
+
+struct c2g_graph {
+    int device = 0;
+    int variant = 0;
+    int32_t V = 0;
+    int64_t E = 0;
+    int32_t* row = nullptr;
+    int2* adj_w = nullptr;
+    int2* adj_f = nullptr;
+    // pruned records
+    int32_t R = -1;
+    int64_t H = 0;
+    int32_t* hv = nullptr;
+    int32_t* he = nullptr;
+    int32_t* hw = nullptr;  // int32 or float bits
+    bool hw_float = false;
+    int32_t* rec_of_vertex = nullptr;
+    // host copies needed for source rules and seed ranges
+    std::vector<int32_t> h_row;
+    std::vector<int32_t> h_hv;
+    std::vector<int32_t> h_rec_of_vertex;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    std::mutex mu;
+    c2g::SsspConfig sssp_cfg;
+    c2g::PprConfig ppr_cfg;
+    c2g::SsspWork sssp;
+    c2g::PprWork ppr;
+    c2g::LaunchGeom geom_sssp, geom_ppr;
+    int num_sms = 0;
+};
+
+namespace c2g {
+
+// Kernel launchers (sssp.cu / ppr.cu).  All work is issued on g->stream.
+int sssp_launch(c2g_graph* g, int32_t source, const int32_t* seed_v, const int32_t* seed_w,
+                int32_t n_seeds, int32_t* dist_dev, float* ms);
+int ppr_launch(c2g_graph* g, int32_t source, const c2g_ppr_params& p, const int32_t* seed_v,
+               const float* seed_w, int32_t n_seeds, float* pr_dev, float* res_dev, float* ms);
+void sssp_free(c2g_graph* g);
+void ppr_free(c2g_graph* g);
+
+}  // namespace c2g

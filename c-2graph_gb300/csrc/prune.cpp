@@ -1,0 +1,336 @@
+// C^2graph-P offline pruners, written to produce the same bytes as the reference's
+// purn-sssp (src/purn-sssp.cpp:61-352) and purn-ppr (src/purn-ppr.cpp:63-344).
+//
+// Both prune edges out of low-in-degree vertices i: an out-edge i->v is removed when
+// every live in-neighbour ("root") r of i, except at most one, already has an edge to
+// v.  The missing root gets r->v, every root's r->v weight is combined with the path
+// through i, and the removed edges of i are appended as one "record" (hvlist/helist/
+// hwlist) that the traversal uses as seeds when i is the source.
+//
+// The pruning is sequential by construction: the order in which vertices are visited
+// changes which edges survive, so this stays a single-threaded host pass.  What this
+// file adds over the reference is the record->vertex sidecar sssp/hvmap.bin: purn-sssp
+// appends records in pruning order (rounds k = 0..29 over all vertices), while the
+// traversal indexes hvlist by vertex id (src/sssp/purn/Main.cu:68-79).
+#include <algorithm>
+#include <cstdint>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "../../include/c2graph.h"
+#include "host_io.h"
+
+namespace c2g {
+
+namespace {
+
+template <typename W>
+using Adj = std::vector<std::vector<std::pair<int32_t, W>>>;
+using InAdj = std::vector<std::vector<std::pair<int32_t, bool>>>;
+
+// Out-adjacency: per row the sorted set of distinct (dst, weight) pairs without
+// self-loops (the reference builds it through std::set, core/util.hpp:94-110).
+template <typename W>
+void build_out(const std::vector<int32_t>& vlist, const std::vector<int32_t>& elist,
+               const std::vector<W>& wl, int32_t V, Adj<W>& out) {
+    out.assign(V, {});
+    for (int32_t v = 0; v < V; ++v) {
+        auto& row = out[v];
+        for (int32_t e = vlist[v]; e < vlist[v + 1]; ++e)
+            if (elist[e] != v) row.emplace_back(elist[e], wl[e]);
+        std::sort(row.begin(), row.end());
+        row.erase(std::unique(row.begin(), row.end()), row.end());
+    }
+}
+
+// In-adjacency: for each v (ascending) its distinct out-neighbours d get (v, alive).
+void build_in(const std::vector<int32_t>& vlist, const std::vector<int32_t>& elist, int32_t V,
+              InAdj& in) {
+    in.assign(V, {});
+    std::vector<int32_t> tmp;
+    for (int32_t v = 0; v < V; ++v) {
+        tmp.clear();
+        for (int32_t e = vlist[v]; e < vlist[v + 1]; ++e)
+            if (elist[e] != v) tmp.push_back(elist[e]);
+        std::sort(tmp.begin(), tmp.end());
+        tmp.erase(std::unique(tmp.begin(), tmp.end()), tmp.end());
+        for (int32_t d : tmp) in[d].emplace_back(v, true);
+    }
+}
+
+std::vector<std::pair<int32_t, bool>>::iterator in_find(std::vector<std::pair<int32_t, bool>>& row,
+                                                         int32_t key) {
+    return std::lower_bound(row.begin(), row.end(), key,
+                            [](const std::pair<int32_t, bool>& a, int32_t b) { return a.first < b; });
+}
+
+// Weight rules of the two pruners.
+struct SsspRule {
+    using W = int32_t;
+    static W combine_new(W d3, W dis) { return d3 + dis; }
+    static W combine_hit(W old, W d3, W dis) { return std::min(old, d3 + dis); }
+    static constexpr bool skip_root_target = true;  // src/purn-sssp.cpp:244,263
+};
+struct PprRule {
+    using W = float;
+    // (float * 0.8) * float evaluated in double, then rounded to float
+    // (src/purn-ppr.cpp:244,255,259).
+    static W combine_new(W d3, W dis) { return (float)((double)d3 * 0.8 * (double)dis); }
+    static W combine_hit(W old, W d3, W dis) {
+        return (float)((double)old + (double)d3 * 0.8 * (double)dis);
+    }
+    static constexpr bool skip_root_target = false;
+};
+
+struct Records {
+    std::vector<int32_t> hv{0};
+    std::vector<int32_t> he;
+    std::vector<int32_t> hw_i;
+    std::vector<float> hw_f;
+    std::vector<int32_t> owner;  // record -> vertex
+};
+
+// Prune vertex i (its in-degree is within the pruner's bound).  Appends i's record.
+template <typename R>
+int prune_vertex(int32_t i, Adj<typename R::W>& out, InAdj& in, std::vector<int32_t>& indeg,
+                 Records& rec) {
+    using W = typename R::W;
+    std::vector<int32_t> roots;
+    std::vector<W> dis;
+    for (auto& p : in[i]) {
+        if (!p.second) continue;
+        const int32_t r = p.first;
+        auto& orow = out[r];
+        auto it = std::lower_bound(orow.begin(), orow.end(), i,
+                                   [](const std::pair<int32_t, W>& a, int32_t b) { return a.first < b; });
+        if (it == orow.end() || it->first != i)
+            return fail(C2G_ERR_FORMAT, "prune: live in-edge %d->%d has no out-edge", r, i);
+        roots.push_back(r);
+        dis.push_back(it->second);
+    }
+    const size_t j = roots.size();
+    if ((int64_t)j != indeg[i])
+        return fail(C2G_ERR_FORMAT, "prune: vertex %d live in-degree %d != %zu roots", i, indeg[i], j);
+
+    std::vector<size_t> cursor(j, 0);
+    std::vector<std::pair<int32_t, W>> kept, removed;
+    std::vector<int32_t> missing;
+    for (const auto& ev : out[i]) {
+        const int32_t v = ev.first;
+        if (std::find(roots.begin(), roots.end(), v) != roots.end()) {
+            kept.push_back(ev);
+            continue;
+        }
+        size_t cnt = 0;
+        missing.clear();
+        for (size_t k = 0; k < j; ++k) {
+            const auto& orow = out[roots[k]];
+            // Monotone cursor over the root's sorted row: the first position at or after
+            // the cursor whose target is >= v, or the row's last element
+            // (src/purn-sssp.cpp:198-200).  Binary search gives the same position as the
+            // reference's linear walk.
+            if (cursor[k] + 1 < orow.size() && orow[cursor[k]].first < v) {
+                auto it = std::lower_bound(orow.begin() + (long)cursor[k], orow.end() - 1, v,
+                                           [](const std::pair<int32_t, W>& a, int32_t b) { return a.first < b; });
+                cursor[k] = (size_t)(it - orow.begin());
+            }
+            if (orow[cursor[k]].first == v)
+                ++cnt;
+            else
+                missing.push_back(roots[k]);
+        }
+        if (cnt + 2 > j) {
+            removed.push_back(ev);
+            for (int32_t r : missing) {
+                if (R::skip_root_target && r == v) continue;
+                auto& irow = in[v];
+                auto it = in_find(irow, r);
+                if (it == irow.end() || it->first != r) {
+                    irow.insert(it, std::make_pair(r, true));
+                    indeg[v]++;
+                } else if (!it->second) {
+                    indeg[v]++;
+                    it->second = true;
+                }
+            }
+            auto it = in_find(in[v], i);
+            if (it == in[v].end() || it->first != i)
+                return fail(C2G_ERR_FORMAT, "prune: edge %d->%d missing from in-list", i, v);
+            indeg[v]--;
+            it->second = false;
+        } else {
+            kept.push_back(ev);
+        }
+    }
+
+    // Merge the removed edges into every root's row with the combined weight (a merge
+    // of nothing leaves a row unchanged, so it is skipped).
+    std::vector<std::pair<int32_t, W>> merged;
+    for (size_t k = 0; k < j && !removed.empty(); ++k) {
+        const int32_t r = roots[k];
+        auto& orow = out[r];
+        merged.clear();
+        merged.reserve(orow.size() + removed.size());
+        size_t a = 0, b = 0;
+        while (a < orow.size() || b < removed.size()) {
+            if (a == orow.size()) {
+                if (R::skip_root_target && removed[b].first == r) { ++b; continue; }
+                merged.emplace_back(removed[b].first, R::combine_new(removed[b].second, dis[k]));
+                ++b;
+            } else if (b == removed.size()) {
+                merged.push_back(orow[a++]);
+            } else if (orow[a].first == removed[b].first) {
+                merged.emplace_back(orow[a].first, R::combine_hit(orow[a].second, removed[b].second, dis[k]));
+                ++a;
+                ++b;
+            } else if (orow[a].first > removed[b].first) {
+                if (R::skip_root_target && removed[b].first == r) { ++b; continue; }
+                merged.emplace_back(removed[b].first, R::combine_new(removed[b].second, dis[k]));
+                ++b;
+            } else {
+                merged.push_back(orow[a++]);
+            }
+        }
+        orow.swap(merged);
+    }
+    out[i].swap(kept);
+
+    for (const auto& ev : removed) {
+        rec.he.push_back(ev.first);
+        if constexpr (std::is_same<W, float>::value)
+            rec.hw_f.push_back(ev.second);
+        else
+            rec.hw_i.push_back(ev.second);
+    }
+    rec.hv.push_back(rec.hv.back() + (int32_t)removed.size());
+    rec.owner.push_back(i);
+    return C2G_OK;
+}
+
+template <typename W>
+void flatten(const Adj<W>& out, int32_t V, std::vector<int32_t>& vlist, std::vector<int32_t>& elist,
+             std::vector<W>& wl) {
+    vlist.assign((size_t)V + 1, 0);
+    size_t E = 0;
+    for (int32_t v = 0; v < V; ++v) E += out[v].size();
+    elist.resize(E);
+    wl.resize(E);
+    size_t e = 0;
+    for (int32_t v = 0; v < V; ++v) {
+        for (const auto& p : out[v]) {
+            elist[e] = p.first;
+            wl[e] = p.second;
+            ++e;
+        }
+        vlist[v + 1] = (int32_t)e;
+    }
+}
+
+}  // namespace
+
+int prune_sssp_dir(const std::string& dir) {
+    std::vector<int32_t> vlist, elist, wlist;
+    int rc;
+    if ((rc = read_array4(dir + "/origin/vlist.bin", vlist))) return rc;
+    if ((rc = read_array4(dir + "/origin/elist.bin", elist))) return rc;
+    if ((rc = read_array4(dir + "/origin/wlist.bin", wlist))) return rc;
+    if ((rc = check_csr(vlist, elist))) return rc;
+    if (wlist.size() < elist.size()) return fail(C2G_ERR_FORMAT, "wlist shorter than elist");
+    const int32_t V = (int32_t)vlist.size() - 1;
+
+    Adj<int32_t> out;
+    InAdj in;
+    build_out(vlist, elist, wlist, V, out);
+    build_in(vlist, elist, V, in);
+    std::vector<int32_t>().swap(elist);
+    std::vector<int32_t>().swap(wlist);
+    std::vector<int32_t> indeg(V);
+    for (int32_t v = 0; v < V; ++v) indeg[v] = (int32_t)in[v].size();
+
+    // Rounds k = 0..29; a vertex is visited once, in the first round whose bound
+    // covers its live in-degree (src/purn-sssp.cpp:139-150).
+    const int32_t dmax = 29;
+    Records rec;
+    std::vector<char> visited(V, 0);
+    for (int32_t k = 0; k <= dmax; ++k) {
+        for (int32_t i = 0; i < V; ++i) {
+            if (indeg[i] > k || visited[i] || indeg[i] == 0) continue;
+            visited[i] = 1;
+            if (!out[i].empty() && indeg[i] > 0 && indeg[i] <= dmax)
+                if ((rc = prune_vertex<SsspRule>(i, out, in, indeg, rec))) return rc;
+        }
+    }
+    InAdj().swap(in);
+    std::vector<int32_t> pv, pe, pw;
+    flatten(out, V, pv, pe, pw);
+    const std::string s = dir + "/sssp/";
+    if ((rc = make_dir(dir + "/sssp"))) return rc;
+    if ((rc = write_array4(s + "hvlist.bin", rec.hv.data(), rec.hv.size()))) return rc;
+    if ((rc = write_array4(s + "helist.bin", rec.he.data(), rec.he.size()))) return rc;
+    if ((rc = write_array4(s + "hwlist.bin", rec.hw_i.data(), rec.hw_i.size()))) return rc;
+    if ((rc = write_array4(s + "hvmap.bin", rec.owner.data(), rec.owner.size()))) return rc;
+    if ((rc = write_array4(s + "vlist.bin", pv.data(), pv.size()))) return rc;
+    if ((rc = write_array4(s + "elist.bin", pe.data(), pe.size()))) return rc;
+    if ((rc = write_array4(s + "wlist.bin", pw.data(), pw.size()))) return rc;
+    return C2G_OK;
+}
+
+int prune_ppr_dir(const std::string& dir) {
+    std::vector<int32_t> vlist, elist;
+    std::vector<float> flist;
+    int rc;
+    if ((rc = read_array4(dir + "/origin/vlist.bin", vlist))) return rc;
+    if ((rc = read_array4(dir + "/origin/elist.bin", elist))) return rc;
+    if ((rc = read_array4(dir + "/origin/flist.bin", flist))) return rc;
+    if ((rc = check_csr(vlist, elist))) return rc;
+    if (flist.size() < elist.size()) return fail(C2G_ERR_FORMAT, "flist shorter than elist");
+    const int32_t V = (int32_t)vlist.size() - 1;
+
+    Adj<float> out;
+    InAdj in;
+    build_out(vlist, elist, flist, V, out);
+    build_in(vlist, elist, V, in);
+    std::vector<int32_t>().swap(elist);
+    std::vector<float>().swap(flist);
+    std::vector<int32_t> indeg(V);
+    for (int32_t v = 0; v < V; ++v) indeg[v] = (int32_t)in[v].size();
+
+    // One pass in vertex order with in-degree bound 5; every vertex gets a record,
+    // empty when it is not pruned (src/purn-ppr.cpp:146-152,281-283).
+    const int32_t dmax = 5;
+    Records rec;
+    for (int32_t i = 0; i < V; ++i) {
+        if (!out[i].empty() && indeg[i] > 0 && indeg[i] <= dmax) {
+            if ((rc = prune_vertex<PprRule>(i, out, in, indeg, rec))) return rc;
+        } else {
+            rec.hv.push_back(rec.hv.back());
+            rec.owner.push_back(i);
+        }
+    }
+    InAdj().swap(in);
+    std::vector<int32_t> pv, pe;
+    std::vector<float> pw;
+    flatten(out, V, pv, pe, pw);
+    const std::string s = dir + "/ppr/";
+    if ((rc = make_dir(dir + "/ppr"))) return rc;
+    if ((rc = write_array4(s + "hvlist.bin", rec.hv.data(), rec.hv.size()))) return rc;
+    if ((rc = write_array4(s + "helist.bin", rec.he.data(), rec.he.size()))) return rc;
+    if ((rc = write_array4(s + "hwlist.bin", rec.hw_f.data(), rec.hw_f.size()))) return rc;
+    if ((rc = write_array4(s + "vlist.bin", pv.data(), pv.size()))) return rc;
+    if ((rc = write_array4(s + "elist.bin", pe.data(), pe.size()))) return rc;
+    if ((rc = write_array4(s + "wlist.bin", pw.data(), pw.size()))) return rc;
+    return C2G_OK;
+}
+
+}  // namespace c2g
+
+extern "C" int c2g_prune_sssp(const char* dir) {
+    if (!dir) return c2g::fail(C2G_ERR_ARG, "prune: dir is NULL");
+    return c2g::prune_sssp_dir(dir);
+}
+
+extern "C" int c2g_prune_ppr(const char* dir) {
+    if (!dir) return c2g::fail(C2G_ERR_ARG, "prune: dir is NULL");
+    return c2g::prune_ppr_dir(dir);
+}

@@ -1,0 +1,383 @@
+// Single-query SSSP for sm_103a: one persistent cooperative launch per query.
+//
+// Replaces CalcuSSSP (reference src/sssp/base/Main.cu:109-356 and
+// src/sssp/purn/Main.cu:136-393).  Same result: the int32 shortest-distance fixed point
+// of dis[source] = 0 plus the pruned-record seeds (sssp-purn), unreachable = 1999999999.
+// Different schedule:
+//   * frontier = sparse list of (vertex, edge base) appended by warp-aggregated atomics
+//     when a distance improves (no O(V) isactive sweep, src/sssp/purn/Main.cu:350-377);
+//   * expansion is edge-tiled: the frontier's out-edges form one index range [0, T),
+//     each warp takes tiles of 2^log_tile edges from a dynamic counter, so low-degree
+//     vertices share a tile (thread-per-edge), high-degree vertices span many tiles
+//     (many warps per vertex), and every lane reads consecutive (target, weight) pairs;
+//   * relaxation is an L2 read guarding int32 atomicMin (src/sssp/purn/Main.cu:257-260);
+//   * optional near/far split (delta-stepping): improvements at or above the bucket
+//     threshold go to a far pile that is filtered into the frontier when the near
+//     frontier runs dry;
+//   * one bounded grid barrier per round instead of four unbounded spins.
+#include <climits>
+
+#include "device_common.cuh"
+#include "internal.h"
+
+namespace c2g {
+
+struct SsspParams {
+    const int* row;
+    const int2* adj;
+    unsigned E;
+    int V;
+    int* dist;
+    int* stamp;
+    int* farstamp;
+    int2* q[2];
+    int* mark[2];
+    int* far[3];
+    TraversalCtl* ctl;
+    StampState* st;
+    int source;
+    const int* seed_v;
+    const int* seed_w;
+    int n_seeds;
+    int delta;
+    int log_tile;
+    int max_iter;
+    unsigned mark_cap;
+    unsigned long long barrier_ns;
+};
+
+__device__ __forceinline__ FrontierOut sssp_out(const SsspParams& p, int buf, int slot) {
+    FrontierOut o;
+    o.q = p.q[buf];
+    o.val = nullptr;
+    o.mark = p.mark[buf];
+    o.ctr = &p.ctl->qctr[slot];
+    o.cap = (unsigned)p.V;
+    o.mark_cap = p.mark_cap;
+    o.log_tile = p.log_tile;
+    o.flags = &p.ctl->flags;
+    return o;
+}
+
+// Near-frontier candidate: dedup by round tag, drop vertices without out-edges.
+__device__ __forceinline__ bool claim_near(const SsspParams& p, int c, int tag, int& deg) {
+    if (ldcg(p.stamp + c) == tag || atomicExch(p.stamp + c, tag) == tag) return false;
+    deg = __ldg(p.row + c + 1) - __ldg(p.row + c);
+    return deg > 0;
+}
+
+// Warp-collective append to far pile fb, keeping the pile's minimum pushed distance.
+__device__ __forceinline__ void far_push(const SsspParams& p, int fb, bool want, int c, int d, int epoch,
+                                         bool dedup) {
+    if (want && dedup) {
+        if (ldcg(p.farstamp + c) == epoch || atomicExch(p.farstamp + c, epoch) == epoch) want = false;
+    }
+    const unsigned m = __ballot_sync(kFull, want);
+    if (m == 0) return;
+    int mn = want ? d : INT_MAX;
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) mn = min(mn, __shfl_xor_sync(kFull, mn, o));
+    if ((threadIdx.x & 31) == __ffs(m) - 1) atomicMin(&p.ctl->farmin[fb], mn);
+    list_push(p.far[fb], &p.ctl->farctr[fb], (unsigned)p.V, &p.ctl->flags, want, c);
+}
+
+template <bool kDelta>
+__device__ __forceinline__ void sssp_expand(const SsspParams& p, int buf, int slot, unsigned F, unsigned T,
+                                            int tag_next, int thresh, int fb, int epoch,
+                                            const FrontierOut& nout) {
+    const int lane = threadIdx.x & 31;
+    const int2* q = p.q[buf];
+    const int* mark = p.mark[buf];
+    const unsigned tw = 1u << p.log_tile;
+    const unsigned ntiles = (T + tw - 1) >> p.log_tile;
+    unsigned* tctr = &p.ctl->tilectr[slot];
+    if (ntiles > p.mark_cap || F > (unsigned)p.V || T > p.E) {
+        if ((threadIdx.x & 31) == 0) atomicOr(&p.ctl->flags, C2G_FLAG_BOUNDS);
+        return;
+    }
+    for (;;) {
+        unsigned t = 0;
+        if (lane == 0) t = atomicAdd(tctr, 1u);
+        t = __shfl_sync(kFull, t, 0);
+        if (t >= ntiles) break;
+        unsigned e0 = t << p.log_tile;
+        const unsigned e1 = min(e0 + tw, T);
+        unsigned o = (unsigned)ldcg(mark + t);
+        while (e0 < e1) {
+            // One frontier entry per lane: edge range [base, end) and snapshot distance.
+            const unsigned j = o + (unsigned)lane;
+            unsigned base = 0x7fffffffu, endv = 0xffffffffu;
+            int rs = 0, du = 0;
+            if (j < F) {
+                const int2 qe = ldcg(q + j);
+                base = (unsigned)qe.y;
+                rs = __ldg(p.row + qe.x);
+                endv = base + (unsigned)(__ldg(p.row + qe.x + 1) - rs);
+                du = ldcg(p.dist + qe.x);
+            }
+            const unsigned seg_end = min(e1, (unsigned)__shfl_sync(kFull, endv, 31));
+            if (seg_end <= e0 || o >= F) {  // the tile marker did not lead to its owner
+                if (lane == 0) atomicOr(&p.ctl->flags, C2G_FLAG_BOUNDS);
+                break;
+            }
+            for (unsigned eb = e0; eb < seg_end; eb += 32) {
+                const unsigned e = eb + (unsigned)lane;
+                const int k = owner_lane(base, e);
+                const int srs = __shfl_sync(kFull, rs, k);
+                const unsigned sb = (unsigned)__shfl_sync(kFull, (int)base, k);
+                const int sdu = __shfl_sync(kFull, du, k);
+                bool near = false, farp = false;
+                int c = 0, nd = 0;
+                const unsigned idx = (unsigned)srs + (e - sb);
+                const bool ok = e < seg_end && sb <= e && idx < p.E;
+                if (e < seg_end && !ok) atomicOr(&p.ctl->flags, C2G_FLAG_BOUNDS);
+                if (ok) {
+                    const int2 ew = __ldg(p.adj + idx);
+                    c = ew.x;
+                    nd = sdu + ew.y;
+                    if (nd < ldcg(p.dist + c)) {
+                        const int old = atomicMin(p.dist + c, nd);
+                        if (nd < old) {
+                            if (!kDelta || nd < thresh)
+                                near = true;
+                            else
+                                farp = true;
+                        }
+                    }
+                }
+                int deg = 0;
+                if (near) near = claim_near(p, c, tag_next, deg);
+                frontier_push(nout, near, c, deg, 0.f);
+                if (kDelta) far_push(p, fb, farp, c, nd, epoch, true);
+            }
+            e0 = seg_end;
+            o += 32;
+        }
+    }
+}
+
+template <bool kDelta>
+__global__ void __launch_bounds__(512, 2) sssp_persistent(const SsspParams p) {
+    TraversalCtl* ctl = p.ctl;
+    GridBarrier* bar = reinterpret_cast<GridBarrier*>(&ctl->bar_count);
+    int* flags = &ctl->flags;
+    const int lane = threadIdx.x & 31;
+    const unsigned gtid = blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned nthreads = gridDim.x * blockDim.x;
+    const unsigned gwarp = gtid >> 5, nwarps = nthreads >> 5;
+    const unsigned V = (unsigned)p.V;
+
+    int sbase = p.st->stamp_base;
+    int ebase = p.st->epoch_base;
+    const bool reset = sbase > (1 << 29) || ebase > (1 << 29);
+    if (reset) sbase = ebase = 0;
+
+    // Init: dis = INF (src/sssp/purn/Main.cu:144-156).
+    for (unsigned v = gtid; v < V; v += nthreads) {
+        p.dist[v] = kInfDist;
+        if (reset) {
+            p.stamp[v] = -1;
+            p.farstamp[v] = -1;
+        }
+    }
+    if (gtid == 0) ctl->farmin[0] = ctl->farmin[1] = ctl->farmin[2] = INT_MAX;
+    if (!grid_sync(bar, flags, p.barrier_ns)) return;
+
+    // Source and pruned-record seeds (src/sssp/purn/Main.cu:160-181).
+    if (gtid == 0) {
+        atomicMin(p.dist + p.source, 0);
+        ctl->seeds = p.n_seeds;
+    }
+    for (unsigned i = gtid; i < (unsigned)p.n_seeds; i += nthreads) atomicMin(p.dist + p.seed_v[i], p.seed_w[i]);
+    if (!grid_sync(bar, flags, p.barrier_ns)) return;
+
+    // Round-1 frontier: the seeds and the source, deduplicated.
+    {
+        const int tag = sbase + 1;
+        const FrontierOut out = sssp_out(p, 1, 1);
+        const unsigned n = (unsigned)p.n_seeds + 1;
+        for (unsigned b = gwarp * 32; b < n; b += nwarps * 32) {
+            const unsigned i = b + (unsigned)lane;
+            bool want = false;
+            int v = 0, deg = 0;
+            if (i < n) {
+                v = (i < (unsigned)p.n_seeds) ? p.seed_v[i] : p.source;
+                want = claim_near(p, v, tag, deg);
+            }
+            frontier_push(out, want, v, deg, 0.f);
+        }
+    }
+    if (!grid_sync(bar, flags, p.barrier_ns)) return;
+
+    int cur = 1, fb = 0, epoch = ebase + 1, iters = 0;
+    int thresh = kDelta ? p.delta : INT_MAX;
+    for (;;) {
+        const unsigned long long c = ldcg(&ctl->qctr[cur % 3]);
+        const unsigned F = (unsigned)(c >> 32), T = (unsigned)c;
+        if (F == 0) {
+            if (!kDelta) break;
+            const unsigned fc = ldcg(&ctl->farctr[fb]);
+            if (fc == 0) break;
+            // Next bucket: at least thresh + delta, and past the far pile's minimum.
+            const int fm = ldcg(&ctl->farmin[fb]);
+            long long nt = (long long)thresh + p.delta;
+            const long long jump = ((long long)fm / p.delta + 1) * (long long)p.delta;
+            if (jump > nt) nt = jump;
+            if (nt > INT_MAX) nt = INT_MAX;
+            const int fdst = (fb + 1) % 3;
+            if (gtid == 0) {
+                const int fold = (fb + 2) % 3;  // read by the previous filter, free now
+                ctl->farctr[fold] = 0;
+                ctl->farmin[fold] = INT_MAX;
+            }
+            const FrontierOut out = sssp_out(p, cur & 1, cur % 3);
+            const int tag = sbase + cur;
+            for (unsigned b = gwarp * 32; b < fc; b += nwarps * 32) {
+                const unsigned i = b + (unsigned)lane;
+                bool near = false, keep = false;
+                int v = 0, deg = 0, d = 0;
+                if (i < fc) {
+                    v = ldcg(p.far[fb] + i);
+                    d = ldcg(p.dist + v);
+                    if (d >= thresh) {
+                        if (d < (int)nt)
+                            near = claim_near(p, v, tag, deg);
+                        else {
+                            keep = true;
+                            p.farstamp[v] = epoch + 1;
+                        }
+                    }
+                }
+                frontier_push(out, near, v, deg, 0.f);
+                far_push(p, fdst, keep, v, d, epoch + 1, false);
+            }
+            thresh = (int)nt;
+            fb = fdst;
+            ++epoch;
+            if (!grid_sync(bar, flags, p.barrier_ns)) return;
+            continue;
+        }
+        if (++iters > p.max_iter) {
+            if (gtid == 0) atomicOr(flags, C2G_FLAG_ITER_CAP);
+            break;
+        }
+        if (gtid == 0) {
+            ctl->qctr[(cur + 2) % 3] = 0ull;
+            ctl->tilectr[(cur + 2) % 3] = 0u;
+            ctl->popped += F;
+            ctl->relaxed += T;
+        }
+        const FrontierOut nout = sssp_out(p, (cur + 1) & 1, (cur + 1) % 3);
+        sssp_expand<kDelta>(p, cur & 1, cur % 3, F, T, sbase + cur + 1, thresh, fb, epoch, nout);
+        if (!grid_sync(bar, flags, p.barrier_ns)) return;
+        ++cur;
+    }
+    if (gtid == 0) {
+        ctl->iterations = iters;
+        p.st->stamp_base = sbase + cur + 2;
+        p.st->epoch_base = epoch + 2;
+    }
+}
+
+// ---------------------------------------------------------------------------------------
+// host side
+
+static int sssp_geometry(c2g_graph* g) {
+    if (g->geom_sssp.blocks > 0) return C2G_OK;
+    int coop = 0;
+    C2G_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, g->device));
+    if (!coop) return fail(C2G_ERR_UNSUPPORTED, "device %d lacks cooperative launch", g->device);
+    int per_sm_a = 0, per_sm_b = 0;
+    C2G_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_a, sssp_persistent<false>, 512, 0));
+    C2G_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_b, sssp_persistent<true>, 512, 0));
+    int per_sm = per_sm_a < per_sm_b ? per_sm_a : per_sm_b;
+    if (per_sm < 1) return fail(C2G_ERR_CUDA, "SSSP kernel cannot be resident (occupancy 0)");
+    g->geom_sssp.blocks = per_sm * g->num_sms;
+    g->geom_sssp.threads = 512;
+    return C2G_OK;
+}
+
+void sssp_free(c2g_graph* g) {
+    SsspWork& w = g->sssp;
+    void* ptrs[] = {w.dist, w.stamp, w.farstamp, w.q[0], w.q[1], w.mark[0], w.mark[1],
+                    w.far, w.ctl, w.st};
+    for (void* ptr : ptrs)
+        if (ptr) cudaFree(ptr);
+    w = SsspWork();
+}
+
+static int sssp_alloc(c2g_graph* g) {
+    SsspWork& w = g->sssp;
+    const int log_tile = g->sssp_cfg.log_tile;
+    if (w.dist && w.log_tile == log_tile) return C2G_OK;
+    if (w.dist) sssp_free(g);
+    const size_t V = (size_t)g->V;
+    const size_t nv = V ? V : 1;
+    const unsigned mark_cap = (unsigned)(((size_t)g->E >> log_tile) + 2);
+    C2G_CUDA(cudaMalloc(&w.dist, sizeof(int) * nv));
+    C2G_CUDA(cudaMalloc(&w.stamp, sizeof(int) * nv));
+    C2G_CUDA(cudaMalloc(&w.farstamp, sizeof(int) * nv));
+    for (int b = 0; b < 2; ++b) {
+        C2G_CUDA(cudaMalloc(&w.q[b], sizeof(int2) * nv));
+        C2G_CUDA(cudaMalloc(&w.mark[b], sizeof(int) * mark_cap));
+    }
+    C2G_CUDA(cudaMalloc(&w.far, sizeof(int) * nv * 3));
+    C2G_CUDA(cudaMalloc(&w.ctl, sizeof(TraversalCtl)));
+    C2G_CUDA(cudaMalloc(&w.st, sizeof(StampState)));
+    C2G_CUDA(cudaMemset(w.stamp, 0xff, sizeof(int) * nv));
+    C2G_CUDA(cudaMemset(w.farstamp, 0xff, sizeof(int) * nv));
+    C2G_CUDA(cudaMemset(w.st, 0, sizeof(StampState)));
+    w.mark_cap = mark_cap;
+    w.log_tile = log_tile;
+    return C2G_OK;
+}
+
+int sssp_launch(c2g_graph* g, int32_t source, const int32_t* seed_v, const int32_t* seed_w, int32_t n_seeds,
+                int32_t* dist_dev, float* ms) {
+    int rc;
+    if ((rc = sssp_geometry(g))) return rc;
+    if ((rc = sssp_alloc(g))) return rc;
+    if (!g->adj_w) return fail(C2G_ERR_UNSUPPORTED, "graph has no int32 weights (wlist)");
+    SsspWork& w = g->sssp;
+    SsspParams p;
+    p.row = g->row;
+    p.adj = g->adj_w;
+    p.V = g->V;
+    p.E = (unsigned)g->E;
+    p.dist = dist_dev ? dist_dev : w.dist;
+    p.stamp = w.stamp;
+    p.farstamp = w.farstamp;
+    p.q[0] = w.q[0];
+    p.q[1] = w.q[1];
+    p.mark[0] = w.mark[0];
+    p.mark[1] = w.mark[1];
+    const size_t nv = g->V ? (size_t)g->V : 1;
+    p.far[0] = w.far;
+    p.far[1] = w.far + nv;
+    p.far[2] = w.far + 2 * nv;
+    p.ctl = w.ctl;
+    p.st = w.st;
+    p.source = source;
+    p.seed_v = seed_v;
+    p.seed_w = seed_w;
+    p.n_seeds = n_seeds;
+    p.delta = g->sssp_cfg.delta;
+    p.log_tile = w.log_tile;
+    p.max_iter = g->sssp_cfg.max_iter;
+    p.mark_cap = w.mark_cap;
+    p.barrier_ns = 2000000000ull;
+    C2G_CUDA(cudaMemsetAsync(w.ctl, 0, sizeof(TraversalCtl), g->stream));
+    void* args[] = {&p};
+    const bool delta = p.delta > 0;
+    C2G_CUDA(cudaEventRecord(g->ev0, g->stream));
+    C2G_CUDA(cudaLaunchCooperativeKernel(delta ? (const void*)sssp_persistent<true> : (const void*)sssp_persistent<false>,
+                                         dim3(g->geom_sssp.blocks), dim3(g->geom_sssp.threads), args, 0, g->stream));
+    C2G_CUDA(cudaEventRecord(g->ev1, g->stream));
+    if (ms) {
+        C2G_CUDA(cudaEventSynchronize(g->ev1));
+        C2G_CUDA(cudaEventElapsedTime(ms, g->ev0, g->ev1));
+    }
+    return C2G_OK;
+}
+
+}  // namespace c2g

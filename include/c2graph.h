@@ -1,0 +1,178 @@
+/*
+ * c2graph.h - C ABI of the GB300 (sm_103a) implementation of C^2graph's weighted
+ * traversal path: SSSP relaxation on the original or pruned CSR, PPR forward push,
+ * adsorption, and the offline C^2graph-P pruners that produce the pruned CSR.
+ *
+ * The reference (lihuaibei7951/C-2graph) has no library API; its boundary is a set of
+ * command-line programs.  Each entry point below names the reference code it replaces
+ * (file:line in the reference project).  The drop-in programs sssp-base, sssp-purn,
+ * ppr-purn, ppr-base, purn-sssp and purn-ppr are thin callers of this ABI.
+ *
+ * Conventions
+ *   - Every function returns int status: C2G_OK (0) or a negative C2G_ERR_* code.
+ *     Nothing here calls exit(); c2g_last_error() gives a message for the calling thread.
+ *   - Output buffers are owned by the caller.  A flag says whether a pointer is host
+ *     memory or device memory of the graph's device.
+ *   - A graph handle owns its device CSR and its per-query workspace, and issues all
+ *     work on one CUDA stream.  Calls on one handle are serialised by the handle;
+ *     distinct handles may be used from distinct threads.
+ *   - Binary files use the reference layout: raw little-endian int32/float32 arrays
+ *     with no header (reference core/io.hpp:25-40).
+ */
+#ifndef C2GRAPH_H
+#define C2GRAPH_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define C2G_ABI_VERSION 1
+
+/* ---- status codes --------------------------------------------------------------- */
+#define C2G_OK               0
+#define C2G_ERR_ARG         -1  /* null pointer, bad enum, bad parameter               */
+#define C2G_ERR_IO          -2  /* file missing, unreadable or short                    */
+#define C2G_ERR_FORMAT      -3  /* arrays inconsistent (vlist not monotone, bad ids)    */
+#define C2G_ERR_CUDA        -4  /* CUDA runtime error                                   */
+#define C2G_ERR_OOM         -5  /* device or host allocation failed                     */
+#define C2G_ERR_RANGE       -6  /* source out of range, or no eligible source           */
+#define C2G_ERR_TIMEOUT     -7  /* a bounded device-side wait ran out                   */
+#define C2G_ERR_OVERFLOW    -8  /* a device queue would overflow                        */
+#define C2G_ERR_UNSUPPORTED -9  /* graph variant lacks what the call needs             */
+#define C2G_ERR_NODEVICE   -10  /* no CUDA device                                       */
+
+/* device-side status bits reported in c2g_stats.status_flags */
+#define C2G_FLAG_BARRIER_TIMEOUT  0x1  /* a grid barrier wait ran out                   */
+#define C2G_FLAG_ITER_CAP         0x2  /* the iteration cap stopped the traversal       */
+#define C2G_FLAG_QUEUE_OVERFLOW   0x4  /* a queue append was dropped                    */
+#define C2G_FLAG_BOUNDS           0x8  /* an index check failed; the access was skipped */
+
+/* which directory of a dataset a graph is read from */
+typedef enum {
+    C2G_GRAPH_ORIGIN = 0, /* <dir>/origin/{vlist,elist,wlist[,flist]}.bin               */
+    C2G_GRAPH_SSSP   = 1, /* <dir>/sssp/{vlist,elist,wlist,hvlist,helist,hwlist}.bin    */
+    C2G_GRAPH_PPR    = 2  /* <dir>/ppr/{vlist,elist,wlist(float),hvlist,helist,hwlist}  */
+} c2g_variant;
+
+/* How sssp-purn picks the pruned-record seeds of a source.
+ *   COMPAT: hvlist is indexed by the source id, exactly as the reference does
+ *           (src/sssp/purn/Main.cu:68-79), although purn-sssp writes one record per
+ *           pruned vertex in pruning order (src/purn-sssp.cpp:279-286).
+ *   EXACT:  the record that belongs to the source is found through the record->vertex
+ *           sidecar (sssp/hvmap.bin) written by c2g_prune_sssp. */
+typedef enum { C2G_SEEDS_COMPAT = 0, C2G_SEEDS_EXACT = 1 } c2g_seed_mode;
+
+typedef struct c2g_graph c2g_graph;
+
+/* per-call statistics (device counters, read back after the call) */
+typedef struct c2g_stats {
+    int32_t source;          /* source actually traversed                              */
+    int32_t iterations;      /* frontier rounds executed (reference iteration_num)     */
+    int64_t vertices_popped; /* sum over rounds of frontier vertices expanded          */
+    int64_t edges_relaxed;   /* sum over rounds of frontier out-edges relaxed/pushed   */
+    int64_t touched;         /* PPR: sum over rounds of vertices that got a message    */
+    int64_t n_seeds;         /* seed entries applied before the first round            */
+    double  alg_bytes;       /* algorithmic bytes of the call (byte model per path)    */
+    float   device_ms;       /* device time of the traversal launch (CUDA events)      */
+    int32_t status_flags;    /* C2G_FLAG_* bits, 0 when clean                          */
+    int32_t reserved;
+} c2g_stats;
+
+/* PPR / adsorption push parameters (reference src/ppr/purn/Main.cu:66-67,
+ * src/ppr/base/Main.cu:61-62, src/adsorption/w-base/Main.cu:63-64,149-152). */
+typedef struct c2g_ppr_params {
+    float   alpha;    /* teleport probability: pr += alpha*r, push (1-alpha)*r*w      */
+    float   rmax;     /* activation threshold: a vertex is pushed when residual > rmax */
+    float   r0;       /* base mode: residual placed on the source                     */
+    float   pr0;      /* base mode: value added to pr[source] before the first round  */
+    int32_t max_iter; /* round cap (reference: 500 for PPR, 2000 for adsorption)       */
+    int32_t seeded;   /* 0: base init (src/ppr/base/Main.cu:146-150)
+                         1: pruned-graph init with host-side first hop
+                            (src/ppr/purn/Main.cu:78-101,173-198)                    */
+} c2g_ppr_params;
+
+/* ---- library ---------------------------------------------------------------------- */
+int         c2g_abi_version(void);
+const char* c2g_last_error(void);
+int         c2g_device_count(int* count);
+
+/* ---- graphs ------------------------------------------------------------------------ */
+/* Load <dir>/{origin|sssp|ppr}/ into device memory of `device`.
+ * Replaces Graph ctors src/sssp/base/Graph.h:30-51, src/sssp/purn/Graph.h:33-48,
+ * src/ppr/purn/Graph.h:34-46 and DeviceMemory::CudaMemcpyGraph
+ * (src/sssp/purn/DeviceMemory.cuh:48-67).  A missing file is C2G_ERR_IO (the
+ * reference prints "file:<f> not exist." and exits 0, core/io.hpp:27-30). */
+int c2g_graph_load(const char* dir, int variant, int device, c2g_graph** out);
+
+/* Build a graph from host CSR arrays (vlist[V+1], elist/wlist/flist[E]); wlist or
+ * flist may be NULL.  Same device layout as c2g_graph_load. */
+int c2g_graph_create(int device, int32_t V, int64_t E, const int32_t* vlist,
+                     const int32_t* elist, const int32_t* wlist, const float* flist,
+                     c2g_graph** out);
+
+/* Attach pruned records (hvlist[R+1], helist/hwlist[hvlist[R]]).  hw_is_float selects
+ * float (ppr/) or int32 (sssp/) weights.  record_vertex[R] (may be NULL) is the
+ * record->vertex sidecar needed by C2G_SEEDS_EXACT. */
+int c2g_graph_set_records(c2g_graph* g, int32_t R, const int32_t* hvlist,
+                          const int32_t* helist, const void* hwlist, int hw_is_float,
+                          const int32_t* record_vertex);
+
+void c2g_graph_free(c2g_graph* g);
+int  c2g_graph_info(const c2g_graph* g, int32_t* V, int64_t* E, int32_t* R);
+/* Use the caller's CUDA stream (cudaStream_t passed as void*) instead of the handle's. */
+int  c2g_graph_set_stream(c2g_graph* g, void* stream);
+
+/* ---- SSSP -------------------------------------------------------------------------- */
+/* Source-skip rule of the drop-in programs: sssp-base skips sources without
+ * out-edges (src/sssp/base/Main.cu:61-64); sssp-purn also skips sources whose record
+ * holds more than 1000 seeds (src/sssp/purn/Main.cu:68-71).  pruned=0/1 selects the
+ * rule; mode is a c2g_seed_mode. */
+int c2g_sssp_resolve_source(const c2g_graph* g, int32_t source, int pruned, int mode,
+                            int32_t* adjusted);
+
+/* Single-source shortest paths with int32 weights; unreachable = 1999999999
+ * (src/sssp/base/Main.cu:121).  Replaces CalcuSSSP (src/sssp/base/Main.cu:109-356,
+ * src/sssp/purn/Main.cu:136-393) and its host loop.  use_seeds=0 runs the plain
+ * traversal (sssp-base); use_seeds=1 applies the source's pruned records selected by
+ * seed_mode (sssp-purn).  dist has V entries; dist_on_device=1 means a device
+ * pointer. */
+int c2g_sssp(c2g_graph* g, int32_t source, int use_seeds, int seed_mode, int32_t* dist,
+             int dist_on_device, c2g_stats* stats);
+
+/* Tuning knobs of the SSSP kernel: delta (bucket width of the near/far split,
+ * <=0 = no split), tile (edges per warp tile, power of two in [32, 4096]),
+ * max_iter (round cap, reference 1000). */
+int c2g_sssp_set_config(c2g_graph* g, int32_t delta, int32_t tile, int32_t max_iter);
+
+/* ---- PPR / adsorption push ------------------------------------------------------- */
+/* Forward push.  Replaces calcuatePPR (src/ppr/base/Main.cu:122-395,
+ * src/ppr/purn/Main.cu:149-428, src/adsorption/w-base/Main.cu:124-395) and the seed
+ * assembly of src/ppr/purn/Main.cu:78-101.  pr and res have V entries (res may be
+ * NULL); on_device=1 means device pointers. */
+int c2g_ppr(c2g_graph* g, int32_t source, const c2g_ppr_params* params, float* pr,
+            float* res, int on_device, c2g_stats* stats);
+
+/* Reference defaults: PPR (alpha 0.2, rmax 0.001/(V+1), cap 500), and the adsorption
+ * program (alpha 0.2, r0 10, pr0 8, rmax 1/V, cap 2000). */
+int c2g_ppr_default_params(const c2g_graph* g, int adsorption, c2g_ppr_params* out);
+
+/* ---- offline tools (host) ---------------------------------------------------------- */
+/* Seeded R-MAT graph written as <dir>/origin/{vlist,elist,wlist,flist}.bin with
+ * V = 2^scale, self-loops and duplicate edges removed, wlist uniform in [wmin,wmax],
+ * flist = per-vertex normalised uniform(0,1).  Replaces utils/convert2binary.cpp's
+ * text path (utils/convert2binary.cpp:82-137) for synthetic inputs. */
+int c2g_rmat_write(const char* dir, int scale, int edge_factor, uint64_t seed,
+                   int32_t wmin, int32_t wmax, double a, double b, double c);
+
+/* C^2graph-P pruners.  Byte-identical outputs to purn-sssp (src/purn-sssp.cpp:61-352)
+ * and purn-ppr (src/purn-ppr.cpp:63-344); purn-sssp additionally writes the
+ * record->vertex sidecar <dir>/sssp/hvmap.bin. */
+int c2g_prune_sssp(const char* dir);
+int c2g_prune_ppr(const char* dir);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* C2GRAPH_H */

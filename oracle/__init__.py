@@ -1,0 +1,125 @@
+"""CPU oracle for the C^2graph traversal path -- TEST INFRASTRUCTURE ONLY.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg import this
+package, as the checker or as the timed CPU baseline; the product library
+(c-2graph_gb300) never does.  The functions wrap oracle/oracle.c (a plain-C
+restatement of the reference algorithms, each citing the reference file:line it
+follows) and read the reference's binary dataset layout with numpy.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+INF_DIST = 1999999999
+_lib = None
+
+_I32 = ctypes.c_int32
+_P = ctypes.c_void_p
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = _build.build_oracle()
+        L = ctypes.CDLL(path)
+        L.orc_bellman_ford.restype = ctypes.c_int
+        L.orc_bellman_ford.argtypes = [_I32, _P, _P, _P, _P, _P, _I32]
+        L.orc_dijkstra.restype = None
+        L.orc_dijkstra.argtypes = [_I32, _P, _P, _P, _I32, _P, _P, _P]
+        L.orc_sssp_seeded.restype = ctypes.c_int
+        L.orc_sssp_seeded.argtypes = [_I32, _P, _P, _P, _I32, _I32, _P, _P, _P]
+        for name in ("orc_ppr_push_f64", "orc_ppr_push_f32"):
+            fn = getattr(L, name)
+            fn.restype = ctypes.c_int
+            fn.argtypes = [_I32, _P, _P, _P, _I32, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                           ctypes.c_double, _I32, _I32, _I32, _I32, _P, _P, _P, _P, _P]
+        L.orc_batch.restype = ctypes.c_int64
+        L.orc_batch.argtypes = [ctypes.c_int, _I32, _P, _P, _P, _P, _I32, _P, ctypes.c_double,
+                                ctypes.c_double, _I32, _I32, _P, _P]
+        _lib = L
+    return _lib
+
+
+def _c(a, dtype):
+    return np.ascontiguousarray(a, dtype=dtype)
+
+
+def _p(a):
+    return None if a is None else ctypes.c_void_p(a.ctypes.data)
+
+
+def load_dataset(dir, variant="origin"):
+    """Arrays of <dir>/<variant>/ as numpy (missing files are left out)."""
+    d = os.path.join(dir, variant)
+    out = {}
+    floats = {"flist"} | ({"wlist", "hwlist"} if variant == "ppr" else set())
+    for name in ("vlist", "elist", "wlist", "flist", "hvlist", "helist", "hwlist", "hvmap"):
+        p = os.path.join(d, name + ".bin")
+        if os.path.exists(p):
+            out[name] = np.fromfile(p, dtype=np.float32 if name in floats else np.int32)
+    return out
+
+
+def bellman_ford(row, col, w, dist, frontier):
+    """Reference CPU Bellman-Ford (src/sssp/base-perk/SSSP.cpp:88-119); dist updated in place."""
+    row, col, w = _c(row, np.int32), _c(col, np.int32), _c(w, np.int32)
+    fr = _c(frontier, np.int32)
+    assert dist.dtype == np.int32 and dist.flags.c_contiguous
+    return lib().orc_bellman_ford(len(row) - 1, _p(row), _p(col), _p(w), _p(dist), _p(fr), len(fr))
+
+
+def dijkstra(row, col, w, init_v, init_d):
+    row, col, w = _c(row, np.int32), _c(col, np.int32), _c(w, np.int32)
+    iv, idd = _c(init_v, np.int32), _c(init_d, np.int32)
+    dist = np.empty(len(row) - 1, dtype=np.int32)
+    lib().orc_dijkstra(len(row) - 1, _p(row), _p(col), _p(w), len(iv), _p(iv), _p(idd), _p(dist))
+    return dist
+
+
+def sssp_seeded(row, col, w, source, seed_v=(), seed_w=()):
+    row, col, w = _c(row, np.int32), _c(col, np.int32), _c(w, np.int32)
+    sv, sw = _c(seed_v, np.int32), _c(seed_w, np.int32)
+    dist = np.empty(len(row) - 1, dtype=np.int32)
+    rounds = lib().orc_sssp_seeded(len(row) - 1, _p(row), _p(col), _p(w), source, len(sv),
+                                   _p(sv) if len(sv) else None, _p(sw) if len(sw) else None, _p(dist))
+    return dist, rounds
+
+
+def ppr_push(row, col, f, source, alpha, rmax, r0=1.0, pr0=None, max_iter=500, seeded=False,
+             seed_v=(), seed_w=(), dtype=np.float64, degree_scaled=False):
+    """BSP forward push restating calcuatePPR; returns (pr, res, rounds, counters)."""
+    row, col, f = _c(row, np.int32), _c(col, np.int32), _c(f, np.float32)
+    sv, sw = _c(seed_v, np.int32), _c(seed_w, np.float32)
+    V = len(row) - 1
+    if pr0 is None:
+        pr0 = alpha * r0
+    pr = np.empty(V, dtype=dtype)
+    res = np.empty(V, dtype=dtype)
+    cnt = np.zeros(3, dtype=np.int64)
+    fn = lib().orc_ppr_push_f64 if dtype == np.float64 else lib().orc_ppr_push_f32
+    rounds = fn(V, _p(row), _p(col), _p(f), source, alpha, rmax, r0, pr0, max_iter, int(seeded),
+                int(degree_scaled), len(sv), _p(sv) if len(sv) else None, _p(sw) if len(sw) else None,
+                _p(pr), _p(res), _p(cnt))
+    return pr, res, rounds, cnt
+
+
+def batch(kind, row, col, w, f, sources, alpha=0.15, rmax=1e-7, max_iter=500, threads=1,
+          keep=False):
+    """Independent queries on `threads` host threads (CPU baseline).  kind 'sssp' or 'ppr'.
+    Returns (edges, outputs-or-None)."""
+    row, col = _c(row, np.int32), _c(col, np.int32)
+    w = None if w is None else _c(w, np.int32)
+    f = None if f is None else _c(f, np.float32)
+    src = _c(sources, np.int32)
+    V = len(row) - 1
+    k = 0 if kind == "sssp" else 1
+    out = None
+    if keep:
+        out = np.empty((len(src), V), dtype=np.int32 if k == 0 else np.float32)
+    edges = lib().orc_batch(k, V, _p(row), _p(col), _p(w), _p(f), len(src), _p(src), alpha, rmax,
+                            max_iter, threads, _p(out) if (keep and k == 0) else None,
+                            _p(out) if (keep and k == 1) else None)
+    return edges, out

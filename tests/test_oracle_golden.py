@@ -1,0 +1,171 @@
+"""The oracle and the host-side tools against the reference's own outputs (CPU only).
+
+The fixtures in tests/golden/ were produced by the reference's own code built from its
+sources (tests/golden/make_golden.py): purn-sssp / purn-ppr, the reference CPU
+Bellman-Ford (src/sssp/base-perk/SSSP.cpp:88-119) and the reference CPU forward push
+(src/ppr/w-purn-perk/PPR.cpp:178-233).
+"""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import golden_cases, load_golden, write_dataset
+
+CASES = golden_cases()
+
+
+@pytest.fixture(scope="module", params=CASES)
+def gold(request):
+    return request.param, load_golden(request.param)
+
+
+def test_golden_present():
+    assert {"rmat_s10_ef8_seed3", "rmat_s12_ef8_seed5", "tiny12"} <= set(CASES)
+
+
+def test_rmat_writer_reproduces_fixture(built, tmp_path):
+    """The seeded R-MAT writer is deterministic (same bytes on any host)."""
+    import c2g
+
+    for name, (scale, ef, seed, wmax) in {"rmat_s10_ef8_seed3": (10, 8, 3, 100),
+                                          "rmat_s12_ef8_seed5": (12, 8, 5, 1000)}.items():
+        g = load_golden(name)
+        d = str(tmp_path / name)
+        c2g.rmat_write(d, scale, ef, seed, 1, wmax)
+        for n in ("vlist", "elist", "wlist", "flist"):
+            a = np.fromfile(os.path.join(d, "origin", n + ".bin"), dtype=g["origin_" + n].dtype)
+            assert a.tobytes() == g["origin_" + n].tobytes(), (name, n)
+
+
+def test_rmat_properties(built, tmp_path):
+    import c2g
+
+    d = str(tmp_path / "g")
+    c2g.rmat_write(d, 11, 8, 9, 1, 1000)
+    vl = np.fromfile(os.path.join(d, "origin", "vlist.bin"), dtype=np.int32)
+    el = np.fromfile(os.path.join(d, "origin", "elist.bin"), dtype=np.int32)
+    wl = np.fromfile(os.path.join(d, "origin", "wlist.bin"), dtype=np.int32)
+    fl = np.fromfile(os.path.join(d, "origin", "flist.bin"), dtype=np.float32)
+    assert len(vl) == 2049 and vl[0] == 0 and vl[-1] == len(el)
+    assert wl.min() >= 1 and wl.max() <= 1000
+    for v in range(2048):
+        row = el[vl[v]:vl[v + 1]]
+        assert not np.any(row == v)                       # no self-loops
+        assert np.all(np.diff(row) > 0)                   # sorted, no duplicates
+        if len(row):
+            assert abs(float(fl[vl[v]:vl[v + 1]].astype(np.float64).sum()) - 1.0) < 1e-5
+
+
+def test_pruners_byte_identical(built, gold, tmp_path):
+    """purn-sssp / purn-ppr restatements write the reference's exact bytes."""
+    import c2g
+
+    name, g = gold
+    d = str(tmp_path / name)
+    os.makedirs(os.path.join(d, "origin"))
+    for sub in ("sssp", "ppr"):
+        os.makedirs(os.path.join(d, sub))
+    for n in ("vlist", "elist", "wlist", "flist"):
+        g["origin_" + n].tofile(os.path.join(d, "origin", n + ".bin"))
+    c2g.prune_sssp(d)
+    c2g.prune_ppr(d)
+    for sub in ("sssp", "ppr"):
+        for n in ("vlist", "elist", "wlist", "hvlist", "helist", "hwlist"):
+            mine = open(os.path.join(d, sub, n + ".bin"), "rb").read()
+            assert mine == g["%s_%s" % (sub, n)].tobytes(), (sub, n)
+    hvmap = np.fromfile(os.path.join(d, "sssp", "hvmap.bin"), dtype=np.int32)
+    assert np.array_equal(hvmap, g["hvmap"])
+    assert len(hvmap) == len(g["sssp_hvlist"]) - 1 and len(np.unique(hvmap)) == len(hvmap)
+
+
+def test_oracle_bellman_ford_matches_reference(built, gold):
+    import oracle
+
+    name, g = gold
+    vl, el, wl = g["origin_vlist"], g["origin_elist"], g["origin_wlist"]
+    for s, ref in zip(g["sources"], g["dist_origin"]):
+        dist, rounds = oracle.sssp_seeded(vl, el, wl, int(s))
+        assert np.array_equal(dist, ref), (name, s)
+        assert rounds < 1000  # the reference kernel's round cap does not bind
+        dj = oracle.dijkstra(vl, el, wl, [int(s)], [0])
+        assert np.array_equal(dj, ref), (name, s)
+
+
+def test_oracle_seeded_matches_reference(built, gold):
+    """sssp-purn semantics (COMPAT: hvlist indexed by source id) and the EXACT mode
+    (the source's own record) against ref-bf on the pruned graph."""
+    import oracle
+
+    name, g = gold
+    vl, el, wl = g["sssp_vlist"], g["sssp_elist"], g["sssp_wlist"]
+    hv, he, hw = g["sssp_hvlist"], g["sssp_helist"], g["sssp_hwlist"]
+    R = len(hv) - 1
+    rec_of = {int(v): r for r, v in enumerate(g["hvmap"])}
+    for s, cref, eref in zip(g["sources"], g["dist_compat"], g["dist_exact"]):
+        s = int(s)
+        if s < R:
+            d, _ = oracle.sssp_seeded(vl, el, wl, s, he[hv[s]:hv[s + 1]], hw[hv[s]:hv[s + 1]])
+            assert np.array_equal(d, cref), (name, s)
+        r = rec_of.get(s)
+        sv, sw = ((), ()) if r is None else (he[hv[r]:hv[r + 1]], hw[hv[r]:hv[r + 1]])
+        d, _ = oracle.sssp_seeded(vl, el, wl, s, sv, sw)
+        assert np.array_equal(d, eref), (name, s)
+
+
+def test_exact_mode_vs_unpruned(built, gold):
+    """Property report: how often pruned SSSP with the source's own record equals SSSP
+    on the unpruned graph (C^2graph-P's claim).  Not an equality the reference makes for
+    every source; recorded, with a floor for the fixtures at hand."""
+    name, g = gold
+    same = [np.array_equal(e, o) for e, o in zip(g["dist_exact"], g["dist_origin"])]
+    assert sum(same) >= len(same) // 2, (name, same)
+
+
+def test_oracle_push_matches_reference_f32(built, gold):
+    """The FP32 push restatement, in the reference CPU threshold mode, equals the
+    reference forward_push bit for bit (origin/ flist and ppr/ pruned weights)."""
+    import oracle
+
+    name, g = gold
+    V = len(g["origin_vlist"]) - 1
+    k = 0
+    for s in g["push_sources"]:
+        for rm in g["push_rmax"]:
+            for sub in ("origin", "ppr"):
+                vl, el = g[sub + "_vlist"], g[sub + "_elist"]
+                f = g["origin_flist"] if sub == "origin" else g["ppr_wlist"]
+                pr, res, rounds, _ = oracle.ppr_push(vl, el, f, int(s), 0.2, float(rm), r0=1.0, pr0=0.2,
+                                                     max_iter=1 << 30, dtype=np.float32, degree_scaled=True)
+                assert pr.tobytes() == g["push_pr_" + sub][k].tobytes(), (name, s, rm, sub)
+                assert res.tobytes() == g["push_res_" + sub][k].tobytes(), (name, s, rm, sub)
+            k += 1
+    assert V > 0
+
+
+def test_oracle_push_f32_vs_f64(built, gold):
+    import oracle
+
+    name, g = gold
+    vl, el, f = g["origin_vlist"], g["origin_elist"], g["origin_flist"]
+    s = int(g["sources"][0])
+    p64, r64, _, c64 = oracle.ppr_push(vl, el, f, s, 0.15, 1e-7)
+    p32, r32, _, c32 = oracle.ppr_push(vl, el, f, s, 0.15, 1e-7, dtype=np.float32)
+    assert np.abs(p32.astype(np.float64) - p64).sum() < 1e-6
+    # mass conservation of the push: pr/alpha + res + lost (dangling) mass = 1
+    assert p64.sum() <= 1.0 + 1e-9 and p64.sum() > 0.0
+
+
+def test_oracle_push_seeded_first_hop(built):
+    """seeded init = the base push with its first hop applied on the host: identical
+    results when every first-hop neighbour exceeds rmax."""
+    import oracle
+
+    g = load_golden("rmat_s10_ef8_seed3")
+    vl, el, f = g["origin_vlist"], g["origin_elist"], g["origin_flist"]
+    s = int(g["sources"][0])
+    pb, rb, nb, _ = oracle.ppr_push(vl, el, f, s, 0.2, 1e-9)
+    sv, sw = el[vl[s]:vl[s + 1]], f[vl[s]:vl[s + 1]]
+    ps, rs, ns, _ = oracle.ppr_push(vl, el, f, s, 0.2, 1e-9, seeded=True, seed_v=sv, seed_w=sw)
+    assert ns == nb - 1
+    assert np.abs(ps - pb).sum() < 1e-12
