@@ -34,13 +34,14 @@ struct TraversalCtl {
     unsigned long long qctr[3];  // frontier counters per round slot: (count<<32)|edges
     unsigned tilectr[3];         // dynamic tile scheduler per round slot
     unsigned listctr[3];         // PPR touched-list counters per round slot
+    unsigned dctr[3];            // PPR activated vertices without out-edges, per slot
     unsigned farctr[3];          // SSSP far piles (rotating: current, target, free)
     int farmin[3];
     unsigned bar_count, bar_gen;  // GridBarrier
     int flags;                    // C2G_FLAG_*
     int iterations;
     long long popped, relaxed, touched, seeds;
-    int pad[4];
+    int pad[1];
 };
 
 // Stamps survive across launches; the kernel advances the bases itself.
@@ -72,6 +73,7 @@ struct PprWork {
     float* qval[2] = {nullptr, nullptr};
     int* mark[2] = {nullptr, nullptr};
     int* touched = nullptr;
+    int* dangle = nullptr;
     TraversalCtl* ctl = nullptr;
     StampState* st = nullptr;
     unsigned mark_cap = 0;

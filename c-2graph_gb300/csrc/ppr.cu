@@ -11,6 +11,9 @@
 // read of res.  Phase A pushes over edge tiles exactly as the SSSP kernel does; it
 // records each vertex's first message of the round in a touched list, so phase B
 // visits only those vertices instead of sweeping all V (src/ppr/purn/Main.cu:379-407).
+// Activated vertices without out-edges join no edge tile; they sit in a side list
+// whose residual is cleared at the start of the next round, which is when the
+// reference pops them (and, when the round cap ends the run first, they keep it).
 #include <climits>
 
 #include "device_common.cuh"
@@ -31,6 +34,7 @@ struct PprParams {
     float* qval[2];
     int* mark[2];
     int* touched;
+    int* dangle;
     TraversalCtl* ctl;
     StampState* st;
     int source;
@@ -155,6 +159,11 @@ __global__ void __launch_bounds__(512, 2) ppr_persistent(const PprParams p) {
             if (lane == 0) {
                 p.pr[s] = p.pr0;
                 ctl->seeds = 0;
+                if (s_deg == 0) {
+                    p.res[s] = p.r0;
+                    p.dangle[0] = s;
+                    ctl->dctr[1] = 1;
+                }
             }
             frontier_push(ppr_out(p, 1, 1), lane == 0 && s_deg > 0, s, s_deg, p.r0);
         }
@@ -187,19 +196,21 @@ __global__ void __launch_bounds__(512, 2) ppr_persistent(const PprParams p) {
         const int tag = sbase;  // distinct from every round's touched tag
         for (unsigned b = gwarp * 32; b < n; b += nwarps * 32) {
             const unsigned i = b + (unsigned)lane;
-            bool want = false;
+            bool want = false, dang = false;
             int v = 0, deg = 0;
             float r = 0.f;
             if (i < n) {
                 v = (i < (unsigned)p.n_rec) ? p.seed_v[i] : __ldg(p.adj + rs + (int)(i - (unsigned)p.n_rec)).x;
                 if (ldcg(p.stamp + v) != tag && atomicExch(p.stamp + v, tag) != tag) {
                     r = ldcg(p.res + v);
-                    p.res[v] = 0.f;
                     deg = __ldg(p.row + v + 1) - __ldg(p.row + v);
                     want = deg > 0;
+                    if (want) p.res[v] = 0.f;
+                    else dang = true;
                 }
             }
             frontier_push(out, want, v, deg, r);
+            list_push(p.dangle, &ctl->dctr[1], (unsigned)p.V, flags, dang, v);
         }
     }
     if (!grid_sync(bar, flags, p.barrier_ns)) return;
@@ -208,7 +219,8 @@ __global__ void __launch_bounds__(512, 2) ppr_persistent(const PprParams p) {
     for (;;) {
         const unsigned long long c = ldcg(&ctl->qctr[cur % 3]);
         const unsigned F = (unsigned)(c >> 32), T = (unsigned)c;
-        if (F == 0) break;
+        const unsigned D = ldcg(&ctl->dctr[cur % 3]);
+        if (F == 0 && D == 0) break;
         if (++iters > p.max_iter) {
             // Round cap (src/ppr/purn/Main.cu:224): the activated vertices keep their
             // residual, as in the reference where they are never popped.
@@ -218,12 +230,19 @@ __global__ void __launch_bounds__(512, 2) ppr_persistent(const PprParams p) {
             for (unsigned j = gtid; j < F; j += nthreads) p.res[ldcg(q + j).x] = ldcg(qv + j);
             break;
         }
+        // Pop the activated vertices without out-edges: their residual is dropped.
+        for (unsigned j = gtid; j < D; j += nthreads) p.res[ldcg(p.dangle + j)] = 0.f;
+        if (F == 0) {
+            if (gtid == 0) ctl->popped += D;
+            break;
+        }
         const int slot = cur % 3, nslot = (cur + 1) % 3, fslot = (cur + 2) % 3;
         if (gtid == 0) {
             ctl->qctr[fslot] = 0ull;
             ctl->tilectr[fslot] = 0u;
             ctl->listctr[fslot] = 0u;
-            ctl->popped += F;
+            ctl->dctr[fslot] = 0u;
+            ctl->popped += F + D;
             ctl->relaxed += T;
         }
         ppr_push(p, cur & 1, slot, F, T, sbase + cur);
@@ -235,7 +254,7 @@ __global__ void __launch_bounds__(512, 2) ppr_persistent(const PprParams p) {
         const FrontierOut out = ppr_out(p, (cur + 1) & 1, nslot);
         for (unsigned b = gwarp * 32; b < n; b += nwarps * 32) {
             const unsigned i = b + (unsigned)lane;
-            bool want = false;
+            bool want = false, dang = false;
             int v = 0, deg = 0;
             float r = 0.f;
             if (i < n) {
@@ -244,14 +263,16 @@ __global__ void __launch_bounds__(512, 2) ppr_persistent(const PprParams p) {
                 p.msg[v] = 0.f;
                 if (r > p.rmax) {
                     p.pr[v] = ldcg(p.pr + v) + a * r;
-                    p.res[v] = 0.f;
                     deg = __ldg(p.row + v + 1) - __ldg(p.row + v);
                     want = deg > 0;
+                    dang = !want;
+                    p.res[v] = want ? 0.f : r;
                 } else {
                     p.res[v] = r;
                 }
             }
             frontier_push(out, want, v, deg, r);
+            list_push(p.dangle, &ctl->dctr[nslot], (unsigned)p.V, flags, dang, v);
         }
         if (!grid_sync(bar, flags, p.barrier_ns)) return;
         ++cur;
@@ -281,7 +302,7 @@ static int ppr_geometry(c2g_graph* g) {
 void ppr_free(c2g_graph* g) {
     PprWork& w = g->ppr;
     void* ptrs[] = {w.pr, w.res, w.msg, w.stamp, w.q[0], w.q[1], w.qval[0], w.qval[1],
-                    w.mark[0], w.mark[1], w.touched, w.ctl, w.st};
+                    w.mark[0], w.mark[1], w.touched, w.dangle, w.ctl, w.st};
     for (void* ptr : ptrs)
         if (ptr) cudaFree(ptr);
     w = PprWork();
@@ -299,6 +320,7 @@ static int ppr_alloc(c2g_graph* g) {
     C2G_CUDA(cudaMalloc(&w.msg, sizeof(float) * nv));
     C2G_CUDA(cudaMalloc(&w.stamp, sizeof(int) * nv));
     C2G_CUDA(cudaMalloc(&w.touched, sizeof(int) * nv));
+    C2G_CUDA(cudaMalloc(&w.dangle, sizeof(int) * nv));
     for (int b = 0; b < 2; ++b) {
         C2G_CUDA(cudaMalloc(&w.q[b], sizeof(int2) * nv));
         C2G_CUDA(cudaMalloc(&w.qval[b], sizeof(float) * nv));
@@ -335,6 +357,7 @@ int ppr_launch(c2g_graph* g, int32_t source, const c2g_ppr_params& pp, const int
         p.mark[b] = w.mark[b];
     }
     p.touched = w.touched;
+    p.dangle = w.dangle;
     p.ctl = w.ctl;
     p.st = w.st;
     p.source = source;
