@@ -61,6 +61,9 @@ __device__ __forceinline__ bool grid_sync(GridBarrier* b, int* flags, unsigned l
     if (threadIdx.x == 0) {
         int ok = 1;
         const unsigned g = ld_acquire_u32(&b->gen);
+        // Publish the whole CTA's writes (ordered before this thread by bar.sync) at
+        // device scope before arriving.
+        __threadfence();
         const unsigned arrived = atom_add_acq_rel_u32(&b->count, 1u);
         if (arrived == gridDim.x - 1) {
             b->count = 0;
@@ -84,6 +87,7 @@ __device__ __forceinline__ bool grid_sync(GridBarrier* b, int* flags, unsigned l
             }
         }
         if (ok && (ld_acquire_u32(reinterpret_cast<unsigned*>(flags)) & C2G_FLAG_BARRIER_TIMEOUT)) ok = 0;
+        __threadfence();
         s_ok = ok;
     }
     __syncthreads();
@@ -170,6 +174,72 @@ __device__ __forceinline__ int owner_lane(unsigned base, unsigned e) {
         if (b <= e) k += s;
     }
     return k;
+}
+
+// Warp-cooperative walk over the edges of a frontier, in tiles of 2^log_tile edges
+// assigned to warps round-robin (tile t goes to warp t mod nwarps, no shared counter).
+// For each group of 32*U edges every lane gets U edges (stride 32, so the warp reads
+// consecutive (target, weight) pairs) and calls
+//     body(ok[U], idx[U], val[U])
+// where idx is the edge's index in the adjacency array, ok says whether the lane holds
+// an edge, and val is owner_val(vertex, entry) of the edge's owning frontier entry.
+// body must be warp-collective-safe: every lane of the warp calls it.
+template <int U, typename OwnerVal, typename Body>
+__device__ __forceinline__ void walk_frontier_edges(const int2* __restrict__ q, const int* __restrict__ mark,
+                                                    const int* __restrict__ row, unsigned F, unsigned T,
+                                                    int log_tile, unsigned mark_cap, unsigned qcap, unsigned E,
+                                                    int* flags, OwnerVal owner_val, Body body) {
+    const int lane = threadIdx.x & 31;
+    const unsigned gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const unsigned nwarps = (gridDim.x * blockDim.x) >> 5;
+    const unsigned tw = 1u << log_tile;
+    const unsigned ntiles = (T + tw - 1) >> log_tile;
+    if (ntiles > mark_cap || F > qcap || T > E) {
+        if (lane == 0) atomicOr(flags, C2G_FLAG_BOUNDS);
+        return;
+    }
+    for (unsigned t = gwarp; t < ntiles; t += nwarps) {
+        unsigned e0 = t << log_tile;
+        const unsigned e1 = min(e0 + tw, T);
+        unsigned o = (unsigned)ldcg(mark + t);
+        while (e0 < e1) {
+            // One frontier entry per lane: its edge range [base, end) and owner value.
+            const unsigned j = o + (unsigned)lane;
+            unsigned base = 0x7fffffffu, endv = 0xffffffffu;
+            int rs = 0, val = 0;
+            if (j < F) {
+                const int2 qe = ldcg(q + j);
+                base = (unsigned)qe.y;
+                rs = __ldg(row + qe.x);
+                endv = base + (unsigned)(__ldg(row + qe.x + 1) - rs);
+                val = owner_val(qe.x, j);
+            }
+            const unsigned seg_end = min(e1, (unsigned)__shfl_sync(kFull, endv, 31));
+            if (seg_end <= e0 || o >= F) {  // the tile marker did not lead to its owner
+                if (lane == 0) atomicOr(flags, C2G_FLAG_BOUNDS);
+                break;
+            }
+            for (unsigned eb = e0; eb < seg_end; eb += 32u * U) {
+                bool ok[U];
+                unsigned idx[U];
+                int sv[U];
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    const unsigned e = eb + (unsigned)lane + 32u * u;
+                    const int k = owner_lane(base, e);
+                    const unsigned srs = (unsigned)__shfl_sync(kFull, rs, k);
+                    const unsigned sb = (unsigned)__shfl_sync(kFull, (int)base, k);
+                    sv[u] = __shfl_sync(kFull, val, k);
+                    idx[u] = srs + (e - sb);
+                    ok[u] = e < seg_end && sb <= e && idx[u] < E;
+                    if (e < seg_end && !ok[u]) atomicOr(flags, C2G_FLAG_BOUNDS);
+                }
+                body(ok, idx, sv);
+            }
+            e0 = seg_end;
+            o += 32;
+        }
+    }
 }
 
 }  // namespace c2g

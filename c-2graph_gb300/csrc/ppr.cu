@@ -62,68 +62,37 @@ __device__ __forceinline__ FrontierOut ppr_out(const PprParams& p, int buf, int 
     return o;
 }
 
-// Phase A: push messages along the frontier's edges.
-__device__ __forceinline__ void ppr_push(const PprParams& p, int buf, int slot, unsigned F, unsigned T, int tag) {
-    const int lane = threadIdx.x & 31;
-    const int2* q = p.q[buf];
-    const float* qv = p.qval[buf];
-    const int* mark = p.mark[buf];
-    const unsigned tw = 1u << p.log_tile;
-    const unsigned ntiles = (T + tw - 1) >> p.log_tile;
-    unsigned* tctr = &p.ctl->tilectr[slot];
-    if (ntiles > p.mark_cap || F > (unsigned)p.V || T > p.E) {
-        if ((threadIdx.x & 31) == 0) atomicOr(&p.ctl->flags, C2G_FLAG_BOUNDS);
-        return;
-    }
+constexpr int kPprUnroll = 4;  // edges in flight per lane
+
+// Phase A: push messages along the frontier's edges.  The first message a vertex gets
+// in a round is the one whose atomicAdd returns 0 (msg[v] is 0 between rounds and every
+// message is positive), so no separate touched flag is needed.  Messages below
+// FLT_MIN are dropped: they cannot change any residual in float, and a vertex outside
+// the frontier never holds a residual above rmax, so a zero message cannot activate it.
+__device__ __forceinline__ void ppr_push(const PprParams& p, int buf, int slot, unsigned F, unsigned T) {
+    constexpr int U = kPprUnroll;
     const float one_m_a = 1.0f - p.alpha;
-    for (;;) {
-        unsigned t = 0;
-        if (lane == 0) t = atomicAdd(tctr, 1u);
-        t = __shfl_sync(kFull, t, 0);
-        if (t >= ntiles) break;
-        unsigned e0 = t << p.log_tile;
-        const unsigned e1 = min(e0 + tw, T);
-        unsigned o = (unsigned)ldcg(mark + t);
-        while (e0 < e1) {
-            const unsigned j = o + (unsigned)lane;
-            unsigned base = 0x7fffffffu, endv = 0xffffffffu;
-            int rs = 0;
-            float qu = 0.f;
-            if (j < F) {
-                const int2 qe = ldcg(q + j);
-                base = (unsigned)qe.y;
-                rs = __ldg(p.row + qe.x);
-                endv = base + (unsigned)(__ldg(p.row + qe.x + 1) - rs);
-                qu = one_m_a * ldcg(qv + j);  // (1-alpha)*r_u, src/ppr/purn/Main.cu:288
+    const float* qv = p.qval[buf];
+    walk_frontier_edges<U>(
+        p.q[buf], p.mark[buf], p.row, F, T, p.log_tile, p.mark_cap, (unsigned)p.V, p.E, &p.ctl->flags,
+        // (1-alpha)*r_u, src/ppr/purn/Main.cu:288
+        [&](int, unsigned j) { return __float_as_int(one_m_a * ldcg(qv + j)); },
+        [&](const bool* ok, const unsigned* idx, const int* qu) {
+            int c[U];
+            float m[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const int2 ew = ok[u] ? __ldg(p.adj + idx[u]) : make_int2(0, 0);
+                c[u] = ew.x;
+                m[u] = __int_as_float(qu[u]) * __int_as_float(ew.y);
             }
-            const unsigned seg_end = min(e1, (unsigned)__shfl_sync(kFull, endv, 31));
-            if (seg_end <= e0 || o >= F) {  // the tile marker did not lead to its owner
-                if (lane == 0) atomicOr(&p.ctl->flags, C2G_FLAG_BOUNDS);
-                break;
-            }
-            for (unsigned eb = e0; eb < seg_end; eb += 32) {
-                const unsigned e = eb + (unsigned)lane;
-                const int k = owner_lane(base, e);
-                const int srs = __shfl_sync(kFull, rs, k);
-                const unsigned sb = (unsigned)__shfl_sync(kFull, (int)base, k);
-                const float squ = __shfl_sync(kFull, qu, k);
-                bool first = false;
-                int c = 0;
-                const unsigned idx = (unsigned)srs + (e - sb);
-                const bool ok = e < seg_end && sb <= e && idx < p.E;
-                if (e < seg_end && !ok) atomicOr(&p.ctl->flags, C2G_FLAG_BOUNDS);
-                if (ok) {
-                    const int2 ew = __ldg(p.adj + idx);
-                    c = ew.x;
-                    atomicAdd(p.msg + c, squ * __int_as_float(ew.y));
-                    first = ldcg(p.stamp + c) != tag && atomicExch(p.stamp + c, tag) != tag;
-                }
-                list_push(p.touched, &p.ctl->listctr[slot], (unsigned)p.V, &p.ctl->flags, first, c);
-            }
-            e0 = seg_end;
-            o += 32;
-        }
-    }
+            float old[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) old[u] = (ok[u] && m[u] >= 1.17549435e-38f) ? atomicAdd(p.msg + c[u], m[u]) : 1.0f;
+#pragma unroll
+            for (int u = 0; u < U; ++u)
+                list_push(p.touched, &p.ctl->listctr[slot], (unsigned)p.V, &p.ctl->flags, old[u] == 0.0f, c[u]);
+        });
 }
 
 __global__ void __launch_bounds__(512, 2) ppr_persistent(const PprParams p) {
@@ -245,7 +214,7 @@ __global__ void __launch_bounds__(512, 2) ppr_persistent(const PprParams p) {
             ctl->popped += F + D;
             ctl->relaxed += T;
         }
-        ppr_push(p, cur & 1, slot, F, T, sbase + cur);
+        ppr_push(p, cur & 1, slot, F, T);
         if (!grid_sync(bar, flags, p.barrier_ns)) return;
 
         // Phase B: apply messages and activate (src/ppr/purn/Main.cu:383-391).

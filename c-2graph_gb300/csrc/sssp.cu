@@ -81,79 +81,48 @@ __device__ __forceinline__ void far_push(const SsspParams& p, int fb, bool want,
     list_push(p.far[fb], &p.ctl->farctr[fb], (unsigned)p.V, &p.ctl->flags, want, c);
 }
 
+constexpr int kSsspUnroll = 4;  // edges in flight per lane
+
 template <bool kDelta>
-__device__ __forceinline__ void sssp_expand(const SsspParams& p, int buf, int slot, unsigned F, unsigned T,
-                                            int tag_next, int thresh, int fb, int epoch,
-                                            const FrontierOut& nout) {
-    const int lane = threadIdx.x & 31;
-    const int2* q = p.q[buf];
-    const int* mark = p.mark[buf];
-    const unsigned tw = 1u << p.log_tile;
-    const unsigned ntiles = (T + tw - 1) >> p.log_tile;
-    unsigned* tctr = &p.ctl->tilectr[slot];
-    if (ntiles > p.mark_cap || F > (unsigned)p.V || T > p.E) {
-        if ((threadIdx.x & 31) == 0) atomicOr(&p.ctl->flags, C2G_FLAG_BOUNDS);
-        return;
-    }
-    for (;;) {
-        unsigned t = 0;
-        if (lane == 0) t = atomicAdd(tctr, 1u);
-        t = __shfl_sync(kFull, t, 0);
-        if (t >= ntiles) break;
-        unsigned e0 = t << p.log_tile;
-        const unsigned e1 = min(e0 + tw, T);
-        unsigned o = (unsigned)ldcg(mark + t);
-        while (e0 < e1) {
-            // One frontier entry per lane: edge range [base, end) and snapshot distance.
-            const unsigned j = o + (unsigned)lane;
-            unsigned base = 0x7fffffffu, endv = 0xffffffffu;
-            int rs = 0, du = 0;
-            if (j < F) {
-                const int2 qe = ldcg(q + j);
-                base = (unsigned)qe.y;
-                rs = __ldg(p.row + qe.x);
-                endv = base + (unsigned)(__ldg(p.row + qe.x + 1) - rs);
-                du = ldcg(p.dist + qe.x);
+__device__ __forceinline__ void sssp_expand(const SsspParams& p, int buf, unsigned F, unsigned T, int tag_next,
+                                            int thresh, int fb, int epoch, const FrontierOut& nout) {
+    constexpr int U = kSsspUnroll;
+    walk_frontier_edges<U>(
+        p.q[buf], p.mark[buf], p.row, F, T, p.log_tile, p.mark_cap, (unsigned)p.V, p.E, &p.ctl->flags,
+        [&](int v, unsigned) { return ldcg(p.dist + v); },  // snapshot distance of the owner
+        [&](const bool* ok, const unsigned* idx, const int* du) {
+            int c[U], nd[U], cur[U];
+            // U independent edge loads, then U independent distance reads.
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const int2 ew = ok[u] ? __ldg(p.adj + idx[u]) : make_int2(0, 0);
+                c[u] = ew.x;
+                nd[u] = du[u] + ew.y;
             }
-            const unsigned seg_end = min(e1, (unsigned)__shfl_sync(kFull, endv, 31));
-            if (seg_end <= e0 || o >= F) {  // the tile marker did not lead to its owner
-                if (lane == 0) atomicOr(&p.ctl->flags, C2G_FLAG_BOUNDS);
-                break;
-            }
-            for (unsigned eb = e0; eb < seg_end; eb += 32) {
-                const unsigned e = eb + (unsigned)lane;
-                const int k = owner_lane(base, e);
-                const int srs = __shfl_sync(kFull, rs, k);
-                const unsigned sb = (unsigned)__shfl_sync(kFull, (int)base, k);
-                const int sdu = __shfl_sync(kFull, du, k);
-                bool near = false, farp = false;
-                int c = 0, nd = 0;
-                const unsigned idx = (unsigned)srs + (e - sb);
-                const bool ok = e < seg_end && sb <= e && idx < p.E;
-                if (e < seg_end && !ok) atomicOr(&p.ctl->flags, C2G_FLAG_BOUNDS);
-                if (ok) {
-                    const int2 ew = __ldg(p.adj + idx);
-                    c = ew.x;
-                    nd = sdu + ew.y;
-                    if (nd < ldcg(p.dist + c)) {
-                        const int old = atomicMin(p.dist + c, nd);
-                        if (nd < old) {
-                            if (!kDelta || nd < thresh)
-                                near = true;
-                            else
-                                farp = true;
-                        }
+#pragma unroll
+            for (int u = 0; u < U; ++u) cur[u] = ok[u] ? ldcg(p.dist + c[u]) : INT_MIN;
+            bool near[U], farp[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                near[u] = farp[u] = false;
+                if (nd[u] < cur[u]) {  // an L2 read guards the atomic
+                    const int old = atomicMin(p.dist + c[u], nd[u]);
+                    if (nd[u] < old) {
+                        if (!kDelta || nd[u] < thresh)
+                            near[u] = true;
+                        else
+                            farp[u] = true;
                     }
                 }
-                int deg = 0;
-                if (near) near = claim_near(p, c, tag_next, deg);
-                frontier_push(nout, near, c, deg, 0.f);
-                if (kDelta) far_push(p, fb, farp, c, nd, epoch, true);
             }
-            e0 = seg_end;
-            o += 32;
-        }
-    }
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                int deg = 0;
+                const bool want = near[u] && claim_near(p, c[u], tag_next, deg);
+                frontier_push(nout, want, c[u], deg, 0.f);
+                if (kDelta) far_push(p, fb, farp[u], c[u], nd[u], epoch, true);
+            }
+        });
 }
 
 template <bool kDelta>
@@ -268,7 +237,7 @@ __global__ void __launch_bounds__(512, 2) sssp_persistent(const SsspParams p) {
             ctl->relaxed += T;
         }
         const FrontierOut nout = sssp_out(p, (cur + 1) & 1, (cur + 1) % 3);
-        sssp_expand<kDelta>(p, cur & 1, cur % 3, F, T, sbase + cur + 1, thresh, fb, epoch, nout);
+        sssp_expand<kDelta>(p, cur & 1, F, T, sbase + cur + 1, thresh, fb, epoch, nout);
         if (!grid_sync(bar, flags, p.barrier_ns)) return;
         ++cur;
     }

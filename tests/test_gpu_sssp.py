@@ -217,3 +217,28 @@ def test_cli_sssp_base_output(gpu_available, gdirs):
     vals = [int(l.split("\t")[1]) for l in lines[:10]]
     assert vals == g["dist_origin"][0][:10].tolist()
     assert "gpu runtime:" in r.stdout
+
+
+def test_sssp_stress_mixed_configs(gpu_available, tmp_path_factory):
+    """Many queries on one handle with weights in [1,1000] (the scale-22 distribution),
+    cycling delta and tile sizes, each against Dijkstra: catches rare ordering races."""
+    import c2g
+    import oracle
+
+    d = str(tmp_path_factory.mktemp("stress18"))
+    c2g.rmat_write(d, 18, 16, 2, 1, 1000)
+    o = oracle.load_dataset(d, "origin")
+    deg = np.diff(o["vlist"])
+    rng = np.random.default_rng(11)
+    srcs = [int(np.argmax(deg))] + [int(x) for x in rng.choice(np.flatnonzero(deg > 0), 7, replace=False)]
+    refs = {s: oracle.dijkstra(o["vlist"], o["elist"], o["wlist"], [s], [0]) for s in srcs}
+    cfgs = [(0, 256), (25, 64), (25, 256), (100, 128), (400, 256), (1600, 1024), (0, 64), (50, 512)]
+    with c2g.Graph.load(d, "origin") as gr:
+        for rep in range(3):
+            for i, (delta, tile) in enumerate(cfgs):
+                gr.sssp_config(delta=delta, tile=tile)
+                for s in srcs[(i + rep) % 4::2]:
+                    dist, st = gr.sssp(s)
+                    bad = int((dist != refs[s]).sum())
+                    assert bad == 0, (rep, delta, tile, s, bad, int((dist > refs[s]).sum()))
+                    assert st.status_flags == 0
