@@ -74,7 +74,9 @@ static int graph_fill(c2g_graph* g, const std::vector<int32_t>& vlist, const int
     g->E = E;
     g->h_row = vlist;
     C2G_CUDA(cudaMalloc(&g->row, sizeof(int32_t) * vlist.size()));
-    C2G_CUDA(cudaMemcpy(g->row, vlist.data(), sizeof(int32_t) * vlist.size(), cudaMemcpyHostToDevice));
+    C2G_CUDA(cudaMemcpyAsync(g->row, vlist.data(), sizeof(int32_t) * vlist.size(), cudaMemcpyHostToDevice,
+                             g->stream));
+    C2G_CUDA(cudaStreamSynchronize(g->stream));
     int rc;
     if (wlist && (rc = build_adj(g, elist, wlist, &g->adj_w))) return rc;
     if (flist && (rc = build_adj(g, elist, reinterpret_cast<const int32_t*>(flist), &g->adj_f))) return rc;
@@ -100,13 +102,14 @@ static int records_fill(c2g_graph* g, int32_t R, const int32_t* hv, const int32_
     g->hw_float = hw_float;
     g->h_hv.assign(hv, hv + R + 1);
     C2G_CUDA(cudaMalloc(&g->hv, sizeof(int32_t) * (R + 1)));
-    C2G_CUDA(cudaMemcpy(g->hv, hv, sizeof(int32_t) * (R + 1), cudaMemcpyHostToDevice));
+    C2G_CUDA(cudaMemcpyAsync(g->hv, hv, sizeof(int32_t) * (R + 1), cudaMemcpyHostToDevice, g->stream));
     C2G_CUDA(cudaMalloc(&g->he, sizeof(int32_t) * (H ? H : 1)));
     C2G_CUDA(cudaMalloc(&g->hw, sizeof(int32_t) * (H ? H : 1)));
     if (H) {
-        C2G_CUDA(cudaMemcpy(g->he, he, sizeof(int32_t) * H, cudaMemcpyHostToDevice));
-        C2G_CUDA(cudaMemcpy(g->hw, hw, sizeof(int32_t) * H, cudaMemcpyHostToDevice));
+        C2G_CUDA(cudaMemcpyAsync(g->he, he, sizeof(int32_t) * H, cudaMemcpyHostToDevice, g->stream));
+        C2G_CUDA(cudaMemcpyAsync(g->hw, hw, sizeof(int32_t) * H, cudaMemcpyHostToDevice, g->stream));
     }
+    C2G_CUDA(cudaStreamSynchronize(g->stream));
     g->h_rec_of_vertex.clear();
     if (rec_vertex) {
         g->h_rec_of_vertex.assign((size_t)g->V, -1);
@@ -125,9 +128,10 @@ static int stats_fill(c2g_graph* g, const TraversalCtl* dctl, int32_t source, fl
     C2G_CUDA(cudaStreamSynchronize(g->stream));
     if (ctl.flags & (C2G_FLAG_BARRIER_TIMEOUT | C2G_FLAG_QUEUE_OVERFLOW | C2G_FLAG_BOUNDS)) {
         // The launch ended early: force the stamp arrays to be reset by the next launch.
-        StampState reset{1 << 30, 1 << 30, {0, 0}};
+        static const StampState reset{1 << 30, 1 << 30, {0, 0}};
         StampState* dst = ppr ? g->ppr.st : g->sssp.st;
-        cudaMemcpy(dst, &reset, sizeof(reset), cudaMemcpyHostToDevice);
+        cudaMemcpyAsync(dst, &reset, sizeof(reset), cudaMemcpyHostToDevice, g->stream);
+        cudaStreamSynchronize(g->stream);
     }
     if (st) {
         std::memset(st, 0, sizeof(*st));
@@ -322,6 +326,9 @@ int c2g_graph_set_stream(c2g_graph* g, void* stream) {
     if (!g) return fail(C2G_ERR_ARG, "graph is NULL");
     std::lock_guard<std::mutex> lk(g->mu);
     DeviceScope ds(g->device);
+    // Work already queued on the old stream (workspace initialisation included) must
+    // finish before the new stream takes over.
+    if (g->stream) C2G_CUDA(cudaStreamSynchronize(g->stream));
     if (g->own_stream && g->stream) cudaStreamDestroy(g->stream);
     g->own_stream = false;
     g->stream = (cudaStream_t)stream;

@@ -176,6 +176,123 @@ __device__ __forceinline__ int owner_lane(unsigned base, unsigned e) {
     return k;
 }
 
+// Per-warp staging of appends in shared memory.  A warp collects appended entries in a
+// 128-entry stage (warp-aggregated with ballot/popc, no atomics) and writes them to the
+// global queue with ONE global atomic per flush.  A single global counter hit by every
+// warp on every push serialises at its L2 slice; staging cuts those atomics by up to
+// 128x.  The stage count n is warp-uniform.
+constexpr int kStageCap = 128;
+
+struct WarpStage {
+    int* v;    // shared [kStageCap] vertex
+    int* d;    // shared [kStageCap] out-degree (frontier stages only)
+    float* x;  // shared [kStageCap] value, or nullptr
+    int n;
+};
+
+// Write the stage to `out`: entries keep their stage order, so slots and edge bases
+// stay monotone, which the owner search of the next round relies on.
+__device__ __forceinline__ void stage_flush(WarpStage& st, const FrontierOut& out) {
+    const int n = st.n;
+    if (n == 0) return;
+    __syncwarp();
+    const int lane = threadIdx.x & 31;
+    int dv[4], dsum = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const int i = 4 * lane + k;
+        dv[k] = i < n ? st.d[i] : 0;
+        dsum += dv[k];
+    }
+    int incl = dsum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(kFull, incl, o);
+        if (lane >= o) incl += t;
+    }
+    const unsigned total = (unsigned)__shfl_sync(kFull, incl, 31);
+    unsigned long long old = 0;
+    if (lane == 0) old = atomicAdd(out.ctr, ((unsigned long long)n << 32) | (unsigned long long)total);
+    old = __shfl_sync(kFull, old, 0);
+    const unsigned slot0 = (unsigned)(old >> 32);
+    unsigned base = (unsigned)old + (unsigned)(incl - dsum);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const int i = 4 * lane + k;
+        if (i < n) {
+            const unsigned slot = slot0 + (unsigned)i;
+            if (slot < out.cap) {
+                out.q[slot] = make_int2(st.v[i], (int)base);
+                if (out.val) out.val[slot] = st.x[i];
+                const unsigned tile = 1u << out.log_tile;
+                const unsigned t0 = (base + tile - 1) >> out.log_tile;
+                const unsigned t1 = (base + (unsigned)dv[k] - 1) >> out.log_tile;
+                for (unsigned t = t0; t <= t1 && t < out.mark_cap; ++t) out.mark[t] = (int)slot;
+            } else {
+                atomicOr(out.flags, C2G_FLAG_QUEUE_OVERFLOW);
+            }
+            base += (unsigned)dv[k];
+        }
+    }
+    st.n = 0;
+    __syncwarp();
+}
+
+// Warp-collective: lanes with `want` stage (v, deg, x); deg must be > 0.
+__device__ __forceinline__ void stage_push(WarpStage& st, const FrontierOut& out, bool want, int v, int deg,
+                                           float x) {
+    const unsigned m = __ballot_sync(kFull, want);
+    if (m == 0) return;
+    const int cnt = __popc(m);
+    if (st.n + cnt > kStageCap) stage_flush(st, out);
+    const int lane = threadIdx.x & 31;
+    if (want) {
+        const int i = st.n + __popc(m & ((1u << lane) - 1u));
+        st.v[i] = v;
+        st.d[i] = deg;
+        if (st.x) st.x[i] = x;
+    }
+    st.n += cnt;
+}
+
+// Stage of a plain id list (count-only counter).
+__device__ __forceinline__ void list_stage_flush(WarpStage& st, int* list, unsigned* ctr, unsigned cap, int* flags) {
+    const int n = st.n;
+    if (n == 0) return;
+    __syncwarp();
+    const int lane = threadIdx.x & 31;
+    unsigned old = 0;
+    if (lane == 0) old = atomicAdd(ctr, (unsigned)n);
+    old = __shfl_sync(kFull, old, 0);
+    for (int i = lane; i < n; i += 32) {
+        if (old + (unsigned)i < cap)
+            list[old + (unsigned)i] = st.v[i];
+        else
+            atomicOr(flags, C2G_FLAG_QUEUE_OVERFLOW);
+    }
+    st.n = 0;
+    __syncwarp();
+}
+
+__device__ __forceinline__ void list_stage_push(WarpStage& st, int* list, unsigned* ctr, unsigned cap, int* flags,
+                                                bool want, int v) {
+    const unsigned m = __ballot_sync(kFull, want);
+    if (m == 0) return;
+    const int cnt = __popc(m);
+    if (st.n + cnt > kStageCap) list_stage_flush(st, list, ctr, cap, flags);
+    const int lane = threadIdx.x & 31;
+    if (want) st.v[st.n + __popc(m & ((1u << lane) - 1u))] = v;
+    st.n += cnt;
+}
+
+// Shared-memory backing for two stages per warp (512-thread blocks: 16 warps).
+struct StageSmem {
+    int v0[16][kStageCap];
+    int d0[16][kStageCap];
+    float x0[16][kStageCap];
+    int v1[16][kStageCap];
+};
+
 // Warp-cooperative walk over the edges of a frontier, in tiles of 2^log_tile edges
 // assigned to warps round-robin (tile t goes to warp t mod nwarps, no shared counter).
 // For each group of 32*U edges every lane gets U edges (stride 32, so the warp reads

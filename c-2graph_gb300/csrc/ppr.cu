@@ -69,7 +69,8 @@ constexpr int kPprUnroll = 4;  // edges in flight per lane
 // message is positive), so no separate touched flag is needed.  Messages below
 // FLT_MIN are dropped: they cannot change any residual in float, and a vertex outside
 // the frontier never holds a residual above rmax, so a zero message cannot activate it.
-__device__ __forceinline__ void ppr_push(const PprParams& p, int buf, int slot, unsigned F, unsigned T) {
+__device__ __forceinline__ void ppr_push(const PprParams& p, int buf, int slot, unsigned F, unsigned T,
+                                         WarpStage& tst) {
     constexpr int U = kPprUnroll;
     const float one_m_a = 1.0f - p.alpha;
     const float* qv = p.qval[buf];
@@ -91,8 +92,10 @@ __device__ __forceinline__ void ppr_push(const PprParams& p, int buf, int slot, 
             for (int u = 0; u < U; ++u) old[u] = (ok[u] && m[u] >= 1.17549435e-38f) ? atomicAdd(p.msg + c[u], m[u]) : 1.0f;
 #pragma unroll
             for (int u = 0; u < U; ++u)
-                list_push(p.touched, &p.ctl->listctr[slot], (unsigned)p.V, &p.ctl->flags, old[u] == 0.0f, c[u]);
+                list_stage_push(tst, p.touched, &p.ctl->listctr[slot], (unsigned)p.V, &p.ctl->flags,
+                                old[u] == 0.0f, c[u]);
         });
+    list_stage_flush(tst, p.touched, &p.ctl->listctr[slot], (unsigned)p.V, &p.ctl->flags);
 }
 
 __global__ void __launch_bounds__(512, 2) ppr_persistent(const PprParams p) {
@@ -105,6 +108,10 @@ __global__ void __launch_bounds__(512, 2) ppr_persistent(const PprParams p) {
     const unsigned gwarp = gtid >> 5, nwarps = nthreads >> 5;
     const unsigned V = (unsigned)p.V;
     const float a = p.alpha, one_m_a = 1.0f - p.alpha;
+    __shared__ StageSmem sm;
+    const int wib = threadIdx.x >> 5;
+    WarpStage fst{sm.v0[wib], sm.d0[wib], sm.x0[wib], 0};
+    WarpStage tst{sm.v1[wib], nullptr, nullptr, 0};
 
     int sbase = p.st->stamp_base;
     const bool reset = sbase > (1 << 29);
@@ -178,9 +185,10 @@ __global__ void __launch_bounds__(512, 2) ppr_persistent(const PprParams p) {
                     else dang = true;
                 }
             }
-            frontier_push(out, want, v, deg, r);
+            stage_push(fst, out, want, v, deg, r);
             list_push(p.dangle, &ctl->dctr[1], (unsigned)p.V, flags, dang, v);
         }
+        stage_flush(fst, out);
     }
     if (!grid_sync(bar, flags, p.barrier_ns)) return;
 
@@ -214,7 +222,7 @@ __global__ void __launch_bounds__(512, 2) ppr_persistent(const PprParams p) {
             ctl->popped += F + D;
             ctl->relaxed += T;
         }
-        ppr_push(p, cur & 1, slot, F, T);
+        ppr_push(p, cur & 1, slot, F, T, tst);
         if (!grid_sync(bar, flags, p.barrier_ns)) return;
 
         // Phase B: apply messages and activate (src/ppr/purn/Main.cu:383-391).
@@ -240,9 +248,10 @@ __global__ void __launch_bounds__(512, 2) ppr_persistent(const PprParams p) {
                     p.res[v] = r;
                 }
             }
-            frontier_push(out, want, v, deg, r);
+            stage_push(fst, out, want, v, deg, r);
             list_push(p.dangle, &ctl->dctr[nslot], (unsigned)p.V, flags, dang, v);
         }
+        stage_flush(fst, out);
         if (!grid_sync(bar, flags, p.barrier_ns)) return;
         ++cur;
     }
@@ -297,8 +306,8 @@ static int ppr_alloc(c2g_graph* g) {
     }
     C2G_CUDA(cudaMalloc(&w.ctl, sizeof(TraversalCtl)));
     C2G_CUDA(cudaMalloc(&w.st, sizeof(StampState)));
-    C2G_CUDA(cudaMemset(w.stamp, 0xff, sizeof(int) * nv));
-    C2G_CUDA(cudaMemset(w.st, 0, sizeof(StampState)));
+    C2G_CUDA(cudaMemsetAsync(w.stamp, 0xff, sizeof(int) * nv, g->stream));
+    C2G_CUDA(cudaMemsetAsync(w.st, 0, sizeof(StampState), g->stream));
     w.mark_cap = mark_cap;
     w.log_tile = log_tile;
     return C2G_OK;

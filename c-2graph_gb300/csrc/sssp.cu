@@ -66,26 +66,39 @@ __device__ __forceinline__ bool claim_near(const SsspParams& p, int c, int tag, 
     return deg > 0;
 }
 
-// Warp-collective append to far pile fb, keeping the pile's minimum pushed distance.
-__device__ __forceinline__ void far_push(const SsspParams& p, int fb, bool want, int c, int d, int epoch,
-                                         bool dedup) {
+// Far pile stage of one warp: staged ids plus the minimum distance staged so far.
+struct FarStage {
+    WarpStage st;
+    int fmin;
+};
+
+// Warp-collective: stage lanes with `want` for far pile fb (deduplicated per epoch when
+// `dedup`), tracking the minimum pushed distance.
+__device__ __forceinline__ void far_stage(const SsspParams& p, FarStage& fs, int fb, bool want, int c, int d,
+                                          int epoch, bool dedup) {
     if (want && dedup) {
         if (ldcg(p.farstamp + c) == epoch || atomicExch(p.farstamp + c, epoch) == epoch) want = false;
     }
-    const unsigned m = __ballot_sync(kFull, want);
-    if (m == 0) return;
+    if (__ballot_sync(kFull, want) == 0) return;
     int mn = want ? d : INT_MAX;
 #pragma unroll
     for (int o = 16; o >= 1; o >>= 1) mn = min(mn, __shfl_xor_sync(kFull, mn, o));
-    if ((threadIdx.x & 31) == __ffs(m) - 1) atomicMin(&p.ctl->farmin[fb], mn);
-    list_push(p.far[fb], &p.ctl->farctr[fb], (unsigned)p.V, &p.ctl->flags, want, c);
+    fs.fmin = min(fs.fmin, mn);
+    list_stage_push(fs.st, p.far[fb], &p.ctl->farctr[fb], (unsigned)p.V, &p.ctl->flags, want, c);
+}
+
+__device__ __forceinline__ void far_flush(const SsspParams& p, FarStage& fs, int fb) {
+    list_stage_flush(fs.st, p.far[fb], &p.ctl->farctr[fb], (unsigned)p.V, &p.ctl->flags);
+    if ((threadIdx.x & 31) == 0 && fs.fmin != INT_MAX) atomicMin(&p.ctl->farmin[fb], fs.fmin);
+    fs.fmin = INT_MAX;
 }
 
 constexpr int kSsspUnroll = 4;  // edges in flight per lane
 
 template <bool kDelta>
 __device__ __forceinline__ void sssp_expand(const SsspParams& p, int buf, unsigned F, unsigned T, int tag_next,
-                                            int thresh, int fb, int epoch, const FrontierOut& nout) {
+                                            int thresh, int fb, int epoch, const FrontierOut& nout,
+                                            WarpStage& fst, FarStage& far) {
     constexpr int U = kSsspUnroll;
     walk_frontier_edges<U>(
         p.q[buf], p.mark[buf], p.row, F, T, p.log_tile, p.mark_cap, (unsigned)p.V, p.E, &p.ctl->flags,
@@ -119,10 +132,12 @@ __device__ __forceinline__ void sssp_expand(const SsspParams& p, int buf, unsign
             for (int u = 0; u < U; ++u) {
                 int deg = 0;
                 const bool want = near[u] && claim_near(p, c[u], tag_next, deg);
-                frontier_push(nout, want, c[u], deg, 0.f);
-                if (kDelta) far_push(p, fb, farp[u], c[u], nd[u], epoch, true);
+                stage_push(fst, nout, want, c[u], deg, 0.f);
+                if (kDelta) far_stage(p, far, fb, farp[u], c[u], nd[u], epoch, true);
             }
         });
+    stage_flush(fst, nout);
+    if (kDelta) far_flush(p, far, fb);
 }
 
 template <bool kDelta>
@@ -135,6 +150,10 @@ __global__ void __launch_bounds__(512, 2) sssp_persistent(const SsspParams p) {
     const unsigned nthreads = gridDim.x * blockDim.x;
     const unsigned gwarp = gtid >> 5, nwarps = nthreads >> 5;
     const unsigned V = (unsigned)p.V;
+    __shared__ StageSmem sm;
+    const int wib = threadIdx.x >> 5;
+    WarpStage fst{sm.v0[wib], sm.d0[wib], nullptr, 0};
+    FarStage far{WarpStage{sm.v1[wib], nullptr, nullptr, 0}, INT_MAX};
 
     int sbase = p.st->stamp_base;
     int ebase = p.st->epoch_base;
@@ -173,8 +192,9 @@ __global__ void __launch_bounds__(512, 2) sssp_persistent(const SsspParams p) {
                 v = (i < (unsigned)p.n_seeds) ? p.seed_v[i] : p.source;
                 want = claim_near(p, v, tag, deg);
             }
-            frontier_push(out, want, v, deg, 0.f);
+            stage_push(fst, out, want, v, deg, 0.f);
         }
+        stage_flush(fst, out);
     }
     if (!grid_sync(bar, flags, p.barrier_ns)) return;
 
@@ -217,9 +237,11 @@ __global__ void __launch_bounds__(512, 2) sssp_persistent(const SsspParams p) {
                         }
                     }
                 }
-                frontier_push(out, near, v, deg, 0.f);
-                far_push(p, fdst, keep, v, d, epoch + 1, false);
+                stage_push(fst, out, near, v, deg, 0.f);
+                far_stage(p, far, fdst, keep, v, d, epoch + 1, false);
             }
+            stage_flush(fst, out);
+            far_flush(p, far, fdst);
             thresh = (int)nt;
             fb = fdst;
             ++epoch;
@@ -237,7 +259,7 @@ __global__ void __launch_bounds__(512, 2) sssp_persistent(const SsspParams p) {
             ctl->relaxed += T;
         }
         const FrontierOut nout = sssp_out(p, (cur + 1) & 1, (cur + 1) % 3);
-        sssp_expand<kDelta>(p, cur & 1, F, T, sbase + cur + 1, thresh, fb, epoch, nout);
+        sssp_expand<kDelta>(p, cur & 1, F, T, sbase + cur + 1, thresh, fb, epoch, nout, fst, far);
         if (!grid_sync(bar, flags, p.barrier_ns)) return;
         ++cur;
     }
@@ -293,9 +315,9 @@ static int sssp_alloc(c2g_graph* g) {
     C2G_CUDA(cudaMalloc(&w.far, sizeof(int) * nv * 3));
     C2G_CUDA(cudaMalloc(&w.ctl, sizeof(TraversalCtl)));
     C2G_CUDA(cudaMalloc(&w.st, sizeof(StampState)));
-    C2G_CUDA(cudaMemset(w.stamp, 0xff, sizeof(int) * nv));
-    C2G_CUDA(cudaMemset(w.farstamp, 0xff, sizeof(int) * nv));
-    C2G_CUDA(cudaMemset(w.st, 0, sizeof(StampState)));
+    C2G_CUDA(cudaMemsetAsync(w.stamp, 0xff, sizeof(int) * nv, g->stream));
+    C2G_CUDA(cudaMemsetAsync(w.farstamp, 0xff, sizeof(int) * nv, g->stream));
+    C2G_CUDA(cudaMemsetAsync(w.st, 0, sizeof(StampState), g->stream));
     w.mark_cap = mark_cap;
     w.log_tile = log_tile;
     return C2G_OK;
