@@ -78,6 +78,8 @@ SIGNATURES = {
     "c2g_sssp": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int, ctypes.c_int, _P, ctypes.c_int,
                                 ctypes.POINTER(Stats)]),
     "c2g_sssp_set_config": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32]),
+    "c2g_sssp_batch": (ctypes.c_int, [_P, ctypes.c_int32, _P, ctypes.c_int, ctypes.c_int, _P, ctypes.c_int,
+                                      ctypes.c_int, ctypes.POINTER(Stats)]),
     "c2g_ppr": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.POINTER(PprParams), _P, _P, ctypes.c_int,
                                ctypes.POINTER(Stats)]),
     "c2g_ppr_default_params": (ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(PprParams)]),
@@ -214,6 +216,21 @@ class Graph:
             return None, st
         dist = out if out is not None else np.empty(self.V, dtype=np.int32)
         _check(lib().c2g_sssp(self._h, source, int(seeds), mode, _ptr(dist), 0, ctypes.byref(st)))
+        return dist, st
+
+    def sssp_batch(self, sources, seeds=False, mode=SEEDS_COMPAT, out=None, out_ptr=None, vertex_major=False):
+        """Batched SSSP: (n, V) int32 distances (query-major), or into device memory."""
+        src = np.ascontiguousarray(sources, dtype=np.int32)
+        st = Stats()
+        layout = 1 if vertex_major else 0
+        if out_ptr is not None:
+            _check(lib().c2g_sssp_batch(self._h, len(src), _ptr(src), int(seeds), mode, ctypes.c_void_p(out_ptr), 1,
+                                        layout, ctypes.byref(st)))
+            return None, st
+        dist = out if out is not None else np.empty((len(src), self.V) if not vertex_major else (self.V, len(src)),
+                                                    dtype=np.int32)
+        _check(lib().c2g_sssp_batch(self._h, len(src), _ptr(src), int(seeds), mode, _ptr(dist), 0, layout,
+                                    ctypes.byref(st)))
         return dist, st
 
     def ppr_params(self, adsorption=False, **kw):

@@ -23,6 +23,7 @@ static void graph_release(c2g_graph* g) {
     cudaSetDevice(g->device);
     sssp_free(g);
     ppr_free(g);
+    batch_free(g);
     void* ptrs[] = {g->row, g->adj_w, g->adj_f, g->hv, g->he, g->hw, g->rec_of_vertex};
     for (void* p : ptrs)
         if (p) cudaFree(p);
@@ -101,6 +102,8 @@ static int records_fill(c2g_graph* g, int32_t R, const int32_t* hv, const int32_
     g->H = H;
     g->hw_float = hw_float;
     g->h_hv.assign(hv, hv + R + 1);
+    g->h_he.assign(he, he + H);
+    g->h_hw.assign(reinterpret_cast<const int32_t*>(hw), reinterpret_cast<const int32_t*>(hw) + H);
     C2G_CUDA(cudaMalloc(&g->hv, sizeof(int32_t) * (R + 1)));
     C2G_CUDA(cudaMemcpyAsync(g->hv, hv, sizeof(int32_t) * (R + 1), cudaMemcpyHostToDevice, g->stream));
     C2G_CUDA(cudaMalloc(&g->he, sizeof(int32_t) * (H ? H : 1)));
@@ -381,6 +384,60 @@ int c2g_sssp(c2g_graph* g, int32_t source, int use_seeds, int seed_mode, int32_t
     if (!dist_on_device)
         C2G_CUDA(cudaMemcpyAsync(dist, g->sssp.dist, sizeof(int32_t) * (size_t)g->V, cudaMemcpyDeviceToHost, g->stream));
     return stats_fill(g, g->sssp.ctl, source, ms, false, stats);
+}
+
+int c2g_sssp_batch(c2g_graph* g, int32_t n, const int32_t* sources, int use_seeds, int seed_mode, int32_t* dist,
+                   int dist_on_device, int layout, c2g_stats* stats) {
+    if (!g || !sources || !dist) return fail(C2G_ERR_ARG, "NULL argument");
+    if (n < 1) return fail(C2G_ERR_ARG, "batch needs at least one source");
+    if (layout != C2G_LAYOUT_QUERY_MAJOR && layout != C2G_LAYOUT_VERTEX_MAJOR)
+        return fail(C2G_ERR_ARG, "bad layout %d", layout);
+    for (int32_t i = 0; i < n; ++i)
+        if (sources[i] < 0 || sources[i] >= g->V)
+            return fail(C2G_ERR_RANGE, "source %d (entry %d) out of range [0,%d)", sources[i], i, g->V);
+    std::lock_guard<std::mutex> lk(g->mu);
+    DeviceScope ds(g->device);
+    std::vector<int32_t> off, sv, sw;
+    if (use_seeds) {
+        off.reserve((size_t)n + 1);
+        off.push_back(0);
+        for (int32_t i = 0; i < n; ++i) {
+            int32_t first = 0, cnt = 0;
+            int rc = record_range(g, sources[i], seed_mode, &first, &cnt);
+            if (rc) return rc;
+            sv.insert(sv.end(), g->h_he.begin() + first, g->h_he.begin() + first + cnt);
+            sw.insert(sw.end(), g->h_hw.begin() + first, g->h_hw.begin() + first + cnt);
+            off.push_back((int32_t)sv.size());
+        }
+    }
+    if (dist_on_device && !is_device_ptr(dist)) return fail(C2G_ERR_ARG, "dist is not a device pointer");
+    float ms = 0.f;
+    long long counters[2] = {0, 0};
+    TraversalCtl ctl;
+    int rc = sssp_batch_launch(g, n, sources, use_seeds ? &off : nullptr, use_seeds ? &sv : nullptr,
+                               use_seeds ? &sw : nullptr, dist, dist_on_device, layout == C2G_LAYOUT_QUERY_MAJOR, &ms,
+                               counters, &ctl);
+    if (rc) return rc;
+    if (stats) {
+        std::memset(stats, 0, sizeof(*stats));
+        stats->source = sources[0];
+        stats->iterations = ctl.iterations;
+        stats->vertices_popped = ctl.popped;  // (vertex, 32-query word) entries
+        stats->edges_relaxed = counters[0];   // (query, edge) relaxations
+        stats->touched = ctl.relaxed;         // edge x word steps
+        stats->n_seeds = (int64_t)sv.size();
+        stats->device_ms = ms;
+        stats->status_flags = ctl.flags;
+        // Byte model: 40 per entry (id + bounds + 32 B mask word/row share) + 8 per
+        // edge-word step + 8 per (query, edge) relaxation (4 B read + 4 B atomic), plus
+        // the 4 B x V x Q initialisation.
+        stats->alg_bytes = 40.0 * (double)ctl.popped + 8.0 * (double)ctl.relaxed + 8.0 * (double)counters[0] +
+                           4.0 * (double)g->V * (double)((n + 31) / 32 * 32);
+    }
+    if (ctl.flags & C2G_FLAG_BARRIER_TIMEOUT) return fail(C2G_ERR_TIMEOUT, "grid barrier wait ran out");
+    if (ctl.flags & C2G_FLAG_QUEUE_OVERFLOW) return fail(C2G_ERR_OVERFLOW, "frontier queue overflow");
+    if (ctl.flags & C2G_FLAG_BOUNDS) return fail(C2G_ERR_OVERFLOW, "device index check failed");
+    return C2G_OK;
 }
 
 int c2g_ppr_default_params(const c2g_graph* g, int adsorption, c2g_ppr_params* out) {

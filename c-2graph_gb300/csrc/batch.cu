@@ -1,0 +1,425 @@
+// Batched multi-query SSSP for sm_103a: up to thousands of sources in ONE persistent
+// cooperative launch, with per-query bitmask frontiers.
+//
+// The reference runs one query per launch (src/sssp/purn/Main.cu:67-99) and, in its
+// PM mode, two queries on two streams (src/sssp/purn-perk/Main.cu:51-53,107,164).  Here
+// Q queries (padded to a multiple of 32) share every pass over the graph:
+//   * state is vertex-major: dist[v][Q] int32, so the 32 queries of one "word" w of a
+//     vertex occupy one 128-byte line;
+//   * a frontier entry is a (vertex, word) pair; its 32-bit mask says which of the
+//     word's queries improved that vertex in the previous round;
+//   * expansion: a warp loads 32 edges (one per lane) of the frontier's edge range, then
+//     walks them; for each edge every lane relaxes one query of the word with one
+//     coalesced 128-byte read of the target's row, so an edge read from HBM serves all
+//     active queries of its word;
+//   * the first improvement of (target, word) in a round sets its mask bits with
+//     atomicOr and the setter that saw an empty mask appends the pair (warp-staged);
+//   * a round is two phases: gather (copy and clear each entry's mask) and expand.
+// Results are the same int32 fixed points as one c2g_sssp call per source.
+#include <climits>
+#include <vector>
+
+#include "device_common.cuh"
+#include "internal.h"
+
+namespace c2g {
+
+struct BatchParams {
+    const int* row;
+    const int2* adj;
+    unsigned E;
+    int V;
+    int logW;  // words per vertex = 1 << logW
+    int Q;     // padded query count = 32 << logW
+    int nq;    // real queries
+    int* dist;          // [V][Q]
+    unsigned* mask;     // [V][W] next-round masks
+    int2* q[2];         // entries (v*W + w, edge base)
+    unsigned* qmask[2]; // gathered masks per entry
+    int* mark[2];
+    TraversalCtl* ctl;
+    const int* sources;   // [nq]
+    const int* seed_off;  // [nq+1] offsets into seed_v/seed_w (or nullptr)
+    const int* seed_v;
+    const int* seed_w;
+    unsigned qcap;
+    unsigned mark_cap;
+    int max_iter;
+    unsigned long long barrier_ns;
+    long long* counters;  // [2]: relaxations (query, edge), edge-word steps
+};
+
+constexpr int kBatchTileLog = 5;  // 32 edge-word steps per warp tile
+
+__device__ __forceinline__ FrontierOut batch_out(const BatchParams& p, int buf, int slot) {
+    FrontierOut o;
+    o.q = p.q[buf];
+    o.val = nullptr;
+    o.mark = p.mark[buf];
+    o.ctr = &p.ctl->qctr[slot];
+    o.cap = p.qcap;
+    o.mark_cap = p.mark_cap;
+    o.log_tile = kBatchTileLog;
+    o.flags = &p.ctl->flags;
+    return o;
+}
+
+// Mark (v, w) improved for the queries in `bits`; returns true for the caller that
+// found the mask empty (it appends the pair to the next frontier).
+__device__ __forceinline__ bool mark_improved(const BatchParams& p, int v, int w, unsigned bits) {
+    return atomicOr(p.mask + (((size_t)v << p.logW) + (unsigned)w), bits) == 0u;
+}
+
+__global__ void __launch_bounds__(512, 2) sssp_batch_persistent(const BatchParams p) {
+    TraversalCtl* ctl = p.ctl;
+    GridBarrier* bar = reinterpret_cast<GridBarrier*>(&ctl->bar_count);
+    int* flags = &ctl->flags;
+    const int lane = threadIdx.x & 31;
+    const unsigned gtid = blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned nthreads = gridDim.x * blockDim.x;
+    const unsigned gwarp = gtid >> 5, nwarps = nthreads >> 5;
+    const int W = 1 << p.logW;
+    __shared__ StageSmem sm;
+    const int wib = threadIdx.x >> 5;
+    WarpStage fst{sm.v0[wib], sm.d0[wib], nullptr, 0};
+
+    // Init: dist = INF (vector stores), masks = 0.
+    {
+        const size_t n4 = ((size_t)p.V * (size_t)p.Q) >> 2;
+        int4* d4 = reinterpret_cast<int4*>(p.dist);
+        const int4 inf4 = make_int4(kInfDist, kInfDist, kInfDist, kInfDist);
+        for (size_t i = gtid; i < n4; i += nthreads) d4[i] = inf4;
+        const size_t nm = (size_t)p.V << p.logW;
+        for (size_t i = gtid; i < nm; i += nthreads) p.mask[i] = 0u;
+    }
+    if (!grid_sync(bar, flags, p.barrier_ns)) return;
+
+    // Sources and their seeds: dist[s][q] = 0, dist[seed][q] = min(w); mark them.
+    for (unsigned qi = gtid; qi < (unsigned)p.nq; qi += nthreads) {
+        const int s = p.sources[qi];
+        atomicMin(p.dist + (size_t)s * p.Q + qi, 0);
+        if (p.seed_off)
+            for (int k = p.seed_off[qi]; k < p.seed_off[qi + 1]; ++k)
+                atomicMin(p.dist + (size_t)p.seed_v[k] * p.Q + qi, p.seed_w[k]);
+    }
+    if (!grid_sync(bar, flags, p.barrier_ns)) return;
+    {
+        // Round-1 frontier: the (source|seed, word) pairs, one warp lane per query.
+        const FrontierOut out = batch_out(p, 1, 1);
+        const unsigned nq32 = ((unsigned)p.nq + 31u) & ~31u;
+        for (unsigned b = gwarp * 32; b < nq32; b += nwarps * 32) {
+            const unsigned qi = b + (unsigned)lane;
+            const int w = (int)(qi >> 5);
+            bool want = false;
+            int v = 0, deg = 0;
+            if (qi < (unsigned)p.nq) {
+                v = p.sources[qi];
+                deg = __ldg(p.row + v + 1) - __ldg(p.row + v);
+                want = deg > 0 && mark_improved(p, v, w, 1u << (qi & 31));
+            }
+            stage_push(fst, out, want, (v << p.logW) + w, deg, 0.f);
+            if (p.seed_off && qi < (unsigned)p.nq) {
+                for (int k = p.seed_off[qi]; k < p.seed_off[qi + 1]; ++k) {
+                    const int sv = p.seed_v[k];
+                    const int sd = __ldg(p.row + sv + 1) - __ldg(p.row + sv);
+                    if (sd > 0 && mark_improved(p, sv, w, 1u << (qi & 31))) {
+                        // Rare path (seeds of the same word may collide): direct append.
+                        const unsigned long long old =
+                            atomicAdd(out.ctr, (1ull << 32) | (unsigned long long)(unsigned)sd);
+                        const unsigned slot = (unsigned)(old >> 32), base = (unsigned)old;
+                        if (slot < out.cap) {
+                            out.q[slot] = make_int2((sv << p.logW) + w, (int)base);
+                            const unsigned t0 = (base + 31u) >> kBatchTileLog, t1 = (base + sd - 1) >> kBatchTileLog;
+                            for (unsigned t = t0; t <= t1 && t < out.mark_cap; ++t) out.mark[t] = (int)slot;
+                        } else {
+                            atomicOr(flags, C2G_FLAG_QUEUE_OVERFLOW);
+                        }
+                    }
+                }
+            }
+        }
+        stage_flush(fst, out);
+    }
+    if (!grid_sync(bar, flags, p.barrier_ns)) return;
+
+    long long relax = 0, steps = 0;
+    int cur = 1, iters = 0;
+    for (;;) {
+        const unsigned long long c = ldcg(&ctl->qctr[cur % 3]);
+        const unsigned F = (unsigned)(c >> 32), T = (unsigned)c;
+        if (F == 0) break;
+        if (++iters > p.max_iter) {
+            if (gtid == 0) atomicOr(flags, C2G_FLAG_ITER_CAP);
+            break;
+        }
+        const int buf = cur & 1;
+        if (F > p.qcap || ((T + 31u) >> kBatchTileLog) > p.mark_cap) {
+            if (gtid == 0) atomicOr(flags, C2G_FLAG_BOUNDS);
+            break;
+        }
+        // Phase 1: gather and clear the masks of this round's entries.
+        for (unsigned j = gtid; j < F; j += nthreads) {
+            const int vw = ldcg(p.q[buf] + j).x;
+            unsigned* mp = p.mask + (unsigned)vw;
+            p.qmask[buf][j] = ldcg(mp);
+            *mp = 0u;
+        }
+        if (gtid == 0) {
+            ctl->qctr[(cur + 2) % 3] = 0ull;
+            ctl->popped += F;
+            ctl->relaxed += T;
+        }
+        if (!grid_sync(bar, flags, p.barrier_ns)) return;
+
+        // Phase 2: expand.
+        const FrontierOut nout = batch_out(p, (cur + 1) & 1, (cur + 1) % 3);
+        const int2* q = p.q[buf];
+        const unsigned* qm = p.qmask[buf];
+        const int* mark = p.mark[buf];
+        const unsigned ntiles = (T + 31u) >> kBatchTileLog;
+        for (unsigned t = gwarp; t < ntiles; t += nwarps) {
+            unsigned e0 = t << kBatchTileLog;
+            const unsigned e1 = min(e0 + 32u, T);
+            unsigned o = (unsigned)ldcg(mark + t);
+            while (e0 < e1) {
+                const unsigned j = o + (unsigned)lane;
+                unsigned base = 0x7fffffffu, endv = 0xffffffffu, msk = 0u;
+                int rs = 0, vw = 0;
+                if (j < F) {
+                    const int2 qe = ldcg(q + j);
+                    vw = qe.x;
+                    base = (unsigned)qe.y;
+                    const int v = vw >> p.logW;
+                    rs = __ldg(p.row + v);
+                    endv = base + (unsigned)(__ldg(p.row + v + 1) - rs);
+                    msk = ldcg(qm + j);
+                }
+                const unsigned seg_end = min(e1, (unsigned)__shfl_sync(kFull, endv, 31));
+                if (seg_end <= e0 || o >= F) {
+                    if (lane == 0) atomicOr(flags, C2G_FLAG_BOUNDS);
+                    break;
+                }
+                // Lane = edge: load this lane's edge and its target's degree.
+                const unsigned e = e0 + (unsigned)lane;
+                const int k = owner_lane(base, e);
+                const unsigned srs = (unsigned)__shfl_sync(kFull, rs, k);
+                const unsigned sb = (unsigned)__shfl_sync(kFull, (int)base, k);
+                const int svw = __shfl_sync(kFull, vw, k);
+                const unsigned smsk = (unsigned)__shfl_sync(kFull, (int)msk, k);
+                const unsigned idx = srs + (e - sb);
+                const bool ok = e < seg_end && sb <= e && idx < p.E;
+                if (e < seg_end && !ok) atomicOr(flags, C2G_FLAG_BOUNDS);
+                int tc = 0, tw = 0, tdeg = 0;
+                if (ok) {
+                    const int2 ew = __ldg(p.adj + idx);
+                    tc = ew.x;
+                    tw = ew.y;
+                    tdeg = __ldg(p.row + tc + 1) - __ldg(p.row + tc);
+                }
+                // Lane = query: walk the segment's edges.
+                const int nseg = (int)(seg_end - e0);
+                bool pend = false;
+                for (int jj = 0; jj < nseg; ++jj) {
+                    const int c = __shfl_sync(kFull, tc, jj);
+                    const int wt = __shfl_sync(kFull, tw, jj);
+                    const int cdeg = __shfl_sync(kFull, tdeg, jj);
+                    const int ovw = __shfl_sync(kFull, svw, jj);
+                    const unsigned om = (unsigned)__shfl_sync(kFull, (int)smsk, jj);
+                    const int u = ovw >> p.logW, w = ovw & (W - 1);
+                    const bool active = (om >> lane) & 1u;
+                    bool imp = false;
+                    if (active) {
+                        // L2-coherent: the owner improved in the previous round.
+                        const int du = ldcg(p.dist + (size_t)u * p.Q + (w << 5) + lane);
+                        const int nd = du + wt;
+                        int* dp = p.dist + (size_t)c * p.Q + (w << 5) + lane;
+                        if (nd < ldcg(dp)) imp = atomicMin(dp, nd) > nd;
+                    }
+                    relax += active;
+                    const unsigned bits = __ballot_sync(kFull, imp);
+                    bool first = false;
+                    if (lane == 0 && bits && cdeg > 0) first = mark_improved(p, c, w, bits);
+                    first = __shfl_sync(kFull, (int)first, 0) != 0;
+                    if (lane == jj) pend = first;
+                }
+                steps += nseg;
+                const int tv = (tc << p.logW) + (svw & (W - 1));
+                stage_push(fst, nout, pend, tv, tdeg, 0.f);
+                e0 = seg_end;
+                o += 32;
+            }
+        }
+        stage_flush(fst, nout);
+        if (!grid_sync(bar, flags, p.barrier_ns)) return;
+        ++cur;
+    }
+    // relax counts lanes; one atomic per warp
+    for (int o = 16; o >= 1; o >>= 1) relax += __shfl_xor_sync(kFull, relax, o);
+    if (lane == 0) {
+        atomicAdd((unsigned long long*)&p.counters[0], (unsigned long long)relax);
+        atomicAdd((unsigned long long*)&p.counters[1], (unsigned long long)steps);
+    }
+    if (gtid == 0) ctl->iterations = iters;
+}
+
+// Copy dist[V][Q] (first nq queries) into the caller's layout.
+__global__ void batch_transpose(const int* __restrict__ dist, int V, int Q, int nq, int* __restrict__ out,
+                                int query_major) {
+    const size_t total = (size_t)V * (size_t)nq;
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += stride) {
+        if (query_major) {
+            const size_t qi = i / (size_t)V, v = i % (size_t)V;  // coalesced writes
+            out[i] = dist[v * Q + qi];
+        } else {
+            const size_t v = i / (size_t)nq, qi = i % (size_t)nq;
+            out[i] = dist[v * Q + qi];
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------------------
+// host side
+
+struct BatchWork {
+    int* dist = nullptr;
+    unsigned* mask = nullptr;
+    int2* q[2] = {nullptr, nullptr};
+    unsigned* qmask[2] = {nullptr, nullptr};
+    int* mark[2] = {nullptr, nullptr};
+    TraversalCtl* ctl = nullptr;
+    long long* counters = nullptr;
+    int* src = nullptr;
+    int* seed_off = nullptr;
+    int* seed_v = nullptr;
+    int* seed_w = nullptr;
+    int* stage = nullptr;  // caller-layout copy for host output
+    size_t seed_cap = 0;
+    int Q = 0;
+    int V = 0;
+};
+
+static void batch_free_work(BatchWork* w) {
+    if (!w) return;
+    void* ptrs[] = {w->dist, w->mask, w->q[0], w->q[1], w->qmask[0], w->qmask[1], w->mark[0], w->mark[1],
+                    w->ctl, w->counters, w->src, w->seed_off, w->seed_v, w->seed_w, w->stage};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    delete w;
+}
+
+void batch_free(c2g_graph* g) {
+    batch_free_work(reinterpret_cast<BatchWork*>(g->batch));
+    g->batch = nullptr;
+}
+
+static int batch_alloc(c2g_graph* g, int Q, size_t n_seeds) {
+    BatchWork* w = reinterpret_cast<BatchWork*>(g->batch);
+    if (w && w->Q >= Q && w->seed_cap >= n_seeds) return C2G_OK;
+    if (w) batch_free(g);
+    w = new BatchWork();
+    g->batch = w;
+    const size_t V = g->V ? (size_t)g->V : 1;
+    const size_t W = (size_t)Q / 32;
+    const size_t qcap = V * W;
+    const size_t mark_cap = (((size_t)g->E * W) >> kBatchTileLog) + 2;
+    C2G_CUDA(cudaMalloc(&w->dist, sizeof(int) * V * (size_t)Q));
+    C2G_CUDA(cudaMalloc(&w->mask, sizeof(unsigned) * qcap));
+    for (int b = 0; b < 2; ++b) {
+        C2G_CUDA(cudaMalloc(&w->q[b], sizeof(int2) * qcap));
+        C2G_CUDA(cudaMalloc(&w->qmask[b], sizeof(unsigned) * qcap));
+        C2G_CUDA(cudaMalloc(&w->mark[b], sizeof(int) * mark_cap));
+    }
+    C2G_CUDA(cudaMalloc(&w->ctl, sizeof(TraversalCtl)));
+    C2G_CUDA(cudaMalloc(&w->counters, sizeof(long long) * 2));
+    C2G_CUDA(cudaMalloc(&w->src, sizeof(int) * (size_t)Q));
+    C2G_CUDA(cudaMalloc(&w->seed_off, sizeof(int) * ((size_t)Q + 1)));
+    w->seed_cap = n_seeds > 0 ? n_seeds : 1;
+    C2G_CUDA(cudaMalloc(&w->seed_v, sizeof(int) * w->seed_cap));
+    C2G_CUDA(cudaMalloc(&w->seed_w, sizeof(int) * w->seed_cap));
+    w->Q = Q;
+    w->V = g->V;
+    return C2G_OK;
+}
+
+int sssp_batch_launch(c2g_graph* g, int32_t nq, const int32_t* sources, const std::vector<int32_t>* seed_off,
+                      const std::vector<int32_t>* seed_v, const std::vector<int32_t>* seed_w, int32_t* out,
+                      int out_on_device, int query_major, float* ms, long long* counters, TraversalCtl* ctl_out) {
+    if (!g->adj_w) return fail(C2G_ERR_UNSUPPORTED, "graph has no int32 weights (wlist)");
+    int Q = 32, logW = 0;
+    while (Q < nq) {
+        Q <<= 1;
+        ++logW;
+    }
+    if ((size_t)g->V * (size_t)(Q / 32) >= (size_t(1) << 31) || (size_t)g->E * (size_t)(Q / 32) >= (size_t(1) << 32))
+        return fail(C2G_ERR_RANGE, "batch of %d queries too large for this graph", nq);
+    int rc;
+    const size_t ns = seed_v ? seed_v->size() : 0;
+    if ((rc = batch_alloc(g, Q, ns))) return rc;
+    BatchWork* w = reinterpret_cast<BatchWork*>(g->batch);
+    int coop = 0, per_sm = 0;
+    C2G_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, g->device));
+    if (!coop) return fail(C2G_ERR_UNSUPPORTED, "device lacks cooperative launch");
+    C2G_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sssp_batch_persistent, 512, 0));
+    if (per_sm < 1) return fail(C2G_ERR_CUDA, "batch kernel cannot be resident");
+
+    C2G_CUDA(cudaMemcpyAsync(w->src, sources, sizeof(int) * (size_t)nq, cudaMemcpyHostToDevice, g->stream));
+    if (seed_off) {
+        C2G_CUDA(cudaMemcpyAsync(w->seed_off, seed_off->data(), sizeof(int) * seed_off->size(),
+                                 cudaMemcpyHostToDevice, g->stream));
+        if (ns) {
+            C2G_CUDA(cudaMemcpyAsync(w->seed_v, seed_v->data(), sizeof(int) * ns, cudaMemcpyHostToDevice, g->stream));
+            C2G_CUDA(cudaMemcpyAsync(w->seed_w, seed_w->data(), sizeof(int) * ns, cudaMemcpyHostToDevice, g->stream));
+        }
+    }
+    BatchParams p;
+    p.row = g->row;
+    p.adj = g->adj_w;
+    p.E = (unsigned)g->E;
+    p.V = g->V;
+    p.logW = logW;
+    p.Q = Q;
+    p.nq = nq;
+    p.dist = w->dist;
+    p.mask = w->mask;
+    for (int b = 0; b < 2; ++b) {
+        p.q[b] = w->q[b];
+        p.qmask[b] = w->qmask[b];
+        p.mark[b] = w->mark[b];
+    }
+    p.ctl = w->ctl;
+    p.sources = w->src;
+    p.seed_off = seed_off ? w->seed_off : nullptr;
+    p.seed_v = w->seed_v;
+    p.seed_w = w->seed_w;
+    p.qcap = (unsigned)((size_t)g->V * (size_t)(Q / 32));
+    p.mark_cap = (unsigned)((((size_t)g->E * (size_t)(Q / 32)) >> kBatchTileLog) + 2);
+    p.max_iter = g->sssp_cfg.max_iter;
+    p.barrier_ns = 4000000000ull;
+    p.counters = w->counters;
+    C2G_CUDA(cudaMemsetAsync(w->ctl, 0, sizeof(TraversalCtl), g->stream));
+    C2G_CUDA(cudaMemsetAsync(w->counters, 0, sizeof(long long) * 2, g->stream));
+    void* args[] = {&p};
+    C2G_CUDA(cudaEventRecord(g->ev0, g->stream));
+    C2G_CUDA(cudaLaunchCooperativeKernel((const void*)sssp_batch_persistent, dim3(per_sm * g->num_sms), dim3(512),
+                                         args, 0, g->stream));
+    C2G_CUDA(cudaEventRecord(g->ev1, g->stream));
+    // Results in the caller's layout.
+    int* dst = out;
+    if (!out_on_device) {
+        if (!w->stage) C2G_CUDA(cudaMalloc(&w->stage, sizeof(int) * (size_t)g->V * (size_t)Q));
+        dst = w->stage;
+    }
+    batch_transpose<<<g->num_sms * 8, 256, 0, g->stream>>>(w->dist, g->V, Q, nq, dst, query_major);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess && !out_on_device)
+        e = cudaMemcpyAsync(out, dst, sizeof(int) * (size_t)g->V * (size_t)nq, cudaMemcpyDeviceToHost, g->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(ctl_out, w->ctl, sizeof(TraversalCtl), cudaMemcpyDeviceToHost, g->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(counters, w->counters, sizeof(long long) * 2, cudaMemcpyDeviceToHost, g->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+    C2G_CUDA(e);
+    C2G_CUDA(cudaEventElapsedTime(ms, g->ev0, g->ev1));
+    return C2G_OK;
+}
+
+}  // namespace c2g

@@ -117,6 +117,8 @@ struct c2g_graph {
     std::vector<int32_t> h_row;
     std::vector<int32_t> h_hv;
     std::vector<int32_t> h_rec_of_vertex;
+    std::vector<int32_t> h_he, h_hw;  // record targets / weights (bits)
+    void* batch = nullptr;            // batched-query workspace (batch.cu)
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -138,5 +140,9 @@ int ppr_launch(c2g_graph* g, int32_t source, const c2g_ppr_params& p, const int3
                const float* seed_w, int32_t n_seeds, float* pr_dev, float* res_dev, float* ms);
 void sssp_free(c2g_graph* g);
 void ppr_free(c2g_graph* g);
+void batch_free(c2g_graph* g);
+int sssp_batch_launch(c2g_graph* g, int32_t nq, const int32_t* sources, const std::vector<int32_t>* seed_off,
+                      const std::vector<int32_t>* seed_v, const std::vector<int32_t>* seed_w, int32_t* out,
+                      int out_on_device, int query_major, float* ms, long long* counters, TraversalCtl* ctl_out);
 
 }  // namespace c2g

@@ -146,6 +146,18 @@ int c2g_sssp(c2g_graph* g, int32_t source, int use_seeds, int seed_mode, int32_t
  * max_iter (round cap, reference 1000). */
 int c2g_sssp_set_config(c2g_graph* g, int32_t delta, int32_t tile, int32_t max_iter);
 
+/* Output layouts of the batched calls. */
+#define C2G_LAYOUT_QUERY_MAJOR  0  /* out[q * V + v] */
+#define C2G_LAYOUT_VERTEX_MAJOR 1  /* out[v * n + q] */
+
+/* Batched multi-tenant SSSP: n sources in one persistent launch with per-query bitmask
+ * frontiers (the reference runs one CalcuSSSP launch per source,
+ * src/sssp/purn/Main.cu:67-99, or two on two streams in its PM mode,
+ * src/sssp/purn-perk/Main.cu:87-246).  Each query's distances equal c2g_sssp's for the
+ * same source, seeds and mode.  dist holds n*V entries in `layout`. */
+int c2g_sssp_batch(c2g_graph* g, int32_t n, const int32_t* sources, int use_seeds, int seed_mode,
+                   int32_t* dist, int dist_on_device, int layout, c2g_stats* stats);
+
 /* ---- PPR / adsorption push ------------------------------------------------------- */
 /* Forward push.  Replaces calcuatePPR (src/ppr/base/Main.cu:122-395,
  * src/ppr/purn/Main.cu:149-428, src/adsorption/w-base/Main.cu:124-395) and the seed
