@@ -51,6 +51,25 @@ class Stats(ctypes.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
 
 
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("max_batch", ctypes.c_int32), ("ads_iterations", ctypes.c_int32), ("alpha", ctypes.c_float),
+                ("rmax", ctypes.c_float), ("hbm_budget_bytes", ctypes.c_int64)]
+
+
+class Request(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int32), ("source", ctypes.c_int32), ("seeds", ctypes.c_void_p),
+                ("out", ctypes.c_void_p)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("completed", ctypes.c_int64), ("batches", ctypes.c_int64 * 3), ("pending", ctypes.c_int64 * 3),
+                ("admit_cap", ctypes.c_int64 * 3), ("max_batch", ctypes.c_int64), ("p50_ms", ctypes.c_double),
+                ("p99_ms", ctypes.c_double), ("queries_per_s", ctypes.c_double)]
+
+
+REQ_SSSP, REQ_PPR, REQ_ADSORPTION = 0, 1, 2
+
+
 class PprParams(ctypes.Structure):
     _fields_ = [("alpha", ctypes.c_float), ("rmax", ctypes.c_float), ("r0", ctypes.c_float),
                 ("pr0", ctypes.c_float), ("max_iter", ctypes.c_int32), ("seeded", ctypes.c_int32)]
@@ -83,6 +102,20 @@ SIGNATURES = {
     "c2g_ppr": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.POINTER(PprParams), _P, _P, ctypes.c_int,
                                ctypes.POINTER(Stats)]),
     "c2g_ppr_default_params": (ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(PprParams)]),
+    "c2g_ppr_batch": (ctypes.c_int, [_P, ctypes.c_int32, _P, ctypes.POINTER(PprParams), _P, _P, ctypes.c_int,
+                                     ctypes.c_int, ctypes.POINTER(Stats)]),
+    "c2g_ppr_adjoint": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.POINTER(PprParams), ctypes.c_int32, _P,
+                                       ctypes.c_float, _P, _P, _P, ctypes.POINTER(ctypes.c_double), ctypes.c_int,
+                                       ctypes.POINTER(Stats)]),
+    "c2g_graph_set_weights": (ctypes.c_int, [_P, _P, ctypes.c_int]),
+    "c2g_adsorption": (ctypes.c_int, [_P, ctypes.c_int32, _P, _P, _P, _P, ctypes.c_int32, _P, ctypes.c_int,
+                                      ctypes.POINTER(Stats)]),
+    "c2g_server_create": (ctypes.c_int, [_P, _P, _P, _P, ctypes.POINTER(ServerConfig), ctypes.POINTER(_P)]),
+    "c2g_server_submit": (ctypes.c_int, [_P, ctypes.POINTER(Request), ctypes.POINTER(ctypes.c_int64)]),
+    "c2g_server_wait": (ctypes.c_int, [_P, ctypes.c_int64, ctypes.c_double, ctypes.POINTER(ctypes.c_int),
+                                       ctypes.POINTER(ctypes.c_double)]),
+    "c2g_server_get_stats": (ctypes.c_int, [_P, ctypes.POINTER(ServerStats)]),
+    "c2g_server_destroy": (ctypes.c_int, [_P]),
     "c2g_rmat_write": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, ctypes.c_uint64,
                                       ctypes.c_int32, ctypes.c_int32, ctypes.c_double, ctypes.c_double,
                                       ctypes.c_double]),
@@ -252,3 +285,98 @@ class Graph:
         res = np.empty(self.V, dtype=np.float32)
         _check(lib().c2g_ppr(self._h, source, ctypes.byref(p), _ptr(pr), _ptr(res), 0, ctypes.byref(st)))
         return pr, res, st
+
+    def ppr_batch(self, sources, params=None, pr_ptr=None, res_ptr=None, want_res=True, vertex_major=False, **kw):
+        """Batched push: (pr, res, stats) with (n, V) float32 arrays (query-major)."""
+        src = np.ascontiguousarray(sources, dtype=np.int32)
+        p = params if params is not None else self.ppr_params(**kw)
+        st = Stats()
+        layout = 1 if vertex_major else 0
+        if pr_ptr is not None:
+            _check(lib().c2g_ppr_batch(self._h, len(src), _ptr(src), ctypes.byref(p), ctypes.c_void_p(pr_ptr),
+                                       ctypes.c_void_p(res_ptr) if res_ptr else None, 1, layout, ctypes.byref(st)))
+            return None, None, st
+        shape = (len(src), self.V) if not vertex_major else (self.V, len(src))
+        pr = np.empty(shape, dtype=np.float32)
+        res = np.empty(shape, dtype=np.float32) if want_res else None
+        _check(lib().c2g_ppr_batch(self._h, len(src), _ptr(src), ctypes.byref(p), _ptr(pr), _ptr(res), 0, layout,
+                                   ctypes.byref(st)))
+        return pr, res, st
+
+    def set_weights(self, flist=None, ptr=None):
+        """Replace the float edge weights (host array, or a device pointer)."""
+        if ptr is not None:
+            _check(lib().c2g_graph_set_weights(self._h, ctypes.c_void_p(ptr), 1))
+        else:
+            f = np.ascontiguousarray(flist, dtype=np.float32)
+            _check(lib().c2g_graph_set_weights(self._h, _ptr(f), 0))
+
+    def ppr_adjoint(self, source, targets, params=None, rmax_backward=1e-8, **kw):
+        """(grad[E], pi[V], lambda[V], loss, stats) of L = sum_t pi_source(t)."""
+        p = params if params is not None else self.ppr_params(**kw)
+        t = np.ascontiguousarray(targets, dtype=np.int32)
+        grad = np.empty(self.E, dtype=np.float32)
+        pi = np.empty(self.V, dtype=np.float32)
+        lam = np.empty(self.V, dtype=np.float32)
+        loss = ctypes.c_double()
+        st = Stats()
+        _check(lib().c2g_ppr_adjoint(self._h, source, ctypes.byref(p), len(t), _ptr(t), rmax_backward, _ptr(grad),
+                                     _ptr(pi), _ptr(lam), ctypes.byref(loss), 0, ctypes.byref(st)))
+        return grad, pi, lam, loss.value, st
+
+    def adsorption(self, seeds, p_inj, p_cont, p_abnd, iterations=30):
+        """Label propagation: (Y[V,16] float32, stats)."""
+        sv = np.ascontiguousarray(seeds, dtype=np.int32)
+        pi = np.ascontiguousarray(p_inj, dtype=np.float32)
+        pc = np.ascontiguousarray(p_cont, dtype=np.float32)
+        pa = np.ascontiguousarray(p_abnd, dtype=np.float32)
+        Y = np.empty((self.V, 16), dtype=np.float32)
+        st = Stats()
+        _check(lib().c2g_adsorption(self._h, len(sv), _ptr(sv), _ptr(pi), _ptr(pc), _ptr(pa), iterations, _ptr(Y), 0,
+                                    ctypes.byref(st)))
+        return Y, st
+
+
+class Server:
+    """Continuous-batching request loop over a device-resident graph."""
+
+    def __init__(self, graph, max_batch=256, alpha=0.15, rmax=1e-7, ads_iterations=30, hbm_budget_bytes=0,
+                 p_inj=None, p_cont=None, p_abnd=None):
+        self.graph = graph
+        cfg = ServerConfig(max_batch, ads_iterations, alpha, rmax, hbm_budget_bytes)
+        self._p = [None if a is None else np.ascontiguousarray(a, dtype=np.float32) for a in (p_inj, p_cont, p_abnd)]
+        h = ctypes.c_void_p()
+        _check(lib().c2g_server_create(graph._h, *[_ptr(a) for a in self._p], ctypes.byref(cfg), ctypes.byref(h)))
+        self._h = h
+        self._keep = {}
+
+    def submit(self, kind, source=0, seeds=None, out=None):
+        sv = None if seeds is None else np.ascontiguousarray(seeds, dtype=np.int32)
+        req = Request(kind, source, _ptr(sv), _ptr(out))
+        t = ctypes.c_int64()
+        _check(lib().c2g_server_submit(self._h, ctypes.byref(req), ctypes.byref(t)))
+        self._keep[t.value] = (sv, out)
+        return t.value
+
+    def wait(self, ticket, timeout=600.0):
+        st = ctypes.c_int()
+        lat = ctypes.c_double()
+        _check(lib().c2g_server_wait(self._h, ticket, timeout, ctypes.byref(st), ctypes.byref(lat)))
+        self._keep.pop(ticket, None)
+        return st.value, lat.value
+
+    def stats(self):
+        s = ServerStats()
+        _check(lib().c2g_server_get_stats(self._h, ctypes.byref(s)))
+        return s
+
+    def close(self):
+        if self._h:
+            lib().c2g_server_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()

@@ -1,0 +1,206 @@
+// Adsorption label propagation for sm_103a.
+//
+// The reference's "adsorption" programs are the PPR push with a different start
+// (src/adsorption/w-base/Main.cu:124-395, served here by c2g_ppr with
+// c2g_ppr_default_params(g, 1, ...)); they carry no labels.  This file is the
+// label-propagation form of adsorption that the serving configuration asks for:
+//     Y_v <- p_inj(v) * I_v + p_cont(v) * sum_{u->v} w(u,v) * Y_u
+// over L = 16 labels per query (I_v = 1 for the vertex seeding label l), iterated a
+// fixed number of times from Y = I.  The abandonment share p_abnd(v) goes to the dummy
+// "none" label, which is not stored.
+//
+// One iteration is a pull over the reverse CSR: the in-edges of all vertices form one
+// range [0, E) cut into 512-edge chunks; a half-warp (16 lanes = 16 labels) walks a
+// chunk, accumulating per-owner sums in registers, and writes each owner's sum with a
+// plain store when the owner's in-edges lie inside the chunk, otherwise with atomicAdd
+// (only owners straddling a chunk boundary).  A vertex pass then applies p_inj / p_cont.
+// Per iteration: (8 + 64) bytes per edge (in-edge record + source label row) and
+// 64 + 64 + 12 bytes per vertex.  The iteration sequence is captured once into a CUDA
+// graph and replayed.
+#include <cstring>
+#include <vector>
+
+#include "device_common.cuh"
+#include "internal.h"
+
+namespace c2g {
+
+constexpr int kAdsL = 16;          // labels per query
+constexpr int kAdsChunkLog = 9;    // 512 in-edges per half-warp chunk
+
+__global__ void ads_edge_pass(const int* __restrict__ row_r, const int2* __restrict__ adj_r, int V, long long E,
+                              const float* __restrict__ Y, float* __restrict__ acc) {
+    const int lane = threadIdx.x & 31;
+    const int l = lane & 15;
+    const unsigned hmask = (lane < 16) ? 0x0000ffffu : 0xffff0000u;
+    const long long half = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 4;
+    const long long nhalf = ((long long)gridDim.x * blockDim.x) >> 4;
+    const long long nchunks = (E + (1 << kAdsChunkLog) - 1) >> kAdsChunkLog;
+    for (long long ch = half; ch < nchunks; ch += nhalf) {
+        const long long c0 = ch << kAdsChunkLog;
+        const long long c1 = min(c0 + (1ll << kAdsChunkLog), E);
+        // owner of c0 (largest v with row_r[v] <= c0), searched by lane l == 0
+        int v = 0;
+        if (l == 0) {
+            int hi = V;
+            while (hi - v > 1) {
+                const int mid = v + ((hi - v) >> 1);
+                if (row_r[mid] <= c0)
+                    v = mid;
+                else
+                    hi = mid;
+            }
+        }
+        v = __shfl_sync(hmask, v, lane & 16);
+        long long vend = row_r[v + 1];
+        bool whole = row_r[v] >= c0;
+        float s = 0.f;
+        for (long long b = c0; b < c1; b += 16) {
+            // 16 in-edges loaded one per lane, then consumed in order
+            const long long my = b + l;
+            int2 ew = make_int2(0, 0);
+            if (my < c1) ew = __ldg(adj_r + my);
+            const int n = (int)min(16ll, c1 - b);
+            for (int k = 0; k < n; ++k) {
+                const long long e = b + k;
+                while (e >= vend) {  // owner changes: write the finished owner
+                    const size_t o = (size_t)v * kAdsL + l;
+                    if (whole)
+                        acc[o] = s;
+                    else
+                        atomicAdd(acc + o, s);
+                    s = 0.f;
+                    ++v;
+                    whole = true;  // rows starting inside the chunk
+                    vend = row_r[v + 1];
+                }
+                const int u = __shfl_sync(hmask, ew.x, (lane & 16) + k);
+                const float w = __int_as_float(__shfl_sync(hmask, ew.y, (lane & 16) + k));
+                s = fmaf(w, __ldg(Y + (size_t)u * kAdsL + l), s);
+            }
+        }
+        const size_t o = (size_t)v * kAdsL + l;
+        if (whole && vend <= c1)
+            acc[o] = s;
+        else
+            atomicAdd(acc + o, s);
+    }
+}
+
+// Y[v][l] = p_cont(v) * acc[v][l] + (label l seeded at v ? p_inj(v) : 0); acc = 0.
+__global__ void ads_vertex_pass(int V, const float* __restrict__ p_inj, const float* __restrict__ p_cont,
+                                const unsigned* __restrict__ seedmask, float* __restrict__ acc, float* __restrict__ Y) {
+    const size_t n = (size_t)V * kAdsL;
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const size_t v = i / kAdsL;
+        const int l = (int)(i % kAdsL);
+        const float inj = ((seedmask[v] >> l) & 1u) ? p_inj[v] : 0.f;
+        Y[i] = fmaf(p_cont[v], acc[i], inj);
+        acc[i] = 0.f;
+    }
+}
+
+// Y = I (seed labels), acc = 0.
+__global__ void ads_init(int V, const unsigned* __restrict__ seedmask, float* __restrict__ acc, float* __restrict__ Y) {
+    const size_t n = (size_t)V * kAdsL;
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        Y[i] = ((seedmask[i / kAdsL] >> (i % kAdsL)) & 1u) ? 1.f : 0.f;
+        acc[i] = 0.f;
+    }
+}
+
+int build_reverse_graph(c2g_graph* g);
+
+}  // namespace c2g
+
+using namespace c2g;
+
+extern "C" int c2g_adsorption(c2g_graph* g, int32_t n_labels, const int32_t* seed_vertices, const float* p_inj,
+                              const float* p_cont, const float* p_abnd, int32_t iterations, float* Y_out,
+                              int on_device, c2g_stats* stats) {
+    if (!g || !seed_vertices || !p_inj || !p_cont || !Y_out) return fail(C2G_ERR_ARG, "NULL argument");
+    if (n_labels != kAdsL) return fail(C2G_ERR_UNSUPPORTED, "adsorption supports %d labels per query", kAdsL);
+    if (iterations < 0) return fail(C2G_ERR_ARG, "iterations must be >= 0");
+    (void)p_abnd;  // the abandonment share goes to the unstored dummy label
+    for (int32_t l = 0; l < n_labels; ++l)
+        if (seed_vertices[l] < 0 || seed_vertices[l] >= g->V)
+            return fail(C2G_ERR_RANGE, "seed vertex %d out of range", seed_vertices[l]);
+    std::lock_guard<std::mutex> lk(g->mu);
+    int prev = -1;
+    cudaGetDevice(&prev);
+    cudaSetDevice(g->device);
+    struct Restore {
+        int d;
+        ~Restore() {
+            if (d >= 0) cudaSetDevice(d);
+        }
+    } restore{prev};
+    int rc = build_reverse_graph(g);
+    if (rc) return rc;
+    const size_t V = (size_t)g->V;
+    std::vector<unsigned> seedmask(V, 0u);
+    for (int32_t l = 0; l < n_labels; ++l) seedmask[seed_vertices[l]] |= 1u << l;
+    float *Y = nullptr, *acc = nullptr, *pi = nullptr, *pc = nullptr;
+    unsigned* sm = nullptr;
+    C2G_CUDA(cudaMalloc(&acc, sizeof(float) * V * kAdsL));
+    C2G_CUDA(cudaMalloc(&sm, sizeof(unsigned) * V));
+    if (on_device) {
+        Y = Y_out;
+        pi = const_cast<float*>(p_inj);
+        pc = const_cast<float*>(p_cont);
+    } else {
+        C2G_CUDA(cudaMalloc(&Y, sizeof(float) * V * kAdsL));
+        C2G_CUDA(cudaMalloc(&pi, sizeof(float) * V));
+        C2G_CUDA(cudaMalloc(&pc, sizeof(float) * V));
+    }
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    float ms = 0.f;
+    cudaError_t e = cudaMemcpyAsync(sm, seedmask.data(), sizeof(unsigned) * V, cudaMemcpyHostToDevice, g->stream);
+    if (e == cudaSuccess && !on_device) e = cudaMemcpyAsync(pi, p_inj, sizeof(float) * V, cudaMemcpyHostToDevice, g->stream);
+    if (e == cudaSuccess && !on_device) e = cudaMemcpyAsync(pc, p_cont, sizeof(float) * V, cudaMemcpyHostToDevice, g->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+    // Capture the whole propagation (init + iterations) once; replay it.
+    if (e == cudaSuccess) e = cudaStreamBeginCapture(g->stream, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+        const int eb = g->num_sms * 8, vb = g->num_sms * 8;
+        ads_init<<<vb, 256, 0, g->stream>>>(g->V, sm, acc, Y);
+        for (int it = 0; it < iterations; ++it) {
+            if (g->E) ads_edge_pass<<<eb, 256, 0, g->stream>>>(g->row_r, g->adj_r, g->V, (long long)g->E, Y, acc);
+            ads_vertex_pass<<<vb, 256, 0, g->stream>>>(g->V, pi, pc, sm, acc, Y);
+        }
+        cudaError_t ce = cudaStreamEndCapture(g->stream, &graph);
+        e = ce;
+    }
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
+    if (e == cudaSuccess) e = cudaEventRecord(g->ev0, g->stream);
+    if (e == cudaSuccess) e = cudaGraphLaunch(exec, g->stream);
+    if (e == cudaSuccess) e = cudaEventRecord(g->ev1, g->stream);
+    if (e == cudaSuccess && !on_device)
+        e = cudaMemcpyAsync(Y_out, Y, sizeof(float) * V * kAdsL, cudaMemcpyDeviceToHost, g->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+    if (e == cudaSuccess) cudaEventElapsedTime(&ms, g->ev0, g->ev1);
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    cudaFree(acc);
+    cudaFree(sm);
+    if (!on_device) {
+        cudaFree(Y);
+        cudaFree(pi);
+        cudaFree(pc);
+    }
+    C2G_CUDA(e);
+    if (stats) {
+        std::memset(stats, 0, sizeof(*stats));
+        stats->source = seed_vertices[0];
+        stats->iterations = iterations;
+        stats->edges_relaxed = (int64_t)g->E * iterations;
+        stats->vertices_popped = (int64_t)g->V * iterations;
+        stats->n_seeds = n_labels;
+        stats->device_ms = ms;
+        stats->alg_bytes = ((8.0 + 64.0) * (double)g->E + (64.0 + 64.0 + 12.0) * (double)g->V) * iterations;
+    }
+    return C2G_OK;
+}

@@ -13,6 +13,7 @@
 namespace c2g {
 
 int build_adj(c2g_graph* g, const int32_t* col, const int32_t* w, int2** out);
+void adjoint_free(c2g_graph* g);
 
 static const int kNoSidecar = -2;
 
@@ -24,9 +25,13 @@ static void graph_release(c2g_graph* g) {
     sssp_free(g);
     ppr_free(g);
     batch_free(g);
-    void* ptrs[] = {g->row, g->adj_w, g->adj_f, g->hv, g->he, g->hw, g->rec_of_vertex};
-    for (void* p : ptrs)
-        if (p) cudaFree(p);
+    ppr_batch_free(g);
+    if (!g->borrowed) adjoint_free(g);
+    if (!g->borrowed) {
+        void* ptrs[] = {g->row, g->adj_w, g->adj_f, g->hv, g->he, g->hw, g->rec_of_vertex};
+        for (void* p : ptrs)
+            if (p) cudaFree(p);
+    }
     if (g->ev0) cudaEventDestroy(g->ev0);
     if (g->ev1) cudaEventDestroy(g->ev1);
     if (g->own_stream && g->stream) cudaStreamDestroy(g->stream);
@@ -191,6 +196,39 @@ static int record_range(const c2g_graph* g, int32_t source, int mode, int32_t* f
     *n = g->h_hv[r + 1] - g->h_hv[r];
     return C2G_OK;
 }
+
+int graph_view(c2g_graph* base, c2g_graph** out) {
+    c2g_graph* g = nullptr;
+    int rc = graph_new(base->device, &g);
+    if (rc) return rc;
+    g->variant = base->variant;
+    g->V = base->V;
+    g->E = base->E;
+    g->row = base->row;
+    g->adj_w = base->adj_w;
+    g->adj_f = base->adj_f;
+    g->row_r = base->row_r;
+    g->adj_r = base->adj_r;
+    g->R = base->R;
+    g->H = base->H;
+    g->hv = base->hv;
+    g->he = base->he;
+    g->hw = base->hw;
+    g->hw_float = base->hw_float;
+    g->rec_of_vertex = base->rec_of_vertex;
+    g->h_row = base->h_row;
+    g->h_hv = base->h_hv;
+    g->h_rec_of_vertex = base->h_rec_of_vertex;
+    g->h_he = base->h_he;
+    g->h_hw = base->h_hw;
+    g->sssp_cfg = base->sssp_cfg;
+    g->ppr_cfg = base->ppr_cfg;
+    g->borrowed = true;
+    *out = g;
+    return C2G_OK;
+}
+
+void graph_free_view(c2g_graph* g) { graph_release(g); }
 
 }  // namespace c2g
 
@@ -433,6 +471,69 @@ int c2g_sssp_batch(c2g_graph* g, int32_t n, const int32_t* sources, int use_seed
         // the 4 B x V x Q initialisation.
         stats->alg_bytes = 40.0 * (double)ctl.popped + 8.0 * (double)ctl.relaxed + 8.0 * (double)counters[0] +
                            4.0 * (double)g->V * (double)((n + 31) / 32 * 32);
+    }
+    if (ctl.flags & C2G_FLAG_BARRIER_TIMEOUT) return fail(C2G_ERR_TIMEOUT, "grid barrier wait ran out");
+    if (ctl.flags & C2G_FLAG_QUEUE_OVERFLOW) return fail(C2G_ERR_OVERFLOW, "frontier queue overflow");
+    if (ctl.flags & C2G_FLAG_BOUNDS) return fail(C2G_ERR_OVERFLOW, "device index check failed");
+    return C2G_OK;
+}
+
+int c2g_ppr_batch(c2g_graph* g, int32_t n, const int32_t* sources, const c2g_ppr_params* params, float* pr,
+                  float* res, int on_device, int layout, c2g_stats* stats) {
+    if (!g || !sources || !params || !pr) return fail(C2G_ERR_ARG, "NULL argument");
+    if (n < 1) return fail(C2G_ERR_ARG, "batch needs at least one source");
+    if (layout != C2G_LAYOUT_QUERY_MAJOR && layout != C2G_LAYOUT_VERTEX_MAJOR)
+        return fail(C2G_ERR_ARG, "bad layout %d", layout);
+    if (!(params->alpha > 0.f && params->alpha <= 1.f)) return fail(C2G_ERR_ARG, "alpha must be in (0,1]");
+    if (!(params->rmax >= 0.f)) return fail(C2G_ERR_ARG, "rmax must be >= 0");
+    if (params->max_iter < 1) return fail(C2G_ERR_ARG, "max_iter must be >= 1");
+    for (int32_t i = 0; i < n; ++i)
+        if (sources[i] < 0 || sources[i] >= g->V)
+            return fail(C2G_ERR_RANGE, "source %d (entry %d) out of range [0,%d)", sources[i], i, g->V);
+    std::lock_guard<std::mutex> lk(g->mu);
+    DeviceScope ds(g->device);
+    std::vector<int32_t> off, sv;
+    std::vector<float> sw;
+    if (params->seeded) {
+        if (g->R < 0 || !g->hw_float) return fail(C2G_ERR_UNSUPPORTED, "seeded push needs ppr/ records");
+        if (g->R != g->V) return fail(C2G_ERR_FORMAT, "ppr/ hvlist has %d records for %d vertices", g->R, g->V);
+        off.push_back(0);
+        for (int32_t i = 0; i < n; ++i) {
+            const int32_t s = sources[i], first = g->h_hv[s], cnt = g->h_hv[s + 1] - first;
+            sv.insert(sv.end(), g->h_he.begin() + first, g->h_he.begin() + first + cnt);
+            for (int32_t k = 0; k < cnt; ++k) {
+                float f;
+                std::memcpy(&f, &g->h_hw[first + k], sizeof(f));
+                sw.push_back(f);
+            }
+            off.push_back((int32_t)sv.size());
+        }
+    }
+    if (on_device && (!is_device_ptr(pr) || (res && !is_device_ptr(res))))
+        return fail(C2G_ERR_ARG, "pr/res are not device pointers");
+    float ms = 0.f;
+    long long counters[2] = {0, 0};
+    TraversalCtl ctl;
+    int rc = ppr_batch_launch(g, n, sources, *params, params->seeded ? &off : nullptr, params->seeded ? &sv : nullptr,
+                              params->seeded ? &sw : nullptr, pr, res, on_device, layout == C2G_LAYOUT_QUERY_MAJOR,
+                              &ms, counters, &ctl);
+    if (rc) return rc;
+    if (stats) {
+        std::memset(stats, 0, sizeof(*stats));
+        stats->source = sources[0];
+        stats->iterations = ctl.iterations;
+        stats->vertices_popped = ctl.popped;
+        stats->edges_relaxed = counters[0];
+        stats->touched = ctl.touched;
+        stats->n_seeds = (int64_t)sv.size();
+        stats->device_ms = ms;
+        stats->status_flags = ctl.flags;
+        // 40 per frontier entry + 8 per edge-word step + 8 per (query, edge) push
+        // (4 B residual share + 4 B message add) + 12 per touched lane-row word read/write
+        // + the pr/res initialisation.
+        const double Qp = (double)((n + 31) / 32 * 32);
+        stats->alg_bytes = 40.0 * (double)ctl.popped + 8.0 * (double)ctl.relaxed + 8.0 * (double)counters[0] +
+                           12.0 * 32.0 * (double)ctl.touched + 8.0 * (double)g->V * Qp;
     }
     if (ctl.flags & C2G_FLAG_BARRIER_TIMEOUT) return fail(C2G_ERR_TIMEOUT, "grid barrier wait ran out");
     if (ctl.flags & C2G_FLAG_QUEUE_OVERFLOW) return fail(C2G_ERR_OVERFLOW, "frontier queue overflow");

@@ -181,6 +181,7 @@ __global__ void __launch_bounds__(512, 2) sssp_batch_persistent(const BatchParam
             unsigned e0 = t << kBatchTileLog;
             const unsigned e1 = min(e0 + 32u, T);
             unsigned o = (unsigned)ldcg(mark + t);
+            int prev_ovw = -1, prev_du = 0;
             while (e0 < e1) {
                 const unsigned j = o + (unsigned)lane;
                 unsigned base = 0x7fffffffu, endv = 0xffffffffu, msk = 0u;
@@ -216,31 +217,44 @@ __global__ void __launch_bounds__(512, 2) sssp_batch_persistent(const BatchParam
                     tw = ew.y;
                     tdeg = __ldg(p.row + tc + 1) - __ldg(p.row + tc);
                 }
-                // Lane = query: walk the segment's edges.
+                // Lane = query: walk the segment's edges, four at a time so that four
+                // target-row reads are in flight; the owner's row is read once per owner.
                 const int nseg = (int)(seg_end - e0);
                 bool pend = false;
-                for (int jj = 0; jj < nseg; ++jj) {
-                    const int c = __shfl_sync(kFull, tc, jj);
-                    const int wt = __shfl_sync(kFull, tw, jj);
-                    const int cdeg = __shfl_sync(kFull, tdeg, jj);
-                    const int ovw = __shfl_sync(kFull, svw, jj);
-                    const unsigned om = (unsigned)__shfl_sync(kFull, (int)smsk, jj);
-                    const int u = ovw >> p.logW, w = ovw & (W - 1);
-                    const bool active = (om >> lane) & 1u;
-                    bool imp = false;
-                    if (active) {
-                        // L2-coherent: the owner improved in the previous round.
-                        const int du = ldcg(p.dist + (size_t)u * p.Q + (w << 5) + lane);
-                        const int nd = du + wt;
-                        int* dp = p.dist + (size_t)c * p.Q + (w << 5) + lane;
-                        if (nd < ldcg(dp)) imp = atomicMin(dp, nd) > nd;
+                for (int j0 = 0; j0 < nseg; j0 += 4) {
+                    int c[4], wt[4], cdeg[4], w[4], nd[4];
+                    bool active[4];
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) {
+                        const int jj = (j0 + k) & 31;
+                        c[k] = __shfl_sync(kFull, tc, jj);
+                        wt[k] = __shfl_sync(kFull, tw, jj);
+                        cdeg[k] = __shfl_sync(kFull, tdeg, jj);
+                        const int ovw = __shfl_sync(kFull, svw, jj);
+                        const unsigned om = (unsigned)__shfl_sync(kFull, (int)smsk, jj);
+                        w[k] = ovw & (W - 1);
+                        active[k] = (j0 + k < nseg) && ((om >> lane) & 1u);
+                        if (ovw != prev_ovw) {  // L2-coherent: the owner improved last round
+                            prev_ovw = ovw;
+                            prev_du = ldcg(p.dist + (size_t)(ovw >> p.logW) * p.Q + (w[k] << 5) + lane);
+                        }
+                        nd[k] = prev_du + wt[k];
                     }
-                    relax += active;
-                    const unsigned bits = __ballot_sync(kFull, imp);
-                    bool first = false;
-                    if (lane == 0 && bits && cdeg > 0) first = mark_improved(p, c, w, bits);
-                    first = __shfl_sync(kFull, (int)first, 0) != 0;
-                    if (lane == jj) pend = first;
+                    int cur[4];
+#pragma unroll
+                    for (int k = 0; k < 4; ++k)
+                        cur[k] = active[k] ? ldcg(p.dist + (size_t)c[k] * p.Q + (w[k] << 5) + lane) : INT_MIN;
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) {
+                        bool imp = false;
+                        if (nd[k] < cur[k]) imp = atomicMin(p.dist + (size_t)c[k] * p.Q + (w[k] << 5) + lane, nd[k]) > nd[k];
+                        relax += active[k];
+                        const unsigned bits = __ballot_sync(kFull, imp);
+                        bool first = false;
+                        if (lane == 0 && bits && cdeg[k] > 0) first = mark_improved(p, c[k], w[k], bits);
+                        first = __shfl_sync(kFull, (int)first, 0) != 0;
+                        if (lane == j0 + k) pend = first;
+                    }
                 }
                 steps += nseg;
                 const int tv = (tc << p.logW) + (svw & (W - 1));
@@ -280,6 +294,13 @@ __global__ void batch_transpose(const int* __restrict__ dist, int V, int Q, int 
 
 // ---------------------------------------------------------------------------------------
 // host side
+
+// Blocks of a batched launch: the whole GPU, or the handle's share when several
+// batched launches run side by side (the serving loop).
+static int grid_blocks(const c2g_graph* g, int per_sm) {
+    int b = (int)((float)(per_sm * g->num_sms) * g->grid_scale);
+    return b < 1 ? 1 : b;
+}
 
 struct BatchWork {
     int* dist = nullptr;
@@ -401,7 +422,8 @@ int sssp_batch_launch(c2g_graph* g, int32_t nq, const int32_t* sources, const st
     C2G_CUDA(cudaMemsetAsync(w->counters, 0, sizeof(long long) * 2, g->stream));
     void* args[] = {&p};
     C2G_CUDA(cudaEventRecord(g->ev0, g->stream));
-    C2G_CUDA(cudaLaunchCooperativeKernel((const void*)sssp_batch_persistent, dim3(per_sm * g->num_sms), dim3(512),
+    const int blocks = grid_blocks(g, per_sm);
+    C2G_CUDA(cudaLaunchCooperativeKernel((const void*)sssp_batch_persistent, dim3(blocks), dim3(512),
                                          args, 0, g->stream));
     C2G_CUDA(cudaEventRecord(g->ev1, g->stream));
     // Results in the caller's layout.
@@ -418,6 +440,515 @@ int sssp_batch_launch(c2g_graph* g, int32_t nq, const int32_t* sources, const st
     if (e == cudaSuccess) e = cudaMemcpyAsync(counters, w->counters, sizeof(long long) * 2, cudaMemcpyDeviceToHost, g->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
     C2G_CUDA(e);
+    C2G_CUDA(cudaEventElapsedTime(ms, g->ev0, g->ev1));
+    return C2G_OK;
+}
+
+}  // namespace c2g
+
+// =======================================================================================
+// Batched forward push (PPR) with per-query bitmask frontiers.
+//
+// Same BSP semantics per query as c2g_ppr (src/ppr/purn/Main.cu:149-428): pop r, push
+// (1-alpha)*r*w into msg, then res += msg; if res > rmax: pr += alpha*res and activate.
+// State is vertex-major [V][Q] float (pr, res, msg, rq = residual being pushed).
+// Frontier entries are (vertex, word) pairs whose mask is complete when appended
+// (phase B visits each touched pair once), so no mask gather is needed here.
+namespace c2g {
+
+struct PprBatchParams {
+    const int* row;
+    const int2* adj;  // (target, float weight bits)
+    unsigned E;
+    int V;
+    int logW, Q, nq;
+    float* pr;        // [V][Q]
+    float* res;       // [V][Q]
+    float* msg;       // [V][Q], zero between launches
+    float* rq;        // [V][Q]
+    unsigned* tmask;  // [V][W] touched lanes this round, zero between rounds
+    int2* q[2];       // frontier entries (v*W + w, edge base)
+    unsigned* qmask[2];
+    int* mark[2];
+    int* touched;     // touched (v*W + w) list
+    int2* dangle;     // (v*W + w, lanes) activated without out-edges, popped next round
+    TraversalCtl* ctl;
+    const int* sources;
+    const int* seed_off;  // seeded mode: per-query record offsets
+    const int* seed_v;
+    const float* seed_w;
+    float alpha, rmax, r0, pr0;
+    int seeded;
+    int max_iter;
+    unsigned qcap, mark_cap;
+    unsigned long long barrier_ns;
+    long long* counters;  // [2] pushes (query, edge), edge-word steps
+};
+
+__device__ __forceinline__ FrontierOut pbatch_out(const PprBatchParams& p, int buf, int slot) {
+    FrontierOut o;
+    o.q = p.q[buf];
+    o.val = reinterpret_cast<float*>(p.qmask[buf]);  // mask bits travel in the value slot
+    o.mark = p.mark[buf];
+    o.ctr = &p.ctl->qctr[slot];
+    o.cap = p.qcap;
+    o.mark_cap = p.mark_cap;
+    o.log_tile = kBatchTileLog;
+    o.flags = &p.ctl->flags;
+    return o;
+}
+
+// Phase-B step for one touched (v, w) pair: lane = query.  force=true activates every
+// touched lane regardless of rmax and without messages (the seeded first hop).
+__device__ __forceinline__ void pbatch_apply(const PprBatchParams& p, int vw, unsigned lanes, bool force,
+                                             WarpStage& fst, const FrontierOut& out, unsigned* dctr) {
+    const int lane = threadIdx.x & 31;
+    const int v = vw >> p.logW, w = vw & ((1 << p.logW) - 1);
+    const size_t off = (size_t)v * p.Q + (w << 5) + lane;
+    const bool mine = (lanes >> lane) & 1u;
+    const int deg = __ldg(p.row + v + 1) - __ldg(p.row + v);
+    bool act = false;
+    if (mine) {
+        float r = ldcg(p.res + off);
+        if (!force) {
+            r += ldcg(p.msg + off);
+            p.msg[off] = 0.f;
+        }
+        if (force || r > p.rmax) {
+            if (!force) p.pr[off] = ldcg(p.pr + off) + p.alpha * r;
+            act = true;
+            if (deg > 0) {
+                p.rq[off] = r;
+                p.res[off] = 0.f;
+            } else {
+                p.res[off] = r;  // popped (zeroed) at the top of the next round
+            }
+        } else {
+            p.res[off] = r;
+        }
+    }
+    const unsigned bits = __ballot_sync(kFull, act);
+    if (bits && deg == 0 && lane == 0) {
+        const unsigned slot = atomicAdd(dctr, 1u);
+        if (slot < p.qcap)
+            p.dangle[slot] = make_int2(vw, (int)bits);
+        else
+            atomicOr(&p.ctl->flags, C2G_FLAG_QUEUE_OVERFLOW);
+    }
+    stage_push(fst, out, lane == 0 && bits != 0u && deg > 0, vw, deg, __int_as_float((int)bits));
+}
+
+__global__ void __launch_bounds__(512, 2) ppr_batch_persistent(const PprBatchParams p) {
+    TraversalCtl* ctl = p.ctl;
+    GridBarrier* bar = reinterpret_cast<GridBarrier*>(&ctl->bar_count);
+    int* flags = &ctl->flags;
+    const int lane = threadIdx.x & 31;
+    const unsigned gtid = blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned nthreads = gridDim.x * blockDim.x;
+    const unsigned gwarp = gtid >> 5, nwarps = nthreads >> 5;
+    const int W = 1 << p.logW;
+    __shared__ StageSmem sm;
+    const int wib = threadIdx.x >> 5;
+    WarpStage fst{sm.v0[wib], sm.d0[wib], sm.x0[wib], 0};
+    WarpStage tst{sm.v1[wib], nullptr, nullptr, 0};
+    const float one_m_a = 1.0f - p.alpha;
+
+    // Init: pr = res = 0 (msg and tmask are zero between launches).
+    {
+        const size_t n4 = ((size_t)p.V * (size_t)p.Q) >> 2;
+        float4* a4 = reinterpret_cast<float4*>(p.pr);
+        float4* b4 = reinterpret_cast<float4*>(p.res);
+        const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+        for (size_t i = gtid; i < n4; i += nthreads) {
+            a4[i] = z;
+            b4[i] = z;
+        }
+    }
+    if (!grid_sync(bar, flags, p.barrier_ns)) return;
+    // Sources: base mode puts r0 on the source; seeded mode applies the host-side first
+    // hop (records + kept out-edges) to pr/res and marks the seeds touched.
+    for (unsigned qi = gtid; qi < (unsigned)p.nq; qi += nthreads) {
+        const int s = p.sources[qi];
+        const int w = (int)(qi >> 5);
+        const unsigned bit = 1u << (qi & 31);
+        if (!p.seeded) {
+            atomicAdd(p.pr + (size_t)s * p.Q + qi, p.pr0);
+            atomicAdd(p.res + (size_t)s * p.Q + qi, p.r0);
+            if (atomicOr(p.tmask + ((size_t)s << p.logW) + w, bit) == 0u) {
+                const unsigned slot = atomicAdd(&ctl->listctr[0], 1u);
+                if (slot < p.qcap) p.touched[slot] = (s << p.logW) + w;
+            }
+        } else {
+            atomicAdd(p.pr + (size_t)s * p.Q + qi, p.alpha);
+            const int rs = __ldg(p.row + s), re = __ldg(p.row + s + 1);
+            const int n_rec = p.seed_off[qi + 1] - p.seed_off[qi];
+            for (int k = 0; k < n_rec + (re - rs); ++k) {
+                int v;
+                float wt;
+                if (k < n_rec) {
+                    v = p.seed_v[p.seed_off[qi] + k];
+                    wt = p.seed_w[p.seed_off[qi] + k];
+                } else {
+                    const int2 ew = __ldg(p.adj + rs + (k - n_rec));
+                    v = ew.x;
+                    wt = __int_as_float(ew.y);
+                }
+                atomicAdd(p.pr + (size_t)v * p.Q + qi, (one_m_a * p.alpha) * wt);
+                atomicAdd(p.res + (size_t)v * p.Q + qi, one_m_a * wt);
+                if (atomicOr(p.tmask + ((size_t)v << p.logW) + w, bit) == 0u) {
+                    const unsigned slot = atomicAdd(&ctl->listctr[0], 1u);
+                    if (slot < p.qcap) p.touched[slot] = (v << p.logW) + w;
+                }
+            }
+        }
+    }
+    if (!grid_sync(bar, flags, p.barrier_ns)) return;
+    {
+        // Round-1 frontier: every touched (vertex, word) activates its touched lanes.
+        const unsigned n = min(ldcg(&ctl->listctr[0]), p.qcap);
+        const FrontierOut out = pbatch_out(p, 1, 1);
+        for (unsigned i = gwarp; i < n; i += nwarps) {
+            const int vw = ldcg(p.touched + i);
+            unsigned* tm = p.tmask + (unsigned)vw;
+            const unsigned lanes = ldcg(tm);
+            pbatch_apply(p, vw, lanes, true, fst, out, &ctl->dctr[1]);
+            __syncwarp();
+            if (lane == 0) *tm = 0u;
+        }
+        stage_flush(fst, out);
+    }
+    if (!grid_sync(bar, flags, p.barrier_ns)) return;
+
+    long long pushes = 0, steps = 0;
+    int cur = 1, iters = 0;
+    for (;;) {
+        const unsigned long long c = ldcg(&ctl->qctr[cur % 3]);
+        const unsigned F = (unsigned)(c >> 32), T = (unsigned)c;
+        const unsigned D = min(ldcg(&ctl->dctr[cur % 3]), p.qcap);
+        const int buf = cur & 1;
+        if (F == 0 && D == 0) break;
+        if (++iters > p.max_iter) {
+            // Round cap: activated lanes keep their residual (never popped).
+            if (gtid == 0) atomicOr(flags, C2G_FLAG_ITER_CAP);
+            for (unsigned j = gwarp; j < F; j += nwarps) {
+                const int vw = ldcg(p.q[buf] + j).x;
+                const unsigned lanes = ldcg(p.qmask[buf] + j);
+                const size_t off = (size_t)(vw >> p.logW) * p.Q + ((vw & (W - 1)) << 5) + lane;
+                if ((lanes >> lane) & 1u) p.res[off] = ldcg(p.rq + off);
+            }
+            break;
+        }
+        // Pop the activated lanes without out-edges.
+        for (unsigned j = gwarp; j < D; j += nwarps) {
+            const int2 dv = ldcg(p.dangle + j);
+            const size_t off = (size_t)(dv.x >> p.logW) * p.Q + ((dv.x & (W - 1)) << 5) + lane;
+            if (((unsigned)dv.y >> lane) & 1u) p.res[off] = 0.f;
+        }
+        if (F == 0) break;
+        if (F > p.qcap || ((T + 31u) >> kBatchTileLog) > p.mark_cap) {
+            if (gtid == 0) atomicOr(flags, C2G_FLAG_BOUNDS);
+            break;
+        }
+        const int slot = cur % 3, nslot = (cur + 1) % 3, fslot = (cur + 2) % 3;
+        if (gtid == 0) {
+            ctl->qctr[fslot] = 0ull;
+            ctl->listctr[fslot] = 0u;
+            ctl->dctr[fslot] = 0u;
+            ctl->popped += F;
+            ctl->relaxed += T;
+        }
+        // Phase A: push along the frontier's edges.
+        {
+            const int2* q = p.q[buf];
+            const unsigned* qm = p.qmask[buf];
+            const int* mark = p.mark[buf];
+            const unsigned ntiles = (T + 31u) >> kBatchTileLog;
+            for (unsigned t = gwarp; t < ntiles; t += nwarps) {
+                unsigned e0 = t << kBatchTileLog;
+                const unsigned e1 = min(e0 + 32u, T);
+                unsigned o = (unsigned)ldcg(mark + t);
+                while (e0 < e1) {
+                    const unsigned j = o + (unsigned)lane;
+                    unsigned base = 0x7fffffffu, endv = 0xffffffffu, msk = 0u;
+                    int rs = 0, vw = 0;
+                    if (j < F) {
+                        const int2 qe = ldcg(q + j);
+                        vw = qe.x;
+                        base = (unsigned)qe.y;
+                        const int v = vw >> p.logW;
+                        rs = __ldg(p.row + v);
+                        endv = base + (unsigned)(__ldg(p.row + v + 1) - rs);
+                        msk = ldcg(qm + j);
+                    }
+                    const unsigned seg_end = min(e1, (unsigned)__shfl_sync(kFull, endv, 31));
+                    if (seg_end <= e0 || o >= F) {
+                        if (lane == 0) atomicOr(flags, C2G_FLAG_BOUNDS);
+                        break;
+                    }
+                    const unsigned e = e0 + (unsigned)lane;
+                    const int k = owner_lane(base, e);
+                    const unsigned srs = (unsigned)__shfl_sync(kFull, rs, k);
+                    const unsigned sb = (unsigned)__shfl_sync(kFull, (int)base, k);
+                    const int svw = __shfl_sync(kFull, vw, k);
+                    const unsigned smsk = (unsigned)__shfl_sync(kFull, (int)msk, k);
+                    const unsigned idx = srs + (e - sb);
+                    const bool ok = e < seg_end && sb <= e && idx < p.E;
+                    if (e < seg_end && !ok) atomicOr(flags, C2G_FLAG_BOUNDS);
+                    int tc = 0;
+                    float tf = 0.f;
+                    if (ok) {
+                        const int2 ew = __ldg(p.adj + idx);
+                        tc = ew.x;
+                        tf = __int_as_float(ew.y);
+                    }
+                    const int nseg = (int)(seg_end - e0);
+                    bool pend = false;
+                    int prev_u = -1;
+                    float qu = 0.f;
+                    for (int jj = 0; jj < nseg; ++jj) {
+                        const int cidx = __shfl_sync(kFull, tc, jj);
+                        const float f = __shfl_sync(kFull, tf, jj);
+                        const int ovw = __shfl_sync(kFull, svw, jj);
+                        const unsigned om = (unsigned)__shfl_sync(kFull, (int)smsk, jj);
+                        const int w = ovw & (W - 1);
+                        const bool active = (om >> lane) & 1u;
+                        if (ovw != prev_u) {  // (1-alpha)*r_u of this lane's query
+                            prev_u = ovw;
+                            qu = active ? one_m_a * ldcg(p.rq + (size_t)(ovw >> p.logW) * p.Q + (w << 5) + lane)
+                                        : 0.f;
+                        }
+                        const float m = qu * f;
+                        const bool send = active && m >= 1.17549435e-38f;
+                        if (send) atomicAdd(p.msg + (size_t)cidx * p.Q + (w << 5) + lane, m);
+                        pushes += send;
+                        const unsigned bits = __ballot_sync(kFull, send);
+                        bool first = false;
+                        if (lane == 0 && bits) first = atomicOr(p.tmask + ((size_t)cidx << p.logW) + w, bits) == 0u;
+                        first = __shfl_sync(kFull, (int)first, 0) != 0;
+                        if (lane == jj) pend = first;
+                    }
+                    steps += nseg;
+                    list_stage_push(tst, p.touched, &ctl->listctr[slot], p.qcap, flags, pend,
+                                    (tc << p.logW) + (svw & (W - 1)));
+                    e0 = seg_end;
+                    o += 32;
+                }
+            }
+            list_stage_flush(tst, p.touched, &ctl->listctr[slot], p.qcap, flags);
+        }
+        if (!grid_sync(bar, flags, p.barrier_ns)) return;
+        // Phase B: apply messages of the touched pairs and activate.
+        {
+            const unsigned n = min(ldcg(&ctl->listctr[slot]), p.qcap);
+            if (gtid == 0) ctl->touched += n;
+            const FrontierOut out = pbatch_out(p, (cur + 1) & 1, nslot);
+            for (unsigned i = gwarp; i < n; i += nwarps) {
+                const int vw = ldcg(p.touched + i);
+                unsigned* tm = p.tmask + (unsigned)vw;
+                const unsigned lanes = ldcg(tm);
+                pbatch_apply(p, vw, lanes, false, fst, out, &ctl->dctr[nslot]);
+                __syncwarp();
+                if (lane == 0) *tm = 0u;
+            }
+            stage_flush(fst, out);
+        }
+        if (!grid_sync(bar, flags, p.barrier_ns)) return;
+        ++cur;
+    }
+    for (int o = 16; o >= 1; o >>= 1) pushes += __shfl_xor_sync(kFull, pushes, o);
+    if (lane == 0) {
+        atomicAdd((unsigned long long*)&p.counters[0], (unsigned long long)pushes);
+        atomicAdd((unsigned long long*)&p.counters[1], (unsigned long long)steps);
+    }
+    if (gtid == 0) ctl->iterations = iters;
+}
+
+// [V][Q] float -> caller layout (first nq queries).
+__global__ void batch_transpose_f(const float* __restrict__ src, int V, int Q, int nq, float* __restrict__ out,
+                                  int query_major) {
+    const size_t total = (size_t)V * (size_t)nq;
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += stride) {
+        if (query_major) {
+            const size_t qi = i / (size_t)V, v = i % (size_t)V;
+            out[i] = src[v * Q + qi];
+        } else {
+            const size_t v = i / (size_t)nq, qi = i % (size_t)nq;
+            out[i] = src[v * Q + qi];
+        }
+    }
+}
+
+struct PprBatchWork {
+    float* pr = nullptr;
+    float* res = nullptr;
+    float* msg = nullptr;
+    float* rq = nullptr;
+    unsigned* tmask = nullptr;
+    int2* q[2] = {nullptr, nullptr};
+    unsigned* qmask[2] = {nullptr, nullptr};
+    int* mark[2] = {nullptr, nullptr};
+    int* touched = nullptr;
+    int2* dangle = nullptr;
+    TraversalCtl* ctl = nullptr;
+    long long* counters = nullptr;
+    int* src = nullptr;
+    int* seed_off = nullptr;
+    int* seed_v = nullptr;
+    float* seed_w = nullptr;
+    float* stage = nullptr;
+    size_t seed_cap = 0;
+    int Q = 0;
+    bool clean = false;  // msg and tmask are zero
+};
+
+void ppr_batch_free(c2g_graph* g) {
+    PprBatchWork* w = reinterpret_cast<PprBatchWork*>(g->ppr_batch);
+    if (!w) return;
+    void* ptrs[] = {w->pr, w->res, w->msg, w->rq, w->tmask, w->q[0], w->q[1], w->qmask[0], w->qmask[1],
+                    w->mark[0], w->mark[1], w->touched, w->dangle, w->ctl, w->counters, w->src, w->seed_off,
+                    w->seed_v, w->seed_w, w->stage};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    delete w;
+    g->ppr_batch = nullptr;
+}
+
+static int ppr_batch_alloc(c2g_graph* g, int Q, size_t n_seeds) {
+    PprBatchWork* w = reinterpret_cast<PprBatchWork*>(g->ppr_batch);
+    if (w && w->Q >= Q && w->seed_cap >= n_seeds) return C2G_OK;
+    if (w) ppr_batch_free(g);
+    w = new PprBatchWork();
+    g->ppr_batch = w;
+    const size_t V = g->V ? (size_t)g->V : 1;
+    const size_t W = (size_t)Q / 32, VQ = V * (size_t)Q;
+    const size_t qcap = V * W;
+    const size_t mark_cap = (((size_t)g->E * W) >> kBatchTileLog) + 2;
+    C2G_CUDA(cudaMalloc(&w->pr, sizeof(float) * VQ));
+    C2G_CUDA(cudaMalloc(&w->res, sizeof(float) * VQ));
+    C2G_CUDA(cudaMalloc(&w->msg, sizeof(float) * VQ));
+    C2G_CUDA(cudaMalloc(&w->rq, sizeof(float) * VQ));
+    C2G_CUDA(cudaMalloc(&w->tmask, sizeof(unsigned) * qcap));
+    for (int b = 0; b < 2; ++b) {
+        C2G_CUDA(cudaMalloc(&w->q[b], sizeof(int2) * qcap));
+        C2G_CUDA(cudaMalloc(&w->qmask[b], sizeof(unsigned) * qcap));
+        C2G_CUDA(cudaMalloc(&w->mark[b], sizeof(int) * mark_cap));
+    }
+    C2G_CUDA(cudaMalloc(&w->touched, sizeof(int) * qcap));
+    C2G_CUDA(cudaMalloc(&w->dangle, sizeof(int2) * qcap));
+    C2G_CUDA(cudaMalloc(&w->ctl, sizeof(TraversalCtl)));
+    C2G_CUDA(cudaMalloc(&w->counters, sizeof(long long) * 2));
+    C2G_CUDA(cudaMalloc(&w->src, sizeof(int) * (size_t)Q));
+    C2G_CUDA(cudaMalloc(&w->seed_off, sizeof(int) * ((size_t)Q + 1)));
+    w->seed_cap = n_seeds > 0 ? n_seeds : 1;
+    C2G_CUDA(cudaMalloc(&w->seed_v, sizeof(int) * w->seed_cap));
+    C2G_CUDA(cudaMalloc(&w->seed_w, sizeof(float) * w->seed_cap));
+    w->Q = Q;
+    w->clean = false;
+    return C2G_OK;
+}
+
+int ppr_batch_launch(c2g_graph* g, int32_t nq, const int32_t* sources, const c2g_ppr_params& prm,
+                     const std::vector<int32_t>* seed_off, const std::vector<int32_t>* seed_v,
+                     const std::vector<float>* seed_w, float* pr_out, float* res_out, int on_device, int query_major,
+                     float* ms, long long* counters, TraversalCtl* ctl_out) {
+    if (!g->adj_f) return fail(C2G_ERR_UNSUPPORTED, "graph has no float weights (flist / ppr wlist)");
+    int Q = 32, logW = 0;
+    while (Q < nq) {
+        Q <<= 1;
+        ++logW;
+    }
+    if ((size_t)g->V * (size_t)(Q / 32) >= (size_t(1) << 31) || (size_t)g->E * (size_t)(Q / 32) >= (size_t(1) << 32))
+        return fail(C2G_ERR_RANGE, "batch of %d queries too large for this graph", nq);
+    int rc;
+    const size_t ns = seed_v ? seed_v->size() : 0;
+    if ((rc = ppr_batch_alloc(g, Q, ns))) return rc;
+    PprBatchWork* w = reinterpret_cast<PprBatchWork*>(g->ppr_batch);
+    int coop = 0, per_sm = 0;
+    C2G_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, g->device));
+    if (!coop) return fail(C2G_ERR_UNSUPPORTED, "device lacks cooperative launch");
+    C2G_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ppr_batch_persistent, 512, 0));
+    if (per_sm < 1) return fail(C2G_ERR_CUDA, "batch kernel cannot be resident");
+    const size_t VQ = (size_t)g->V * (size_t)w->Q;
+    if (!w->clean) {
+        C2G_CUDA(cudaMemsetAsync(w->msg, 0, sizeof(float) * VQ, g->stream));
+        C2G_CUDA(cudaMemsetAsync(w->tmask, 0, sizeof(unsigned) * (size_t)g->V * (size_t)(w->Q / 32), g->stream));
+        w->clean = true;
+    }
+    C2G_CUDA(cudaMemcpyAsync(w->src, sources, sizeof(int) * (size_t)nq, cudaMemcpyHostToDevice, g->stream));
+    if (seed_off) {
+        C2G_CUDA(cudaMemcpyAsync(w->seed_off, seed_off->data(), sizeof(int) * seed_off->size(), cudaMemcpyHostToDevice,
+                                 g->stream));
+        if (ns) {
+            C2G_CUDA(cudaMemcpyAsync(w->seed_v, seed_v->data(), sizeof(int) * ns, cudaMemcpyHostToDevice, g->stream));
+            C2G_CUDA(cudaMemcpyAsync(w->seed_w, seed_w->data(), sizeof(float) * ns, cudaMemcpyHostToDevice, g->stream));
+        }
+    }
+    PprBatchParams p;
+    p.row = g->row;
+    p.adj = g->adj_f;
+    p.E = (unsigned)g->E;
+    p.V = g->V;
+    p.logW = logW;
+    p.Q = Q;
+    p.nq = nq;
+    p.pr = w->pr;
+    p.res = w->res;
+    p.msg = w->msg;
+    p.rq = w->rq;
+    p.tmask = w->tmask;
+    for (int b = 0; b < 2; ++b) {
+        p.q[b] = w->q[b];
+        p.qmask[b] = w->qmask[b];
+        p.mark[b] = w->mark[b];
+    }
+    p.touched = w->touched;
+    p.dangle = w->dangle;
+    p.ctl = w->ctl;
+    p.sources = w->src;
+    p.seed_off = seed_off ? w->seed_off : nullptr;
+    p.seed_v = w->seed_v;
+    p.seed_w = w->seed_w;
+    p.alpha = prm.alpha;
+    p.rmax = prm.rmax;
+    p.r0 = prm.r0;
+    p.pr0 = prm.pr0;
+    p.seeded = prm.seeded;
+    p.max_iter = prm.max_iter;
+    p.qcap = (unsigned)((size_t)g->V * (size_t)(p.Q / 32));
+    p.mark_cap = (unsigned)((((size_t)g->E * (size_t)(p.Q / 32)) >> kBatchTileLog) + 2);
+    p.barrier_ns = 4000000000ull;
+    p.counters = w->counters;
+    C2G_CUDA(cudaMemsetAsync(w->ctl, 0, sizeof(TraversalCtl), g->stream));
+    C2G_CUDA(cudaMemsetAsync(w->counters, 0, sizeof(long long) * 2, g->stream));
+    void* args[] = {&p};
+    C2G_CUDA(cudaEventRecord(g->ev0, g->stream));
+    const int blocks = grid_blocks(g, per_sm);
+    C2G_CUDA(cudaLaunchCooperativeKernel((const void*)ppr_batch_persistent, dim3(blocks), dim3(512), args,
+                                         0, g->stream));
+    C2G_CUDA(cudaEventRecord(g->ev1, g->stream));
+    cudaError_t e = cudaSuccess;
+    float* outs[2] = {pr_out, res_out};
+    float* srcs[2] = {w->pr, w->res};
+    for (int k = 0; k < 2 && e == cudaSuccess; ++k) {
+        if (!outs[k]) continue;
+        float* dst = outs[k];
+        if (!on_device) {
+            if (!w->stage) e = cudaMalloc(&w->stage, sizeof(float) * VQ);
+            dst = w->stage;
+        }
+        if (e != cudaSuccess) break;
+        batch_transpose_f<<<g->num_sms * 8, 256, 0, g->stream>>>(srcs[k], g->V, p.Q, nq, dst, query_major);
+        e = cudaGetLastError();
+        if (e == cudaSuccess && !on_device)
+            e = cudaMemcpyAsync(outs[k], dst, sizeof(float) * (size_t)g->V * (size_t)nq, cudaMemcpyDeviceToHost,
+                                g->stream);
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(ctl_out, w->ctl, sizeof(TraversalCtl), cudaMemcpyDeviceToHost, g->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(counters, w->counters, sizeof(long long) * 2, cudaMemcpyDeviceToHost, g->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+    C2G_CUDA(e);
+    if (ctl_out->flags & (C2G_FLAG_BARRIER_TIMEOUT | C2G_FLAG_QUEUE_OVERFLOW | C2G_FLAG_BOUNDS)) w->clean = false;
     C2G_CUDA(cudaEventElapsedTime(ms, g->ev0, g->ev1));
     return C2G_OK;
 }

@@ -43,4 +43,37 @@ int build_adj(c2g_graph* g, const int32_t* col, const int32_t* w, int2** out) {
     return C2G_OK;
 }
 
+__global__ void set_weight_bits_kernel(int2* __restrict__ adj, const int* __restrict__ w, long long E) {
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < E; e += stride) adj[e].y = w[e];
+}
+
+void adjoint_free(c2g_graph* g);
+
+// Replace the float edge weights (flist order) of a graph in place; the reverse CSR
+// built for the adjoint is dropped and rebuilt on next use.
+int set_float_weights(c2g_graph* g, const float* w, int on_device) {
+    if (!g->adj_f) return fail(C2G_ERR_UNSUPPORTED, "graph has no float weights to replace");
+    const size_t E = (size_t)g->E;
+    if (E == 0) return C2G_OK;
+    const int* src = reinterpret_cast<const int*>(w);
+    int* tmp = nullptr;
+    if (!on_device) {
+        C2G_CUDA(cudaMalloc(&tmp, sizeof(int) * E));
+        cudaError_t e = cudaMemcpyAsync(tmp, w, sizeof(int) * E, cudaMemcpyHostToDevice, g->stream);
+        if (e != cudaSuccess) {
+            cudaFree(tmp);
+            C2G_CUDA(e);
+        }
+        src = tmp;
+    }
+    set_weight_bits_kernel<<<g->num_sms * 4, 256, 0, g->stream>>>(g->adj_f, src, (long long)E);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+    if (tmp) cudaFree(tmp);
+    C2G_CUDA(e);
+    adjoint_free(g);
+    return C2G_OK;
+}
+
 }  // namespace c2g

@@ -105,6 +105,8 @@ struct c2g_graph {
     int32_t* row = nullptr;
     int2* adj_w = nullptr;
     int2* adj_f = nullptr;
+    int32_t* row_r = nullptr;  // reverse CSR with float weights (adjoint), built on demand
+    int2* adj_r = nullptr;
     // pruned records
     int32_t R = -1;
     int64_t H = 0;
@@ -118,7 +120,8 @@ struct c2g_graph {
     std::vector<int32_t> h_hv;
     std::vector<int32_t> h_rec_of_vertex;
     std::vector<int32_t> h_he, h_hw;  // record targets / weights (bits)
-    void* batch = nullptr;            // batched-query workspace (batch.cu)
+    void* batch = nullptr;            // batched-query workspaces (batch.cu)
+    void* ppr_batch = nullptr;
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -129,6 +132,8 @@ struct c2g_graph {
     c2g::PprWork ppr;
     c2g::LaunchGeom geom_sssp, geom_ppr;
     int num_sms = 0;
+    float grid_scale = 1.0f;  // fraction of the GPU a batched launch may occupy
+    bool borrowed = false;    // a view: graph arrays belong to another handle
 };
 
 namespace c2g {
@@ -138,9 +143,19 @@ int sssp_launch(c2g_graph* g, int32_t source, const int32_t* seed_v, const int32
                 int32_t n_seeds, int32_t* dist_dev, float* ms);
 int ppr_launch(c2g_graph* g, int32_t source, const c2g_ppr_params& p, const int32_t* seed_v,
                const float* seed_w, int32_t n_seeds, float* pr_dev, float* res_dev, float* ms);
+int ppr_launch_view(c2g_graph* g, const int32_t* row, const int2* adj, int32_t source, const c2g_ppr_params& pp,
+                    float absorb, int32_t n_src, const int32_t* src_list, const float* src_r0, const int32_t* seed_v,
+                    const float* seed_w, int32_t n_rec, float* pr_dev, float* res_dev, float* ms);
 void sssp_free(c2g_graph* g);
 void ppr_free(c2g_graph* g);
+// A handle sharing `base`'s device graph arrays with its own stream, workspaces and lock.
+int graph_view(c2g_graph* base, c2g_graph** out);
 void batch_free(c2g_graph* g);
+void ppr_batch_free(c2g_graph* g);
+int ppr_batch_launch(c2g_graph* g, int32_t nq, const int32_t* sources, const c2g_ppr_params& prm,
+                     const std::vector<int32_t>* seed_off, const std::vector<int32_t>* seed_v,
+                     const std::vector<float>* seed_w, float* pr_out, float* res_out, int on_device, int query_major,
+                     float* ms, long long* counters, TraversalCtl* ctl_out);
 int sssp_batch_launch(c2g_graph* g, int32_t nq, const int32_t* sources, const std::vector<int32_t>* seed_off,
                       const std::vector<int32_t>* seed_v, const std::vector<int32_t>* seed_w, int32_t* out,
                       int out_on_device, int query_major, float* ms, long long* counters, TraversalCtl* ctl_out);

@@ -39,6 +39,10 @@ struct PprParams {
     StampState* st;
     int source;
     float alpha, rmax, r0, pr0;
+    float absorb;         // pr += absorb * r at activation (alpha for PPR, 1 for the adjoint)
+    int n_src;            // base init over a list of distinct sources (adjoint targets)
+    const int* src_list;  // nullptr: the single `source`
+    const float* src_r0;
     int max_iter;
     int seeded;
     const int* seed_v;  // pruned records of the source (seeded mode)
@@ -128,7 +132,29 @@ __global__ void __launch_bounds__(512, 2) ppr_persistent(const PprParams p) {
 
     const int s = p.source;
     const int s_deg = __ldg(p.row + s + 1) - __ldg(p.row + s);
-    if (!p.seeded) {
+    if (p.src_list) {
+        // Several sources with their own residual (the adjoint's target set).
+        const FrontierOut out = ppr_out(p, 1, 1);
+        if (gtid == 0) ctl->seeds = p.n_src;
+        for (unsigned b = gwarp * 32; b < (unsigned)p.n_src; b += nwarps * 32) {
+            const unsigned i = b + (unsigned)lane;
+            bool want = false, dang = false;
+            int v = 0, deg = 0;
+            float r = 0.f;
+            if (i < (unsigned)p.n_src) {
+                v = p.src_list[i];
+                r = p.src_r0[i];
+                p.pr[v] = p.absorb * r;
+                deg = __ldg(p.row + v + 1) - __ldg(p.row + v);
+                want = deg > 0;
+                dang = !want;
+                if (dang) p.res[v] = r;
+            }
+            stage_push(fst, out, want, v, deg, r);
+            list_push(p.dangle, &ctl->dctr[1], (unsigned)p.V, flags, dang, v);
+        }
+        stage_flush(fst, out);
+    } else if (!p.seeded) {
         // Base init (src/ppr/base/Main.cu:146-150): residual r0 on the source, pr0 added
         // to pr[source]; the source is the round-1 frontier and is popped (res = 0).
         if (gwarp == 0) {
@@ -239,7 +265,7 @@ __global__ void __launch_bounds__(512, 2) ppr_persistent(const PprParams p) {
                 r = ldcg(p.res + v) + ldcg(p.msg + v);
                 p.msg[v] = 0.f;
                 if (r > p.rmax) {
-                    p.pr[v] = ldcg(p.pr + v) + a * r;
+                    p.pr[v] = ldcg(p.pr + v) + p.absorb * r;
                     deg = __ldg(p.row + v + 1) - __ldg(p.row + v);
                     want = deg > 0;
                     dang = !want;
@@ -313,16 +339,17 @@ static int ppr_alloc(c2g_graph* g) {
     return C2G_OK;
 }
 
-int ppr_launch(c2g_graph* g, int32_t source, const c2g_ppr_params& pp, const int32_t* seed_v,
-               const float* seed_w, int32_t n_rec, float* pr_dev, float* res_dev, float* ms) {
+int ppr_launch_view(c2g_graph* g, const int32_t* row, const int2* adj, int32_t source, const c2g_ppr_params& pp,
+                    float absorb, int32_t n_src, const int32_t* src_list, const float* src_r0, const int32_t* seed_v,
+                    const float* seed_w, int32_t n_rec, float* pr_dev, float* res_dev, float* ms) {
     int rc;
     if ((rc = ppr_geometry(g))) return rc;
     if ((rc = ppr_alloc(g))) return rc;
-    if (!g->adj_f) return fail(C2G_ERR_UNSUPPORTED, "graph has no float weights (flist / ppr wlist)");
+    if (!adj) return fail(C2G_ERR_UNSUPPORTED, "graph has no float weights (flist / ppr wlist)");
     PprWork& w = g->ppr;
     PprParams p;
-    p.row = g->row;
-    p.adj = g->adj_f;
+    p.row = row;
+    p.adj = adj;
     p.V = g->V;
     p.E = (unsigned)g->E;
     p.pr = pr_dev ? pr_dev : w.pr;
@@ -343,6 +370,10 @@ int ppr_launch(c2g_graph* g, int32_t source, const c2g_ppr_params& pp, const int
     p.rmax = pp.rmax;
     p.r0 = pp.r0;
     p.pr0 = pp.pr0;
+    p.absorb = absorb;
+    p.n_src = n_src;
+    p.src_list = src_list;
+    p.src_r0 = src_r0;
     p.max_iter = pp.max_iter;
     p.seeded = pp.seeded;
     p.seed_v = seed_v;
@@ -362,6 +393,12 @@ int ppr_launch(c2g_graph* g, int32_t source, const c2g_ppr_params& pp, const int
         C2G_CUDA(cudaEventElapsedTime(ms, g->ev0, g->ev1));
     }
     return C2G_OK;
+}
+
+int ppr_launch(c2g_graph* g, int32_t source, const c2g_ppr_params& pp, const int32_t* seed_v,
+               const float* seed_w, int32_t n_rec, float* pr_dev, float* res_dev, float* ms) {
+    return ppr_launch_view(g, g->row, g->adj_f, source, pp, pp.alpha, 0, nullptr, nullptr, seed_v, seed_w, n_rec,
+                           pr_dev, res_dev, ms);
 }
 
 }  // namespace c2g

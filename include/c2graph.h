@@ -166,9 +166,96 @@ int c2g_sssp_batch(c2g_graph* g, int32_t n, const int32_t* sources, int use_seed
 int c2g_ppr(c2g_graph* g, int32_t source, const c2g_ppr_params* params, float* pr,
             float* res, int on_device, c2g_stats* stats);
 
+/* Batched forward push: n sources in one persistent launch with per-query bitmask
+ * frontiers (the reference launches calcuatePPR once per source,
+ * src/ppr/purn/Main.cu:78-117).  Each query follows c2g_ppr's BSP push with the same
+ * parameters (seeded = 1 applies each source's records + kept out-edges); FP32 results
+ * equal it within summation order.  pr (and res, which may be NULL) hold n*V floats in
+ * `layout`. */
+int c2g_ppr_batch(c2g_graph* g, int32_t n, const int32_t* sources, const c2g_ppr_params* params,
+                  float* pr, float* res, int on_device, int layout, c2g_stats* stats);
+
 /* Reference defaults: PPR (alpha 0.2, rmax 0.001/(V+1), cap 500), and the adsorption
  * program (alpha 0.2, r0 10, pr0 8, rmax 1/V, cap 2000). */
 int c2g_ppr_default_params(const c2g_graph* g, int adsorption, c2g_ppr_params* out);
+
+/* ---- PPR adjoint ------------------------------------------------------------------- */
+/* Gradient of L = sum over targets t of pi_source(t) with respect to every float edge
+ * weight (flist order), pi being the base-mode push of c2g_ppr with `params`
+ * (alpha = teleport, as src/ppr/base/Main.cu:146-150).  dL/dw(u,v) =
+ * (1-alpha) * pi(u) * lambda(v), lambda = (I - (1-alpha) P)^{-1} 1_T computed by a
+ * transposed push on the reverse CSR with threshold rmax_backward (no counterpart in the
+ * reference; the forward push it differentiates replaces calcuatePPR).  Repeated targets
+ * count with their multiplicity.  grad has E entries; pi_out / lambda_out (V entries,
+ * may be NULL) return the two vectors; loss (may be NULL) returns L. */
+int c2g_ppr_adjoint(c2g_graph* g, int32_t source, const c2g_ppr_params* params, int32_t n_targets,
+                    const int32_t* targets, float rmax_backward, float* grad, float* pi_out,
+                    float* lambda_out, double* loss, int on_device, c2g_stats* stats);
+
+/* Replace the float edge weights (E entries, flist order) in place. */
+int c2g_graph_set_weights(c2g_graph* g, const float* flist, int on_device);
+
+/* ---- adsorption label propagation --------------------------------------------------- */
+/* Y_v <- p_inj(v) I_v + p_cont(v) sum_{u->v} w(u,v) Y_u over 16 labels (label l seeded
+ * at seed_vertices[l]), from Y = I, for `iterations` Jacobi steps, FP32; p_abnd goes to
+ * the unstored dummy label.  The reference's adsorption programs carry no labels
+ * (src/adsorption/w-base/Main.cu:124-395 is the PPR push, served by c2g_ppr); this is
+ * the labelled form of the serving configuration.  p_* have V entries; Y_out has V*16
+ * floats (row v = labels of v). */
+int c2g_adsorption(c2g_graph* g, int32_t n_labels, const int32_t* seed_vertices, const float* p_inj,
+                   const float* p_cont, const float* p_abnd, int32_t iterations, float* Y_out,
+                   int on_device, c2g_stats* stats);
+
+/* ---- serving loop ------------------------------------------------------------------ */
+/* Continuous-batching request loop with the graph and per-query state resident on the
+ * device (replaces the reference's C^2graph-PM CPU/GPU migration loop,
+ * src/sssp/purn-perk/Main.cu:87-246).  One worker per request kind, each on its own
+ * stream; requests that arrive while a batch runs join the next batch of their kind,
+ * within an HBM budget split between the kinds (state bytes per query).  The three
+ * kinds' batches run on the device concurrently.  A request's result equals the
+ * corresponding single call (c2g_sssp / c2g_ppr base mode / c2g_adsorption). */
+#define C2G_REQ_SSSP       0
+#define C2G_REQ_PPR        1
+#define C2G_REQ_ADSORPTION 2
+
+typedef struct c2g_server c2g_server;
+
+typedef struct c2g_server_config {
+    int32_t max_batch;        /* queries per batched launch, per kind (1..1024)        */
+    int32_t ads_iterations;   /* adsorption iterations                                 */
+    float   alpha, rmax;      /* PPR parameters (base mode)                            */
+    int64_t hbm_budget_bytes; /* admission budget for per-query state, 0 = 80% of free */
+} c2g_server_config;
+
+typedef struct c2g_request {
+    int32_t kind;             /* C2G_REQ_*                                              */
+    int32_t source;           /* SSSP / PPR source                                      */
+    const int32_t* seeds;     /* adsorption: 16 seed vertices (copied at submit)        */
+    void* out;                /* host result buffer or NULL: int32[V] SSSP distances,
+                                 float[V] PPR pagerank, float[V*16] adsorption labels   */
+} c2g_request;
+
+typedef struct c2g_server_stats {
+    int64_t completed;
+    int64_t batches[3];
+    int64_t pending[3];
+    int64_t admit_cap[3];     /* queries per batch allowed by the HBM budget            */
+    int64_t max_batch;        /* largest batch run so far                               */
+    double  p50_ms, p99_ms;   /* latency percentiles of completed requests              */
+    double  queries_per_s;    /* completed / (last completion - first submit)           */
+} c2g_server_stats;
+
+/* g must carry int32 weights (SSSP) and float weights (PPR, adsorption); p_* (V
+ * entries, host) are the adsorption probabilities (may be NULL without adsorption). */
+int c2g_server_create(c2g_graph* g, const float* p_inj, const float* p_cont, const float* p_abnd,
+                      const c2g_server_config* cfg, c2g_server** out);
+int c2g_server_submit(c2g_server* s, const c2g_request* req, int64_t* ticket);
+/* Block until the request finishes (timeout_s <= 0: no limit); status is its result
+ * code, latency_ms its submit-to-completion time. */
+int c2g_server_wait(c2g_server* s, int64_t ticket, double timeout_s, int* status, double* latency_ms);
+int c2g_server_get_stats(c2g_server* s, c2g_server_stats* out);
+/* Finish queued requests, stop the workers and release the server. */
+int c2g_server_destroy(c2g_server* s);
 
 /* ---- offline tools (host) ---------------------------------------------------------- */
 /* Seeded R-MAT graph written as <dir>/origin/{vlist,elist,wlist,flist}.bin with

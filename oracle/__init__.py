@@ -123,3 +123,23 @@ def batch(kind, row, col, w, f, sources, alpha=0.15, rmax=1e-7, max_iter=500, th
                             max_iter, threads, _p(out) if (keep and k == 0) else None,
                             _p(out) if (keep and k == 1) else None)
     return edges, out
+
+
+def adsorption_labels(row, col, f, seeds, p_inj, p_cont, iterations):
+    """FP64 label propagation Y <- p_inj*I + p_cont * (A^T Y), A[u][v] = f(u,v), from
+    Y = I (I[seed_l][l] = 1), with numpy/scipy."""
+    import scipy.sparse as sp
+
+    V = len(row) - 1
+    L = len(seeds)
+    A = sp.csr_matrix((np.asarray(f, dtype=np.float64), np.asarray(col), np.asarray(row)), shape=(V, V))
+    AT = A.T.tocsr()
+    I = np.zeros((V, L))
+    for l, v in enumerate(seeds):
+        I[v, l] += 1.0
+    Y = I.copy()
+    pi = np.asarray(p_inj, dtype=np.float64)[:, None]
+    pc = np.asarray(p_cont, dtype=np.float64)[:, None]
+    for _ in range(iterations):
+        Y = pi * I + pc * (AT @ Y)
+    return Y

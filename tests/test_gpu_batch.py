@@ -93,3 +93,76 @@ def test_batch_rejects_bad_sources(gpu_available, g16):
         with pytest.raises(c2g.C2GError) as e:
             gr.sssp_batch(np.array([0, gr.V], np.int32))
         assert e.value.code == c2g.ERR_RANGE
+
+
+@pytest.fixture(scope="module")
+def g14p(tmp_path_factory, built):
+    import c2g
+
+    d = str(tmp_path_factory.mktemp("pb14"))
+    c2g.rmat_write(d, 14, 16, 2, 1, 1000)
+    c2g.prune_ppr(d)
+    return d
+
+
+def _l1(a, b):
+    return float(np.abs(a.astype(np.float64) - b).sum())
+
+
+@pytest.mark.parametrize("n", [1, 33, 70])
+def test_ppr_batch_base_vs_fp64(gpu_available, g14p, n):
+    """Batched push, base init: each query within L1 <= 1e-6 of the FP64 oracle."""
+    import c2g
+    import oracle
+
+    o = oracle.load_dataset(g14p, "origin")
+    src = _sources(o["vlist"], n, 100 + n)
+    with c2g.Graph.load(g14p, "origin") as gr:
+        prm = gr.ppr_params(alpha=0.15, rmax=1e-7, seeded=0, pr0=0.15, r0=1.0, max_iter=500)
+        pr, res, st = gr.ppr_batch(src, prm)
+        assert st.status_flags == 0 and pr.shape == (n, gr.V)
+        for i, s in enumerate(src):
+            rp, rr, _, _ = oracle.ppr_push(o["vlist"], o["elist"], o["flist"], int(s), 0.15, 1e-7)
+            assert _l1(pr[i], rp) <= 1e-6, (i, s, _l1(pr[i], rp))
+            assert _l1(res[i], rr) <= 1e-6
+
+
+def test_ppr_batch_seeded_pruned_vs_fp64(gpu_available, g14p):
+    import c2g
+    import oracle
+
+    p = oracle.load_dataset(g14p, "ppr")
+    hv, he, hw = p["hvlist"], p["helist"], p["hwlist"]
+    src = np.concatenate([np.flatnonzero(np.diff(hv) > 0)[:10], _sources(p["vlist"], 22, 9)]).astype(np.int32)
+    with c2g.Graph.load(g14p, "ppr") as gr:
+        prm = gr.ppr_params(alpha=0.15, rmax=1e-7, seeded=1)
+        pr, res, st = gr.ppr_batch(src, prm)
+        for i, s in enumerate(src):
+            s = int(s)
+            sv = np.concatenate([he[hv[s]:hv[s + 1]], p["elist"][p["vlist"][s]:p["vlist"][s + 1]]])
+            sw = np.concatenate([hw[hv[s]:hv[s + 1]], p["wlist"][p["vlist"][s]:p["vlist"][s + 1]]])
+            rp, rr, _, _ = oracle.ppr_push(p["vlist"], p["elist"], p["wlist"], s, 0.15, 1e-7, seeded=True,
+                                           seed_v=sv, seed_w=sw)
+            assert _l1(pr[i], rp) <= 1e-6, (i, s)
+            assert _l1(res[i], rr) <= 1e-6
+
+
+def test_ppr_batch_matches_single_and_cap(gpu_available, g14p):
+    import c2g
+    import oracle
+
+    o = oracle.load_dataset(g14p, "origin")
+    src = _sources(o["vlist"], 40, 77)
+    with c2g.Graph.load(g14p, "origin") as gr:
+        prm = gr.ppr_params(alpha=0.2, rmax=1e-6, seeded=0, pr0=0.2, r0=1.0)
+        pr, res, _ = gr.ppr_batch(src, prm, vertex_major=True)
+        for i in (0, 13, 39):
+            p1, r1, _ = gr.ppr(int(src[i]), prm)
+            assert _l1(pr[:, i], p1.astype(np.float64)) <= 2e-6
+        prm.max_iter = 3
+        pr, res, st = gr.ppr_batch(src, prm)
+        assert st.status_flags & c2g.FLAG_ITER_CAP
+        for i in (0, 21):
+            rp, rr, rounds, _ = oracle.ppr_push(o["vlist"], o["elist"], o["flist"], int(src[i]), 0.2, 1e-6,
+                                                max_iter=3)
+            assert _l1(pr[i], rp) <= 1e-6 and _l1(res[i], rr) <= 1e-6
