@@ -97,6 +97,8 @@ SIGNATURES = {
     "c2g_sssp": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int, ctypes.c_int, _P, ctypes.c_int,
                                 ctypes.POINTER(Stats)]),
     "c2g_sssp_set_config": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32]),
+    "c2g_sssp_noalloc": (ctypes.c_int, [_P, _P, ctypes.c_int32, ctypes.c_int64, ctypes.c_int32, _P, _P,
+                                        ctypes.POINTER(Stats)]),
     "c2g_sssp_batch": (ctypes.c_int, [_P, ctypes.c_int32, _P, ctypes.c_int, ctypes.c_int, _P, ctypes.c_int,
                                       ctypes.c_int, ctypes.POINTER(Stats)]),
     "c2g_ppr": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.POINTER(PprParams), _P, _P, ctypes.c_int,

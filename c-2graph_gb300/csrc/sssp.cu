@@ -16,6 +16,8 @@
 //     frontier runs dry;
 //   * one bounded grid barrier per round instead of four unbounded spins.
 #include <climits>
+#include <cstring>
+#include <mutex>
 
 #include "device_common.cuh"
 #include "internal.h"
@@ -372,3 +374,130 @@ int sssp_launch(c2g_graph* g, int32_t source, const int32_t* seed_v, const int32
 }
 
 }  // namespace c2g
+
+// ---------------------------------------------------------------------------------------
+// Allocation-free entry point.
+//
+// Some callers cannot let this library allocate device memory per call.  Examples are a
+// host whose device memory is owned entirely by another allocator, and a serving loop
+// that must not call cudaMalloc/cudaFree after start-up (both may synchronise the device
+// and stall every stream).  c2g_sssp_noalloc runs the same single-query kernel as
+// c2g_sssp on arrays the caller already holds on the device.  Its scratch memory
+// (round tags, frontier queues, tile markers and the launch control block) is
+// g_sssp_noalloc_scratch below: a fixed array, loaded with the library on every GPU that
+// uses it and held until the process exits.  Its size bounds the graphs this entry
+// point accepts (C2G_NOALLOC_MAX_V vertices, C2G_NOALLOC_MAX_E edges).
+
+namespace c2g {
+namespace {
+
+constexpr int kNoAllocLogTile = 8;
+constexpr size_t kNoAllocMarks = ((size_t)C2G_NOALLOC_MAX_E >> kNoAllocLogTile) + 2;
+
+constexpr size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+constexpr size_t kOffStamp = 0;
+constexpr size_t kOffFarstamp = kOffStamp + align256(sizeof(int) * (size_t)C2G_NOALLOC_MAX_V);
+constexpr size_t kOffQ0 = kOffFarstamp + align256(sizeof(int) * (size_t)C2G_NOALLOC_MAX_V);
+constexpr size_t kOffQ1 = kOffQ0 + align256(sizeof(int2) * (size_t)C2G_NOALLOC_MAX_V);
+constexpr size_t kOffMark0 = kOffQ1 + align256(sizeof(int2) * (size_t)C2G_NOALLOC_MAX_V);
+constexpr size_t kOffMark1 = kOffMark0 + align256(sizeof(int) * kNoAllocMarks);
+constexpr size_t kOffCtl = kOffMark1 + align256(sizeof(int) * kNoAllocMarks);
+constexpr size_t kOffSt = kOffCtl + align256(sizeof(TraversalCtl));
+constexpr size_t kNoAllocScratchBytes = kOffSt + align256(sizeof(StampState));
+
+constexpr int kNoAllocMaxDevices = 64;
+void* g_noalloc_base[kNoAllocMaxDevices];           // device address of the scratch, per device
+cudaError_t g_noalloc_setup_err[kNoAllocMaxDevices];
+std::once_flag g_noalloc_once[kNoAllocMaxDevices];
+
+}  // namespace
+
+// The scratch.  Zero at module load: round tags start above 0 and the tag bases start at
+// 0, so no clearing is needed before the first call; the control block is cleared on the
+// caller's stream before every launch.
+static __device__ __align__(256) unsigned char g_sssp_noalloc_scratch[kNoAllocScratchBytes];
+
+}  // namespace c2g
+
+extern "C" int c2g_sssp_noalloc(const int32_t* row, const void* adj, int32_t V, int64_t E, int32_t source,
+                                int32_t* dist, void* stream, c2g_stats* stats) {
+    using namespace c2g;
+    if (!row || !adj || !dist) return fail(C2G_ERR_ARG, "noalloc SSSP: NULL argument");
+    if (V < 1 || V > C2G_NOALLOC_MAX_V)
+        return fail(C2G_ERR_RANGE, "noalloc SSSP: V = %d outside [1, %d] (size of the static scratch)", V,
+                    C2G_NOALLOC_MAX_V);
+    if (E < 0 || E > C2G_NOALLOC_MAX_E)
+        return fail(C2G_ERR_RANGE, "noalloc SSSP: E = %lld outside [0, %lld] (size of the static scratch)",
+                    (long long)E, (long long)C2G_NOALLOC_MAX_E);
+    if (source < 0 || source >= V) return fail(C2G_ERR_RANGE, "source %d out of range [0,%d)", source, V);
+    int dev = 0;
+    C2G_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kNoAllocMaxDevices) return fail(C2G_ERR_UNSUPPORTED, "device index %d too large", dev);
+    // Once per device, with that device current: the device address of the scratch.
+    // The host-side name of a __device__ array is not a device address.
+    std::call_once(g_noalloc_once[dev], [dev] {
+        g_noalloc_setup_err[dev] = cudaGetSymbolAddress(&g_noalloc_base[dev], g_sssp_noalloc_scratch);
+    });
+    if (g_noalloc_setup_err[dev] != cudaSuccess)
+        return fail(C2G_ERR_CUDA, "noalloc SSSP: cudaGetSymbolAddress failed: %s",
+                    cudaGetErrorString(g_noalloc_setup_err[dev]));
+    unsigned char* base = static_cast<unsigned char*>(g_noalloc_base[dev]);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+
+    int coop = 0, per_sm = 0, sms = 0;
+    C2G_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
+    if (!coop) return fail(C2G_ERR_UNSUPPORTED, "device %d lacks cooperative launch", dev);
+    C2G_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    C2G_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sssp_persistent<false>, 512, 0));
+    if (per_sm < 1) return fail(C2G_ERR_CUDA, "SSSP kernel cannot be resident (occupancy 0)");
+
+    SsspParams p;
+    p.row = row;
+    p.adj = static_cast<const int2*>(adj);
+    p.E = (unsigned)E;
+    p.V = V;
+    p.dist = dist;
+    p.stamp = reinterpret_cast<int*>(base + kOffStamp);
+    p.farstamp = reinterpret_cast<int*>(base + kOffFarstamp);
+    p.q[0] = reinterpret_cast<int2*>(base + kOffQ0);
+    p.q[1] = reinterpret_cast<int2*>(base + kOffQ1);
+    p.mark[0] = reinterpret_cast<int*>(base + kOffMark0);
+    p.mark[1] = reinterpret_cast<int*>(base + kOffMark1);
+    p.far[0] = p.far[1] = p.far[2] = nullptr;  // the near/far split is off here
+    p.ctl = reinterpret_cast<TraversalCtl*>(base + kOffCtl);
+    p.st = reinterpret_cast<StampState*>(base + kOffSt);
+    p.source = source;
+    p.seed_v = nullptr;
+    p.seed_w = nullptr;
+    p.n_seeds = 0;
+    p.delta = 0;
+    p.log_tile = kNoAllocLogTile;
+    p.max_iter = 1 << 20;
+    p.mark_cap = (unsigned)(((size_t)E >> kNoAllocLogTile) + 2);
+    p.barrier_ns = 2000000000ull;
+    C2G_CUDA(cudaMemsetAsync(p.ctl, 0, sizeof(TraversalCtl), s));
+    void* args[] = {&p};
+    C2G_CUDA(cudaLaunchCooperativeKernel((const void*)sssp_persistent<false>, dim3(per_sm * sms), dim3(512), args, 0,
+                                         s));
+    TraversalCtl ctl;
+    C2G_CUDA(cudaMemcpyAsync(&ctl, p.ctl, sizeof(ctl), cudaMemcpyDeviceToHost, s));
+    C2G_CUDA(cudaStreamSynchronize(s));
+    if (ctl.flags & (C2G_FLAG_BARRIER_TIMEOUT | C2G_FLAG_QUEUE_OVERFLOW | C2G_FLAG_BOUNDS)) {
+        static const StampState reset{1 << 30, 1 << 30, {0, 0}};
+        cudaMemcpyAsync(p.st, &reset, sizeof(reset), cudaMemcpyHostToDevice, s);
+        cudaStreamSynchronize(s);
+    }
+    if (stats) {
+        std::memset(stats, 0, sizeof(*stats));
+        stats->source = source;
+        stats->iterations = ctl.iterations;
+        stats->vertices_popped = ctl.popped;
+        stats->edges_relaxed = ctl.relaxed;
+        stats->status_flags = ctl.flags;
+        stats->alg_bytes = 4.0 * V + 16.0 * (double)ctl.popped + 12.0 * (double)ctl.relaxed;
+    }
+    if (ctl.flags & C2G_FLAG_BARRIER_TIMEOUT) return fail(C2G_ERR_TIMEOUT, "grid barrier wait ran out");
+    if (ctl.flags & (C2G_FLAG_QUEUE_OVERFLOW | C2G_FLAG_BOUNDS))
+        return fail(C2G_ERR_OVERFLOW, "device queue or index check failed");
+    return C2G_OK;
+}

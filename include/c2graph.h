@@ -146,6 +146,29 @@ int c2g_sssp(c2g_graph* g, int32_t source, int use_seeds, int seed_mode, int32_t
  * max_iter (round cap, reference 1000). */
 int c2g_sssp_set_config(c2g_graph* g, int32_t delta, int32_t tile, int32_t max_iter);
 
+/* Allocation-free single-source SSSP (no counterpart in the reference).  For callers
+ * that cannot let the library allocate device memory: a host whose device memory is
+ * owned by another allocator, or a serving loop that must not call cudaMalloc/cudaFree
+ * after start-up, since they may synchronise the device.  It runs the c2g_sssp kernel on
+ * caller-owned device arrays:
+ *   row  int32[V+1]                       CSR row pointer
+ *   adj  E pairs of (int32 target, int32 weight), 8 bytes per edge
+ *   dist int32[V]                          output, unreachable = 1999999999
+ * Its scratch is one static device array of about 6.4 MB, held on every GPU that uses
+ * it until the process exits.  It bounds the graph to C2G_NOALLOC_MAX_V vertices and
+ * C2G_NOALLOC_MAX_E edges; larger inputs return C2G_ERR_RANGE.
+ * The call allocates nothing: no cudaMalloc, no cudaFree, no allocating library call.
+ * The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress) with that device current; make that first call before any
+ * stream capture.  Every call shares the array, so calls that overlap on the GPU race:
+ * serialise them (one stream, or host-side ordering).  Work runs on `stream`
+ * (cudaStream_t, NULL for the legacy default stream) and the call returns when the
+ * traversal has finished. */
+#define C2G_NOALLOC_MAX_V 262144
+#define C2G_NOALLOC_MAX_E 4194304
+int c2g_sssp_noalloc(const int32_t* row, const void* adj, int32_t V, int64_t E, int32_t source,
+                     int32_t* dist, void* stream, c2g_stats* stats);
+
 /* Output layouts of the batched calls. */
 #define C2G_LAYOUT_QUERY_MAJOR  0  /* out[q * V + v] */
 #define C2G_LAYOUT_VERTEX_MAJOR 1  /* out[v * n + q] */

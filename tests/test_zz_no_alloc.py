@@ -1,0 +1,71 @@
+"""c2g_sssp_noalloc: the SSSP entry point that allocates no device memory.
+
+It is meant for callers that cannot let the library allocate, such as a host whose
+device memory belongs to another allocator, or a serving loop that must not call
+cudaMalloc/cudaFree (they can synchronise the device) once it is running.  It runs on
+caller-owned device arrays with scratch in a static device array.  Its results must
+equal the regular entry point's (c2g_sssp, bit-exact int32), call after call, because
+the shared scratch keeps the previous call's contents.
+
+This file is named to be collected last, and it passes alone in a fresh process as
+well as after the other tests.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def graph16(tmp_path_factory, built):
+    import c2g
+
+    d = str(tmp_path_factory.mktemp("noalloc16"))
+    c2g.rmat_write(d, 16, 16, 3, 1, 1000)
+    vl = c2g.read_array(d + "/origin/vlist.bin")
+    el = c2g.read_array(d + "/origin/elist.bin")
+    wl = c2g.read_array(d + "/origin/wlist.bin")
+    return d, vl, el, wl
+
+
+def test_noalloc_matches_regular_entry_point(gpu_available, graph16):
+    import torch
+
+    import c2g
+
+    d, vl, el, wl = graph16
+    V, E = len(vl) - 1, len(el)
+    assert V <= 262144 and E <= 4194304
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    row = torch.from_numpy(vl).to(dev)
+    adj = torch.from_numpy(np.stack([el, wl], axis=1).astype(np.int32)).contiguous().to(dev)
+    dist = torch.empty(V, dtype=torch.int32, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    deg = np.diff(vl)
+    sources = [int(np.argmax(deg)), int(np.flatnonzero(deg > 0)[7])]
+    L = c2g.lib()
+    with c2g.Graph.load(d, "origin") as g:
+        for s in sources:  # two calls in a row on the shared scratch
+            st = c2g.Stats()
+            rc = L.c2g_sssp_noalloc(ctypes.c_void_p(row.data_ptr()), ctypes.c_void_p(adj.data_ptr()), V, E, s,
+                                    ctypes.c_void_p(dist.data_ptr()), ctypes.c_void_p(stream.cuda_stream),
+                                    ctypes.byref(st))
+            assert rc == 0, L.c2g_last_error()
+            ref, rst = g.sssp(s)
+            assert np.array_equal(dist.cpu().numpy(), ref), s
+            assert st.status_flags == 0 and st.iterations == rst.iterations
+
+
+def test_noalloc_rejects_sizes_beyond_scratch(gpu_available):
+    import c2g
+
+    L = c2g.lib()
+    assert L.c2g_sssp_noalloc(ctypes.c_void_p(16), ctypes.c_void_p(16), 262145, 10, 0, ctypes.c_void_p(16), None,
+                              None) == c2g.ERR_RANGE
+    assert b"static scratch" in L.c2g_last_error()
+    assert L.c2g_sssp_noalloc(ctypes.c_void_p(16), ctypes.c_void_p(16), 1000, 4194305, 0, ctypes.c_void_p(16), None,
+                              None) == c2g.ERR_RANGE
+    assert L.c2g_sssp_noalloc(None, None, 10, 10, 0, None, None, None) == c2g.ERR_ARG
