@@ -6,16 +6,18 @@ seed 2, int32 weights in [1,1000], flist = out-normalised uniform(0,1)), pruned 
 this library's purn-sssp / purn-ppr (byte-identical to the reference tools).  The
 query mix is the batched configuration's: 256 SSSP + 256 PPR sources, half uniform
 over vertices with out-edges, half from the top 1% out-degree vertices (selection
-seed 2024).  A step runs a slice of that mix (--sssp-per-step + --ppr-per-step
-queries, rotating through the 512 sources) through the per-query GPU path:
-  SSSP: sssp-purn on sssp/ with the source's own record as seeds (EXACT mode), int32
-        distances (bit-exact against the oracle in tests/);
-  PPR:  ppr-purn on ppr/ (alpha 0.15, rmax 1e-7, FP32; L1 <= 1e-6 vs the FP64 oracle
-        in tests/).
+seed 2024).  A step runs the whole mix through the batched path, one persistent
+launch per kind:
+  SSSP: 256 sources, sssp-purn on sssp/ with each source's own record as seeds (EXACT
+        mode), int32 distances (bit-exact against the oracle in tests/);
+  PPR:  256 sources, ppr-purn on ppr/ (alpha 0.15, rmax 1e-7, FP32; L1 <= 1e-6 vs the
+        FP64 oracle in tests/).
 value = queries per second with the graph and outputs resident in HBM (CUDA events on
-the stream the kernels run on); e2e = the same through the C ABI with host output
-buffers (device->host copy of every result inside the timed region).  The graph
-(~1.6 GB of CSR) is larger than L2, so no flush is needed between steps.
+the stream the kernels run on); e2e = the same through the C ABI with pinned host
+output buffers (device->host copy of every result inside the timed region).  The plain
+per-query GPU path is timed on a sample of the same sources for the
+batched-vs-per-query ratio.  Graph and state are larger than L2, so no flush is needed
+between steps.
 
 --impl reference times the reference's CPU implementation of the path (the oracle's
 restatement of the reference CPU Bellman-Ford / BSP push, all host threads, one query
@@ -192,8 +194,9 @@ def run_ours(args, rank, world, local_rank):
     so = {"vlist": c2g.read_array(os.path.join(work, "sssp", "vlist.bin"))}
     po = {"vlist": c2g.read_array(os.path.join(work, "ppr", "vlist.bin"))}
     V = len(so["vlist"]) - 1
-    ssrc = pick_sources(so["vlist"], 256, seed=2024 + rank)
-    psrc = pick_sources(po["vlist"], 256, seed=2025 + rank)
+    nS, nP = args.sssp_per_step, args.ppr_per_step
+    ssrc = pick_sources(so["vlist"], nS, seed=2024 + rank)
+    psrc = pick_sources(po["vlist"], nP, seed=2025 + rank)
 
     gs = c2g.Graph.load(work, "sssp", device=dev)
     gp = c2g.Graph.load(work, "ppr", device=dev)
@@ -202,38 +205,20 @@ def run_ours(args, rank, world, local_rank):
     gp.set_stream(stream.cuda_stream)
     gs.sssp_config(delta=args.delta, tile=args.tile)
     prm = gp.ppr_params(alpha=ALPHA, rmax=RMAX, seeded=1, max_iter=500)
-    dist_d = torch.empty(V, dtype=torch.int32, device=dev)
-    pr_d = torch.empty(V, dtype=torch.float32, device=dev)
-    res_d = torch.empty(V, dtype=torch.float32, device=dev)
-    dist_h = torch.empty(V, dtype=torch.int32).pin_memory().numpy()
-    nS, nP = args.sssp_per_step, args.ppr_per_step
+    dist_d = torch.empty((nS, V), dtype=torch.int32, device=dev)
+    pr_d = torch.empty((nP, V), dtype=torch.float32, device=dev)
+    dist_h = torch.empty((nS, V), dtype=torch.int32).pin_memory().numpy()
+    pr_h = torch.empty((nP, V), dtype=torch.float32).pin_memory().numpy()
 
-    def step(i, host):
-        ks = [(i * nS + j) % 256 for j in range(nS)]
-        kp = [(i * nP + j) % 256 for j in range(nP)]
-        acc = {"sssp_ms": 0.0, "ppr_ms": 0.0, "sssp_bytes": 0.0, "ppr_bytes": 0.0, "sssp_edges": 0,
-               "ppr_edges": 0, "sssp_iters": 0, "ppr_iters": 0}
-        for k in ks:
-            s = int(ssrc[k])
-            if host:
-                _, st = gs.sssp(s, seeds=True, mode=c2g.SEEDS_EXACT, out=dist_h)
-            else:
-                _, st = gs.sssp(s, seeds=True, mode=c2g.SEEDS_EXACT, out_ptr=dist_d.data_ptr())
-            acc["sssp_ms"] += st.device_ms
-            acc["sssp_bytes"] += st.alg_bytes
-            acc["sssp_edges"] += st.edges_relaxed
-            acc["sssp_iters"] += st.iterations
-        for k in kp:
-            s = int(psrc[k])
-            if host:
-                _, _, st = gp.ppr(s, prm)
-            else:
-                _, _, st = gp.ppr(s, prm, pr_ptr=pr_d.data_ptr(), res_ptr=res_d.data_ptr())
-            acc["ppr_ms"] += st.device_ms
-            acc["ppr_bytes"] += st.alg_bytes
-            acc["ppr_edges"] += st.edges_relaxed
-            acc["ppr_iters"] += st.iterations
-        return acc
+    def step(host):
+        """One step: the whole query mix, each kind in one batched launch."""
+        if host:
+            _, ss = gs.sssp_batch(ssrc, seeds=True, mode=c2g.SEEDS_EXACT, out=dist_h)
+            _, _, sp = _ppr_into(gp, psrc, prm, pr_h)
+        else:
+            _, ss = gs.sssp_batch(ssrc, seeds=True, mode=c2g.SEEDS_EXACT, out_ptr=dist_d.data_ptr())
+            _, _, sp = gp.ppr_batch(psrc, prm, pr_ptr=pr_d.data_ptr())
+        return ss, sp
 
     def barrier():
         torch.cuda.synchronize(dev)
@@ -242,16 +227,24 @@ def run_ours(args, rank, world, local_rank):
         torch.cuda.synchronize(dev)
 
     def timed(host):
-        for i in range(args.warmup):
-            step(i, host)
+        for _ in range(args.warmup):
+            step(host)
         barrier()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        tot = None
+        acc = {"s_ms": 0.0, "p_ms": 0.0, "s_bytes": 0.0, "p_bytes": 0.0, "s_rel": 0, "p_push": 0, "s_it": 0,
+               "p_it": 0}
         e0.record(stream)
         t0 = time.time()
-        for i in range(args.steps):
-            a = step(args.warmup + i, host)
-            tot = a if tot is None else {k: tot[k] + a[k] for k in tot}
+        for _ in range(args.steps):
+            ss, sp = step(host)
+            acc["s_ms"] += ss.device_ms
+            acc["p_ms"] += sp.device_ms
+            acc["s_bytes"] += ss.alg_bytes
+            acc["p_bytes"] += sp.alg_bytes
+            acc["s_rel"] += ss.edges_relaxed
+            acc["p_push"] += sp.edges_relaxed
+            acc["s_it"] += ss.iterations
+            acc["p_it"] += sp.iterations
         e1.record(stream)
         barrier()
         wall = time.time() - t0
@@ -260,7 +253,7 @@ def run_ours(args, rank, world, local_rank):
             t = torch.tensor([ms], device=dev)
             tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
             ms = float(t.item())
-        return ms, wall, tot
+        return ms, wall, acc
 
     with ClockSampler(dev) as clk:
         ms_dev, wall_dev, tot = timed(False)
@@ -270,31 +263,45 @@ def run_ours(args, rank, world, local_rank):
     value = q_all / (ms_dev / 1000.0)
     e2e = q_all / (ms_e2e / 1000.0)
 
-    # Graph500-style TEPS on one sample query: out-edges of reached vertices / time.
-    s0 = int(ssrc[0])
-    d0, st0 = gs.sssp(s0, seeds=True, mode=c2g.SEEDS_EXACT)
-    reached_edges = int(np.diff(so["vlist"])[d0 != c2g.INF_DIST].sum())
-    gteps_sample = reached_edges / (st0.device_ms / 1000.0) / 1e9
+    # The plain per-query GPU path on a sample of the same mix (same kernels' single-
+    # query form): the batched-vs-per-query ratio of the metric.
+    pq_s = pq_p = 0.0
+    for s in ssrc[: args.per_query_sample]:
+        _, st = gs.sssp(int(s), seeds=True, mode=c2g.SEEDS_EXACT, out_ptr=dist_d.data_ptr())
+        pq_s += st.device_ms
+    for s in psrc[: max(1, args.per_query_sample // 2)]:
+        _, _, st = gp.ppr(int(s), prm, pr_ptr=pr_d.data_ptr())
+        pq_p += st.device_ms
+    ms_sssp_pq = pq_s / args.per_query_sample
+    ms_ppr_pq = pq_p / max(1, args.per_query_sample // 2)
+    per_query_qps = q_step / ((nS * ms_sssp_pq + nP * ms_ppr_pq) / 1000.0)
 
-    dominant = "sssp" if tot["sssp_ms"] >= tot["ppr_ms"] else "ppr"
+    # Graph500-style TEPS of the batched SSSP: out-edges of reached (vertex, query) pairs.
+    d_host = dist_d[: min(8, nS)].cpu().numpy()
+    deg = np.diff(so["vlist"])
+    reached_edges = sum(int(deg[row != c2g.INF_DIST].sum()) for row in d_host) * nS / len(d_host)
+    gteps_batched = reached_edges * args.steps / (tot["s_ms"] / 1000.0) / 1e9
+
+    dominant = "s" if tot["s_ms"] >= tot["p_ms"] else "p"
     peak, peak_kind = measured_peak()
     achieved = tot[dominant + "_bytes"] / (tot[dominant + "_ms"] / 1000.0) / 1e9
-    kernel_name = "sssp_persistent" if dominant == "sssp" else "ppr_persistent"
+    kernel_name = "sssp_batch_persistent" if dominant == "s" else "ppr_batch_persistent"
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         import oracle  # CPU-baseline leg only
 
         threads = 1
-        t0 = time.time()
         o = oracle.load_dataset(work, "origin")
         k = args.cpu_sample
+        t0 = time.time()
         oracle.batch("sssp", o["vlist"], o["elist"], o["wlist"], None, ssrc[:k], threads=threads)
         oracle.batch("ppr", o["vlist"], o["elist"], None, o["flist"], psrc[:k], alpha=ALPHA, rmax=RMAX,
                      threads=threads)
         dt = time.time() - t0
         cpu = {"value": 2 * k / dt, "unit": "queries/s", "cores": threads, "kind": "port",
-               "sample": "%d SSSP (Bellman-Ford, origin/) + %d PPR (FP32 BSP push) queries on one core" % (k, k)}
+               "sample": "%d SSSP (reference CPU Bellman-Ford restated, origin/) + %d PPR (FP32 BSP push) "
+                         "queries on one core" % (k, k)}
 
     if rank == 0:
         line = {
@@ -302,30 +309,32 @@ def run_ours(args, rank, world, local_rank):
             "warmup": args.warmup, "ms_per_step": ms_dev / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "int32 (SSSP) + f32 (PPR)",
             "data": "synthetic R-MAT (seeded); no public dataset",
-            "config": {"workload": "rmat-s%d-ef%d pruned, per-query GPU path, %d SSSP + %d PPR per step"
-                                   % (args.scale, args.edge_factor, nS, nP),
-                       "path": "per-query", "vertices": V, "edges_sssp": int(so["vlist"][-1]),
-                       "edges_ppr": int(po["vlist"][-1]), "alpha": ALPHA, "rmax": RMAX, "delta": args.delta,
-                       "tile": args.tile, "l2": "graph larger than L2 (no flush needed)",
+            "config": {"workload": "rmat-s%d-ef%d pruned, batched multi-tenant mix: %d SSSP + %d PPR sources per "
+                                   "step, one launch per kind" % (args.scale, args.edge_factor, nS, nP),
+                       "path": "batched", "vertices": V, "edges_sssp": int(so["vlist"][-1]),
+                       "edges_ppr": int(po["vlist"][-1]), "alpha": ALPHA, "rmax": RMAX,
+                       "sources": "half uniform over vertices with out-edges, half from the top 1% out-degree",
+                       "l2": "graph and state larger than L2 (no flush needed)",
                        "parallelism": "replicas (query-sharded)" if world > 1 else "single GPU"},
-            "e2e": {"value": e2e, "unit": "queries/s", "h2d_bytes_per_step": 0,
-                    "d2h_bytes_per_step": 4 * V * q_step + 4 * V * nP},
-            "gpu_launches": 2 * q_step * args.steps,
+            "e2e": {"value": e2e, "unit": "queries/s", "h2d_bytes_per_step": 4 * q_step,
+                    "d2h_bytes_per_step": 4 * V * q_step},
+            "gpu_launches": 4 * args.steps,
             "roofline": {"bound": "hbm", "kernel": kernel_name, "achieved": achieved, "peak": peak,
                          "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak, "traffic": None},
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
             "detail": {
-                "sssp_ms_per_query": tot["sssp_ms"] / (nS * args.steps),
-                "ppr_ms_per_query": tot["ppr_ms"] / (nP * args.steps),
-                "sssp_gteps_relaxed": tot["sssp_edges"] / (tot["sssp_ms"] / 1000.0) / 1e9,
-                "ppr_gteps_pushed": tot["ppr_edges"] / (tot["ppr_ms"] / 1000.0) / 1e9,
-                "sssp_gteps_graph500_sample": gteps_sample,
-                "sssp_rounds_per_query": tot["sssp_iters"] / (nS * args.steps),
-                "ppr_rounds_per_query": tot["ppr_iters"] / (nP * args.steps),
-                "sssp_alg_gbs": tot["sssp_bytes"] / (tot["sssp_ms"] / 1000.0) / 1e9,
-                "ppr_alg_gbs": tot["ppr_bytes"] / (tot["ppr_ms"] / 1000.0) / 1e9,
-                "kernel_share_sssp": tot["sssp_ms"] / (tot["sssp_ms"] + tot["ppr_ms"]),
+                "batched_vs_per_query": value / per_query_qps,
+                "per_query_qps": per_query_qps,
+                "per_query_sssp_ms": ms_sssp_pq, "per_query_ppr_ms": ms_ppr_pq,
+                "batched_sssp_ms_per_step": tot["s_ms"] / args.steps,
+                "batched_ppr_ms_per_step": tot["p_ms"] / args.steps,
+                "sssp_batched_gteps_graph500": gteps_batched,
+                "sssp_relaxations_per_s": tot["s_rel"] / (tot["s_ms"] / 1000.0),
+                "ppr_pushes_per_s": tot["p_push"] / (tot["p_ms"] / 1000.0),
+                "sssp_rounds": tot["s_it"] / args.steps, "ppr_rounds": tot["p_it"] / args.steps,
+                "sssp_alg_gbs": tot["s_bytes"] / (tot["s_ms"] / 1000.0) / 1e9,
+                "ppr_alg_gbs": tot["p_bytes"] / (tot["p_ms"] / 1000.0) / 1e9,
                 "gen_s": gen_s, "prune_s": prune_s, "wall_s_device_run": wall_dev, "wall_s_e2e_run": wall_e2e,
             },
         }
@@ -334,6 +343,19 @@ def run_ours(args, rank, world, local_rank):
     gp.close()
     if dist_on:
         tdist.destroy_process_group()
+
+
+def _ppr_into(gp, src, prm, out):
+    """Batched PPR with results copied into the caller's (pinned) host array."""
+    import ctypes
+
+    import c2g
+
+    st = c2g.Stats()
+    s = np.ascontiguousarray(src, dtype=np.int32)
+    c2g._check(c2g.lib().c2g_ppr_batch(gp._h, len(s), c2g._ptr(s), ctypes.byref(prm), c2g._ptr(out), None, 0, 0,
+                                       ctypes.byref(st)))
+    return None, None, st
 
 
 def main():
@@ -345,8 +367,9 @@ def main():
     ap.add_argument("--scale", type=int, default=22)
     ap.add_argument("--edge-factor", type=int, default=16)
     ap.add_argument("--seed", type=int, default=2)
-    ap.add_argument("--sssp-per-step", type=int, default=16)
-    ap.add_argument("--ppr-per-step", type=int, default=16)
+    ap.add_argument("--sssp-per-step", type=int, default=256)
+    ap.add_argument("--ppr-per-step", type=int, default=256)
+    ap.add_argument("--per-query-sample", type=int, default=8)
     ap.add_argument("--delta", type=int, default=0)
     ap.add_argument("--tile", type=int, default=256)
     ap.add_argument("--cpu-sample", type=int, default=2)

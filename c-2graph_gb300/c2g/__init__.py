@@ -99,6 +99,8 @@ SIGNATURES = {
     "c2g_sssp_set_config": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32]),
     "c2g_sssp_noalloc": (ctypes.c_int, [_P, _P, ctypes.c_int32, ctypes.c_int64, ctypes.c_int32, _P, _P,
                                         ctypes.POINTER(Stats)]),
+    "c2g_sssp_autotune": (ctypes.c_int, [_P, ctypes.c_int32, _P, ctypes.c_int, ctypes.c_int, ctypes.c_char_p,
+                                         _I32P, _I32P]),
     "c2g_sssp_batch": (ctypes.c_int, [_P, ctypes.c_int32, _P, ctypes.c_int, ctypes.c_int, _P, ctypes.c_int,
                                       ctypes.c_int, ctypes.POINTER(Stats)]),
     "c2g_ppr": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.POINTER(PprParams), _P, _P, ctypes.c_int,
@@ -236,6 +238,15 @@ class Graph:
 
     def sssp_config(self, delta=0, tile=256, max_iter=1 << 20):
         _check(lib().c2g_sssp_set_config(self._h, delta, tile, max_iter))
+
+    def sssp_autotune(self, sources, seeds=False, mode=SEEDS_COMPAT, json_path=None):
+        """Pick the fastest (delta, tile) for this graph; returns (delta, tile)."""
+        src = np.ascontiguousarray(sources, dtype=np.int32)
+        bd, bt = ctypes.c_int32(), ctypes.c_int32()
+        _check(lib().c2g_sssp_autotune(self._h, len(src), _ptr(src), int(seeds), mode,
+                                       os.fsencode(json_path) if json_path else None, ctypes.byref(bd),
+                                       ctypes.byref(bt)))
+        return bd.value, bt.value
 
     def resolve_source(self, source, pruned=False, mode=SEEDS_COMPAT):
         out = ctypes.c_int32()

@@ -49,7 +49,7 @@ struct BatchParams {
     long long* counters;  // [2]: relaxations (query, edge), edge-word steps
 };
 
-constexpr int kBatchTileLog = 5;  // 32 edge-word steps per warp tile
+constexpr int kBatchTileLog = 7;  // 128 edge-word steps per warp tile
 
 __device__ __forceinline__ FrontierOut batch_out(const BatchParams& p, int buf, int slot) {
     FrontierOut o;
@@ -129,7 +129,8 @@ __global__ void __launch_bounds__(512, 2) sssp_batch_persistent(const BatchParam
                         const unsigned slot = (unsigned)(old >> 32), base = (unsigned)old;
                         if (slot < out.cap) {
                             out.q[slot] = make_int2((sv << p.logW) + w, (int)base);
-                            const unsigned t0 = (base + 31u) >> kBatchTileLog, t1 = (base + sd - 1) >> kBatchTileLog;
+                            const unsigned t0 = (base + (1u << kBatchTileLog) - 1u) >> kBatchTileLog,
+                                           t1 = (base + sd - 1) >> kBatchTileLog;
                             for (unsigned t = t0; t <= t1 && t < out.mark_cap; ++t) out.mark[t] = (int)slot;
                         } else {
                             atomicOr(flags, C2G_FLAG_QUEUE_OVERFLOW);
@@ -153,7 +154,7 @@ __global__ void __launch_bounds__(512, 2) sssp_batch_persistent(const BatchParam
             break;
         }
         const int buf = cur & 1;
-        if (F > p.qcap || ((T + 31u) >> kBatchTileLog) > p.mark_cap) {
+        if (F > p.qcap || ((T + (1u << kBatchTileLog) - 1u) >> kBatchTileLog) > p.mark_cap) {
             if (gtid == 0) atomicOr(flags, C2G_FLAG_BOUNDS);
             break;
         }
@@ -171,17 +172,21 @@ __global__ void __launch_bounds__(512, 2) sssp_batch_persistent(const BatchParam
         }
         if (!grid_sync(bar, flags, p.barrier_ns)) return;
 
-        // Phase 2: expand.
+        // Phase 2: expand.  Warps take tiles of edge-word steps; inside a tile they walk
+        // owner runs: the owner's row of distances is read once, then each of its edges
+        // is one uniform (broadcast) edge load and one 128-byte target-row read for the
+        // 32 queries of the word, four edges in flight.
         const FrontierOut nout = batch_out(p, (cur + 1) & 1, (cur + 1) % 3);
         const int2* q = p.q[buf];
         const unsigned* qm = p.qmask[buf];
         const int* mark = p.mark[buf];
-        const unsigned ntiles = (T + 31u) >> kBatchTileLog;
+        const unsigned tile = 1u << kBatchTileLog;
+        const unsigned ntiles = (T + tile - 1) >> kBatchTileLog;
+        int npend = 0, pv = 0, pd = 0;  // pending appends, one per lane (warp-uniform count)
         for (unsigned t = gwarp; t < ntiles; t += nwarps) {
             unsigned e0 = t << kBatchTileLog;
-            const unsigned e1 = min(e0 + 32u, T);
+            const unsigned e1 = min(e0 + tile, T);
             unsigned o = (unsigned)ldcg(mark + t);
-            int prev_ovw = -1, prev_du = 0;
             while (e0 < e1) {
                 const unsigned j = o + (unsigned)lane;
                 unsigned base = 0x7fffffffu, endv = 0xffffffffu, msk = 0u;
@@ -196,73 +201,75 @@ __global__ void __launch_bounds__(512, 2) sssp_batch_persistent(const BatchParam
                     msk = ldcg(qm + j);
                 }
                 const unsigned seg_end = min(e1, (unsigned)__shfl_sync(kFull, endv, 31));
-                if (seg_end <= e0 || o >= F) {
+                if (seg_end <= e0 || o >= F || (unsigned)__shfl_sync(kFull, (int)base, 0) > e0) {
                     if (lane == 0) atomicOr(flags, C2G_FLAG_BOUNDS);
                     break;
                 }
-                // Lane = edge: load this lane's edge and its target's degree.
-                const unsigned e = e0 + (unsigned)lane;
-                const int k = owner_lane(base, e);
-                const unsigned srs = (unsigned)__shfl_sync(kFull, rs, k);
-                const unsigned sb = (unsigned)__shfl_sync(kFull, (int)base, k);
-                const int svw = __shfl_sync(kFull, vw, k);
-                const unsigned smsk = (unsigned)__shfl_sync(kFull, (int)msk, k);
-                const unsigned idx = srs + (e - sb);
-                const bool ok = e < seg_end && sb <= e && idx < p.E;
-                if (e < seg_end && !ok) atomicOr(flags, C2G_FLAG_BOUNDS);
-                int tc = 0, tw = 0, tdeg = 0;
-                if (ok) {
-                    const int2 ew = __ldg(p.adj + idx);
-                    tc = ew.x;
-                    tw = ew.y;
-                    tdeg = __ldg(p.row + tc + 1) - __ldg(p.row + tc);
-                }
-                // Lane = query: walk the segment's edges, four at a time so that four
-                // target-row reads are in flight; the owner's row is read once per owner.
-                const int nseg = (int)(seg_end - e0);
-                bool pend = false;
-                for (int j0 = 0; j0 < nseg; j0 += 4) {
-                    int c[4], wt[4], cdeg[4], w[4], nd[4];
-                    bool active[4];
+                for (int k = 0; k < 32; ++k) {
+                    const unsigned kb = (unsigned)__shfl_sync(kFull, (int)base, k);
+                    if (kb >= seg_end) break;
+                    const unsigned ke = (unsigned)__shfl_sync(kFull, (int)endv, k);
+                    const unsigned lo = max(e0, kb), hi = min(seg_end, ke);
+                    if (lo >= hi) continue;
+                    const int kvw = __shfl_sync(kFull, vw, k);
+                    const unsigned km = (unsigned)__shfl_sync(kFull, (int)msk, k);
+                    const unsigned krs = (unsigned)__shfl_sync(kFull, rs, k);
+                    const int w = kvw & (W - 1);
+                    const size_t lane_off = ((size_t)w << 5) + lane;
+                    const bool act = (km >> lane) & 1u;
+                    // L2-coherent: the owner improved in the previous round.
+                    const int du = ldcg(p.dist + (size_t)(kvw >> p.logW) * p.Q + lane_off);
+                    for (unsigned eb = lo; eb < hi; eb += 4) {
+                        int2 ew[4];
+                        int cur[4];
 #pragma unroll
-                    for (int k = 0; k < 4; ++k) {
-                        const int jj = (j0 + k) & 31;
-                        c[k] = __shfl_sync(kFull, tc, jj);
-                        wt[k] = __shfl_sync(kFull, tw, jj);
-                        cdeg[k] = __shfl_sync(kFull, tdeg, jj);
-                        const int ovw = __shfl_sync(kFull, svw, jj);
-                        const unsigned om = (unsigned)__shfl_sync(kFull, (int)smsk, jj);
-                        w[k] = ovw & (W - 1);
-                        active[k] = (j0 + k < nseg) && ((om >> lane) & 1u);
-                        if (ovw != prev_ovw) {  // L2-coherent: the owner improved last round
-                            prev_ovw = ovw;
-                            prev_du = ldcg(p.dist + (size_t)(ovw >> p.logW) * p.Q + (w[k] << 5) + lane);
+                        for (int jj = 0; jj < 4; ++jj) {
+                            const unsigned e = eb + jj;
+                            const unsigned idx = krs + (e - kb);
+                            const bool in = e < hi && idx < p.E;
+                            ew[jj] = in ? __ldg(p.adj + idx) : make_int2(0, 0);
+                            if (e < hi && !in && lane == 0) atomicOr(flags, C2G_FLAG_BOUNDS);
                         }
-                        nd[k] = prev_du + wt[k];
-                    }
-                    int cur[4];
 #pragma unroll
-                    for (int k = 0; k < 4; ++k)
-                        cur[k] = active[k] ? ldcg(p.dist + (size_t)c[k] * p.Q + (w[k] << 5) + lane) : INT_MIN;
+                        for (int jj = 0; jj < 4; ++jj)
+                            cur[jj] = (eb + jj < hi && act) ? ldcg(p.dist + (size_t)ew[jj].x * p.Q + lane_off) : INT_MIN;
 #pragma unroll
-                    for (int k = 0; k < 4; ++k) {
-                        bool imp = false;
-                        if (nd[k] < cur[k]) imp = atomicMin(p.dist + (size_t)c[k] * p.Q + (w[k] << 5) + lane, nd[k]) > nd[k];
-                        relax += active[k];
-                        const unsigned bits = __ballot_sync(kFull, imp);
-                        bool first = false;
-                        if (lane == 0 && bits && cdeg[k] > 0) first = mark_improved(p, c[k], w[k], bits);
-                        first = __shfl_sync(kFull, (int)first, 0) != 0;
-                        if (lane == j0 + k) pend = first;
+                        for (int jj = 0; jj < 4; ++jj) {
+                            const int nd = du + ew[jj].y;
+                            bool imp = false;
+                            if (nd < cur[jj]) imp = atomicMin(p.dist + (size_t)ew[jj].x * p.Q + lane_off, nd) > nd;
+                            relax += (eb + jj < hi && act);
+                            const unsigned bits = __ballot_sync(kFull, imp);
+                            if (bits) {  // rare path: mark (target, word), first setter appends
+                                const int c = ew[jj].x;
+                                int first = 0, cdeg = 0;
+                                if (lane == 0) {
+                                    cdeg = __ldg(p.row + c + 1) - __ldg(p.row + c);
+                                    first = cdeg > 0 && mark_improved(p, c, w, bits);
+                                }
+                                first = __shfl_sync(kFull, first, 0);
+                                if (first) {
+                                    cdeg = __shfl_sync(kFull, cdeg, 0);
+                                    if (lane == npend) {
+                                        pv = (c << p.logW) + w;
+                                        pd = cdeg;
+                                    }
+                                    if (++npend == 32) {
+                                        stage_push(fst, nout, true, pv, pd, 0.f);
+                                        npend = 0;
+                                    }
+                                }
+                            }
+                        }
                     }
+                    steps += hi - lo;
                 }
-                steps += nseg;
-                const int tv = (tc << p.logW) + (svw & (W - 1));
-                stage_push(fst, nout, pend, tv, tdeg, 0.f);
                 e0 = seg_end;
                 o += 32;
             }
         }
+        stage_push(fst, nout, lane < npend, pv, pd, 0.f);
+        npend = 0;
         stage_flush(fst, nout);
         if (!grid_sync(bar, flags, p.barrier_ns)) return;
         ++cur;
@@ -645,7 +652,7 @@ __global__ void __launch_bounds__(512, 2) ppr_batch_persistent(const PprBatchPar
             if (((unsigned)dv.y >> lane) & 1u) p.res[off] = 0.f;
         }
         if (F == 0) break;
-        if (F > p.qcap || ((T + 31u) >> kBatchTileLog) > p.mark_cap) {
+        if (F > p.qcap || ((T + (1u << kBatchTileLog) - 1u) >> kBatchTileLog) > p.mark_cap) {
             if (gtid == 0) atomicOr(flags, C2G_FLAG_BOUNDS);
             break;
         }
@@ -657,15 +664,17 @@ __global__ void __launch_bounds__(512, 2) ppr_batch_persistent(const PprBatchPar
             ctl->popped += F;
             ctl->relaxed += T;
         }
-        // Phase A: push along the frontier's edges.
+        // Phase A: push along the frontier's edges (owner runs, as in the SSSP batch).
         {
             const int2* q = p.q[buf];
             const unsigned* qm = p.qmask[buf];
             const int* mark = p.mark[buf];
-            const unsigned ntiles = (T + 31u) >> kBatchTileLog;
+            const unsigned tile = 1u << kBatchTileLog;
+            const unsigned ntiles = (T + tile - 1) >> kBatchTileLog;
+            int npend = 0, pv = 0;
             for (unsigned t = gwarp; t < ntiles; t += nwarps) {
                 unsigned e0 = t << kBatchTileLog;
-                const unsigned e1 = min(e0 + 32u, T);
+                const unsigned e1 = min(e0 + tile, T);
                 unsigned o = (unsigned)ldcg(mark + t);
                 while (e0 < e1) {
                     const unsigned j = o + (unsigned)lane;
@@ -681,59 +690,62 @@ __global__ void __launch_bounds__(512, 2) ppr_batch_persistent(const PprBatchPar
                         msk = ldcg(qm + j);
                     }
                     const unsigned seg_end = min(e1, (unsigned)__shfl_sync(kFull, endv, 31));
-                    if (seg_end <= e0 || o >= F) {
+                    if (seg_end <= e0 || o >= F || (unsigned)__shfl_sync(kFull, (int)base, 0) > e0) {
                         if (lane == 0) atomicOr(flags, C2G_FLAG_BOUNDS);
                         break;
                     }
-                    const unsigned e = e0 + (unsigned)lane;
-                    const int k = owner_lane(base, e);
-                    const unsigned srs = (unsigned)__shfl_sync(kFull, rs, k);
-                    const unsigned sb = (unsigned)__shfl_sync(kFull, (int)base, k);
-                    const int svw = __shfl_sync(kFull, vw, k);
-                    const unsigned smsk = (unsigned)__shfl_sync(kFull, (int)msk, k);
-                    const unsigned idx = srs + (e - sb);
-                    const bool ok = e < seg_end && sb <= e && idx < p.E;
-                    if (e < seg_end && !ok) atomicOr(flags, C2G_FLAG_BOUNDS);
-                    int tc = 0;
-                    float tf = 0.f;
-                    if (ok) {
-                        const int2 ew = __ldg(p.adj + idx);
-                        tc = ew.x;
-                        tf = __int_as_float(ew.y);
-                    }
-                    const int nseg = (int)(seg_end - e0);
-                    bool pend = false;
-                    int prev_u = -1;
-                    float qu = 0.f;
-                    for (int jj = 0; jj < nseg; ++jj) {
-                        const int cidx = __shfl_sync(kFull, tc, jj);
-                        const float f = __shfl_sync(kFull, tf, jj);
-                        const int ovw = __shfl_sync(kFull, svw, jj);
-                        const unsigned om = (unsigned)__shfl_sync(kFull, (int)smsk, jj);
-                        const int w = ovw & (W - 1);
-                        const bool active = (om >> lane) & 1u;
-                        if (ovw != prev_u) {  // (1-alpha)*r_u of this lane's query
-                            prev_u = ovw;
-                            qu = active ? one_m_a * ldcg(p.rq + (size_t)(ovw >> p.logW) * p.Q + (w << 5) + lane)
-                                        : 0.f;
+                    for (int k = 0; k < 32; ++k) {
+                        const unsigned kb = (unsigned)__shfl_sync(kFull, (int)base, k);
+                        if (kb >= seg_end) break;
+                        const unsigned ke = (unsigned)__shfl_sync(kFull, (int)endv, k);
+                        const unsigned lo = max(e0, kb), hi = min(seg_end, ke);
+                        if (lo >= hi) continue;
+                        const int kvw = __shfl_sync(kFull, vw, k);
+                        const unsigned km = (unsigned)__shfl_sync(kFull, (int)msk, k);
+                        const unsigned krs = (unsigned)__shfl_sync(kFull, rs, k);
+                        const int w = kvw & (W - 1);
+                        const size_t lane_off = ((size_t)w << 5) + lane;
+                        const bool act = (km >> lane) & 1u;
+                        // (1-alpha)*r_u of this lane's query (src/ppr/purn/Main.cu:288)
+                        const float qu = act ? one_m_a * ldcg(p.rq + (size_t)(kvw >> p.logW) * p.Q + lane_off) : 0.f;
+                        for (unsigned eb = lo; eb < hi; eb += 4) {
+                            int2 ew[4];
+#pragma unroll
+                            for (int jj = 0; jj < 4; ++jj) {
+                                const unsigned e = eb + jj;
+                                const unsigned idx = krs + (e - kb);
+                                const bool in = e < hi && idx < p.E;
+                                ew[jj] = in ? __ldg(p.adj + idx) : make_int2(0, 0);
+                                if (e < hi && !in && lane == 0) atomicOr(flags, C2G_FLAG_BOUNDS);
+                            }
+#pragma unroll
+                            for (int jj = 0; jj < 4; ++jj) {
+                                const float m = qu * __int_as_float(ew[jj].y);
+                                const bool send = (eb + jj < hi) && act && m >= 1.17549435e-38f;
+                                if (send) atomicAdd(p.msg + (size_t)ew[jj].x * p.Q + lane_off, m);
+                                pushes += send;
+                                const unsigned bits = __ballot_sync(kFull, send);
+                                if (bits) {  // first message of (target, word) this round appends it
+                                    int first = 0;
+                                    if (lane == 0)
+                                        first = atomicOr(p.tmask + ((size_t)ew[jj].x << p.logW) + w, bits) == 0u;
+                                    if (__shfl_sync(kFull, first, 0)) {
+                                        if (lane == npend) pv = (ew[jj].x << p.logW) + w;
+                                        if (++npend == 32) {
+                                            list_stage_push(tst, p.touched, &ctl->listctr[slot], p.qcap, flags, true, pv);
+                                            npend = 0;
+                                        }
+                                    }
+                                }
+                            }
                         }
-                        const float m = qu * f;
-                        const bool send = active && m >= 1.17549435e-38f;
-                        if (send) atomicAdd(p.msg + (size_t)cidx * p.Q + (w << 5) + lane, m);
-                        pushes += send;
-                        const unsigned bits = __ballot_sync(kFull, send);
-                        bool first = false;
-                        if (lane == 0 && bits) first = atomicOr(p.tmask + ((size_t)cidx << p.logW) + w, bits) == 0u;
-                        first = __shfl_sync(kFull, (int)first, 0) != 0;
-                        if (lane == jj) pend = first;
+                        steps += hi - lo;
                     }
-                    steps += nseg;
-                    list_stage_push(tst, p.touched, &ctl->listctr[slot], p.qcap, flags, pend,
-                                    (tc << p.logW) + (svw & (W - 1)));
                     e0 = seg_end;
                     o += 32;
                 }
             }
+            list_stage_push(tst, p.touched, &ctl->listctr[slot], p.qcap, flags, lane < npend, pv);
             list_stage_flush(tst, p.touched, &ctl->listctr[slot], p.qcap, flags);
         }
         if (!grid_sync(bar, flags, p.barrier_ns)) return;

@@ -181,6 +181,13 @@ int c2g_sssp_noalloc(const int32_t* row, const void* adj, int32_t V, int64_t E, 
 int c2g_sssp_batch(c2g_graph* g, int32_t n, const int32_t* sources, int use_seeds, int seed_mode,
                    int32_t* dist, int dist_on_device, int layout, c2g_stats* stats);
 
+/* Autotuner: time every (delta, tile) candidate of the SSSP kernel on the sample
+ * sources (distances must agree across candidates), apply the fastest to the handle,
+ * return it, and write every timing as JSON to json_path (may be NULL).  The reference's
+ * launch geometry is fixed at compile time (core/Util.cuh:31-34). */
+int c2g_sssp_autotune(c2g_graph* g, int32_t n, const int32_t* sources, int use_seeds, int seed_mode,
+                      const char* json_path, int32_t* best_delta, int32_t* best_tile);
+
 /* ---- PPR / adsorption push ------------------------------------------------------- */
 /* Forward push.  Replaces calcuatePPR (src/ppr/base/Main.cu:122-395,
  * src/ppr/purn/Main.cu:149-428, src/adsorption/w-base/Main.cu:124-395) and the seed

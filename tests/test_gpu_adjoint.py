@@ -114,7 +114,9 @@ def test_adjoint_autograd_function(gpu_available, g12):
     loss = PPRScore.apply(w0)
     (gw,) = torch.autograd.grad(loss, w0)
     grad_direct, _, _, L, _ = g.ppr_adjoint(s, targets, prm, rmax_backward=EPS)
-    assert np.allclose(gw.numpy(), grad_direct, rtol=0, atol=0)
+    # two adjoint runs agree up to FP32 atomic summation order
+    rel = np.linalg.norm(gw.numpy() - grad_direct) / np.linalg.norm(grad_direct)
+    assert rel <= 1e-5, rel
     assert abs(loss.item() - L) <= 1e-6
     # a small step along the gradient raises the loss by about |g|^2 * step
     step = 1e-3 / float(np.linalg.norm(grad_direct))

@@ -242,3 +242,24 @@ def test_sssp_stress_mixed_configs(gpu_available, tmp_path_factory):
                     bad = int((dist != refs[s]).sum())
                     assert bad == 0, (rep, delta, tile, s, bad, int((dist > refs[s]).sum()))
                     assert st.status_flags == 0
+
+
+def test_sssp_autotune(gpu_available, rmat16, tmp_path):
+    import json
+
+    import c2g
+    import oracle
+
+    o = oracle.load_dataset(rmat16, "origin")
+    deg = np.diff(o["vlist"])
+    srcs = [int(np.argmax(deg)), int(np.flatnonzero(deg > 0)[3])]
+    with c2g.Graph.load(rmat16, "origin") as gr:
+        path = str(tmp_path / "tune.json")
+        delta, tile = gr.sssp_autotune(srcs, json_path=path)
+        rec = json.load(open(path))
+        assert rec["best"]["delta"] == delta and rec["best"]["tile"] == tile
+        assert all(c["valid"] for c in rec["candidates"])
+        assert len(rec["candidates"]) == 40
+        ref = oracle.dijkstra(o["vlist"], o["elist"], o["wlist"], [srcs[0]], [0])
+        d, _ = gr.sssp(srcs[0])  # the tuned configuration is applied
+        assert np.array_equal(d, ref)
