@@ -103,14 +103,19 @@ int build_reverse_graph(c2g_graph* g) {
     if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
     cudaFree(indeg);
     C2G_CUDA(e);
-    return C2G_OK;
+    int rc = build_markers(g, g->row_r, &g->mark_r);
+    if (!rc) rc = build_markers(g, g->row, &g->mark_f);
+    return rc;
 }
 
 void adjoint_free(c2g_graph* g) {
-    if (g->row_r) cudaFree(g->row_r);
-    if (g->adj_r) cudaFree(g->adj_r);
+    void* ptrs[] = {g->row_r, g->adj_r, g->mark_r, g->mark_f};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
     g->row_r = nullptr;
     g->adj_r = nullptr;
+    g->mark_r = nullptr;
+    g->mark_f = nullptr;
 }
 
 int set_float_weights(c2g_graph* g, const float* w, int on_device);
@@ -188,8 +193,8 @@ extern "C" int c2g_ppr_adjoint(c2g_graph* g, int32_t source, const c2g_ppr_param
     c2g_ppr_params fp = *params;
     fp.r0 = 1.0f;
     fp.pr0 = fp.alpha;
-    rc = ppr_launch_view(g, g->row, g->adj_f, source, fp, fp.alpha, 0, nullptr, nullptr, nullptr, nullptr, 0, pi,
-                         nullptr, &ms_f);
+    rc = ppr_launch_view(g, g->row, g->adj_f, g->row_r, g->adj_r, g->mark_r, source, fp, fp.alpha, 0, nullptr,
+                         nullptr, nullptr, nullptr, 0, pi, nullptr, &ms_f);
     if (!rc && (cudaMemcpyAsync(&cf, g->ppr.ctl, sizeof(cf), cudaMemcpyDeviceToHost, g->stream) != cudaSuccess ||
                 cudaStreamSynchronize(g->stream) != cudaSuccess))
         rc = fail(C2G_ERR_CUDA, "adjoint: reading the forward push status failed");
@@ -197,8 +202,8 @@ extern "C" int c2g_ppr_adjoint(c2g_graph* g, int32_t source, const c2g_ppr_param
     c2g_ppr_params bp = *params;
     bp.rmax = rmax_backward;
     if (!rc)
-        rc = ppr_launch_view(g, g->row_r, g->adj_r, tv[0], bp, 1.0f, (int32_t)tv.size(), dtv, dtr, nullptr, nullptr, 0,
-                             lam, nullptr, &ms_b);
+        rc = ppr_launch_view(g, g->row_r, g->adj_r, g->row, g->adj_f, g->mark_f, tv[0], bp, 1.0f, (int32_t)tv.size(),
+                             dtv, dtr, nullptr, nullptr, 0, lam, nullptr, &ms_b);
     if (!rc && (cudaMemcpyAsync(&cb, g->ppr.ctl, sizeof(cb), cudaMemcpyDeviceToHost, g->stream) != cudaSuccess ||
                 cudaStreamSynchronize(g->stream) != cudaSuccess))
         rc = fail(C2G_ERR_CUDA, "adjoint: reading the backward push status failed");

@@ -209,6 +209,8 @@ int graph_view(c2g_graph* base, c2g_graph** out) {
     g->adj_f = base->adj_f;
     g->row_r = base->row_r;
     g->adj_r = base->adj_r;
+    g->mark_r = base->mark_r;
+    g->mark_f = base->mark_f;
     g->R = base->R;
     g->H = base->H;
     g->hv = base->hv;
@@ -386,6 +388,14 @@ int c2g_sssp_set_config(c2g_graph* g, int32_t delta, int32_t tile, int32_t max_i
     g->sssp_cfg.delta = delta > 0 ? delta : 0;
     g->sssp_cfg.log_tile = lt;
     g->sssp_cfg.max_iter = max_iter;
+    return C2G_OK;
+}
+
+int c2g_ppr_set_config(c2g_graph* g, int32_t pull_div) {
+    if (!g) return fail(C2G_ERR_ARG, "graph is NULL");
+    if (pull_div < 0) return fail(C2G_ERR_ARG, "pull_div must be >= 0");
+    std::lock_guard<std::mutex> lk(g->mu);
+    g->ppr_cfg.pull_div = pull_div;
     return C2G_OK;
 }
 
@@ -587,7 +597,7 @@ int c2g_ppr(c2g_graph* g, int32_t source, const c2g_ppr_params* params, float* p
     if (!on_device) {
         C2G_CUDA(cudaMemcpyAsync(pr, g->ppr.pr, sizeof(float) * (size_t)g->V, cudaMemcpyDeviceToHost, g->stream));
         if (res)
-            C2G_CUDA(cudaMemcpyAsync(res, g->ppr.res, sizeof(float) * (size_t)g->V, cudaMemcpyDeviceToHost, g->stream));
+            C2G_CUDA(cudaMemcpyAsync(res, g->ppr.res_f, sizeof(float) * (size_t)g->V, cudaMemcpyDeviceToHost, g->stream));
     }
     return stats_fill(g, g->ppr.ctl, source, ms, true, stats);
 }

@@ -470,9 +470,9 @@ struct PprBatchParams {
     int V;
     int logW, Q, nq;
     float* pr;        // [V][Q]
-    float* res;       // [V][Q]
-    float* msg;       // [V][Q], zero between launches
-    float* rq;        // [V][Q]
+    double* res;      // [V][Q] FP64 residuals (see ppr.cu: threshold decisions)
+    double* msg;      // [V][Q], zero between launches
+    double* rq;       // [V][Q] residual being pushed
     unsigned* tmask;  // [V][W] touched lanes this round, zero between rounds
     int2* q[2];       // frontier entries (v*W + w, edge base)
     unsigned* qmask[2];
@@ -516,17 +516,17 @@ __device__ __forceinline__ void pbatch_apply(const PprBatchParams& p, int vw, un
     const int deg = __ldg(p.row + v + 1) - __ldg(p.row + v);
     bool act = false;
     if (mine) {
-        float r = ldcg(p.res + off);
+        double r = ldcg(p.res + off);
         if (!force) {
             r += ldcg(p.msg + off);
-            p.msg[off] = 0.f;
+            p.msg[off] = 0.0;
         }
-        if (force || r > p.rmax) {
-            if (!force) p.pr[off] = ldcg(p.pr + off) + p.alpha * r;
+        if (force || r > (double)p.rmax) {
+            if (!force) p.pr[off] = ldcg(p.pr + off) + (float)((double)p.alpha * r);
             act = true;
             if (deg > 0) {
                 p.rq[off] = r;
-                p.res[off] = 0.f;
+                p.res[off] = 0.0;
             } else {
                 p.res[off] = r;  // popped (zeroed) at the top of the next round
             }
@@ -558,17 +558,19 @@ __global__ void __launch_bounds__(512, 2) ppr_batch_persistent(const PprBatchPar
     const int wib = threadIdx.x >> 5;
     WarpStage fst{sm.v0[wib], sm.d0[wib], sm.x0[wib], 0};
     WarpStage tst{sm.v1[wib], nullptr, nullptr, 0};
-    const float one_m_a = 1.0f - p.alpha;
+    const double one_m_a = 1.0 - (double)p.alpha;
 
     // Init: pr = res = 0 (msg and tmask are zero between launches).
     {
         const size_t n4 = ((size_t)p.V * (size_t)p.Q) >> 2;
         float4* a4 = reinterpret_cast<float4*>(p.pr);
-        float4* b4 = reinterpret_cast<float4*>(p.res);
+        double2* b2 = reinterpret_cast<double2*>(p.res);
         const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+        const double2 zd = make_double2(0.0, 0.0);
         for (size_t i = gtid; i < n4; i += nthreads) {
             a4[i] = z;
-            b4[i] = z;
+            b2[2 * i] = zd;
+            b2[2 * i + 1] = zd;
         }
     }
     if (!grid_sync(bar, flags, p.barrier_ns)) return;
@@ -580,7 +582,7 @@ __global__ void __launch_bounds__(512, 2) ppr_batch_persistent(const PprBatchPar
         const unsigned bit = 1u << (qi & 31);
         if (!p.seeded) {
             atomicAdd(p.pr + (size_t)s * p.Q + qi, p.pr0);
-            atomicAdd(p.res + (size_t)s * p.Q + qi, p.r0);
+            atomicAdd(p.res + (size_t)s * p.Q + qi, (double)p.r0);
             if (atomicOr(p.tmask + ((size_t)s << p.logW) + w, bit) == 0u) {
                 const unsigned slot = atomicAdd(&ctl->listctr[0], 1u);
                 if (slot < p.qcap) p.touched[slot] = (s << p.logW) + w;
@@ -600,8 +602,8 @@ __global__ void __launch_bounds__(512, 2) ppr_batch_persistent(const PprBatchPar
                     v = ew.x;
                     wt = __int_as_float(ew.y);
                 }
-                atomicAdd(p.pr + (size_t)v * p.Q + qi, (one_m_a * p.alpha) * wt);
-                atomicAdd(p.res + (size_t)v * p.Q + qi, one_m_a * wt);
+                atomicAdd(p.pr + (size_t)v * p.Q + qi, (float)(one_m_a * (double)p.alpha * (double)wt));
+                atomicAdd(p.res + (size_t)v * p.Q + qi, one_m_a * (double)wt);
                 if (atomicOr(p.tmask + ((size_t)v << p.logW) + w, bit) == 0u) {
                     const unsigned slot = atomicAdd(&ctl->listctr[0], 1u);
                     if (slot < p.qcap) p.touched[slot] = (v << p.logW) + w;
@@ -649,7 +651,7 @@ __global__ void __launch_bounds__(512, 2) ppr_batch_persistent(const PprBatchPar
         for (unsigned j = gwarp; j < D; j += nwarps) {
             const int2 dv = ldcg(p.dangle + j);
             const size_t off = (size_t)(dv.x >> p.logW) * p.Q + ((dv.x & (W - 1)) << 5) + lane;
-            if (((unsigned)dv.y >> lane) & 1u) p.res[off] = 0.f;
+            if (((unsigned)dv.y >> lane) & 1u) p.res[off] = 0.0;
         }
         if (F == 0) break;
         if (F > p.qcap || ((T + (1u << kBatchTileLog) - 1u) >> kBatchTileLog) > p.mark_cap) {
@@ -707,7 +709,7 @@ __global__ void __launch_bounds__(512, 2) ppr_batch_persistent(const PprBatchPar
                         const size_t lane_off = ((size_t)w << 5) + lane;
                         const bool act = (km >> lane) & 1u;
                         // (1-alpha)*r_u of this lane's query (src/ppr/purn/Main.cu:288)
-                        const float qu = act ? one_m_a * ldcg(p.rq + (size_t)(kvw >> p.logW) * p.Q + lane_off) : 0.f;
+                        const double qu = act ? one_m_a * ldcg(p.rq + (size_t)(kvw >> p.logW) * p.Q + lane_off) : 0.0;
                         for (unsigned eb = lo; eb < hi; eb += 4) {
                             int2 ew[4];
 #pragma unroll
@@ -720,8 +722,8 @@ __global__ void __launch_bounds__(512, 2) ppr_batch_persistent(const PprBatchPar
                             }
 #pragma unroll
                             for (int jj = 0; jj < 4; ++jj) {
-                                const float m = qu * __int_as_float(ew[jj].y);
-                                const bool send = (eb + jj < hi) && act && m >= 1.17549435e-38f;
+                                const double m = qu * (double)__int_as_float(ew[jj].y);
+                                const bool send = (eb + jj < hi) && act && m > 0.0;
                                 if (send) atomicAdd(p.msg + (size_t)ew[jj].x * p.Q + lane_off, m);
                                 pushes += send;
                                 const unsigned bits = __ballot_sync(kFull, send);
@@ -791,11 +793,27 @@ __global__ void batch_transpose_f(const float* __restrict__ src, int V, int Q, i
     }
 }
 
+// [V][Q] double -> caller layout as float (first nq queries).
+__global__ void batch_transpose_d2f(const double* __restrict__ src, int V, int Q, int nq, float* __restrict__ out,
+                                    int query_major) {
+    const size_t total = (size_t)V * (size_t)nq;
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += stride) {
+        if (query_major) {
+            const size_t qi = i / (size_t)V, v = i % (size_t)V;
+            out[i] = (float)src[v * Q + qi];
+        } else {
+            const size_t v = i / (size_t)nq, qi = i % (size_t)nq;
+            out[i] = (float)src[v * Q + qi];
+        }
+    }
+}
+
 struct PprBatchWork {
     float* pr = nullptr;
-    float* res = nullptr;
-    float* msg = nullptr;
-    float* rq = nullptr;
+    double* res = nullptr;
+    double* msg = nullptr;
+    double* rq = nullptr;
     unsigned* tmask = nullptr;
     int2* q[2] = {nullptr, nullptr};
     unsigned* qmask[2] = {nullptr, nullptr};
@@ -837,9 +855,9 @@ static int ppr_batch_alloc(c2g_graph* g, int Q, size_t n_seeds) {
     const size_t qcap = V * W;
     const size_t mark_cap = (((size_t)g->E * W) >> kBatchTileLog) + 2;
     C2G_CUDA(cudaMalloc(&w->pr, sizeof(float) * VQ));
-    C2G_CUDA(cudaMalloc(&w->res, sizeof(float) * VQ));
-    C2G_CUDA(cudaMalloc(&w->msg, sizeof(float) * VQ));
-    C2G_CUDA(cudaMalloc(&w->rq, sizeof(float) * VQ));
+    C2G_CUDA(cudaMalloc(&w->res, sizeof(double) * VQ));
+    C2G_CUDA(cudaMalloc(&w->msg, sizeof(double) * VQ));
+    C2G_CUDA(cudaMalloc(&w->rq, sizeof(double) * VQ));
     C2G_CUDA(cudaMalloc(&w->tmask, sizeof(unsigned) * qcap));
     for (int b = 0; b < 2; ++b) {
         C2G_CUDA(cudaMalloc(&w->q[b], sizeof(int2) * qcap));
@@ -883,7 +901,7 @@ int ppr_batch_launch(c2g_graph* g, int32_t nq, const int32_t* sources, const c2g
     if (per_sm < 1) return fail(C2G_ERR_CUDA, "batch kernel cannot be resident");
     const size_t VQ = (size_t)g->V * (size_t)w->Q;
     if (!w->clean) {
-        C2G_CUDA(cudaMemsetAsync(w->msg, 0, sizeof(float) * VQ, g->stream));
+        C2G_CUDA(cudaMemsetAsync(w->msg, 0, sizeof(double) * VQ, g->stream));
         C2G_CUDA(cudaMemsetAsync(w->tmask, 0, sizeof(unsigned) * (size_t)g->V * (size_t)(w->Q / 32), g->stream));
         w->clean = true;
     }
@@ -941,7 +959,6 @@ int ppr_batch_launch(c2g_graph* g, int32_t nq, const int32_t* sources, const c2g
     C2G_CUDA(cudaEventRecord(g->ev1, g->stream));
     cudaError_t e = cudaSuccess;
     float* outs[2] = {pr_out, res_out};
-    float* srcs[2] = {w->pr, w->res};
     for (int k = 0; k < 2 && e == cudaSuccess; ++k) {
         if (!outs[k]) continue;
         float* dst = outs[k];
@@ -950,7 +967,10 @@ int ppr_batch_launch(c2g_graph* g, int32_t nq, const int32_t* sources, const c2g
             dst = w->stage;
         }
         if (e != cudaSuccess) break;
-        batch_transpose_f<<<g->num_sms * 8, 256, 0, g->stream>>>(srcs[k], g->V, p.Q, nq, dst, query_major);
+        if (k == 0)
+            batch_transpose_f<<<g->num_sms * 8, 256, 0, g->stream>>>(w->pr, g->V, p.Q, nq, dst, query_major);
+        else
+            batch_transpose_d2f<<<g->num_sms * 8, 256, 0, g->stream>>>(w->res, g->V, p.Q, nq, dst, query_major);
         e = cudaGetLastError();
         if (e == cudaSuccess && !on_device)
             e = cudaMemcpyAsync(outs[k], dst, sizeof(float) * (size_t)g->V * (size_t)nq, cudaMemcpyDeviceToHost,

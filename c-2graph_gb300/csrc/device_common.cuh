@@ -51,6 +51,7 @@ __device__ __forceinline__ unsigned ldcg(const unsigned* p) { return __ldcg(p); 
 __device__ __forceinline__ float ldcg(const float* p) { return __ldcg(p); }
 __device__ __forceinline__ int2 ldcg(const int2* p) { return __ldcg(p); }
 __device__ __forceinline__ unsigned long long ldcg(const unsigned long long* p) { return __ldcg(p); }
+__device__ __forceinline__ double ldcg(const double* p) { return __ldcg(p); }
 
 // Grid barrier with a time limit.  Every CTA of a cooperative launch calls it; it
 // returns false (and all later calls return false) once any CTA has given up, so the
@@ -101,7 +102,8 @@ __device__ __forceinline__ bool grid_sync(GridBarrier* b, int* flags, unsigned l
 // which lets a warp start expanding any edge tile without a search.
 struct FrontierOut {
     int2* q;                  // entries (vertex, base)
-    float* val;               // optional per-entry value (PPR residual)
+    float* val;               // optional per-entry 32-bit value (batched masks)
+    double* vald = nullptr;   // optional per-entry FP64 value (pushed residual)
     int* mark;                // tile -> owning entry
     unsigned long long* ctr;  // packed counter
     unsigned cap;             // entry capacity
@@ -188,6 +190,7 @@ struct WarpStage {
     int* d;    // shared [kStageCap] out-degree (frontier stages only)
     float* x;  // shared [kStageCap] value, or nullptr
     int n;
+    double* xd = nullptr;  // shared [kStageCap] FP64 value, or nullptr
 };
 
 // Write the stage to `out`: entries keep their stage order, so slots and edge bases
@@ -224,6 +227,7 @@ __device__ __forceinline__ void stage_flush(WarpStage& st, const FrontierOut& ou
             if (slot < out.cap) {
                 out.q[slot] = make_int2(st.v[i], (int)base);
                 if (out.val) out.val[slot] = st.x[i];
+                if (out.vald) out.vald[slot] = st.xd[i];
                 const unsigned tile = 1u << out.log_tile;
                 const unsigned t0 = (base + tile - 1) >> out.log_tile;
                 const unsigned t1 = (base + (unsigned)dv[k] - 1) >> out.log_tile;
@@ -240,7 +244,7 @@ __device__ __forceinline__ void stage_flush(WarpStage& st, const FrontierOut& ou
 
 // Warp-collective: lanes with `want` stage (v, deg, x); deg must be > 0.
 __device__ __forceinline__ void stage_push(WarpStage& st, const FrontierOut& out, bool want, int v, int deg,
-                                           float x) {
+                                           float x, double xd = 0.0) {
     const unsigned m = __ballot_sync(kFull, want);
     if (m == 0) return;
     const int cnt = __popc(m);
@@ -251,6 +255,7 @@ __device__ __forceinline__ void stage_push(WarpStage& st, const FrontierOut& out
         st.v[i] = v;
         st.d[i] = deg;
         if (st.x) st.x[i] = x;
+        if (st.xd) st.xd[i] = xd;
     }
     st.n += cnt;
 }
@@ -293,11 +298,19 @@ struct StageSmem {
     int v1[16][kStageCap];
 };
 
+// Stage backing for the push kernels: FP64 values instead of 32-bit ones.
+struct StageSmemD {
+    int v0[16][kStageCap];
+    int d0[16][kStageCap];
+    double xd0[16][kStageCap];
+    int v1[16][kStageCap];
+};
+
 // Warp-cooperative walk over the edges of a frontier, in tiles of 2^log_tile edges
 // assigned to warps round-robin (tile t goes to warp t mod nwarps, no shared counter).
 // For each group of 32*U edges every lane gets U edges (stride 32, so the warp reads
 // consecutive (target, weight) pairs) and calls
-//     body(ok[U], idx[U], val[U])
+//     body(ok[U], idx[U], val[U])   (val: the owner value type, int or double)
 // where idx is the edge's index in the adjacency array, ok says whether the lane holds
 // an edge, and val is owner_val(vertex, entry) of the edge's owning frontier entry.
 // body must be warp-collective-safe: every lane of the warp calls it.
@@ -306,6 +319,7 @@ __device__ __forceinline__ void walk_frontier_edges(const int2* __restrict__ q, 
                                                     const int* __restrict__ row, unsigned F, unsigned T,
                                                     int log_tile, unsigned mark_cap, unsigned qcap, unsigned E,
                                                     int* flags, OwnerVal owner_val, Body body) {
+    using VT = decltype(owner_val(0, 0u));  // int or double
     const int lane = threadIdx.x & 31;
     const unsigned gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const unsigned nwarps = (gridDim.x * blockDim.x) >> 5;
@@ -323,7 +337,8 @@ __device__ __forceinline__ void walk_frontier_edges(const int2* __restrict__ q, 
             // One frontier entry per lane: its edge range [base, end) and owner value.
             const unsigned j = o + (unsigned)lane;
             unsigned base = 0x7fffffffu, endv = 0xffffffffu;
-            int rs = 0, val = 0;
+            int rs = 0;
+            VT val = VT(0);
             if (j < F) {
                 const int2 qe = ldcg(q + j);
                 base = (unsigned)qe.y;
@@ -339,7 +354,7 @@ __device__ __forceinline__ void walk_frontier_edges(const int2* __restrict__ q, 
             for (unsigned eb = e0; eb < seg_end; eb += 32u * U) {
                 bool ok[U];
                 unsigned idx[U];
-                int sv[U];
+                VT sv[U];
 #pragma unroll
                 for (int u = 0; u < U; ++u) {
                     const unsigned e = eb + (unsigned)lane + 32u * u;

@@ -66,11 +66,13 @@ struct SsspWork {
 
 struct PprWork {
     float* pr = nullptr;
-    float* res = nullptr;
-    float* msg = nullptr;
+    double* res = nullptr;
+    double* msg = nullptr;
+    double* qd = nullptr;
+    float* res_f = nullptr;  // residual as float for the caller
     int* stamp = nullptr;
     int2* q[2] = {nullptr, nullptr};
-    float* qval[2] = {nullptr, nullptr};
+    double* qval[2] = {nullptr, nullptr};
     int* mark[2] = {nullptr, nullptr};
     int* touched = nullptr;
     int* dangle = nullptr;
@@ -88,7 +90,10 @@ struct SsspConfig {
 
 struct PprConfig {
     int log_tile = 8;
+    int pull_div = 8;  // pull round when frontier out-edges * pull_div > E; 0 = push only
 };
+
+constexpr int kPullTileLog = 8;  // in-edges per pull tile (reverse-CSR markers)
 
 struct LaunchGeom {
     int blocks = 0;
@@ -105,8 +110,10 @@ struct c2g_graph {
     int32_t* row = nullptr;
     int2* adj_w = nullptr;
     int2* adj_f = nullptr;
-    int32_t* row_r = nullptr;  // reverse CSR with float weights (adjoint), built on demand
+    int32_t* row_r = nullptr;  // reverse CSR with float weights (pull rounds, adjoint), on demand
     int2* adj_r = nullptr;
+    int32_t* mark_r = nullptr;  // pull-tile owner markers over row_r
+    int32_t* mark_f = nullptr;  // pull-tile owner markers over row (pulls on the reverse graph)
     // pruned records
     int32_t R = -1;
     int64_t H = 0;
@@ -143,9 +150,11 @@ int sssp_launch(c2g_graph* g, int32_t source, const int32_t* seed_v, const int32
                 int32_t n_seeds, int32_t* dist_dev, float* ms);
 int ppr_launch(c2g_graph* g, int32_t source, const c2g_ppr_params& p, const int32_t* seed_v,
                const float* seed_w, int32_t n_seeds, float* pr_dev, float* res_dev, float* ms);
-int ppr_launch_view(c2g_graph* g, const int32_t* row, const int2* adj, int32_t source, const c2g_ppr_params& pp,
-                    float absorb, int32_t n_src, const int32_t* src_list, const float* src_r0, const int32_t* seed_v,
-                    const float* seed_w, int32_t n_rec, float* pr_dev, float* res_dev, float* ms);
+int ppr_launch_view(c2g_graph* g, const int32_t* row, const int2* adj, const int32_t* row_rev, const int2* adj_rev,
+                    const int32_t* mark_rev, int32_t source, const c2g_ppr_params& pp, float absorb, int32_t n_src,
+                    const int32_t* src_list, const float* src_r0, const int32_t* seed_v, const float* seed_w,
+                    int32_t n_rec, float* pr_dev, float* res_dev, float* ms);
+int build_markers(c2g_graph* g, const int* row, int** out);
 void sssp_free(c2g_graph* g);
 void ppr_free(c2g_graph* g);
 // A handle sharing `base`'s device graph arrays with its own stream, workspaces and lock.

@@ -35,8 +35,10 @@ def l1(a, b):
     return float(np.abs(a.astype(np.float64) - b).sum())
 
 
+@pytest.mark.parametrize("pull_div", [0, 8, 1 << 30])
 @pytest.mark.parametrize("alpha,rmax", [(0.15, 1e-7), (0.2, None), (0.15, 1e-5)])
-def test_ppr_base_vs_fp64(gpu_available, gdirs, rmat14, alpha, rmax):
+def test_ppr_base_vs_fp64(gpu_available, gdirs, rmat14, alpha, rmax, pull_div):
+    """Push-only, mixed push/pull and pull-every-round give the same BSP rounds."""
     import c2g
     import oracle
 
@@ -48,6 +50,7 @@ def test_ppr_base_vs_fp64(gpu_available, gdirs, rmat14, alpha, rmax):
         deg = np.diff(o["vlist"])
         srcs = [int(np.argmax(deg)), int(np.flatnonzero(deg > 0)[-1])]
         with c2g.Graph.load(d, "origin") as gr:
+            gr.ppr_config(pull_div=pull_div)
             for s in srcs:
                 p = gr.ppr_params(alpha=alpha, rmax=rm, r0=1.0, pr0=alpha, seeded=0, max_iter=500)
                 pr, res, st = gr.ppr(s, p)
@@ -58,7 +61,8 @@ def test_ppr_base_vs_fp64(gpu_available, gdirs, rmat14, alpha, rmax):
                 assert st.status_flags == 0
 
 
-def test_ppr_seeded_pruned_vs_fp64(gpu_available, gdirs, rmat14):
+@pytest.mark.parametrize("pull_div", [0, 8])
+def test_ppr_seeded_pruned_vs_fp64(gpu_available, gdirs, rmat14, pull_div):
     """ppr-purn: pruned ppr/ graph, first hop = the source's records + kept edges."""
     import c2g
     import oracle
@@ -70,6 +74,7 @@ def test_ppr_seeded_pruned_vs_fp64(gpu_available, gdirs, rmat14):
         deg = np.diff(p["vlist"])
         cand = [int(np.argmax(deg))] + [int(v) for v in np.flatnonzero(np.diff(hv) > 0)[:3]]
         with c2g.Graph.load(d, "ppr") as gr:
+            gr.ppr_config(pull_div=pull_div)
             for s in cand:
                 for alpha, rm in ((0.2, 0.001 / (V + 1)), (0.15, 1e-7)):
                     prm = gr.ppr_params(alpha=alpha, rmax=rm, seeded=1)
@@ -147,3 +152,21 @@ def test_ppr_dangling_source(gpu_available):
         assert np.allclose(pr, [0, 0.2, 0]) and np.allclose(res, 0)
         pr, res, st = gr.ppr(0, prm)
         assert pr[0] > 0.2 and pr.sum() <= 1.0 + 1e-6
+
+
+def test_ppr_many_sources_fp64_parity(gpu_available, rmat14):
+    """Forty sources on one handle: every result within L1 1e-6 of the FP64 oracle in pr
+    and res (FP64 residual bookkeeping keeps threshold decisions with the oracle)."""
+    import c2g
+    import oracle
+
+    o = oracle.load_dataset(rmat14, "origin")
+    deg = np.diff(o["vlist"])
+    rng = np.random.default_rng(21)
+    srcs = rng.choice(np.flatnonzero(deg > 0), 40, replace=False)
+    with c2g.Graph.load(rmat14, "origin") as gr:
+        prm = gr.ppr_params(alpha=0.15, rmax=1e-7, seeded=0, pr0=0.15, r0=1.0)
+        for s in srcs:
+            pr, res, _ = gr.ppr(int(s), prm)
+            rp, rr, _, _ = oracle.ppr_push(o["vlist"], o["elist"], o["flist"], int(s), 0.15, 1e-7)
+            assert l1(pr, rp) <= L1_TOL and l1(res, rr) <= L1_TOL, (s, l1(pr, rp), l1(res, rr))
