@@ -143,10 +143,14 @@ __device__ __forceinline__ void ppr_pull(const PprParams& p) {
                 base = (unsigned)__ldg(p.row_r + j);
                 endv = (unsigned)__ldg(p.row_r + j + 1);
             }
-            const unsigned seg_end = min(e1, (unsigned)__shfl_sync(kFull, endv, 31));
-            if (seg_end <= e0 || o >= V || (unsigned)__shfl_sync(kFull, (int)base, 0) > e0) {
+            if (o >= V || (unsigned)__shfl_sync(kFull, (int)base, 0) > e0) {
                 if (lane == 0) atomicOr(&p.ctl->flags, C2G_FLAG_BOUNDS);
                 break;
+            }
+            const unsigned seg_end = min(e1, (unsigned)__shfl_sync(kFull, endv, 31));
+            if (seg_end <= e0) {  // 32 owners without in-edges: move on (o grows to V at most)
+                o += 32;
+                continue;
             }
             for (unsigned eb = e0; eb < seg_end; eb += 32) {
                 const unsigned e = eb + (unsigned)lane;

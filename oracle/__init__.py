@@ -89,13 +89,20 @@ def sssp_seeded(row, col, w, source, seed_v=(), seed_w=()):
 
 
 def ppr_push(row, col, f, source, alpha, rmax, r0=1.0, pr0=None, max_iter=500, seeded=False,
-             seed_v=(), seed_w=(), dtype=np.float64, degree_scaled=False):
-    """BSP forward push restating calcuatePPR; returns (pr, res, rounds, counters)."""
+             seed_v=(), seed_w=(), dtype=np.float64, degree_scaled=False, params_f32=True):
+    """BSP forward push restating calcuatePPR; returns (pr, res, rounds, counters).
+
+    The reference holds alpha, rmax and the start values as ValueType = float
+    (src/ppr/purn/Main.cu:66-67, src/ppr/w-purn-perk/PPR.cpp:21); with params_f32 they
+    are rounded to float32 first, so an FP64 run differs from an FP32 one only in its
+    arithmetic, not in its threshold (double 1e-7 and float 1e-7 differ by 1.2e-15)."""
     row, col, f = _c(row, np.int32), _c(col, np.int32), _c(f, np.float32)
     sv, sw = _c(seed_v, np.int32), _c(seed_w, np.float32)
     V = len(row) - 1
     if pr0 is None:
         pr0 = alpha * r0
+    if params_f32:
+        alpha, rmax, r0, pr0 = (float(np.float32(x)) for x in (alpha, rmax, r0, pr0))
     pr = np.empty(V, dtype=dtype)
     res = np.empty(V, dtype=dtype)
     cnt = np.zeros(3, dtype=np.int64)
