@@ -90,7 +90,7 @@ struct SsspConfig {
 
 struct PprConfig {
     int log_tile = 8;
-    int pull_div = 8;  // pull round when frontier out-edges * pull_div > E; 0 = push only
+    int pull_div = 0;  // pull round when frontier out-edges * pull_div > E; 0 = push only (default)
 };
 
 constexpr int kPullTileLog = 8;  // in-edges per pull tile (reverse-CSR markers)

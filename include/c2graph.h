@@ -207,7 +207,8 @@ int c2g_ppr_batch(c2g_graph* g, int32_t n, const int32_t* sources, const c2g_ppr
 
 /* Round shape of the push kernel: a round whose frontier has more than E / pull_div
  * out-edges pulls over the reverse CSR (built on first use) instead of pushing;
- * pull_div = 0 keeps every round a push.  Results are the same BSP rounds either way. */
+ * pull_div = 0 (the default) keeps every round a push.  Results are the same BSP rounds
+ * either way. */
 int c2g_ppr_set_config(c2g_graph* g, int32_t pull_div);
 
 /* Reference defaults: PPR (alpha 0.2, rmax 0.001/(V+1), cap 500), and the adsorption
