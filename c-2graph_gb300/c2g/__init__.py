@@ -105,7 +105,7 @@ SIGNATURES = {
                                       ctypes.c_int, ctypes.POINTER(Stats)]),
     "c2g_ppr": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.POINTER(PprParams), _P, _P, ctypes.c_int,
                                ctypes.POINTER(Stats)]),
-    "c2g_ppr_set_config": (ctypes.c_int, [_P, ctypes.c_int32]),
+    "c2g_ppr_set_config": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int32]),
     "c2g_ppr_default_params": (ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(PprParams)]),
     "c2g_ppr_batch": (ctypes.c_int, [_P, ctypes.c_int32, _P, ctypes.POINTER(PprParams), _P, _P, ctypes.c_int,
                                      ctypes.c_int, ctypes.POINTER(Stats)]),
@@ -280,8 +280,8 @@ class Graph:
                                     ctypes.byref(st)))
         return dist, st
 
-    def ppr_config(self, pull_div=0):
-        _check(lib().c2g_ppr_set_config(self._h, pull_div))
+    def ppr_config(self, pull_div=0, dense_div=8):
+        _check(lib().c2g_ppr_set_config(self._h, pull_div, dense_div))
 
     def ppr_params(self, adsorption=False, **kw):
         p = PprParams()

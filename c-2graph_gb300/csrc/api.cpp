@@ -391,11 +391,12 @@ int c2g_sssp_set_config(c2g_graph* g, int32_t delta, int32_t tile, int32_t max_i
     return C2G_OK;
 }
 
-int c2g_ppr_set_config(c2g_graph* g, int32_t pull_div) {
+int c2g_ppr_set_config(c2g_graph* g, int32_t pull_div, int32_t dense_div) {
     if (!g) return fail(C2G_ERR_ARG, "graph is NULL");
-    if (pull_div < 0) return fail(C2G_ERR_ARG, "pull_div must be >= 0");
+    if (pull_div < 0 || dense_div < 0) return fail(C2G_ERR_ARG, "pull_div and dense_div must be >= 0");
     std::lock_guard<std::mutex> lk(g->mu);
     g->ppr_cfg.pull_div = pull_div;
+    g->ppr_cfg.dense_div = dense_div;
     return C2G_OK;
 }
 

@@ -6,15 +6,16 @@
 // Q queries (padded to a multiple of 32) share every pass over the graph:
 //   * state is vertex-major: dist[v][Q] int32, so the 32 queries of one "word" w of a
 //     vertex occupy one 128-byte line;
-//   * a frontier entry is a (vertex, word) pair; its 32-bit mask says which of the
-//     word's queries improved that vertex in the previous round;
-//   * expansion: a warp loads 32 edges (one per lane) of the frontier's edge range, then
-//     walks them; for each edge every lane relaxes one query of the word with one
-//     coalesced 128-byte read of the target's row, so an edge read from HBM serves all
-//     active queries of its word;
-//   * the first improvement of (target, word) in a round sets its mask bits with
-//     atomicOr and the setter that saw an empty mask appends the pair (warp-staged);
-//   * a round is two phases: gather (copy and clear each entry's mask) and expand.
+//   * a frontier entry is a (vertex, word) pair with a 32-bit mask of the word's queries
+//     that improved the vertex in the previous round;
+//   * expansion: a warp reads 32 edges of an entry (one per lane) and broadcasts them;
+//     for each edge every lane relaxes one query of the word with one coalesced
+//     128-byte read of the target's row, so an edge read from HBM serves all active
+//     queries of its word;
+//   * an improvement is red.min on the distance and red.or of the query bits into the
+//     target's (vertex, word) mask: nothing on the relaxation path waits for an atomic;
+//   * a round is two phases: a sweep of the mask words that builds the frontier (with
+//     edge-base prefix and tile markers), then the expansion.
 // Results are the same int32 fixed points as one c2g_sssp call per source.
 #include <climits>
 #include <vector>
@@ -54,7 +55,7 @@ constexpr int kBatchTileLog = 7;  // 128 edge-word steps per warp tile
 __device__ __forceinline__ FrontierOut batch_out(const BatchParams& p, int buf, int slot) {
     FrontierOut o;
     o.q = p.q[buf];
-    o.val = nullptr;
+    o.val = reinterpret_cast<float*>(p.qmask[buf]);  // mask bits travel in the value slot
     o.mark = p.mark[buf];
     o.ctr = &p.ctl->qctr[slot];
     o.cap = p.qcap;
@@ -64,11 +65,32 @@ __device__ __forceinline__ FrontierOut batch_out(const BatchParams& p, int buf, 
     return o;
 }
 
-// Mark (v, w) improved for the queries in `bits`; returns true for the caller that
-// found the mask empty (it appends the pair to the next frontier).
-__device__ __forceinline__ bool mark_improved(const BatchParams& p, int v, int w, unsigned bits) {
-    return atomicOr(p.mask + (((size_t)v << p.logW) + (unsigned)w), bits) == 0u;
+// Build a round's frontier from the improvement masks: a sweep over all (vertex, word)
+// mask words; each non-zero word is cleared and, when the vertex has out-edges, becomes an
+// entry (v * W + w, edge base) carrying the mask.  Entries come out in sweep order per
+// warp.  Relaxations set masks with fire-and-forget red.or, so no relaxation waits on an
+// atomic's return; the sweep reads V * W words per round.
+__device__ __forceinline__ void batch_sweep(const BatchParams& p, const FrontierOut& out, WarpStage& fst,
+                                            unsigned gwarp, unsigned nwarps, int lane) {
+    const unsigned nm = (unsigned)p.V << p.logW;
+    for (unsigned b = gwarp * 32u; b < nm; b += nwarps * 32u) {
+        const unsigned i = b + (unsigned)lane;
+        unsigned m = 0u;
+        int deg = 0;
+        if (i < nm) {
+            m = ldcg(p.mask + i);
+            if (m) {
+                p.mask[i] = 0u;
+                const int v = (int)(i >> p.logW);
+                deg = __ldg(p.row + v + 1) - __ldg(p.row + v);
+            }
+        }
+        stage_push(fst, out, m != 0u && deg > 0, (int)i, deg, __int_as_float((int)m));
+    }
+    stage_flush(fst, out);
 }
+
+constexpr int kBatchUnroll = 6;  // target rows in flight per lane (8 spills at 64 registers)
 
 __global__ void __launch_bounds__(512, 2) sssp_batch_persistent(const BatchParams p) {
     TraversalCtl* ctl = p.ctl;
@@ -79,9 +101,10 @@ __global__ void __launch_bounds__(512, 2) sssp_batch_persistent(const BatchParam
     const unsigned nthreads = gridDim.x * blockDim.x;
     const unsigned gwarp = gtid >> 5, nwarps = nthreads >> 5;
     const int W = 1 << p.logW;
+    const unsigned Qu = (unsigned)p.Q;
     __shared__ StageSmem sm;
     const int wib = threadIdx.x >> 5;
-    WarpStage fst{sm.v0[wib], sm.d0[wib], nullptr, 0};
+    WarpStage fst{sm.v0[wib], sm.d0[wib], sm.x0[wib], 0};
 
     // Init: dist = INF (vector stores), masks = 0.
     {
@@ -97,111 +120,74 @@ __global__ void __launch_bounds__(512, 2) sssp_batch_persistent(const BatchParam
     // Sources and their seeds: dist[s][q] = 0, dist[seed][q] = min(w); mark them.
     for (unsigned qi = gtid; qi < (unsigned)p.nq; qi += nthreads) {
         const int s = p.sources[qi];
+        const unsigned bit = 1u << (qi & 31), w = qi >> 5;
         atomicMin(p.dist + (size_t)s * p.Q + qi, 0);
+        atomicOr(p.mask + ((size_t)s << p.logW) + w, bit);
         if (p.seed_off)
-            for (int k = p.seed_off[qi]; k < p.seed_off[qi + 1]; ++k)
+            for (int k = p.seed_off[qi]; k < p.seed_off[qi + 1]; ++k) {
                 atomicMin(p.dist + (size_t)p.seed_v[k] * p.Q + qi, p.seed_w[k]);
-    }
-    if (!grid_sync(bar, flags, p.barrier_ns)) return;
-    {
-        // Round-1 frontier: the (source|seed, word) pairs, one warp lane per query.
-        const FrontierOut out = batch_out(p, 1, 1);
-        const unsigned nq32 = ((unsigned)p.nq + 31u) & ~31u;
-        for (unsigned b = gwarp * 32; b < nq32; b += nwarps * 32) {
-            const unsigned qi = b + (unsigned)lane;
-            const int w = (int)(qi >> 5);
-            bool want = false;
-            int v = 0, deg = 0;
-            if (qi < (unsigned)p.nq) {
-                v = p.sources[qi];
-                deg = __ldg(p.row + v + 1) - __ldg(p.row + v);
-                want = deg > 0 && mark_improved(p, v, w, 1u << (qi & 31));
+                atomicOr(p.mask + ((size_t)p.seed_v[k] << p.logW) + w, bit);
             }
-            stage_push(fst, out, want, (v << p.logW) + w, deg, 0.f);
-            if (p.seed_off && qi < (unsigned)p.nq) {
-                for (int k = p.seed_off[qi]; k < p.seed_off[qi + 1]; ++k) {
-                    const int sv = p.seed_v[k];
-                    const int sd = __ldg(p.row + sv + 1) - __ldg(p.row + sv);
-                    if (sd > 0 && mark_improved(p, sv, w, 1u << (qi & 31))) {
-                        // Rare path (seeds of the same word may collide): direct append.
-                        const unsigned long long old =
-                            atomicAdd(out.ctr, (1ull << 32) | (unsigned long long)(unsigned)sd);
-                        const unsigned slot = (unsigned)(old >> 32), base = (unsigned)old;
-                        if (slot < out.cap) {
-                            out.q[slot] = make_int2((sv << p.logW) + w, (int)base);
-                            const unsigned t0 = (base + (1u << kBatchTileLog) - 1u) >> kBatchTileLog,
-                                           t1 = (base + sd - 1) >> kBatchTileLog;
-                            for (unsigned t = t0; t <= t1 && t < out.mark_cap; ++t) out.mark[t] = (int)slot;
-                        } else {
-                            atomicOr(flags, C2G_FLAG_QUEUE_OVERFLOW);
-                        }
-                    }
-                }
-            }
-        }
-        stage_flush(fst, out);
     }
     if (!grid_sync(bar, flags, p.barrier_ns)) return;
 
     long long relax = 0, steps = 0;
     int cur = 1, iters = 0;
     for (;;) {
-        const unsigned long long c = ldcg(&ctl->qctr[cur % 3]);
+        const int buf = cur & 1, slot = cur % 3;
+        // Phase 1: this round's frontier from the masks of the previous one.
+        if (gtid == 0) ctl->qctr[(cur + 1) % 3] = 0ull;
+        batch_sweep(p, batch_out(p, buf, slot), fst, gwarp, nwarps, lane);
+        if (!grid_sync(bar, flags, p.barrier_ns)) return;
+        const unsigned long long c = ldcg(&ctl->qctr[slot]);
         const unsigned F = (unsigned)(c >> 32), T = (unsigned)c;
         if (F == 0) break;
         if (++iters > p.max_iter) {
             if (gtid == 0) atomicOr(flags, C2G_FLAG_ITER_CAP);
             break;
         }
-        const int buf = cur & 1;
         if (F > p.qcap || ((T + (1u << kBatchTileLog) - 1u) >> kBatchTileLog) > p.mark_cap) {
             if (gtid == 0) atomicOr(flags, C2G_FLAG_BOUNDS);
             break;
         }
-        // Phase 1: gather and clear the masks of this round's entries.
-        for (unsigned j = gtid; j < F; j += nthreads) {
-            const int vw = ldcg(p.q[buf] + j).x;
-            unsigned* mp = p.mask + (unsigned)vw;
-            p.qmask[buf][j] = ldcg(mp);
-            *mp = 0u;
-        }
         if (gtid == 0) {
-            ctl->qctr[(cur + 2) % 3] = 0ull;
             ctl->popped += F;
             ctl->relaxed += T;
         }
-        if (!grid_sync(bar, flags, p.barrier_ns)) return;
 
-        // Phase 2: expand.  Warps take tiles of edge-word steps; inside a tile they walk
-        // owner runs: the owner's row of distances is read once, then each of its edges
-        // is one uniform (broadcast) edge load and one 128-byte target-row read for the
-        // 32 queries of the word, four edges in flight.
-        const FrontierOut nout = batch_out(p, (cur + 1) & 1, (cur + 1) % 3);
+        // Phase 2: expand.  Warps take tiles of edge-word steps and walk owner runs: the
+        // owner's row of distances is read once; its edges are read 32 at a time (one per
+        // lane, coalesced) and broadcast by shuffles; each edge costs one 128-byte read of
+        // the target's row for the 32 queries of the word, kBatchUnroll rows in flight.
+        // Improvements are red.min on the distance and red.or on the target's mask.
         const int2* q = p.q[buf];
         const unsigned* qm = p.qmask[buf];
         const int* mark = p.mark[buf];
         const unsigned tile = 1u << kBatchTileLog;
         const unsigned ntiles = (T + tile - 1) >> kBatchTileLog;
-        int npend = 0, pv = 0, pd = 0;  // pending appends, one per lane (warp-uniform count)
         for (unsigned t = gwarp; t < ntiles; t += nwarps) {
             unsigned e0 = t << kBatchTileLog;
             const unsigned e1 = min(e0 + tile, T);
             unsigned o = (unsigned)ldcg(mark + t);
             while (e0 < e1) {
                 const unsigned j = o + (unsigned)lane;
-                unsigned base = 0x7fffffffu, endv = 0xffffffffu, msk = 0u;
-                int rs = 0, vw = 0;
+                unsigned base = 0x7fffffffu, endv = 0xffffffffu, msk = 0u, rs = 0u;
+                int vw = 0;
+                bool bad = false;
                 if (j < F) {
                     const int2 qe = ldcg(q + j);
                     vw = qe.x;
                     base = (unsigned)qe.y;
                     const int v = vw >> p.logW;
-                    rs = __ldg(p.row + v);
-                    endv = base + (unsigned)(__ldg(p.row + v + 1) - rs);
+                    rs = (unsigned)__ldg(p.row + v);
+                    const unsigned deg = (unsigned)__ldg(p.row + v + 1) - rs;
+                    endv = base + deg;
+                    bad = rs + deg > p.E || deg == 0u;
                     msk = ldcg(qm + j);
                 }
                 const unsigned seg_end = min(e1, (unsigned)__shfl_sync(kFull, endv, 31));
-                if (seg_end <= e0 || o >= F || (unsigned)__shfl_sync(kFull, (int)base, 0) > e0) {
+                if (__any_sync(kFull, bad) || seg_end <= e0 || o >= F ||
+                    (unsigned)__shfl_sync(kFull, (int)base, 0) > e0) {
                     if (lane == 0) atomicOr(flags, C2G_FLAG_BOUNDS);
                     break;
                 }
@@ -213,69 +199,47 @@ __global__ void __launch_bounds__(512, 2) sssp_batch_persistent(const BatchParam
                     if (lo >= hi) continue;
                     const int kvw = __shfl_sync(kFull, vw, k);
                     const unsigned km = (unsigned)__shfl_sync(kFull, (int)msk, k);
-                    const unsigned krs = (unsigned)__shfl_sync(kFull, rs, k);
-                    const int w = kvw & (W - 1);
-                    const size_t lane_off = ((size_t)w << 5) + lane;
+                    const unsigned krs = (unsigned)__shfl_sync(kFull, (int)rs, k);
+                    const unsigned w = (unsigned)kvw & (unsigned)(W - 1);
+                    int* drow = p.dist + (w << 5) + lane;  // + v * Q: row of vertex v
+                    unsigned* mrow = p.mask + w;           // + (v << logW): mask word of v
                     const bool act = (km >> lane) & 1u;
                     // L2-coherent: the owner improved in the previous round.
-                    const int du = ldcg(p.dist + (size_t)(kvw >> p.logW) * p.Q + lane_off);
-                    for (unsigned eb = lo; eb < hi; eb += 4) {
-                        int2 ew[4];
-                        int cur[4];
+                    const int du = act ? ldcg(drow + (size_t)((unsigned)kvw >> p.logW) * Qu) : 0;
+                    for (unsigned eb = lo; eb < hi; eb += 32) {
+                        const unsigned n = min(32u, hi - eb);
+                        const int2 my = (unsigned)lane < n ? __ldg(p.adj + krs + (eb - kb) + lane) : make_int2(0, 0);
+                        for (unsigned g = 0; g < n; g += kBatchUnroll) {
+                            int tv[kBatchUnroll], tw[kBatchUnroll], cd[kBatchUnroll];
 #pragma unroll
-                        for (int jj = 0; jj < 4; ++jj) {
-                            const unsigned e = eb + jj;
-                            const unsigned idx = krs + (e - kb);
-                            const bool in = e < hi && idx < p.E;
-                            ew[jj] = in ? __ldg(p.adj + idx) : make_int2(0, 0);
-                            if (e < hi && !in && lane == 0) atomicOr(flags, C2G_FLAG_BOUNDS);
-                        }
+                            for (int jj = 0; jj < kBatchUnroll; ++jj) {
+                                tv[jj] = __shfl_sync(kFull, my.x, (int)g + jj);
+                                tw[jj] = __shfl_sync(kFull, my.y, (int)g + jj);
+                            }
 #pragma unroll
-                        for (int jj = 0; jj < 4; ++jj)
-                            cur[jj] = (eb + jj < hi && act) ? ldcg(p.dist + (size_t)ew[jj].x * p.Q + lane_off) : INT_MIN;
+                            for (int jj = 0; jj < kBatchUnroll; ++jj)
+                                cd[jj] = (act && g + jj < n) ? ldcg(drow + (size_t)(unsigned)tv[jj] * Qu) : INT_MIN;
 #pragma unroll
-                        for (int jj = 0; jj < 4; ++jj) {
-                            const int nd = du + ew[jj].y;
-                            bool imp = false;
-                            if (nd < cur[jj]) imp = atomicMin(p.dist + (size_t)ew[jj].x * p.Q + lane_off, nd) > nd;
-                            relax += (eb + jj < hi && act);
-                            const unsigned bits = __ballot_sync(kFull, imp);
-                            if (bits) {  // rare path: mark (target, word), first setter appends
-                                const int c = ew[jj].x;
-                                int first = 0, cdeg = 0;
-                                if (lane == 0) {
-                                    cdeg = __ldg(p.row + c + 1) - __ldg(p.row + c);
-                                    first = cdeg > 0 && mark_improved(p, c, w, bits);
-                                }
-                                first = __shfl_sync(kFull, first, 0);
-                                if (first) {
-                                    cdeg = __shfl_sync(kFull, cdeg, 0);
-                                    if (lane == npend) {
-                                        pv = (c << p.logW) + w;
-                                        pd = cdeg;
-                                    }
-                                    if (++npend == 32) {
-                                        stage_push(fst, nout, true, pv, pd, 0.f);
-                                        npend = 0;
-                                    }
-                                }
+                            for (int jj = 0; jj < kBatchUnroll; ++jj) {
+                                const int nd = du + tw[jj];
+                                const bool imp = nd < cd[jj];
+                                if (imp) atomicMin(drow + (size_t)(unsigned)tv[jj] * Qu, nd);
+                                const unsigned bits = __ballot_sync(kFull, imp);
+                                if (bits && lane == 0) atomicOr(mrow + ((size_t)(unsigned)tv[jj] << p.logW), bits);
                             }
                         }
                     }
+                    if (lane == 0) relax += (long long)__popc(km) * (hi - lo);
                     steps += hi - lo;
                 }
                 e0 = seg_end;
                 o += 32;
             }
         }
-        stage_push(fst, nout, lane < npend, pv, pd, 0.f);
-        npend = 0;
-        stage_flush(fst, nout);
         if (!grid_sync(bar, flags, p.barrier_ns)) return;
         ++cur;
     }
-    // relax counts lanes; one atomic per warp
-    for (int o = 16; o >= 1; o >>= 1) relax += __shfl_xor_sync(kFull, relax, o);
+    // relax is counted by lane 0 of each warp
     if (lane == 0) {
         atomicAdd((unsigned long long*)&p.counters[0], (unsigned long long)relax);
         atomicAdd((unsigned long long*)&p.counters[1], (unsigned long long)steps);
@@ -458,9 +422,10 @@ int sssp_batch_launch(c2g_graph* g, int32_t nq, const int32_t* sources, const st
 //
 // Same BSP semantics per query as c2g_ppr (src/ppr/purn/Main.cu:149-428): pop r, push
 // (1-alpha)*r*w into msg, then res += msg; if res > rmax: pr += alpha*res and activate.
-// State is vertex-major [V][Q] float (pr, res, msg, rq = residual being pushed).
-// Frontier entries are (vertex, word) pairs whose mask is complete when appended
-// (phase B visits each touched pair once), so no mask gather is needed here.
+// State is vertex-major [V][Q]: pr float; res, msg and rq (the residual being pushed)
+// FP64.  A push marks the target's (vertex, word) touched mask with red.or; phase B
+// sweeps the touched masks, applies the messages and activates, building the frontier
+// entries (vertex, word) with the activated lanes as their mask.
 namespace c2g {
 
 struct PprBatchParams {
@@ -477,7 +442,6 @@ struct PprBatchParams {
     int2* q[2];       // frontier entries (v*W + w, edge base)
     unsigned* qmask[2];
     int* mark[2];
-    int* touched;     // touched (v*W + w) list
     int2* dangle;     // (v*W + w, lanes) activated without out-edges, popped next round
     TraversalCtl* ctl;
     const int* sources;
@@ -545,6 +509,33 @@ __device__ __forceinline__ void pbatch_apply(const PprBatchParams& p, int vw, un
     stage_push(fst, out, lane == 0 && bits != 0u && deg > 0, vw, deg, __int_as_float((int)bits));
 }
 
+constexpr int kPprBatchUnroll = 8;  // messages in flight per lane
+
+// Apply sweep: every (vertex, word) whose touched mask is non-zero gets pbatch_apply for
+// its touched lanes; the mask is cleared.  Pushes mark targets with red.or, so the push
+// never waits on an atomic's return; the sweep reads V * W mask words per round.
+__device__ __forceinline__ unsigned pbatch_sweep(const PprBatchParams& p, bool force, WarpStage& fst,
+                                                 const FrontierOut& out, unsigned* dctr, unsigned gwarp,
+                                                 unsigned nwarps, int lane) {
+    const unsigned nm = (unsigned)p.V << p.logW;
+    unsigned cnt = 0;
+    for (unsigned b = gwarp * 32u; b < nm; b += nwarps * 32u) {
+        const unsigned i = b + (unsigned)lane;
+        const unsigned tm = i < nm ? ldcg(p.tmask + i) : 0u;
+        if (tm) p.tmask[i] = 0u;
+        unsigned nz = __ballot_sync(kFull, tm != 0u);
+        cnt += (unsigned)__popc(nz);
+        while (nz) {
+            const int k = __ffs(nz) - 1;
+            nz &= nz - 1u;
+            const unsigned lanes = (unsigned)__shfl_sync(kFull, (int)tm, k);
+            pbatch_apply(p, (int)(b + (unsigned)k), lanes, force, fst, out, dctr);
+        }
+    }
+    stage_flush(fst, out);
+    return cnt;
+}
+
 __global__ void __launch_bounds__(512, 2) ppr_batch_persistent(const PprBatchParams p) {
     TraversalCtl* ctl = p.ctl;
     GridBarrier* bar = reinterpret_cast<GridBarrier*>(&ctl->bar_count);
@@ -554,10 +545,10 @@ __global__ void __launch_bounds__(512, 2) ppr_batch_persistent(const PprBatchPar
     const unsigned nthreads = gridDim.x * blockDim.x;
     const unsigned gwarp = gtid >> 5, nwarps = nthreads >> 5;
     const int W = 1 << p.logW;
+    const unsigned Qu = (unsigned)p.Q;
     __shared__ StageSmem sm;
     const int wib = threadIdx.x >> 5;
     WarpStage fst{sm.v0[wib], sm.d0[wib], sm.x0[wib], 0};
-    WarpStage tst{sm.v1[wib], nullptr, nullptr, 0};
     const double one_m_a = 1.0 - (double)p.alpha;
 
     // Init: pr = res = 0 (msg and tmask are zero between launches).
@@ -575,7 +566,7 @@ __global__ void __launch_bounds__(512, 2) ppr_batch_persistent(const PprBatchPar
     }
     if (!grid_sync(bar, flags, p.barrier_ns)) return;
     // Sources: base mode puts r0 on the source; seeded mode applies the host-side first
-    // hop (records + kept out-edges) to pr/res and marks the seeds touched.
+    // hop (records + kept out-edges) to pr/res.  Either way the touched lanes are marked.
     for (unsigned qi = gtid; qi < (unsigned)p.nq; qi += nthreads) {
         const int s = p.sources[qi];
         const int w = (int)(qi >> 5);
@@ -583,10 +574,7 @@ __global__ void __launch_bounds__(512, 2) ppr_batch_persistent(const PprBatchPar
         if (!p.seeded) {
             atomicAdd(p.pr + (size_t)s * p.Q + qi, p.pr0);
             atomicAdd(p.res + (size_t)s * p.Q + qi, (double)p.r0);
-            if (atomicOr(p.tmask + ((size_t)s << p.logW) + w, bit) == 0u) {
-                const unsigned slot = atomicAdd(&ctl->listctr[0], 1u);
-                if (slot < p.qcap) p.touched[slot] = (s << p.logW) + w;
-            }
+            atomicOr(p.tmask + ((size_t)s << p.logW) + w, bit);
         } else {
             atomicAdd(p.pr + (size_t)s * p.Q + qi, p.alpha);
             const int rs = __ldg(p.row + s), re = __ldg(p.row + s + 1);
@@ -604,31 +592,17 @@ __global__ void __launch_bounds__(512, 2) ppr_batch_persistent(const PprBatchPar
                 }
                 atomicAdd(p.pr + (size_t)v * p.Q + qi, (float)(one_m_a * (double)p.alpha * (double)wt));
                 atomicAdd(p.res + (size_t)v * p.Q + qi, one_m_a * (double)wt);
-                if (atomicOr(p.tmask + ((size_t)v << p.logW) + w, bit) == 0u) {
-                    const unsigned slot = atomicAdd(&ctl->listctr[0], 1u);
-                    if (slot < p.qcap) p.touched[slot] = (v << p.logW) + w;
-                }
+                atomicOr(p.tmask + ((size_t)v << p.logW) + w, bit);
             }
         }
     }
     if (!grid_sync(bar, flags, p.barrier_ns)) return;
-    {
-        // Round-1 frontier: every touched (vertex, word) activates its touched lanes.
-        const unsigned n = min(ldcg(&ctl->listctr[0]), p.qcap);
-        const FrontierOut out = pbatch_out(p, 1, 1);
-        for (unsigned i = gwarp; i < n; i += nwarps) {
-            const int vw = ldcg(p.touched + i);
-            unsigned* tm = p.tmask + (unsigned)vw;
-            const unsigned lanes = ldcg(tm);
-            pbatch_apply(p, vw, lanes, true, fst, out, &ctl->dctr[1]);
-            __syncwarp();
-            if (lane == 0) *tm = 0u;
-        }
-        stage_flush(fst, out);
-    }
+    // Round-1 frontier: every touched (vertex, word) activates its touched lanes.
+    pbatch_sweep(p, true, fst, pbatch_out(p, 1, 1), &ctl->dctr[1], gwarp, nwarps, lane);
     if (!grid_sync(bar, flags, p.barrier_ns)) return;
 
     long long pushes = 0, steps = 0;
+    unsigned touched = 0;
     int cur = 1, iters = 0;
     for (;;) {
         const unsigned long long c = ldcg(&ctl->qctr[cur % 3]);
@@ -658,41 +632,45 @@ __global__ void __launch_bounds__(512, 2) ppr_batch_persistent(const PprBatchPar
             if (gtid == 0) atomicOr(flags, C2G_FLAG_BOUNDS);
             break;
         }
-        const int slot = cur % 3, nslot = (cur + 1) % 3, fslot = (cur + 2) % 3;
+        const int nslot = (cur + 1) % 3, fslot = (cur + 2) % 3;
         if (gtid == 0) {
             ctl->qctr[fslot] = 0ull;
-            ctl->listctr[fslot] = 0u;
             ctl->dctr[fslot] = 0u;
             ctl->popped += F;
             ctl->relaxed += T;
         }
-        // Phase A: push along the frontier's edges (owner runs, as in the SSSP batch).
+        // Phase A: push along the frontier's edges (owner runs, as in the SSSP batch):
+        // red.add of the FP64 message per active lane, red.or of the word's sending lanes
+        // into the target's touched mask.
         {
             const int2* q = p.q[buf];
             const unsigned* qm = p.qmask[buf];
             const int* mark = p.mark[buf];
             const unsigned tile = 1u << kBatchTileLog;
             const unsigned ntiles = (T + tile - 1) >> kBatchTileLog;
-            int npend = 0, pv = 0;
             for (unsigned t = gwarp; t < ntiles; t += nwarps) {
                 unsigned e0 = t << kBatchTileLog;
                 const unsigned e1 = min(e0 + tile, T);
                 unsigned o = (unsigned)ldcg(mark + t);
                 while (e0 < e1) {
                     const unsigned j = o + (unsigned)lane;
-                    unsigned base = 0x7fffffffu, endv = 0xffffffffu, msk = 0u;
-                    int rs = 0, vw = 0;
+                    unsigned base = 0x7fffffffu, endv = 0xffffffffu, msk = 0u, rs = 0u;
+                    int vw = 0;
+                    bool bad = false;
                     if (j < F) {
                         const int2 qe = ldcg(q + j);
                         vw = qe.x;
                         base = (unsigned)qe.y;
                         const int v = vw >> p.logW;
-                        rs = __ldg(p.row + v);
-                        endv = base + (unsigned)(__ldg(p.row + v + 1) - rs);
+                        rs = (unsigned)__ldg(p.row + v);
+                        const unsigned deg = (unsigned)__ldg(p.row + v + 1) - rs;
+                        endv = base + deg;
+                        bad = rs + deg > p.E || deg == 0u;
                         msk = ldcg(qm + j);
                     }
                     const unsigned seg_end = min(e1, (unsigned)__shfl_sync(kFull, endv, 31));
-                    if (seg_end <= e0 || o >= F || (unsigned)__shfl_sync(kFull, (int)base, 0) > e0) {
+                    if (__any_sync(kFull, bad) || seg_end <= e0 || o >= F ||
+                        (unsigned)__shfl_sync(kFull, (int)base, 0) > e0) {
                         if (lane == 0) atomicOr(flags, C2G_FLAG_BOUNDS);
                         break;
                     }
@@ -704,75 +682,51 @@ __global__ void __launch_bounds__(512, 2) ppr_batch_persistent(const PprBatchPar
                         if (lo >= hi) continue;
                         const int kvw = __shfl_sync(kFull, vw, k);
                         const unsigned km = (unsigned)__shfl_sync(kFull, (int)msk, k);
-                        const unsigned krs = (unsigned)__shfl_sync(kFull, rs, k);
-                        const int w = kvw & (W - 1);
-                        const size_t lane_off = ((size_t)w << 5) + lane;
+                        const unsigned krs = (unsigned)__shfl_sync(kFull, (int)rs, k);
+                        const unsigned w = (unsigned)kvw & (unsigned)(W - 1);
+                        double* mrow = p.msg + (w << 5) + lane;  // + v * Q: message row of v
+                        unsigned* trow = p.tmask + w;            // + (v << logW): touched word of v
                         const bool act = (km >> lane) & 1u;
                         // (1-alpha)*r_u of this lane's query (src/ppr/purn/Main.cu:288)
-                        const double qu = act ? one_m_a * ldcg(p.rq + (size_t)(kvw >> p.logW) * p.Q + lane_off) : 0.0;
-                        for (unsigned eb = lo; eb < hi; eb += 4) {
-                            int2 ew[4];
+                        const double qu =
+                            act ? one_m_a * ldcg(p.rq + (size_t)((unsigned)kvw >> p.logW) * Qu + (w << 5) + lane) : 0.0;
+                        for (unsigned eb = lo; eb < hi; eb += 32) {
+                            const unsigned n = min(32u, hi - eb);
+                            const int2 my =
+                                (unsigned)lane < n ? __ldg(p.adj + krs + (eb - kb) + lane) : make_int2(0, 0);
+                            for (unsigned g = 0; g < n; g += kPprBatchUnroll) {
 #pragma unroll
-                            for (int jj = 0; jj < 4; ++jj) {
-                                const unsigned e = eb + jj;
-                                const unsigned idx = krs + (e - kb);
-                                const bool in = e < hi && idx < p.E;
-                                ew[jj] = in ? __ldg(p.adj + idx) : make_int2(0, 0);
-                                if (e < hi && !in && lane == 0) atomicOr(flags, C2G_FLAG_BOUNDS);
-                            }
-#pragma unroll
-                            for (int jj = 0; jj < 4; ++jj) {
-                                const double m = qu * (double)__int_as_float(ew[jj].y);
-                                const bool send = (eb + jj < hi) && act && m > 0.0;
-                                if (send) atomicAdd(p.msg + (size_t)ew[jj].x * p.Q + lane_off, m);
-                                pushes += send;
-                                const unsigned bits = __ballot_sync(kFull, send);
-                                if (bits) {  // first message of (target, word) this round appends it
-                                    int first = 0;
-                                    if (lane == 0)
-                                        first = atomicOr(p.tmask + ((size_t)ew[jj].x << p.logW) + w, bits) == 0u;
-                                    if (__shfl_sync(kFull, first, 0)) {
-                                        if (lane == npend) pv = (ew[jj].x << p.logW) + w;
-                                        if (++npend == 32) {
-                                            list_stage_push(tst, p.touched, &ctl->listctr[slot], p.qcap, flags, true, pv);
-                                            npend = 0;
-                                        }
-                                    }
+                                for (int jj = 0; jj < kPprBatchUnroll; ++jj) {
+                                    const unsigned tv = (unsigned)__shfl_sync(kFull, my.x, (int)g + jj);
+                                    const float tw = __int_as_float(__shfl_sync(kFull, my.y, (int)g + jj));
+                                    const double m = qu * (double)tw;
+                                    const bool send = act && g + jj < n && m > 0.0;
+                                    if (send) atomicAdd(mrow + (size_t)tv * Qu, m);
+                                    const unsigned bits = __ballot_sync(kFull, send);
+                                    if (bits && lane == 0) atomicOr(trow + ((size_t)tv << p.logW), bits);
                                 }
                             }
                         }
+                        if (lane == 0) pushes += (long long)__popc(km) * (hi - lo);
                         steps += hi - lo;
                     }
                     e0 = seg_end;
                     o += 32;
                 }
             }
-            list_stage_push(tst, p.touched, &ctl->listctr[slot], p.qcap, flags, lane < npend, pv);
-            list_stage_flush(tst, p.touched, &ctl->listctr[slot], p.qcap, flags);
         }
         if (!grid_sync(bar, flags, p.barrier_ns)) return;
-        // Phase B: apply messages of the touched pairs and activate.
-        {
-            const unsigned n = min(ldcg(&ctl->listctr[slot]), p.qcap);
-            if (gtid == 0) ctl->touched += n;
-            const FrontierOut out = pbatch_out(p, (cur + 1) & 1, nslot);
-            for (unsigned i = gwarp; i < n; i += nwarps) {
-                const int vw = ldcg(p.touched + i);
-                unsigned* tm = p.tmask + (unsigned)vw;
-                const unsigned lanes = ldcg(tm);
-                pbatch_apply(p, vw, lanes, false, fst, out, &ctl->dctr[nslot]);
-                __syncwarp();
-                if (lane == 0) *tm = 0u;
-            }
-            stage_flush(fst, out);
-        }
+        // Phase B: apply the messages of the touched pairs and activate.
+        touched += pbatch_sweep(p, false, fst, pbatch_out(p, (cur + 1) & 1, nslot), &ctl->dctr[nslot], gwarp,
+                                nwarps, lane);
         if (!grid_sync(bar, flags, p.barrier_ns)) return;
         ++cur;
     }
-    for (int o = 16; o >= 1; o >>= 1) pushes += __shfl_xor_sync(kFull, pushes, o);
+    // pushes are counted by lane 0 of each warp; touched pairs once per warp
     if (lane == 0) {
         atomicAdd((unsigned long long*)&p.counters[0], (unsigned long long)pushes);
         atomicAdd((unsigned long long*)&p.counters[1], (unsigned long long)steps);
+        atomicAdd((unsigned long long*)&ctl->touched, (unsigned long long)touched);
     }
     if (gtid == 0) ctl->iterations = iters;
 }
@@ -818,7 +772,6 @@ struct PprBatchWork {
     int2* q[2] = {nullptr, nullptr};
     unsigned* qmask[2] = {nullptr, nullptr};
     int* mark[2] = {nullptr, nullptr};
-    int* touched = nullptr;
     int2* dangle = nullptr;
     TraversalCtl* ctl = nullptr;
     long long* counters = nullptr;
@@ -836,7 +789,7 @@ void ppr_batch_free(c2g_graph* g) {
     PprBatchWork* w = reinterpret_cast<PprBatchWork*>(g->ppr_batch);
     if (!w) return;
     void* ptrs[] = {w->pr, w->res, w->msg, w->rq, w->tmask, w->q[0], w->q[1], w->qmask[0], w->qmask[1],
-                    w->mark[0], w->mark[1], w->touched, w->dangle, w->ctl, w->counters, w->src, w->seed_off,
+                    w->mark[0], w->mark[1], w->dangle, w->ctl, w->counters, w->src, w->seed_off,
                     w->seed_v, w->seed_w, w->stage};
     for (void* p : ptrs)
         if (p) cudaFree(p);
@@ -864,7 +817,6 @@ static int ppr_batch_alloc(c2g_graph* g, int Q, size_t n_seeds) {
         C2G_CUDA(cudaMalloc(&w->qmask[b], sizeof(unsigned) * qcap));
         C2G_CUDA(cudaMalloc(&w->mark[b], sizeof(int) * mark_cap));
     }
-    C2G_CUDA(cudaMalloc(&w->touched, sizeof(int) * qcap));
     C2G_CUDA(cudaMalloc(&w->dangle, sizeof(int2) * qcap));
     C2G_CUDA(cudaMalloc(&w->ctl, sizeof(TraversalCtl)));
     C2G_CUDA(cudaMalloc(&w->counters, sizeof(long long) * 2));
@@ -932,7 +884,6 @@ int ppr_batch_launch(c2g_graph* g, int32_t nq, const int32_t* sources, const c2g
         p.qmask[b] = w->qmask[b];
         p.mark[b] = w->mark[b];
     }
-    p.touched = w->touched;
     p.dangle = w->dangle;
     p.ctl = w->ctl;
     p.sources = w->src;

@@ -42,6 +42,7 @@ struct PprParams {
     const int2* adj_r;
     const int* mark_r;  // owner of in-edge t * 2^kPullTileLog
     int pull_div;       // pull when T * pull_div > E (0: never)
+    int dense_div;      // dense push round (no touched list) when T * dense_div > E (0: never)
     float* pr;
     double* res;
     double* msg;
@@ -90,8 +91,10 @@ constexpr int kPprUnroll = 4;  // edges in flight per lane
 // atomicAdd returns 0 (msg[v] is 0 between rounds and every message is positive), so no
 // separate touched flag is needed.  Zero messages are dropped: a vertex outside the
 // frontier never holds a residual above rmax, so a zero message cannot activate it.
+// With track = false (a dense round) the adds are fire-and-forget red.add and the
+// apply pass sweeps all vertices instead of a touched list.
 __device__ __forceinline__ void ppr_push(const PprParams& p, int buf, int slot, unsigned F, unsigned T,
-                                         WarpStage& tst) {
+                                         WarpStage& tst, bool track) {
     constexpr int U = kPprUnroll;
     const double one_m_a = 1.0 - (double)p.alpha;
     const double* qv = p.qval[buf];
@@ -111,6 +114,12 @@ __device__ __forceinline__ void ppr_push(const PprParams& p, int buf, int slot, 
                 c[u] = ew.x;
                 m[u] = qu[u] * (double)__int_as_float(ew.y);
             }
+            if (!track) {
+#pragma unroll
+                for (int u = 0; u < U; ++u)
+                    if (ok[u] && m[u] > 0.0) atomicAdd(p.msg + c[u], m[u]);
+                return;
+            }
             double old[U];
 #pragma unroll
             for (int u = 0; u < U; ++u) old[u] = (ok[u] && m[u] > 0.0) ? atomicAdd(p.msg + c[u], m[u]) : 1.0;
@@ -119,7 +128,7 @@ __device__ __forceinline__ void ppr_push(const PprParams& p, int buf, int slot, 
                 list_stage_push(tst, p.touched, &p.ctl->listctr[slot], (unsigned)p.V, &p.ctl->flags,
                                 old[u] == 0.0, c[u]);
         });
-    list_stage_flush(tst, p.touched, &p.ctl->listctr[slot], (unsigned)p.V, &p.ctl->flags);
+    if (track) list_stage_flush(tst, p.touched, &p.ctl->listctr[slot], (unsigned)p.V, &p.ctl->flags);
 }
 
 // Pull round, phase A: msg[v] = sum over in-edges (u, w) of qd[u] * w.  In-edges are
@@ -328,6 +337,7 @@ __global__ void __launch_bounds__(512, 2) ppr_persistent(const PprParams p) {
         }
         const int slot = cur % 3, nslot = (cur + 1) % 3, fslot = (cur + 2) % 3;
         const bool pull = p.row_r && p.pull_div > 0 && (unsigned long long)T * (unsigned)p.pull_div > p.E;
+        const bool dense = pull || (p.dense_div > 0 && (unsigned long long)T * (unsigned)p.dense_div > p.E);
         if (gtid == 0) {
             ctl->qctr[fslot] = 0ull;
             ctl->tilectr[fslot] = 0u;
@@ -338,9 +348,12 @@ __global__ void __launch_bounds__(512, 2) ppr_persistent(const PprParams p) {
             if (pull) ctl->pad[0] += 1;  // pull rounds
         }
         const FrontierOut out = ppr_out(p, (cur + 1) & 1, nslot);
-        if (!pull) {
-            ppr_push(p, cur & 1, slot, F, T, tst);
-            if (!grid_sync(bar, flags, p.barrier_ns)) return;
+        if (pull)
+            ppr_pull(p);
+        else
+            ppr_push(p, cur & 1, slot, F, T, tst, !dense);
+        if (!grid_sync(bar, flags, p.barrier_ns)) return;
+        if (!dense) {
             // Phase B: apply messages and activate (src/ppr/purn/Main.cu:383-391).
             const unsigned n = ldcg(&ctl->listctr[slot]);
             if (gtid == 0) ctl->touched += n;
@@ -368,8 +381,6 @@ __global__ void __launch_bounds__(512, 2) ppr_persistent(const PprParams p) {
                 list_push(p.dangle, &ctl->dctr[nslot], (unsigned)p.V, flags, dang, v);
             }
         } else {
-            ppr_pull(p);
-            if (!grid_sync(bar, flags, p.barrier_ns)) return;
             // Dense apply: every vertex (an untouched one has msg 0 and res <= rmax, so
             // it is left as it is).
             if (gtid == 0) ctl->touched += V;
@@ -380,7 +391,7 @@ __global__ void __launch_bounds__(512, 2) ppr_persistent(const PprParams p) {
                 double r = 0.0;
                 if (v < V) {
                     const double m = __ldcg(p.msg + v);
-                    const double q0 = __ldcg(p.qd + v);
+                    const double q0 = p.qd ? __ldcg(p.qd + v) : 0.0;
                     if (m != 0.0) {
                         p.msg[v] = 0.0;
                         r = __ldcg(p.res + v) + m;
@@ -395,7 +406,7 @@ __global__ void __launch_bounds__(512, 2) ppr_persistent(const PprParams p) {
                         }
                     }
                     const double q1 = want ? one_m_a * r : 0.0;
-                    if (q1 != q0) p.qd[v] = q1;
+                    if (p.qd && q1 != q0) p.qd[v] = q1;
                 }
                 stage_push(fst, out, want, (int)v, deg, 0.f, r);
                 list_push(p.dangle, &ctl->dctr[nslot], (unsigned)p.V, flags, dang, (int)v);
@@ -517,6 +528,7 @@ int ppr_launch_view(c2g_graph* g, const int32_t* row, const int2* adj, const int
     p.adj_r = adj_rev;
     p.mark_r = mark_rev;
     p.pull_div = row_rev ? g->ppr_cfg.pull_div : 0;
+    p.dense_div = g->ppr_cfg.dense_div;
     p.pr = pr_dev ? pr_dev : w.pr;
     p.res = w.res;
     p.msg = w.msg;

@@ -205,11 +205,13 @@ int c2g_ppr(c2g_graph* g, int32_t source, const c2g_ppr_params* params, float* p
 int c2g_ppr_batch(c2g_graph* g, int32_t n, const int32_t* sources, const c2g_ppr_params* params,
                   float* pr, float* res, int on_device, int layout, c2g_stats* stats);
 
-/* Round shape of the push kernel: a round whose frontier has more than E / pull_div
- * out-edges pulls over the reverse CSR (built on first use) instead of pushing;
- * pull_div = 0 (the default) keeps every round a push.  Results are the same BSP rounds
- * either way. */
-int c2g_ppr_set_config(c2g_graph* g, int32_t pull_div);
+/* Round shapes of the push kernel.  A round whose frontier has more than E / pull_div
+ * out-edges pulls over the reverse CSR (built on first use) instead of pushing
+ * (pull_div = 0, the default: never).  A push round whose frontier has more than
+ * E / dense_div out-edges adds its messages without tracking first touches and applies
+ * them in one sweep over all vertices (dense_div = 0: never; default 8).  Results are
+ * the same BSP rounds either way. */
+int c2g_ppr_set_config(c2g_graph* g, int32_t pull_div, int32_t dense_div);
 
 /* Reference defaults: PPR (alpha 0.2, rmax 0.001/(V+1), cap 500), and the adsorption
  * program (alpha 0.2, r0 10, pr0 8, rmax 1/V, cap 2000). */
