@@ -280,7 +280,7 @@ class Graph:
                                     ctypes.byref(st)))
         return dist, st
 
-    def ppr_config(self, pull_div=0, dense_div=8):
+    def ppr_config(self, pull_div=0, dense_div=16):
         _check(lib().c2g_ppr_set_config(self._h, pull_div, dense_div))
 
     def ppr_params(self, adsorption=False, **kw):

@@ -21,6 +21,7 @@
 #include <vector>
 
 #include "device_common.cuh"
+#include "fp64_mul.h"
 #include "internal.h"
 
 namespace c2g {
@@ -690,6 +691,7 @@ __global__ void __launch_bounds__(512, 2) ppr_batch_persistent(const PprBatchPar
                         // (1-alpha)*r_u of this lane's query (src/ppr/purn/Main.cu:288)
                         const double qu =
                             act ? one_m_a * ldcg(p.rq + (size_t)((unsigned)kvw >> p.logW) * Qu + (w << 5) + lane) : 0.0;
+                        const DSplit qs = c2g_dsplit(qu);
                         for (unsigned eb = lo; eb < hi; eb += 32) {
                             const unsigned n = min(32u, hi - eb);
                             const int2 my =
@@ -698,9 +700,15 @@ __global__ void __launch_bounds__(512, 2) ppr_batch_persistent(const PprBatchPar
 #pragma unroll
                                 for (int jj = 0; jj < kPprBatchUnroll; ++jj) {
                                     const unsigned tv = (unsigned)__shfl_sync(kFull, my.x, (int)g + jj);
-                                    const float tw = __int_as_float(__shfl_sync(kFull, my.y, (int)g + jj));
-                                    const double m = qu * (double)tw;
-                                    const bool send = act && g + jj < n && m > 0.0;
+                                    const unsigned wb = (unsigned)__shfl_sync(kFull, my.y, (int)g + jj);
+                                    // m = qu * w in FP64, on the integer pipes (fp64_mul.h)
+                                    bool send = act && g + jj < n && (int)wb > 0;
+                                    const bool ok = c2g_mul_ok(qs, wb);
+                                    double m = c2g_mul(qs, wb);
+                                    if (__any_sync(kFull, send && !ok)) {  // w subnormal: FP64 pipe
+                                        if (!ok) m = qu * (double)__uint_as_float(wb);
+                                        send = send && (ok || m > 0.0);
+                                    }
                                     if (send) atomicAdd(mrow + (size_t)tv * Qu, m);
                                     const unsigned bits = __ballot_sync(kFull, send);
                                     if (bits && lane == 0) atomicOr(trow + ((size_t)tv << p.logW), bits);

@@ -1,0 +1,102 @@
+// Exact IEEE-754 binary64 product q * (double)w for a positive normal double q and a
+// positive normal float w, rounded to nearest-even, computed with 32-bit integer
+// multiplies only.
+//
+// Why: the FP64 residual push multiplies every frontier residual by every edge weight
+// (q * w, src/ppr/purn/Main.cu:288).  GB300 issues FP64 instructions at a small
+// fraction of its integer rate, so the float->double conversion, the double multiply
+// and the double compare of each push kept the FP64 pipe busy (ncu
+// sm__pipe_fp64_cycles_active) while memory sat idle.  The result here is bit-identical
+// to the hardware multiply (checked against it on the host in tests), so parity with
+// the FP64 push is unchanged.
+//
+// Method (IEEE-754 arithmetic, nothing library-specific): with significands
+// Sq = 2^52 + mq (53 bits) and Sw = 2^23 + mw (24 bits), the exact product
+// P = Sq * Sw lies in [2^75, 2^77).  Keep its top 53 bits (shift s = 23 or 24), round
+// the s dropped bits to nearest-even, and set the exponent to eq + ew + s - 150
+// (biased).  A carry out of the rounding lands in the exponent field by adding the
+// 53-bit significand (implicit bit included) to (exponent - 1) << 52.
+//
+// Outside the domain (w zero or subnormal, a product exponent outside the normal
+// range) c2g_mul_ok() is false and the caller multiplies in FP64 instead.
+#pragma once
+
+#include <stdint.h>
+
+#if defined(__CUDACC__)
+#define C2G_HD __host__ __device__ __forceinline__
+#else
+#define C2G_HD inline
+#endif
+
+namespace c2g {
+
+struct DSplit {
+    uint32_t lo;  // low 32 bits of the significand
+    uint32_t hi;  // high 21 bits of the significand, implicit bit included
+    int32_t e;    // biased exponent
+};
+
+C2G_HD uint64_t c2g_dbits(double x) {
+#if defined(__CUDA_ARCH__)
+    return (uint64_t)__double_as_longlong(x);
+#else
+    union {
+        double d;
+        uint64_t u;
+    } c;
+    c.d = x;
+    return c.u;
+#endif
+}
+
+C2G_HD double c2g_bitsd(uint64_t b) {
+#if defined(__CUDA_ARCH__)
+    return __longlong_as_double((long long)b);
+#else
+    union {
+        double d;
+        uint64_t u;
+    } c;
+    c.u = b;
+    return c.d;
+#endif
+}
+
+// Split of a positive normal double (done once per frontier residual).
+C2G_HD DSplit c2g_dsplit(double q) {
+    const uint64_t b = c2g_dbits(q);
+    DSplit s;
+    s.lo = (uint32_t)b;
+    s.hi = ((uint32_t)(b >> 32) & 0xfffffu) | 0x100000u;
+    s.e = (int32_t)((b >> 52) & 0x7ffu);
+    return s;
+}
+
+// True when q (split) * w (float bits, sign 0) stays in the domain of c2g_mul.
+C2G_HD bool c2g_mul_ok(const DSplit& q, uint32_t wb) {
+    const int32_t ew = (int32_t)(wb >> 23);
+    const int32_t e = q.e + ew - 127;  // product exponent before the +1 of s = 24 and of rounding
+    return ew > 0 && ew < 255 && q.e > 0 && q.e < 2047 && e >= 1 && e <= 2044;
+}
+
+// q * (double)w, exact and rounded to nearest-even; requires c2g_mul_ok(q, wb).
+C2G_HD double c2g_mul(const DSplit& q, uint32_t wb) {
+    const uint32_t ew = wb >> 23;
+    const uint32_t sw = (wb & 0x7fffffu) | 0x800000u;
+    const uint64_t a = (uint64_t)q.lo * sw;  // < 2^56
+    const uint64_t b = (uint64_t)q.hi * sw;  // < 2^45
+    // P = b * 2^32 + a = ph * 2^64 + pl, ph < 2^13
+    const uint64_t pl = a + (b << 32);
+    const uint32_t ph = (uint32_t)(b >> 32) + (pl < a ? 1u : 0u);
+    const uint32_t top = ph >> 12;  // 1 when P >= 2^76
+    const uint32_t s = 23u + top;
+    uint64_t m = (pl >> s) | ((uint64_t)ph << (64u - s));  // top 53 bits of P
+    const uint64_t r = pl & ((1ull << s) - 1ull);           // dropped bits
+    const uint64_t half = 1ull << (s - 1u);
+    m += (r > half || (r == half && (m & 1ull))) ? 1ull : 0ull;
+    const int64_t e = (int64_t)q.e + (int64_t)ew + (int64_t)s - 150;
+    return c2g_bitsd(((uint64_t)(e - 1) << 52) + m);
+}
+
+}  // namespace c2g

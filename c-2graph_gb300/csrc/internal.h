@@ -91,7 +91,7 @@ struct SsspConfig {
 struct PprConfig {
     int log_tile = 8;
     int pull_div = 0;   // pull round when frontier out-edges * pull_div > E; 0 = push only (default)
-    int dense_div = 8;  // dense push round (red.add, apply sweep over V) when out-edges * dense_div > E
+    int dense_div = 16;  // dense push round (red.add, apply sweep over V) when out-edges * dense_div > E
 };
 
 constexpr int kPullTileLog = 8;  // in-edges per pull tile (reverse-CSR markers)

@@ -29,6 +29,7 @@
 #include <climits>
 
 #include "device_common.cuh"
+#include "fp64_mul.h"
 #include "internal.h"
 
 namespace c2g {
@@ -108,25 +109,37 @@ __device__ __forceinline__ void ppr_push(const PprParams& p, int buf, int slot, 
         [&](const bool* ok, const unsigned* idx, const double* qu) {
             int c[U];
             double m[U];
+            bool send[U];
 #pragma unroll
             for (int u = 0; u < U; ++u) {
                 const int2 ew = ok[u] ? __ldg(p.adj + idx[u]) : make_int2(0, 0);
                 c[u] = ew.x;
-                m[u] = qu[u] * (double)__int_as_float(ew.y);
+                // m = qu * w in FP64, on the integer pipes (fp64_mul.h); a message is sent
+                // when it is positive (w > 0: qu > 0 for every activated vertex)
+                const unsigned wb = (unsigned)ew.y;
+                const DSplit qs = c2g_dsplit(qu[u]);
+                const bool mok = c2g_mul_ok(qs, wb);
+                send[u] = ok[u] && ew.y > 0;
+                m[u] = c2g_mul(qs, wb);
+                if (__any_sync(kFull, send[u] && !mok)) {  // w subnormal: FP64 pipe
+                    if (!mok) m[u] = qu[u] * (double)__int_as_float(ew.y);
+                    send[u] = send[u] && (mok || m[u] > 0.0);
+                }
             }
             if (!track) {
 #pragma unroll
                 for (int u = 0; u < U; ++u)
-                    if (ok[u] && m[u] > 0.0) atomicAdd(p.msg + c[u], m[u]);
+                    if (send[u]) atomicAdd(p.msg + c[u], m[u]);
                 return;
             }
-            double old[U];
+            unsigned long long old[U];
 #pragma unroll
-            for (int u = 0; u < U; ++u) old[u] = (ok[u] && m[u] > 0.0) ? atomicAdd(p.msg + c[u], m[u]) : 1.0;
+            for (int u = 0; u < U; ++u)
+                old[u] = send[u] ? c2g_dbits(atomicAdd(p.msg + c[u], m[u])) : 1ull;
 #pragma unroll
             for (int u = 0; u < U; ++u)
                 list_stage_push(tst, p.touched, &p.ctl->listctr[slot], (unsigned)p.V, &p.ctl->flags,
-                                old[u] == 0.0, c[u]);
+                                old[u] == 0ull, c[u]);
         });
     if (track) list_stage_flush(tst, p.touched, &p.ctl->listctr[slot], (unsigned)p.V, &p.ctl->flags);
 }
@@ -392,7 +405,7 @@ __global__ void __launch_bounds__(512, 2) ppr_persistent(const PprParams p) {
                 if (v < V) {
                     const double m = __ldcg(p.msg + v);
                     const double q0 = p.qd ? __ldcg(p.qd + v) : 0.0;
-                    if (m != 0.0) {
+                    if (c2g_dbits(m) != 0ull) {  // messages are positive; msg is +0 otherwise
                         p.msg[v] = 0.0;
                         r = __ldcg(p.res + v) + m;
                         if (r > rmax) {

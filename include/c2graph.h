@@ -209,7 +209,7 @@ int c2g_ppr_batch(c2g_graph* g, int32_t n, const int32_t* sources, const c2g_ppr
  * out-edges pulls over the reverse CSR (built on first use) instead of pushing
  * (pull_div = 0, the default: never).  A push round whose frontier has more than
  * E / dense_div out-edges adds its messages without tracking first touches and applies
- * them in one sweep over all vertices (dense_div = 0: never; default 8).  Results are
+ * them in one sweep over all vertices (dense_div = 0: never; default 16).  Results are
  * the same BSP rounds either way. */
 int c2g_ppr_set_config(c2g_graph* g, int32_t pull_div, int32_t dense_div);
 
