@@ -106,6 +106,7 @@ SIGNATURES = {
     "c2g_ppr": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.POINTER(PprParams), _P, _P, ctypes.c_int,
                                ctypes.POINTER(Stats)]),
     "c2g_ppr_set_config": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int32]),
+    "c2g_graph_set_watchdog": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int32]),
     "c2g_ppr_default_params": (ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(PprParams)]),
     "c2g_ppr_batch": (ctypes.c_int, [_P, ctypes.c_int32, _P, ctypes.POINTER(PprParams), _P, _P, ctypes.c_int,
                                      ctypes.c_int, ctypes.POINTER(Stats)]),
@@ -279,6 +280,9 @@ class Graph:
         _check(lib().c2g_sssp_batch(self._h, len(src), _ptr(src), int(seeds), mode, _ptr(dist), 0, layout,
                                     ctypes.byref(st)))
         return dist, st
+
+    def watchdog(self, barrier_timeout_ms=0, stall_next_sssp=False):
+        _check(lib().c2g_graph_set_watchdog(self._h, barrier_timeout_ms, int(bool(stall_next_sssp))))
 
     def ppr_config(self, pull_div=0, dense_div=16):
         _check(lib().c2g_ppr_set_config(self._h, pull_div, dense_div))

@@ -391,6 +391,15 @@ int c2g_sssp_set_config(c2g_graph* g, int32_t delta, int32_t tile, int32_t max_i
     return C2G_OK;
 }
 
+int c2g_graph_set_watchdog(c2g_graph* g, int32_t barrier_timeout_ms, int32_t stall_next_sssp) {
+    if (!g) return fail(C2G_ERR_ARG, "graph is NULL");
+    if (barrier_timeout_ms < 0) return fail(C2G_ERR_ARG, "barrier_timeout_ms must be >= 0");
+    std::lock_guard<std::mutex> lk(g->mu);
+    g->barrier_ns = (unsigned long long)barrier_timeout_ms * 1000000ull;
+    g->stall_next_sssp = stall_next_sssp ? 1 : 0;
+    return C2G_OK;
+}
+
 int c2g_ppr_set_config(c2g_graph* g, int32_t pull_div, int32_t dense_div) {
     if (!g) return fail(C2G_ERR_ARG, "graph is NULL");
     if (pull_div < 0 || dense_div < 0) return fail(C2G_ERR_ARG, "pull_div and dense_div must be >= 0");

@@ -388,7 +388,7 @@ int sssp_batch_launch(c2g_graph* g, int32_t nq, const int32_t* sources, const st
     p.qcap = (unsigned)((size_t)g->V * (size_t)(Q / 32));
     p.mark_cap = (unsigned)((((size_t)g->E * (size_t)(Q / 32)) >> kBatchTileLog) + 2);
     p.max_iter = g->sssp_cfg.max_iter;
-    p.barrier_ns = 4000000000ull;
+    p.barrier_ns = g->barrier_ns ? g->barrier_ns : 4000000000ull;
     p.counters = w->counters;
     C2G_CUDA(cudaMemsetAsync(w->ctl, 0, sizeof(TraversalCtl), g->stream));
     C2G_CUDA(cudaMemsetAsync(w->counters, 0, sizeof(long long) * 2, g->stream));
@@ -906,7 +906,7 @@ int ppr_batch_launch(c2g_graph* g, int32_t nq, const int32_t* sources, const c2g
     p.max_iter = prm.max_iter;
     p.qcap = (unsigned)((size_t)g->V * (size_t)(p.Q / 32));
     p.mark_cap = (unsigned)((((size_t)g->E * (size_t)(p.Q / 32)) >> kBatchTileLog) + 2);
-    p.barrier_ns = 4000000000ull;
+    p.barrier_ns = g->barrier_ns ? g->barrier_ns : 4000000000ull;
     p.counters = w->counters;
     C2G_CUDA(cudaMemsetAsync(w->ctl, 0, sizeof(TraversalCtl), g->stream));
     C2G_CUDA(cudaMemsetAsync(w->counters, 0, sizeof(long long) * 2, g->stream));

@@ -56,7 +56,10 @@ __device__ __forceinline__ double ldcg(const double* p) { return __ldcg(p); }
 // Grid barrier with a time limit.  Every CTA of a cooperative launch calls it; it
 // returns false (and all later calls return false) once any CTA has given up, so the
 // caller returns and the launch ends with C2G_FLAG_BARRIER_TIMEOUT recorded.
-__device__ __forceinline__ bool grid_sync(GridBarrier* b, int* flags, unsigned long long limit_ns) {
+// `extra` > 0 makes the barrier wait for that many blocks beyond the grid, so every wait
+// runs out (the failure-detection test of c2g_graph_set_watchdog; no block hangs).
+__device__ __forceinline__ bool grid_sync(GridBarrier* b, int* flags, unsigned long long limit_ns,
+                                          unsigned extra = 0) {
     __shared__ int s_ok;
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -66,7 +69,7 @@ __device__ __forceinline__ bool grid_sync(GridBarrier* b, int* flags, unsigned l
         // device scope before arriving.
         __threadfence();
         const unsigned arrived = atom_add_acq_rel_u32(&b->count, 1u);
-        if (arrived == gridDim.x - 1) {
+        if (arrived == gridDim.x - 1 + extra) {
             b->count = 0;
             st_release_u32(&b->gen, g + 1);
         } else {

@@ -141,6 +141,8 @@ struct c2g_graph {
     c2g::LaunchGeom geom_sssp, geom_ppr;
     int num_sms = 0;
     float grid_scale = 1.0f;  // fraction of the GPU a batched launch may occupy
+    unsigned long long barrier_ns = 0;  // grid-barrier wait limit (0: per-kernel default)
+    int stall_next_sssp = 0;            // failure-detection test: next SSSP barrier cannot complete
     bool borrowed = false;    // a view: graph arrays belong to another handle
 };
 

@@ -572,7 +572,7 @@ int ppr_launch_view(c2g_graph* g, const int32_t* row, const int2* adj, const int
     p.n_rec = n_rec;
     p.log_tile = w.log_tile;
     p.mark_cap = w.mark_cap;
-    p.barrier_ns = 2000000000ull;
+    p.barrier_ns = g->barrier_ns ? g->barrier_ns : 2000000000ull;
     C2G_CUDA(cudaMemsetAsync(w.ctl, 0, sizeof(TraversalCtl), g->stream));
     void* args[] = {&p};
     C2G_CUDA(cudaEventRecord(g->ev0, g->stream));

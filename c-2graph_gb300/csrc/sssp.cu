@@ -46,6 +46,7 @@ struct SsspParams {
     int max_iter;
     unsigned mark_cap;
     unsigned long long barrier_ns;
+    unsigned bar_extra;  // > 0: barriers wait for blocks that do not exist (watchdog test)
 };
 
 __device__ __forceinline__ FrontierOut sssp_out(const SsspParams& p, int buf, int slot) {
@@ -171,7 +172,7 @@ __global__ void __launch_bounds__(512, 2) sssp_persistent(const SsspParams p) {
         }
     }
     if (gtid == 0) ctl->farmin[0] = ctl->farmin[1] = ctl->farmin[2] = INT_MAX;
-    if (!grid_sync(bar, flags, p.barrier_ns)) return;
+    if (!grid_sync(bar, flags, p.barrier_ns, p.bar_extra)) return;
 
     // Source and pruned-record seeds (src/sssp/purn/Main.cu:160-181).
     if (gtid == 0) {
@@ -179,7 +180,7 @@ __global__ void __launch_bounds__(512, 2) sssp_persistent(const SsspParams p) {
         ctl->seeds = p.n_seeds;
     }
     for (unsigned i = gtid; i < (unsigned)p.n_seeds; i += nthreads) atomicMin(p.dist + p.seed_v[i], p.seed_w[i]);
-    if (!grid_sync(bar, flags, p.barrier_ns)) return;
+    if (!grid_sync(bar, flags, p.barrier_ns, p.bar_extra)) return;
 
     // Round-1 frontier: the seeds and the source, deduplicated.
     {
@@ -198,7 +199,7 @@ __global__ void __launch_bounds__(512, 2) sssp_persistent(const SsspParams p) {
         }
         stage_flush(fst, out);
     }
-    if (!grid_sync(bar, flags, p.barrier_ns)) return;
+    if (!grid_sync(bar, flags, p.barrier_ns, p.bar_extra)) return;
 
     int cur = 1, fb = 0, epoch = ebase + 1, iters = 0;
     int thresh = kDelta ? p.delta : INT_MAX;
@@ -247,7 +248,7 @@ __global__ void __launch_bounds__(512, 2) sssp_persistent(const SsspParams p) {
             thresh = (int)nt;
             fb = fdst;
             ++epoch;
-            if (!grid_sync(bar, flags, p.barrier_ns)) return;
+            if (!grid_sync(bar, flags, p.barrier_ns, p.bar_extra)) return;
             continue;
         }
         if (++iters > p.max_iter) {
@@ -262,7 +263,7 @@ __global__ void __launch_bounds__(512, 2) sssp_persistent(const SsspParams p) {
         }
         const FrontierOut nout = sssp_out(p, (cur + 1) & 1, (cur + 1) % 3);
         sssp_expand<kDelta>(p, cur & 1, F, T, sbase + cur + 1, thresh, fb, epoch, nout, fst, far);
-        if (!grid_sync(bar, flags, p.barrier_ns)) return;
+        if (!grid_sync(bar, flags, p.barrier_ns, p.bar_extra)) return;
         ++cur;
     }
     if (gtid == 0) {
@@ -358,7 +359,9 @@ int sssp_launch(c2g_graph* g, int32_t source, const int32_t* seed_v, const int32
     p.log_tile = w.log_tile;
     p.max_iter = g->sssp_cfg.max_iter;
     p.mark_cap = w.mark_cap;
-    p.barrier_ns = 2000000000ull;
+    p.barrier_ns = g->barrier_ns ? g->barrier_ns : 2000000000ull;
+    p.bar_extra = g->stall_next_sssp ? 1u : 0u;
+    g->stall_next_sssp = 0;
     C2G_CUDA(cudaMemsetAsync(w.ctl, 0, sizeof(TraversalCtl), g->stream));
     void* args[] = {&p};
     const bool delta = p.delta > 0;
@@ -475,6 +478,7 @@ extern "C" int c2g_sssp_noalloc(const int32_t* row, const void* adj, int32_t V, 
     p.max_iter = 1 << 20;
     p.mark_cap = (unsigned)(((size_t)E >> kNoAllocLogTile) + 2);
     p.barrier_ns = 2000000000ull;
+    p.bar_extra = 0u;
     C2G_CUDA(cudaMemsetAsync(p.ctl, 0, sizeof(TraversalCtl), s));
     void* args[] = {&p};
     C2G_CUDA(cudaLaunchCooperativeKernel((const void*)sssp_persistent<false>, dim3(per_sm * sms), dim3(512), args, 0,

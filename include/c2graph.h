@@ -123,6 +123,15 @@ void c2g_graph_free(c2g_graph* g);
 int  c2g_graph_info(const c2g_graph* g, int32_t* V, int64_t* E, int32_t* R);
 /* Use the caller's CUDA stream (cudaStream_t passed as void*) instead of the handle's. */
 int  c2g_graph_set_stream(c2g_graph* g, void* stream);
+/* Watchdog of the persistent launches (no counterpart in the reference, whose software
+ * grid barrier spins without limit, src/sssp/purn/Main.cu:173-189).  Every grid barrier
+ * wait of a launch on this handle gives up after barrier_timeout_ms (0: the defaults,
+ * 2 s single-query, 4 s batched); the call then returns C2G_ERR_TIMEOUT with
+ * C2G_FLAG_BARRIER_TIMEOUT in the stats, and the handle stays usable.
+ * stall_next_sssp = 1 makes the next c2g_sssp launch's barriers wait for one block more
+ * than the grid has, so the wait runs out on purpose: a failure-detection test that
+ * faults and hangs nothing. */
+int  c2g_graph_set_watchdog(c2g_graph* g, int32_t barrier_timeout_ms, int32_t stall_next_sssp);
 
 /* ---- SSSP -------------------------------------------------------------------------- */
 /* Source-skip rule of the drop-in programs: sssp-base skips sources without

@@ -263,3 +263,29 @@ def test_sssp_autotune(gpu_available, rmat16, tmp_path):
         ref = oracle.dijkstra(o["vlist"], o["elist"], o["wlist"], [srcs[0]], [0])
         d, _ = gr.sssp(srcs[0])  # the tuned configuration is applied
         assert np.array_equal(d, ref)
+
+
+def test_watchdog_barrier_timeout_is_reported_and_recoverable(gpu_available, rmat16):
+    """Failure detection without a fault: the next launch's grid barrier waits for one
+    block more than the grid has, every bounded wait runs out after 100 ms, the call
+    returns C2G_ERR_TIMEOUT, and the same handle answers the next query correctly."""
+    import time
+
+    import c2g
+    import oracle
+
+    o = oracle.load_dataset(rmat16, "origin")
+    deg = np.diff(o["vlist"])
+    s = int(np.argmax(deg))
+    with c2g.Graph.load(rmat16, "origin") as g:
+        g.watchdog(barrier_timeout_ms=100, stall_next_sssp=True)
+        t0 = time.time()
+        with pytest.raises(c2g.C2GError) as ei:
+            g.sssp(s)
+        assert ei.value.code == -7  # C2G_ERR_TIMEOUT
+        assert time.time() - t0 < 10.0
+        g.watchdog()  # default limits again
+        dist, st = g.sssp(s)
+        assert st.status_flags == 0
+        ref = oracle.dijkstra(o["vlist"], o["elist"], o["wlist"], [s], [0])
+        assert np.array_equal(dist, ref)
