@@ -548,12 +548,12 @@ int c2g_ppr_batch(c2g_graph* g, int32_t n, const int32_t* sources, const c2g_ppr
         stats->n_seeds = (int64_t)sv.size();
         stats->device_ms = ms;
         stats->status_flags = ctl.flags;
-        // 40 per frontier entry + 8 per edge-word step + 8 per (query, edge) push
-        // (4 B residual share + 4 B message add) + 12 per touched lane-row word read/write
-        // + the pr/res initialisation.
+        // 40 per frontier entry + 8 per edge-word step + 8 per (query, edge) push (FP64
+        // message add) + 32 per touched (vertex, query) lane (res and msg read and
+        // write) + the pr/res initialisation (12 per vertex and query).
         const double Qp = (double)((n + 31) / 32 * 32);
         stats->alg_bytes = 40.0 * (double)ctl.popped + 8.0 * (double)ctl.relaxed + 8.0 * (double)counters[0] +
-                           12.0 * 32.0 * (double)ctl.touched + 8.0 * (double)g->V * Qp;
+                           32.0 * (double)ctl.touched + 12.0 * (double)g->V * Qp;
     }
     if (ctl.flags & C2G_FLAG_BARRIER_TIMEOUT) return fail(C2G_ERR_TIMEOUT, "grid barrier wait ran out");
     if (ctl.flags & C2G_FLAG_QUEUE_OVERFLOW) return fail(C2G_ERR_OVERFLOW, "frontier queue overflow");

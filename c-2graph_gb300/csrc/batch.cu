@@ -91,7 +91,37 @@ __device__ __forceinline__ void batch_sweep(const BatchParams& p, const Frontier
     stage_flush(fst, out);
 }
 
-constexpr int kBatchUnroll = 6;  // target rows in flight per lane (8 spills at 64 registers)
+constexpr int kBatchUnroll = 4;  // relaxation items in flight per lane
+
+// Lane compaction of one owner run: the run's work is the items (edge ei, active-query
+// slot j) for ei in [0, len) and j in [0, cnt), numbered i = ei * cnt + j; lane l takes
+// items l, l + 32, l + 64, ... so every lane of a warp step relaxes something even when
+// few of the word's 32 queries are active.  The (ei, j) of a lane advance by 32 items
+// per step without a division (32 = dq * cnt + dr).  Lane 0 holds the lowest item, so
+// the loop condition is warp-uniform; body(ei[U], j[U]) must check ei < len.
+template <int U, typename Body>
+__device__ __forceinline__ void owner_items(unsigned cnt, unsigned len, int lane, Body body) {
+    const float rc = __frcp_rn((float)cnt);  // exact enough: (l + 0.5) / cnt is >= 1/64 from an integer
+    int ei = (int)(((float)lane + 0.5f) * rc);
+    int j = lane - ei * (int)cnt;
+    const int dq = (int)(32.5f * rc);
+    const int dr = 32 - dq * (int)cnt;
+    while ((unsigned)__shfl_sync(kFull, ei, 0) < len) {
+        int eis[U], js[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            eis[u] = ei;
+            js[u] = j;
+            ei += dq;
+            j += dr;
+            if (j >= (int)cnt) {
+                j -= (int)cnt;
+                ++ei;
+            }
+        }
+        body(eis, js);
+    }
+}
 
 __global__ void __launch_bounds__(512, 2) sssp_batch_persistent(const BatchParams p) {
     TraversalCtl* ctl = p.ctl;
@@ -106,6 +136,7 @@ __global__ void __launch_bounds__(512, 2) sssp_batch_persistent(const BatchParam
     __shared__ StageSmem sm;
     const int wib = threadIdx.x >> 5;
     WarpStage fst{sm.v0[wib], sm.d0[wib], sm.x0[wib], 0};
+    int* qtab = sm.v1[wib];  // slot -> query position table of the owner being expanded
 
     // Init: dist = INF (vector stores), masks = 0.
     {
@@ -202,36 +233,46 @@ __global__ void __launch_bounds__(512, 2) sssp_batch_persistent(const BatchParam
                     const unsigned km = (unsigned)__shfl_sync(kFull, (int)msk, k);
                     const unsigned krs = (unsigned)__shfl_sync(kFull, (int)rs, k);
                     const unsigned w = (unsigned)kvw & (unsigned)(W - 1);
-                    int* drow = p.dist + (w << 5) + lane;  // + v * Q: row of vertex v
-                    unsigned* mrow = p.mask + w;           // + (v << logW): mask word of v
-                    const bool act = (km >> lane) & 1u;
+                    const unsigned cnt = (unsigned)__popc(km);
+                    // slot -> query position of the word's active queries
+                    if ((km >> lane) & 1u) qtab[__popc(km & ((1u << lane) - 1u))] = lane;
+                    __syncwarp();
+                    const int qp = (unsigned)lane < cnt ? qtab[lane] : 0;
+                    __syncwarp();
+                    int* dw = p.dist + (w << 5);  // + v * Q + query position
+                    unsigned* mrow = p.mask + w;  // + (v << logW): mask word of v
                     // L2-coherent: the owner improved in the previous round.
-                    const int du = act ? ldcg(drow + (size_t)((unsigned)kvw >> p.logW) * Qu) : 0;
-                    for (unsigned eb = lo; eb < hi; eb += 32) {
-                        const unsigned n = min(32u, hi - eb);
-                        const int2 my = (unsigned)lane < n ? __ldg(p.adj + krs + (eb - kb) + lane) : make_int2(0, 0);
-                        for (unsigned g = 0; g < n; g += kBatchUnroll) {
-                            int tv[kBatchUnroll], tw[kBatchUnroll], cd[kBatchUnroll];
+                    const int du = (unsigned)lane < cnt ? ldcg(dw + (size_t)((unsigned)kvw >> p.logW) * Qu + qp) : 0;
+                    const unsigned len = hi - lo;
+                    const int2* eadj = p.adj + krs + (lo - kb);
+                    owner_items<kBatchUnroll>(cnt, len, lane, [&](const int* eis, const int* js) {
+                        int2 ew[kBatchUnroll];
+                        int dq[kBatchUnroll], qq[kBatchUnroll], cd[kBatchUnroll];
+                        bool ok[kBatchUnroll];
 #pragma unroll
-                            for (int jj = 0; jj < kBatchUnroll; ++jj) {
-                                tv[jj] = __shfl_sync(kFull, my.x, (int)g + jj);
-                                tw[jj] = __shfl_sync(kFull, my.y, (int)g + jj);
-                            }
+                        for (int u = 0; u < kBatchUnroll; ++u) {
+                            ok[u] = (unsigned)eis[u] < len;
+                            ew[u] = ok[u] ? __ldg(eadj + eis[u]) : make_int2(0, 0);
+                        }
 #pragma unroll
-                            for (int jj = 0; jj < kBatchUnroll; ++jj)
-                                cd[jj] = (act && g + jj < n) ? ldcg(drow + (size_t)(unsigned)tv[jj] * Qu) : INT_MIN;
+                        for (int u = 0; u < kBatchUnroll; ++u) {
+                            dq[u] = __shfl_sync(kFull, du, js[u]);
+                            qq[u] = __shfl_sync(kFull, qp, js[u]);
+                        }
 #pragma unroll
-                            for (int jj = 0; jj < kBatchUnroll; ++jj) {
-                                const int nd = du + tw[jj];
-                                const bool imp = nd < cd[jj];
-                                if (imp) atomicMin(drow + (size_t)(unsigned)tv[jj] * Qu, nd);
-                                const unsigned bits = __ballot_sync(kFull, imp);
-                                if (bits && lane == 0) atomicOr(mrow + ((size_t)(unsigned)tv[jj] << p.logW), bits);
+                        for (int u = 0; u < kBatchUnroll; ++u)
+                            cd[u] = ok[u] ? ldcg(dw + (size_t)(unsigned)ew[u].x * Qu + qq[u]) : INT_MIN;
+#pragma unroll
+                        for (int u = 0; u < kBatchUnroll; ++u) {
+                            const int nd = dq[u] + ew[u].y;
+                            if (nd < cd[u]) {
+                                atomicMin(dw + (size_t)(unsigned)ew[u].x * Qu + qq[u], nd);
+                                atomicOr(mrow + ((size_t)(unsigned)ew[u].x << p.logW), 1u << qq[u]);
                             }
                         }
-                    }
-                    if (lane == 0) relax += (long long)__popc(km) * (hi - lo);
-                    steps += hi - lo;
+                    });
+                    if (lane == 0) relax += (long long)cnt * len;
+                    steps += len;
                 }
                 e0 = seg_end;
                 o += 32;
@@ -510,7 +551,7 @@ __device__ __forceinline__ void pbatch_apply(const PprBatchParams& p, int vw, un
     stage_push(fst, out, lane == 0 && bits != 0u && deg > 0, vw, deg, __int_as_float((int)bits));
 }
 
-constexpr int kPprBatchUnroll = 8;  // messages in flight per lane
+constexpr int kPprBatchUnroll = 3;  // push items in flight per lane (4 spills at 64 registers)
 
 // Apply sweep: every (vertex, word) whose touched mask is non-zero gets pbatch_apply for
 // its touched lanes; the mask is cleared.  Pushes mark targets with red.or, so the push
@@ -525,7 +566,7 @@ __device__ __forceinline__ unsigned pbatch_sweep(const PprBatchParams& p, bool f
         const unsigned tm = i < nm ? ldcg(p.tmask + i) : 0u;
         if (tm) p.tmask[i] = 0u;
         unsigned nz = __ballot_sync(kFull, tm != 0u);
-        cnt += (unsigned)__popc(nz);
+        cnt += (unsigned)__popc(tm);  // touched (vertex, query) lanes seen by this lane
         while (nz) {
             const int k = __ffs(nz) - 1;
             nz &= nz - 1u;
@@ -550,6 +591,7 @@ __global__ void __launch_bounds__(512, 2) ppr_batch_persistent(const PprBatchPar
     __shared__ StageSmem sm;
     const int wib = threadIdx.x >> 5;
     WarpStage fst{sm.v0[wib], sm.d0[wib], sm.x0[wib], 0};
+    int* qtab = sm.v1[wib];  // slot -> query position table of the owner being expanded
     const double one_m_a = 1.0 - (double)p.alpha;
 
     // Init: pr = res = 0 (msg and tmask are zero between launches).
@@ -603,7 +645,7 @@ __global__ void __launch_bounds__(512, 2) ppr_batch_persistent(const PprBatchPar
     if (!grid_sync(bar, flags, p.barrier_ns)) return;
 
     long long pushes = 0, steps = 0;
-    unsigned touched = 0;
+    unsigned long long touched = 0;
     int cur = 1, iters = 0;
     for (;;) {
         const unsigned long long c = ldcg(&ctl->qctr[cur % 3]);
@@ -685,38 +727,60 @@ __global__ void __launch_bounds__(512, 2) ppr_batch_persistent(const PprBatchPar
                         const unsigned km = (unsigned)__shfl_sync(kFull, (int)msk, k);
                         const unsigned krs = (unsigned)__shfl_sync(kFull, (int)rs, k);
                         const unsigned w = (unsigned)kvw & (unsigned)(W - 1);
-                        double* mrow = p.msg + (w << 5) + lane;  // + v * Q: message row of v
-                        unsigned* trow = p.tmask + w;            // + (v << logW): touched word of v
-                        const bool act = (km >> lane) & 1u;
-                        // (1-alpha)*r_u of this lane's query (src/ppr/purn/Main.cu:288)
-                        const double qu =
-                            act ? one_m_a * ldcg(p.rq + (size_t)((unsigned)kvw >> p.logW) * Qu + (w << 5) + lane) : 0.0;
+                        const unsigned cnt = (unsigned)__popc(km);
+                        // slot -> query position of the word's active queries
+                        if ((km >> lane) & 1u) qtab[__popc(km & ((1u << lane) - 1u))] = lane;
+                        __syncwarp();
+                        const int qp = (unsigned)lane < cnt ? qtab[lane] : 0;
+                        __syncwarp();
+                        double* mw = p.msg + (w << 5);  // + v * Q + query position
+                        unsigned* trow = p.tmask + w;   // + (v << logW): touched word of v
+                        // (1-alpha)*r_u of slot `lane`'s query (src/ppr/purn/Main.cu:288)
+                        const double qu = (unsigned)lane < cnt
+                                              ? one_m_a * ldcg(p.rq + (size_t)((unsigned)kvw >> p.logW) * Qu + (w << 5) + qp)
+                                              : 0.0;
                         const DSplit qs = c2g_dsplit(qu);
-                        for (unsigned eb = lo; eb < hi; eb += 32) {
-                            const unsigned n = min(32u, hi - eb);
-                            const int2 my =
-                                (unsigned)lane < n ? __ldg(p.adj + krs + (eb - kb) + lane) : make_int2(0, 0);
-                            for (unsigned g = 0; g < n; g += kPprBatchUnroll) {
+                        const unsigned len = hi - lo;
+                        const int2* eadj = p.adj + krs + (lo - kb);
+                        owner_items<kPprBatchUnroll>(cnt, len, lane, [&](const int* eis, const int* js) {
+                            int2 ew[kPprBatchUnroll];
+                            bool ok[kPprBatchUnroll];
 #pragma unroll
-                                for (int jj = 0; jj < kPprBatchUnroll; ++jj) {
-                                    const unsigned tv = (unsigned)__shfl_sync(kFull, my.x, (int)g + jj);
-                                    const unsigned wb = (unsigned)__shfl_sync(kFull, my.y, (int)g + jj);
-                                    // m = qu * w in FP64, on the integer pipes (fp64_mul.h)
-                                    bool send = act && g + jj < n && (int)wb > 0;
-                                    const bool ok = c2g_mul_ok(qs, wb);
-                                    double m = c2g_mul(qs, wb);
-                                    if (__any_sync(kFull, send && !ok)) {  // w subnormal: FP64 pipe
-                                        if (!ok) m = qu * (double)__uint_as_float(wb);
-                                        send = send && (ok || m > 0.0);
-                                    }
-                                    if (send) atomicAdd(mrow + (size_t)tv * Qu, m);
-                                    const unsigned bits = __ballot_sync(kFull, send);
-                                    if (bits && lane == 0) atomicOr(trow + ((size_t)tv << p.logW), bits);
+                            for (int u = 0; u < kPprBatchUnroll; ++u) {
+                                ok[u] = (unsigned)eis[u] < len;
+                                ew[u] = ok[u] ? __ldg(eadj + eis[u]) : make_int2(0, 0);
+                            }
+#pragma unroll
+                            for (int u = 0; u < kPprBatchUnroll; ++u) {
+                                DSplit sj;
+                                sj.lo = (unsigned)__shfl_sync(kFull, (int)qs.lo, js[u]);
+                                sj.hi = (unsigned)__shfl_sync(kFull, (int)qs.hi, js[u]);
+                                sj.e = __shfl_sync(kFull, qs.e, js[u]);
+                                const int qq = __shfl_sync(kFull, qp, js[u]);
+                                const unsigned wb = (unsigned)ew[u].y;
+                                // m = qu * w in FP64, on the integer pipes (fp64_mul.h)
+                                bool send = ok[u] && (int)wb > 0;
+                                const bool mok = c2g_mul_ok(sj, wb);
+                                double m = c2g_mul(sj, wb);
+                                const bool slow = __any_sync(kFull, send && !mok);
+                                if (slow) {  // w subnormal: FP64 pipe
+                                    const double quj = __shfl_sync(kFull, qu, js[u]);
+                                    if (!mok) m = quj * (double)__uint_as_float(wb);
+                                    send = send && (mok || m > 0.0);
+                                }
+                                const size_t tv = (size_t)(unsigned)ew[u].x;
+                                if (send) atomicAdd(mw + tv * Qu + qq, m);
+                                // Touched lanes: every active query sends along a positive
+                                // weight, so slot 0 marks the whole word at once.
+                                if (!slow) {
+                                    if (send && js[u] == 0) atomicOr(trow + (tv << p.logW), km);
+                                } else if (send) {
+                                    atomicOr(trow + (tv << p.logW), 1u << qq);
                                 }
                             }
-                        }
-                        if (lane == 0) pushes += (long long)__popc(km) * (hi - lo);
-                        steps += hi - lo;
+                        });
+                        if (lane == 0) pushes += (long long)cnt * len;
+                        steps += len;
                     }
                     e0 = seg_end;
                     o += 32;
@@ -730,11 +794,13 @@ __global__ void __launch_bounds__(512, 2) ppr_batch_persistent(const PprBatchPar
         if (!grid_sync(bar, flags, p.barrier_ns)) return;
         ++cur;
     }
-    // pushes are counted by lane 0 of each warp; touched pairs once per warp
+    // pushes are counted by lane 0 of each warp; touched lanes by every lane
+    unsigned long long tl = touched;
+    for (int o = 16; o >= 1; o >>= 1) tl += __shfl_xor_sync(kFull, tl, o);
     if (lane == 0) {
         atomicAdd((unsigned long long*)&p.counters[0], (unsigned long long)pushes);
         atomicAdd((unsigned long long*)&p.counters[1], (unsigned long long)steps);
-        atomicAdd((unsigned long long*)&ctl->touched, (unsigned long long)touched);
+        atomicAdd((unsigned long long*)&ctl->touched, tl);
     }
     if (gtid == 0) ctl->iterations = iters;
 }
