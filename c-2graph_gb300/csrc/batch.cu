@@ -93,6 +93,15 @@ __device__ __forceinline__ void batch_sweep(const BatchParams& p, const Frontier
 
 constexpr int kBatchUnroll = 4;  // relaxation items in flight per lane
 
+// Next tile of a round for this warp from the round's tile counter (lane 0 takes it, the
+// warp shares it).  Tiles differ in cost (active queries per step), so a dynamic queue
+// balances the warps better than a fixed round-robin.
+__device__ __forceinline__ unsigned next_tile(unsigned* ctr, int lane) {
+    unsigned t = 0;
+    if (lane == 0) t = atomicAdd(ctr, 1u);
+    return (unsigned)__shfl_sync(kFull, (int)t, 0);
+}
+
 // Lane compaction of one owner run: the run's work is the items (edge ei, active-query
 // slot j) for ei in [0, len) and j in [0, cnt), numbered i = ei * cnt + j; lane l takes
 // items l, l + 32, l + 64, ... so every lane of a warp step relaxes something even when
@@ -168,7 +177,10 @@ __global__ void __launch_bounds__(512, 2) sssp_batch_persistent(const BatchParam
     for (;;) {
         const int buf = cur & 1, slot = cur % 3;
         // Phase 1: this round's frontier from the masks of the previous one.
-        if (gtid == 0) ctl->qctr[(cur + 1) % 3] = 0ull;
+        if (gtid == 0) {
+            ctl->qctr[(cur + 1) % 3] = 0ull;
+            ctl->tilectr[(cur + 1) % 3] = 0u;
+        }
         batch_sweep(p, batch_out(p, buf, slot), fst, gwarp, nwarps, lane);
         if (!grid_sync(bar, flags, p.barrier_ns)) return;
         const unsigned long long c = ldcg(&ctl->qctr[slot]);
@@ -197,7 +209,10 @@ __global__ void __launch_bounds__(512, 2) sssp_batch_persistent(const BatchParam
         const int* mark = p.mark[buf];
         const unsigned tile = 1u << kBatchTileLog;
         const unsigned ntiles = (T + tile - 1) >> kBatchTileLog;
-        for (unsigned t = gwarp; t < ntiles; t += nwarps) {
+        unsigned* tctr = &ctl->tilectr[slot];
+        unsigned tn = next_tile(tctr, lane);
+        for (unsigned t = tn; t < ntiles; t = tn) {
+            tn = next_tile(tctr, lane);  // the next tile, fetched while this one runs
             unsigned e0 = t << kBatchTileLog;
             const unsigned e1 = min(e0 + tile, T);
             unsigned o = (unsigned)ldcg(mark + t);
@@ -679,6 +694,7 @@ __global__ void __launch_bounds__(512, 2) ppr_batch_persistent(const PprBatchPar
         if (gtid == 0) {
             ctl->qctr[fslot] = 0ull;
             ctl->dctr[fslot] = 0u;
+            ctl->tilectr[fslot] = 0u;
             ctl->popped += F;
             ctl->relaxed += T;
         }
@@ -691,7 +707,10 @@ __global__ void __launch_bounds__(512, 2) ppr_batch_persistent(const PprBatchPar
             const int* mark = p.mark[buf];
             const unsigned tile = 1u << kBatchTileLog;
             const unsigned ntiles = (T + tile - 1) >> kBatchTileLog;
-            for (unsigned t = gwarp; t < ntiles; t += nwarps) {
+            unsigned* tctr = &ctl->tilectr[cur % 3];
+            unsigned tn = next_tile(tctr, lane);
+            for (unsigned t = tn; t < ntiles; t = tn) {
+                tn = next_tile(tctr, lane);  // the next tile, fetched while this one runs
                 unsigned e0 = t << kBatchTileLog;
                 const unsigned e1 = min(e0 + tile, T);
                 unsigned o = (unsigned)ldcg(mark + t);
@@ -740,6 +759,9 @@ __global__ void __launch_bounds__(512, 2) ppr_batch_persistent(const PprBatchPar
                                               ? one_m_a * ldcg(p.rq + (size_t)((unsigned)kvw >> p.logW) * Qu + (w << 5) + qp)
                                               : 0.0;
                         const DSplit qs = c2g_dsplit(qu);
+                        // exponent and high significand in one word (0: residual outside the
+                        // integer product's range, multiply on the FP64 pipe)
+                        const unsigned qpk = c2g_mul_q_ok(qs) ? ((unsigned)qs.e << 21) | qs.hi : 0u;
                         const unsigned len = hi - lo;
                         const int2* eadj = p.adj + krs + (lo - kb);
                         owner_items<kPprBatchUnroll>(cnt, len, lane, [&](const int* eis, const int* js) {
@@ -752,15 +774,16 @@ __global__ void __launch_bounds__(512, 2) ppr_batch_persistent(const PprBatchPar
                             }
 #pragma unroll
                             for (int u = 0; u < kPprBatchUnroll; ++u) {
+                                const unsigned pk = (unsigned)__shfl_sync(kFull, (int)qpk, js[u]);
                                 DSplit sj;
                                 sj.lo = (unsigned)__shfl_sync(kFull, (int)qs.lo, js[u]);
-                                sj.hi = (unsigned)__shfl_sync(kFull, (int)qs.hi, js[u]);
-                                sj.e = __shfl_sync(kFull, qs.e, js[u]);
+                                sj.hi = pk & 0x1fffffu;
+                                sj.e = (int)(pk >> 21);
                                 const int qq = __shfl_sync(kFull, qp, js[u]);
                                 const unsigned wb = (unsigned)ew[u].y;
                                 // m = qu * w in FP64, on the integer pipes (fp64_mul.h)
                                 bool send = ok[u] && (int)wb > 0;
-                                const bool mok = c2g_mul_ok(sj, wb);
+                                const bool mok = pk != 0u && c2g_mul_w_ok(wb);
                                 double m = c2g_mul(sj, wb);
                                 const bool slow = __any_sync(kFull, send && !mok);
                                 if (slow) {  // w subnormal: FP64 pipe

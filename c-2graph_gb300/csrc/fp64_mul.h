@@ -81,22 +81,31 @@ C2G_HD bool c2g_mul_ok(const DSplit& q, uint32_t wb) {
 }
 
 // q * (double)w, exact and rounded to nearest-even; requires c2g_mul_ok(q, wb).
+// With A = lo * Sw (< 2^56) and B = hi * Sw (< 2^45), P = B * 2^32 + A, so
+// P >> 24 = (B << 8) + (A >> 24) and P >> 23 = (B << 9) + (A >> 23) exactly (B * 2^32 is a
+// multiple of 2^24); the dropped s bits (s <= 24) are the low bits of A.
 C2G_HD double c2g_mul(const DSplit& q, uint32_t wb) {
     const uint32_t ew = wb >> 23;
     const uint32_t sw = (wb & 0x7fffffu) | 0x800000u;
     const uint64_t a = (uint64_t)q.lo * sw;  // < 2^56
     const uint64_t b = (uint64_t)q.hi * sw;  // < 2^45
-    // P = b * 2^32 + a = ph * 2^64 + pl, ph < 2^13
-    const uint64_t pl = a + (b << 32);
-    const uint32_t ph = (uint32_t)(b >> 32) + (pl < a ? 1u : 0u);
-    const uint32_t top = ph >> 12;  // 1 when P >= 2^76
+    const uint64_t m24 = (b << 8) + (a >> 24);
+    const uint32_t top = (uint32_t)(m24 >> 52);  // 1 when P >= 2^76: keep P >> 24
     const uint32_t s = 23u + top;
-    uint64_t m = (pl >> s) | ((uint64_t)ph << (64u - s));  // top 53 bits of P
-    const uint64_t r = pl & ((1ull << s) - 1ull);           // dropped bits
-    const uint64_t half = 1ull << (s - 1u);
-    m += (r > half || (r == half && (m & 1ull))) ? 1ull : 0ull;
+    uint64_t m = top ? m24 : (b << 9) + (a >> 23);  // top 53 bits of P
+    const uint32_t alo = (uint32_t)a;
+    const uint32_t rb = (alo >> (s - 1u)) & 1u;                    // first dropped bit
+    const uint32_t sticky = (alo & ((1u << (s - 1u)) - 1u)) != 0u;  // any lower dropped bit
+    m += (uint64_t)(rb & (sticky | (uint32_t)(m & 1u)));
     const int64_t e = (int64_t)q.e + (int64_t)ew + (int64_t)s - 150;
     return c2g_bitsd(((uint64_t)(e - 1) << 52) + m);
 }
+
+// Range part of c2g_mul_ok that depends on q alone: a residual exponent for which every
+// normal float weight keeps the product normal (checked once per frontier residual).
+C2G_HD bool c2g_mul_q_ok(const DSplit& q) { return q.e >= 128 && q.e <= 1916; }
+
+// Weight part: w positive, normal and finite (exponent field 1..254).
+C2G_HD bool c2g_mul_w_ok(uint32_t wb) { return wb - 0x00800000u < 0x7f000000u; }
 
 }  // namespace c2g

@@ -118,7 +118,7 @@ __device__ __forceinline__ void ppr_push(const PprParams& p, int buf, int slot, 
                 // when it is positive (w > 0: qu > 0 for every activated vertex)
                 const unsigned wb = (unsigned)ew.y;
                 const DSplit qs = c2g_dsplit(qu[u]);
-                const bool mok = c2g_mul_ok(qs, wb);
+                const bool mok = c2g_mul_q_ok(qs) && c2g_mul_w_ok(wb);
                 send[u] = ok[u] && ew.y > 0;
                 m[u] = c2g_mul(qs, wb);
                 if (__any_sync(kFull, send[u] && !mok)) {  // w subnormal: FP64 pipe

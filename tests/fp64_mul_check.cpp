@@ -19,6 +19,10 @@ static int check(double q, float w) {
     uint32_t wb;
     std::memcpy(&wb, &w, 4);
     const c2g::DSplit s = c2g::c2g_dsplit(q);
+    if (c2g::c2g_mul_q_ok(s) && c2g::c2g_mul_w_ok(wb) && !c2g::c2g_mul_ok(s, wb)) {
+        std::printf("split range check admits q=%a w=%a\n", q, (double)w);
+        return -1;
+    }
     if (!c2g::c2g_mul_ok(s, wb)) return 0;
     const volatile double ref = q * (double)w;
     const double got = c2g::c2g_mul(s, wb);
