@@ -107,6 +107,7 @@ SIGNATURES = {
                                ctypes.POINTER(Stats)]),
     "c2g_ppr_set_config": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int32]),
     "c2g_graph_set_watchdog": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int32]),
+    "c2g_graph_last_phases": (ctypes.c_int, [_P, _P]),
     "c2g_ppr_default_params": (ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(PprParams)]),
     "c2g_ppr_batch": (ctypes.c_int, [_P, ctypes.c_int32, _P, ctypes.POINTER(PprParams), _P, _P, ctypes.c_int,
                                      ctypes.c_int, ctypes.POINTER(Stats)]),
@@ -280,6 +281,12 @@ class Graph:
         _check(lib().c2g_sssp_batch(self._h, len(src), _ptr(src), int(seeds), mode, _ptr(dist), 0, layout,
                                     ctypes.byref(st)))
         return dist, st
+
+    def last_phases(self):
+        """(init, frontier build/apply, expand/push, reserved) ms of the last launch."""
+        out = np.zeros(4, dtype=np.float64)
+        _check(lib().c2g_graph_last_phases(self._h, _ptr(out)))
+        return tuple(float(x) for x in out)
 
     def watchdog(self, barrier_timeout_ms=0, stall_next_sssp=False):
         _check(lib().c2g_graph_set_watchdog(self._h, barrier_timeout_ms, int(bool(stall_next_sssp))))

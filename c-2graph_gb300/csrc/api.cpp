@@ -134,6 +134,7 @@ static int stats_fill(c2g_graph* g, const TraversalCtl* dctl, int32_t source, fl
     TraversalCtl ctl;
     C2G_CUDA(cudaMemcpyAsync(&ctl, dctl, sizeof(ctl), cudaMemcpyDeviceToHost, g->stream));
     C2G_CUDA(cudaStreamSynchronize(g->stream));
+    std::memcpy(g->last_phase_ns, ctl.phase_ns, sizeof(g->last_phase_ns));
     if (ctl.flags & (C2G_FLAG_BARRIER_TIMEOUT | C2G_FLAG_QUEUE_OVERFLOW | C2G_FLAG_BOUNDS)) {
         // The launch ended early: force the stamp arrays to be reset by the next launch.
         static const StampState reset{1 << 30, 1 << 30, {0, 0}};
@@ -391,6 +392,12 @@ int c2g_sssp_set_config(c2g_graph* g, int32_t delta, int32_t tile, int32_t max_i
     return C2G_OK;
 }
 
+int c2g_graph_last_phases(const c2g_graph* g, double ms[4]) {
+    if (!g || !ms) return fail(C2G_ERR_ARG, "NULL argument");
+    for (int k = 0; k < 4; ++k) ms[k] = (double)g->last_phase_ns[k] * 1e-6;
+    return C2G_OK;
+}
+
 int c2g_graph_set_watchdog(c2g_graph* g, int32_t barrier_timeout_ms, int32_t stall_next_sssp) {
     if (!g) return fail(C2G_ERR_ARG, "graph is NULL");
     if (barrier_timeout_ms < 0) return fail(C2G_ERR_ARG, "barrier_timeout_ms must be >= 0");
@@ -476,6 +483,7 @@ int c2g_sssp_batch(c2g_graph* g, int32_t n, const int32_t* sources, int use_seed
                                use_seeds ? &sw : nullptr, dist, dist_on_device, layout == C2G_LAYOUT_QUERY_MAJOR, &ms,
                                counters, &ctl);
     if (rc) return rc;
+    std::memcpy(g->last_phase_ns, ctl.phase_ns, sizeof(g->last_phase_ns));
     if (stats) {
         std::memset(stats, 0, sizeof(*stats));
         stats->source = sources[0];
@@ -538,6 +546,7 @@ int c2g_ppr_batch(c2g_graph* g, int32_t n, const int32_t* sources, const c2g_ppr
                               params->seeded ? &sw : nullptr, pr, res, on_device, layout == C2G_LAYOUT_QUERY_MAJOR,
                               &ms, counters, &ctl);
     if (rc) return rc;
+    std::memcpy(g->last_phase_ns, ctl.phase_ns, sizeof(g->last_phase_ns));
     if (stats) {
         std::memset(stats, 0, sizeof(*stats));
         stats->source = sources[0];

@@ -144,6 +144,7 @@ __global__ void __launch_bounds__(512, 2) sssp_batch_persistent(const BatchParam
     const unsigned Qu = (unsigned)p.Q;
     __shared__ StageSmem sm;
     const int wib = threadIdx.x >> 5;
+    unsigned long long tph = globaltimer_ns();
     WarpStage fst{sm.v0[wib], sm.d0[wib], sm.x0[wib], 0};
     int* qtab = sm.v1[wib];  // slot -> query position table of the owner being expanded
 
@@ -171,6 +172,7 @@ __global__ void __launch_bounds__(512, 2) sssp_batch_persistent(const BatchParam
             }
     }
     if (!grid_sync(bar, flags, p.barrier_ns)) return;
+    phase_mark(ctl->phase_ns, tph, 0);
 
     long long relax = 0, steps = 0;
     int cur = 1, iters = 0;
@@ -183,6 +185,7 @@ __global__ void __launch_bounds__(512, 2) sssp_batch_persistent(const BatchParam
         }
         batch_sweep(p, batch_out(p, buf, slot), fst, gwarp, nwarps, lane);
         if (!grid_sync(bar, flags, p.barrier_ns)) return;
+        phase_mark(ctl->phase_ns, tph, 1);
         const unsigned long long c = ldcg(&ctl->qctr[slot]);
         const unsigned F = (unsigned)(c >> 32), T = (unsigned)c;
         if (F == 0) break;
@@ -294,6 +297,7 @@ __global__ void __launch_bounds__(512, 2) sssp_batch_persistent(const BatchParam
             }
         }
         if (!grid_sync(bar, flags, p.barrier_ns)) return;
+        phase_mark(ctl->phase_ns, tph, 2);
         ++cur;
     }
     // relax is counted by lane 0 of each warp
@@ -608,6 +612,7 @@ __global__ void __launch_bounds__(512, 2) ppr_batch_persistent(const PprBatchPar
     WarpStage fst{sm.v0[wib], sm.d0[wib], sm.x0[wib], 0};
     int* qtab = sm.v1[wib];  // slot -> query position table of the owner being expanded
     const double one_m_a = 1.0 - (double)p.alpha;
+    unsigned long long tph = globaltimer_ns();
 
     // Init: pr = res = 0 (msg and tmask are zero between launches).
     {
@@ -658,6 +663,7 @@ __global__ void __launch_bounds__(512, 2) ppr_batch_persistent(const PprBatchPar
     // Round-1 frontier: every touched (vertex, word) activates its touched lanes.
     pbatch_sweep(p, true, fst, pbatch_out(p, 1, 1), &ctl->dctr[1], gwarp, nwarps, lane);
     if (!grid_sync(bar, flags, p.barrier_ns)) return;
+    phase_mark(ctl->phase_ns, tph, 0);
 
     long long pushes = 0, steps = 0;
     unsigned long long touched = 0;
@@ -811,10 +817,12 @@ __global__ void __launch_bounds__(512, 2) ppr_batch_persistent(const PprBatchPar
             }
         }
         if (!grid_sync(bar, flags, p.barrier_ns)) return;
+        phase_mark(ctl->phase_ns, tph, 2);
         // Phase B: apply the messages of the touched pairs and activate.
         touched += pbatch_sweep(p, false, fst, pbatch_out(p, (cur + 1) & 1, nslot), &ctl->dctr[nslot], gwarp,
                                 nwarps, lane);
         if (!grid_sync(bar, flags, p.barrier_ns)) return;
+        phase_mark(ctl->phase_ns, tph, 1);
         ++cur;
     }
     // pushes are counted by lane 0 of each warp; touched lanes by every lane

@@ -98,6 +98,18 @@ __device__ __forceinline__ bool grid_sync(GridBarrier* b, int* flags, unsigned l
     return s_ok != 0;
 }
 
+// Phase timing of a persistent launch, read by c2g_graph_last_phases: block 0's
+// thread 0 adds the time since the previous mark to phase_ns[phase].  Called right
+// after a grid barrier, so each interval is one phase of the whole grid (wait included).
+// Phases: 0 initialisation, 1 frontier build / apply / far-pile filter, 2 expansion / push.
+__device__ __forceinline__ void phase_mark(unsigned long long* phase_ns, unsigned long long& t, int phase) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        const unsigned long long now = globaltimer_ns();
+        phase_ns[phase] += now - t;
+        t = now;
+    }
+}
+
 // Destination of a frontier append.  Entries are (vertex, base) where base is the
 // exclusive prefix of the out-degrees of all entries before it, obtained from one
 // 64-bit atomic on ctr = (count << 32) | edge_total, so the frontier's edges form one

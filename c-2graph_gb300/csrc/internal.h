@@ -42,6 +42,7 @@ struct TraversalCtl {
     int iterations;
     long long popped, relaxed, touched, seeds;
     int pad[1];
+    unsigned long long phase_ns[4];  // block 0's time per phase (see phase_mark)
 };
 
 // Stamps survive across launches; the kernel advances the bases itself.
@@ -142,6 +143,7 @@ struct c2g_graph {
     int num_sms = 0;
     float grid_scale = 1.0f;  // fraction of the GPU a batched launch may occupy
     unsigned long long barrier_ns = 0;  // grid-barrier wait limit (0: per-kernel default)
+    unsigned long long last_phase_ns[4] = {0, 0, 0, 0};  // phases of the last launch
     int stall_next_sssp = 0;            // failure-detection test: next SSSP barrier cannot complete
     bool borrowed = false;    // a view: graph arrays belong to another handle
 };

@@ -215,6 +215,7 @@ __global__ void __launch_bounds__(512, 2) ppr_persistent(const PprParams p) {
     const int wib = threadIdx.x >> 5;
     WarpStage fst{sm.v0[wib], sm.d0[wib], nullptr, 0, sm.xd0[wib]};
     WarpStage tst{sm.v1[wib], nullptr, nullptr, 0};
+    unsigned long long tph = globaltimer_ns();
 
     int sbase = p.st->stamp_base;
     const bool reset = sbase > (1 << 29);
@@ -326,6 +327,7 @@ __global__ void __launch_bounds__(512, 2) ppr_persistent(const PprParams p) {
         stage_flush(fst, out);
     }
     if (!grid_sync(bar, flags, p.barrier_ns)) return;
+    phase_mark(ctl->phase_ns, tph, 0);
 
     int cur = 1, iters = 0;
     for (;;) {
@@ -366,6 +368,7 @@ __global__ void __launch_bounds__(512, 2) ppr_persistent(const PprParams p) {
         else
             ppr_push(p, cur & 1, slot, F, T, tst, !dense);
         if (!grid_sync(bar, flags, p.barrier_ns)) return;
+        phase_mark(ctl->phase_ns, tph, 2);
         if (!dense) {
             // Phase B: apply messages and activate (src/ppr/purn/Main.cu:383-391).
             const unsigned n = ldcg(&ctl->listctr[slot]);
@@ -427,6 +430,7 @@ __global__ void __launch_bounds__(512, 2) ppr_persistent(const PprParams p) {
         }
         stage_flush(fst, out);
         if (!grid_sync(bar, flags, p.barrier_ns)) return;
+        phase_mark(ctl->phase_ns, tph, 1);
         ++cur;
     }
     if (gtid == 0) {

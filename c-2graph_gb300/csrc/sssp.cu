@@ -157,6 +157,7 @@ __global__ void __launch_bounds__(512, 2) sssp_persistent(const SsspParams p) {
     const int wib = threadIdx.x >> 5;
     WarpStage fst{sm.v0[wib], sm.d0[wib], nullptr, 0};
     FarStage far{WarpStage{sm.v1[wib], nullptr, nullptr, 0}, INT_MAX};
+    unsigned long long tph = globaltimer_ns();
 
     int sbase = p.st->stamp_base;
     int ebase = p.st->epoch_base;
@@ -200,6 +201,7 @@ __global__ void __launch_bounds__(512, 2) sssp_persistent(const SsspParams p) {
         stage_flush(fst, out);
     }
     if (!grid_sync(bar, flags, p.barrier_ns, p.bar_extra)) return;
+    phase_mark(ctl->phase_ns, tph, 0);
 
     int cur = 1, fb = 0, epoch = ebase + 1, iters = 0;
     int thresh = kDelta ? p.delta : INT_MAX;
@@ -249,6 +251,7 @@ __global__ void __launch_bounds__(512, 2) sssp_persistent(const SsspParams p) {
             fb = fdst;
             ++epoch;
             if (!grid_sync(bar, flags, p.barrier_ns, p.bar_extra)) return;
+            phase_mark(ctl->phase_ns, tph, 1);
             continue;
         }
         if (++iters > p.max_iter) {
@@ -264,6 +267,7 @@ __global__ void __launch_bounds__(512, 2) sssp_persistent(const SsspParams p) {
         const FrontierOut nout = sssp_out(p, (cur + 1) & 1, (cur + 1) % 3);
         sssp_expand<kDelta>(p, cur & 1, F, T, sbase + cur + 1, thresh, fb, epoch, nout, fst, far);
         if (!grid_sync(bar, flags, p.barrier_ns, p.bar_extra)) return;
+        phase_mark(ctl->phase_ns, tph, 2);
         ++cur;
     }
     if (gtid == 0) {

@@ -132,6 +132,12 @@ int  c2g_graph_set_stream(c2g_graph* g, void* stream);
  * than the grid has, so the wait runs out on purpose: a failure-detection test that
  * faults and hangs nothing. */
 int  c2g_graph_set_watchdog(c2g_graph* g, int32_t barrier_timeout_ms, int32_t stall_next_sssp);
+/* Tracing (no counterpart in the reference): time per phase of the last SSSP / PPR
+ * launch on this handle, single or batched, as seen by block 0 at each grid barrier
+ * (waits included): ms[0] initialisation, ms[1] frontier build / apply / far-pile
+ * filter, ms[2] expansion / push, ms[3] reserved (0).  The phases add up to the
+ * launch's device time. */
+int  c2g_graph_last_phases(const c2g_graph* g, double ms[4]);
 
 /* ---- SSSP -------------------------------------------------------------------------- */
 /* Source-skip rule of the drop-in programs: sssp-base skips sources without
