@@ -530,67 +530,95 @@ __device__ __forceinline__ FrontierOut pbatch_out(const PprBatchParams& p, int b
     return o;
 }
 
-// Phase-B step for one touched (v, w) pair: lane = query.  force=true activates every
-// touched lane regardless of rmax and without messages (the seeded first hop).
-__device__ __forceinline__ void pbatch_apply(const PprBatchParams& p, int vw, unsigned lanes, bool force,
-                                             WarpStage& fst, const FrontierOut& out, unsigned* dctr) {
-    const int lane = threadIdx.x & 31;
-    const int v = vw >> p.logW, w = vw & ((1 << p.logW) - 1);
-    const size_t off = (size_t)v * p.Q + (w << 5) + lane;
-    const bool mine = (lanes >> lane) & 1u;
-    const int deg = __ldg(p.row + v + 1) - __ldg(p.row + v);
-    bool act = false;
-    if (mine) {
-        double r = ldcg(p.res + off);
-        if (!force) {
-            r += ldcg(p.msg + off);
-            p.msg[off] = 0.0;
-        }
-        if (force || r > (double)p.rmax) {
-            if (!force) p.pr[off] = ldcg(p.pr + off) + (float)((double)p.alpha * r);
-            act = true;
-            if (deg > 0) {
-                p.rq[off] = r;
-                p.res[off] = 0.0;
-            } else {
-                p.res[off] = r;  // popped (zeroed) at the top of the next round
-            }
-        } else {
-            p.res[off] = r;
-        }
-    }
-    const unsigned bits = __ballot_sync(kFull, act);
-    if (bits && deg == 0 && lane == 0) {
-        const unsigned slot = atomicAdd(dctr, 1u);
-        if (slot < p.qcap)
-            p.dangle[slot] = make_int2(vw, (int)bits);
-        else
-            atomicOr(&p.ctl->flags, C2G_FLAG_QUEUE_OVERFLOW);
-    }
-    stage_push(fst, out, lane == 0 && bits != 0u && deg > 0, vw, deg, __int_as_float((int)bits));
-}
-
 constexpr int kPprBatchUnroll = 3;  // push items in flight per lane (4 spills at 64 registers)
 
-// Apply sweep: every (vertex, word) whose touched mask is non-zero gets pbatch_apply for
-// its touched lanes; the mask is cleared.  Pushes mark targets with red.or, so the push
-// never waits on an atomic's return; the sweep reads V * W mask words per round.
+// Apply sweep: every (vertex, word) whose touched mask is non-zero applies its messages
+// lane by lane (lane = query) and activates; the mask is cleared.  Pushes mark targets
+// with red.or, so the push never waits on an atomic's return; the sweep reads V * W mask
+// words per round.  A warp takes 32 words at a time (their degrees loaded lane-parallel)
+// and applies up to kApplyGroup touched words at once: all their residual, message and
+// pr loads are issued before any of them is used, so the words' memory latencies
+// overlap instead of adding up.  force = true: the seeded first hop (activate every
+// touched lane, no messages).
+constexpr int kApplyGroup = 3;  // 4 spills at 64 registers
+
 __device__ __forceinline__ unsigned pbatch_sweep(const PprBatchParams& p, bool force, WarpStage& fst,
                                                  const FrontierOut& out, unsigned* dctr, unsigned gwarp,
                                                  unsigned nwarps, int lane) {
     const unsigned nm = (unsigned)p.V << p.logW;
+    const unsigned long long rmax_bits = c2g_dbits((double)p.rmax);
+    const double alpha = (double)p.alpha;
     unsigned cnt = 0;
     for (unsigned b = gwarp * 32u; b < nm; b += nwarps * 32u) {
         const unsigned i = b + (unsigned)lane;
         const unsigned tm = i < nm ? ldcg(p.tmask + i) : 0u;
-        if (tm) p.tmask[i] = 0u;
+        int dg = 0;
+        if (tm) {
+            p.tmask[i] = 0u;
+            const int v = (int)(i >> p.logW);
+            dg = __ldg(p.row + v + 1) - __ldg(p.row + v);
+        }
         unsigned nz = __ballot_sync(kFull, tm != 0u);
         cnt += (unsigned)__popc(tm);  // touched (vertex, query) lanes seen by this lane
         while (nz) {
-            const int k = __ffs(nz) - 1;
-            nz &= nz - 1u;
-            const unsigned lanes = (unsigned)__shfl_sync(kFull, (int)tm, k);
-            pbatch_apply(p, (int)(b + (unsigned)k), lanes, force, fst, out, dctr);
+            int ks[kApplyGroup];
+#pragma unroll
+            for (int u = 0; u < kApplyGroup; ++u) {
+                ks[u] = nz ? __ffs(nz) - 1 : -1;
+                nz &= nz - 1u;
+            }
+            // element (v, w*32 + lane) of a [V][Q] array sits at (v*W + w)*32 + lane
+            double r[kApplyGroup], m[kApplyGroup];
+            float pv[kApplyGroup];
+#pragma unroll
+            for (int u = 0; u < kApplyGroup; ++u) {
+                const int k = ks[u] < 0 ? 0 : ks[u];
+                const unsigned ln = ks[u] < 0 ? 0u : (unsigned)__shfl_sync(kFull, (int)tm, k);
+                const size_t off = ((size_t)(b + (unsigned)k) << 5) + lane;
+                const bool mine = (ln >> lane) & 1u;
+                r[u] = mine ? ldcg(p.res + off) : 0.0;
+                m[u] = (mine && !force) ? ldcg(p.msg + off) : 0.0;
+                pv[u] = (mine && !force) ? ldcg(p.pr + off) : 0.f;
+            }
+#pragma unroll
+            for (int u = 0; u < kApplyGroup; ++u) {
+                if (ks[u] < 0) break;  // warp-uniform
+                const unsigned ln = (unsigned)__shfl_sync(kFull, (int)tm, ks[u]);
+                const int dgu = __shfl_sync(kFull, dg, ks[u]);
+                const int vw = (int)(b + (unsigned)ks[u]);
+                const size_t off = ((size_t)(unsigned)vw << 5) + lane;
+                const bool mine = (ln >> lane) & 1u;
+                bool act = false;
+                if (mine) {
+                    double rr = r[u];
+                    if (!force) {
+                        rr += m[u];
+                        p.msg[off] = 0.0;
+                    }
+                    // rr and rmax are non-negative: compare their bit patterns
+                    if (force || c2g_dbits(rr) > rmax_bits) {
+                        if (!force) p.pr[off] = pv[u] + (float)(alpha * rr);
+                        act = true;
+                        if (dgu > 0) {
+                            p.rq[off] = rr;
+                            p.res[off] = 0.0;
+                        } else {
+                            p.res[off] = rr;  // popped (zeroed) at the top of the next round
+                        }
+                    } else {
+                        p.res[off] = rr;
+                    }
+                }
+                const unsigned bits = __ballot_sync(kFull, act);
+                if (bits && dgu == 0 && lane == 0) {
+                    const unsigned slot = atomicAdd(dctr, 1u);
+                    if (slot < p.qcap)
+                        p.dangle[slot] = make_int2(vw, (int)bits);
+                    else
+                        atomicOr(&p.ctl->flags, C2G_FLAG_QUEUE_OVERFLOW);
+                }
+                stage_push(fst, out, lane == 0 && bits != 0u && dgu > 0, vw, dgu, __int_as_float((int)bits));
+            }
         }
     }
     stage_flush(fst, out);

@@ -210,7 +210,7 @@ __global__ void __launch_bounds__(512, 2) ppr_persistent(const PprParams p) {
     const unsigned gwarp = gtid >> 5, nwarps = nthreads >> 5;
     const unsigned V = (unsigned)p.V;
     const double a = (double)p.alpha, one_m_a = 1.0 - (double)p.alpha, absorb = (double)p.absorb;
-    const double rmax = (double)p.rmax;
+    const unsigned long long rmax_bits = c2g_dbits((double)p.rmax);
     __shared__ StageSmemD sm;
     const int wib = threadIdx.x >> 5;
     WarpStage fst{sm.v0[wib], sm.d0[wib], nullptr, 0, sm.xd0[wib]};
@@ -382,7 +382,7 @@ __global__ void __launch_bounds__(512, 2) ppr_persistent(const PprParams p) {
                     v = ldcg(p.touched + i);
                     r = __ldcg(p.res + v) + __ldcg(p.msg + v);
                     p.msg[v] = 0.0;
-                    if (r > rmax) {
+                    if (c2g_dbits(r) > rmax_bits) {  // both non-negative
                         p.pr[v] = ldcg(p.pr + v) + (float)(absorb * r);
                         deg = __ldg(p.row + v + 1) - __ldg(p.row + v);
                         want = deg > 0;
@@ -411,7 +411,7 @@ __global__ void __launch_bounds__(512, 2) ppr_persistent(const PprParams p) {
                     if (c2g_dbits(m) != 0ull) {  // messages are positive; msg is +0 otherwise
                         p.msg[v] = 0.0;
                         r = __ldcg(p.res + v) + m;
-                        if (r > rmax) {
+                        if (c2g_dbits(r) > rmax_bits) {  // both non-negative
                             p.pr[v] = ldcg(p.pr + v) + (float)(absorb * r);
                             deg = __ldg(p.row + v + 1) - __ldg(p.row + v);
                             want = deg > 0;

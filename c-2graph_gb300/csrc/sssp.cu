@@ -223,9 +223,15 @@ __global__ void __launch_bounds__(512, 2) sssp_persistent(const SsspParams p) {
                 const int fold = (fb + 2) % 3;  // read by the previous filter, free now
                 ctl->farctr[fold] = 0;
                 ctl->farmin[fold] = INT_MAX;
+                ctl->qctr[(cur + 2) % 3] = 0ull;
+                ctl->tilectr[(cur + 2) % 3] = 0u;
             }
-            const FrontierOut out = sssp_out(p, cur & 1, cur % 3);
-            const int tag = sbase + cur;
+            // The filter's frontier is the next round's (slot cur + 1): every thread has
+            // read slot cur above to see it empty, and a late reader must not see these
+            // appends there (it would take the expansion branch and skip its share of
+            // the pile).
+            const FrontierOut out = sssp_out(p, (cur + 1) & 1, (cur + 1) % 3);
+            const int tag = sbase + cur + 1;
             for (unsigned b = gwarp * 32; b < fc; b += nwarps * 32) {
                 const unsigned i = b + (unsigned)lane;
                 bool near = false, keep = false;
@@ -252,6 +258,7 @@ __global__ void __launch_bounds__(512, 2) sssp_persistent(const SsspParams p) {
             ++epoch;
             if (!grid_sync(bar, flags, p.barrier_ns, p.bar_extra)) return;
             phase_mark(ctl->phase_ns, tph, 1);
+            ++cur;
             continue;
         }
         if (++iters > p.max_iter) {
