@@ -152,7 +152,8 @@ def run_reference(args, rank, world):
         o = oracle.load_dataset(d, "origin")
         ssrc = pick_sources(o["vlist"], 256)
         psrc = pick_sources(o["vlist"], 256, seed=2025)
-        ns, npq = min(args.cpu_sample, 256), min(args.cpu_sample, 256)
+        # one query per host thread and kind, so every thread works in each kind's pass
+        ns = npq = min(max(args.cpu_sample, threads), 256)
         times, q_total = [], 0
         for step in range(args.warmup + args.steps):
             k = (step * ns) % 256
