@@ -287,6 +287,13 @@ def run_ours(args, rank, world, local_rank):
     peak, peak_kind = measured_peak()
     achieved = tot[dominant + "_bytes"] / (tot[dominant + "_ms"] / 1000.0) / 1e9
     kernel_name = "sssp_batch_persistent" if dominant == "s" else "ppr_batch_persistent"
+    # DRAM bytes (read + write) per launch from a one-pass ncu capture of this step at full
+    # size (profiles/ppr_batch_persistent_rmat-s20-ef16_32q.md,
+    # profiles/sssp_batch_persistent_rmat-s20-ef16_32q.md), expressed per unit processed
+    # and scaled to this run's average launch.
+    traffic_per_unit = {"p": 5.8214e12 / 371.88e9, "s": 315.08e9 / 61.15e9}[dominant]
+    units = tot["p_push"] if dominant == "p" else tot["s_rel"]
+    traffic = traffic_per_unit * units / args.steps
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -321,7 +328,8 @@ def run_ours(args, rank, world, local_rank):
                     "d2h_bytes_per_step": 4 * V * q_step},
             "gpu_launches": 4 * args.steps,
             "roofline": {"bound": "hbm", "kernel": kernel_name, "achieved": achieved, "peak": peak,
-                         "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak, "traffic": None},
+                         "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
+                         "traffic_note": "DRAM bytes per launch, full-size one-pass ncu capture scaled by units"},
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
             "detail": {
