@@ -367,6 +367,100 @@ def _ppr_into(gp, src, prm, out):
     return None, None, st
 
 
+def run_serve(args):
+    """Serving loop (config 5): Poisson arrivals, mix 50% SSSP / 35% PPR / 15% adsorption
+    (16 seed labels, per-vertex p_inj/p_cont/p_abnd ~ Dirichlet(1,1,1), 30 iterations) on an
+    unpruned R-MAT graph resident in HBM; reports queries/s and p50/p99 latency."""
+    import c2g
+
+    rng = np.random.default_rng(7)
+    with tempfile.TemporaryDirectory(dir=args.workdir) as d:
+        t0 = time.time()
+        c2g.rmat_write(d, args.serve_scale, args.edge_factor, 3, 1, 1000)
+        gen_s = time.time() - t0
+        vl = c2g.read_array(os.path.join(d, "origin", "vlist.bin"))
+        V = len(vl) - 1
+        cand = np.flatnonzero(np.diff(vl) > 0)
+        pp = rng.dirichlet((1.0, 1.0, 1.0), size=V).astype(np.float32)
+        g = c2g.Graph.load(d, "origin")
+        n = args.serve_requests
+        kinds = [c2g.REQ_SSSP] * (n * 50 // 100) + [c2g.REQ_PPR] * (n * 35 // 100)
+        kinds += [c2g.REQ_ADSORPTION] * (n - len(kinds))
+        rng.shuffle(kinds)
+        gaps = rng.exponential(1.0 / args.serve_rate, size=n)
+        with c2g.Server(g, max_batch=256, alpha=ALPHA, rmax=RMAX, ads_iterations=30, p_inj=pp[:, 0],
+                        p_cont=pp[:, 1], p_abnd=pp[:, 2]) as srv:
+            # warm-up: one request of each kind (workspaces, graph capture)
+            for k in (c2g.REQ_SSSP, c2g.REQ_PPR, c2g.REQ_ADSORPTION):
+                t = srv.submit(k, source=int(cand[0]), seeds=rng.choice(V, 16, replace=False) if k == 2 else None)
+                srv.wait(t)
+            base = srv.stats().completed
+            tickets = []
+            t_start = time.time()
+            t_next = t_start
+            for k, gap in zip(kinds, gaps):
+                t_next += gap
+                while time.time() < t_next:
+                    pass
+                if k == c2g.REQ_ADSORPTION:
+                    tickets.append(srv.submit(k, seeds=rng.choice(V, 16, replace=False)))
+                else:
+                    tickets.append(srv.submit(k, source=int(rng.choice(cand))))
+            lat = []
+            for t in tickets:
+                st, ms = srv.wait(t)
+                assert st == 0, st
+                lat.append(ms)
+            wall = time.time() - t_start
+            stats = srv.stats()
+        g.close()
+    lat = np.array(lat)
+    line = {"mode": "serve", "metric": "serving: queries/s and p50/p99 latency, Poisson arrivals, mix 50/35/15",
+            "value": n / wall, "unit": "queries/s", "p50_ms": float(np.percentile(lat, 50)),
+            "p99_ms": float(np.percentile(lat, 99)), "higher_is_better": True, "n_gpus": 1,
+            "data": "synthetic R-MAT (seeded); no public dataset",
+            "config": {"workload": "rmat-s%d-ef%d unpruned, %d requests (%d SSSP / %d PPR / %d adsorption)" % (
+                args.serve_scale, args.edge_factor, n, kinds.count(0), kinds.count(1), kinds.count(2)),
+                "offered_rate_qps": args.serve_rate, "alpha": ALPHA, "rmax": RMAX, "ads_iterations": 30,
+                "ads_labels": 16},
+            "detail": {"batches": list(stats.batches), "max_batch": stats.max_batch, "admit_cap": list(stats.admit_cap),
+                       "completed_after_warmup": stats.completed - base, "gen_s": gen_s, "wall_s": wall}}
+    print(json.dumps(line), flush=True)
+
+
+def run_adjoint(args):
+    """PPR adjoint throughput (config 4): gradient of the summed PPR score of 64 random
+    targets w.r.t. every edge weight, alpha 0.15, eps 1e-8 forward and backward."""
+    import c2g
+
+    rng = np.random.default_rng(9)
+    with tempfile.TemporaryDirectory(dir=args.workdir) as d:
+        c2g.rmat_write(d, args.adjoint_scale, args.edge_factor, 4, 1, 1000)
+        vl = c2g.read_array(os.path.join(d, "origin", "vlist.bin"))
+        V = len(vl) - 1
+        cand = np.flatnonzero(np.diff(vl) > 0)
+        with c2g.Graph.load(d, "origin") as g:
+            prm = g.ppr_params(alpha=ALPHA, rmax=1e-8, seeded=0, pr0=ALPHA, r0=1.0, max_iter=10000)
+            srcs = rng.choice(cand, args.warmup + args.steps, replace=False)
+            ms = byt = 0.0
+            for i, s in enumerate(srcs):
+                targets = rng.choice(V, 64, replace=False).astype(np.int32)
+                _, _, _, _, st = g.ppr_adjoint(int(s), targets, prm, rmax_backward=1e-8)
+                if i >= args.warmup:
+                    ms += st.device_ms
+                    byt += st.alg_bytes
+            E = g.E
+    peak, peak_kind = measured_peak()
+    line = {"mode": "adjoint", "metric": "PPR adjoint gradients/s (dL/dw for every edge, 64 targets)",
+            "value": args.steps / (ms / 1000.0), "unit": "gradients/s", "ms_per_gradient": ms / args.steps,
+            "higher_is_better": True, "n_gpus": 1, "data": "synthetic R-MAT (seeded); no public dataset",
+            "config": {"workload": "rmat-s%d-ef%d, %d vertices, %d edges" % (args.adjoint_scale, args.edge_factor, V, E),
+                       "alpha": ALPHA, "eps_forward": 1e-8, "eps_backward": 1e-8, "targets": 64},
+            "roofline": {"bound": "hbm", "achieved": byt / (ms / 1000.0) / 1e9, "peak": peak, "peak_kind": peak_kind,
+                         "unit": "GB/s", "frac": byt / (ms / 1000.0) / 1e9 / peak}}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -384,12 +478,23 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workdir", default=None)
+    ap.add_argument("--mode", default="step", choices=["step", "serve", "adjoint"],
+                    help="step: the batched multi-tenant step (headline); serve: the serving loop; "
+                         "adjoint: PPR adjoint throughput")
+    ap.add_argument("--serve-scale", type=int, default=24)
+    ap.add_argument("--serve-requests", type=int, default=200)
+    ap.add_argument("--serve-rate", type=float, default=5000.0)
+    ap.add_argument("--adjoint-scale", type=int, default=20)
     args = ap.parse_args()
     rank, world, local_rank = env_rank()
     import __graft_entry__
 
     if rank == 0:
         __graft_entry__.build()
+    if args.mode != "step":
+        if rank == 0:
+            (run_serve if args.mode == "serve" else run_adjoint)(args)
+        return
     if args.impl == "reference":
         run_reference(args, rank, world)
     else:

@@ -15,8 +15,8 @@
 // plain store when the owner's in-edges lie inside the chunk, otherwise with atomicAdd
 // (only owners straddling a chunk boundary).  A vertex pass then applies p_inj / p_cont.
 // Per iteration: (8 + 64) bytes per edge (in-edge record + source label row) and
-// 64 + 64 + 12 bytes per vertex.  The iteration sequence is captured once into a CUDA
-// graph and replayed.
+// 64 + 64 + 12 bytes per vertex.  The iteration sequence is captured once per handle
+// (and iteration count) into a CUDA graph and replayed; its buffers stay with the handle.
 #include <cstring>
 #include <vector>
 
@@ -111,6 +111,80 @@ __global__ void ads_init(int V, const unsigned* __restrict__ seedmask, float* __
     }
 }
 
+// Seed mask from the 16 seed vertices: bit l of mask[v] says label l is seeded at v.
+__global__ void ads_seed_mask(const int* __restrict__ seeds, int n, unsigned* __restrict__ mask) {
+    const int l = threadIdx.x;
+    if (l < n) atomicOr(mask + seeds[l], 1u << l);
+}
+
+// Per-handle workspace of the label propagation, kept across calls so that a serving
+// loop's adsorption requests allocate nothing after the first one (cudaMalloc and
+// cudaFree synchronise the device and would stall the other kinds' batches), with the
+// iteration sequence captured once into a CUDA graph and replayed.
+struct AdsWork {
+    float* Y = nullptr;    // [V][16]
+    float* acc = nullptr;  // [V][16]
+    unsigned* mask = nullptr;
+    float* pi = nullptr;
+    float* pc = nullptr;
+    int* seeds = nullptr;  // [16]
+    cudaGraphExec_t exec = nullptr;
+    int iterations = -1;
+};
+
+void ads_free(c2g_graph* g) {
+    AdsWork* w = reinterpret_cast<AdsWork*>(g->ads);
+    if (!w) return;
+    if (w->exec) cudaGraphExecDestroy(w->exec);
+    void* ptrs[] = {w->Y, w->acc, w->mask, w->pi, w->pc, w->seeds};
+    for (void* q : ptrs)
+        if (q) cudaFree(q);
+    delete w;
+    g->ads = nullptr;
+}
+
+static int ads_alloc(c2g_graph* g, AdsWork** out) {
+    AdsWork* w = reinterpret_cast<AdsWork*>(g->ads);
+    if (!w) {
+        w = new AdsWork();
+        g->ads = w;
+        const size_t V = g->V ? (size_t)g->V : 1;
+        C2G_CUDA(cudaMalloc(&w->Y, sizeof(float) * V * kAdsL));
+        C2G_CUDA(cudaMalloc(&w->acc, sizeof(float) * V * kAdsL));
+        C2G_CUDA(cudaMalloc(&w->mask, sizeof(unsigned) * V));
+        C2G_CUDA(cudaMalloc(&w->pi, sizeof(float) * V));
+        C2G_CUDA(cudaMalloc(&w->pc, sizeof(float) * V));
+        C2G_CUDA(cudaMalloc(&w->seeds, sizeof(int) * kAdsL));
+    }
+    *out = w;
+    return C2G_OK;
+}
+
+// Capture init + `iterations` x (edge pass, vertex pass) on the handle's stream.
+static int ads_capture(c2g_graph* g, AdsWork* w, int iterations) {
+    if (w->exec && w->iterations == iterations) return C2G_OK;
+    if (w->exec) {
+        cudaGraphExecDestroy(w->exec);
+        w->exec = nullptr;
+    }
+    cudaGraph_t graph = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(g->stream, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+        const int eb = g->num_sms * 8, vb = g->num_sms * 8;
+        ads_init<<<vb, 256, 0, g->stream>>>(g->V, w->mask, w->acc, w->Y);
+        for (int it = 0; it < iterations; ++it) {
+            if (g->E) ads_edge_pass<<<eb, 256, 0, g->stream>>>(g->row_r, g->adj_r, g->V, (long long)g->E, w->Y, w->acc);
+            ads_vertex_pass<<<vb, 256, 0, g->stream>>>(g->V, w->pi, w->pc, w->mask, w->acc, w->Y);
+        }
+        e = cudaStreamEndCapture(g->stream, &graph);
+    }
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&w->exec, graph, 0);
+    if (graph) cudaGraphDestroy(graph);
+    C2G_CUDA(e);
+    w->iterations = iterations;
+    return C2G_OK;
+}
+
 int build_reverse_graph(c2g_graph* g);
 
 }  // namespace c2g
@@ -139,58 +213,29 @@ extern "C" int c2g_adsorption(c2g_graph* g, int32_t n_labels, const int32_t* see
     } restore{prev};
     int rc = build_reverse_graph(g);
     if (rc) return rc;
+    AdsWork* w = nullptr;
+    if ((rc = ads_alloc(g, &w))) return rc;
     const size_t V = (size_t)g->V;
-    std::vector<unsigned> seedmask(V, 0u);
-    for (int32_t l = 0; l < n_labels; ++l) seedmask[seed_vertices[l]] |= 1u << l;
-    float *Y = nullptr, *acc = nullptr, *pi = nullptr, *pc = nullptr;
-    unsigned* sm = nullptr;
-    C2G_CUDA(cudaMalloc(&acc, sizeof(float) * V * kAdsL));
-    C2G_CUDA(cudaMalloc(&sm, sizeof(unsigned) * V));
-    if (on_device) {
-        Y = Y_out;
-        pi = const_cast<float*>(p_inj);
-        pc = const_cast<float*>(p_cont);
-    } else {
-        C2G_CUDA(cudaMalloc(&Y, sizeof(float) * V * kAdsL));
-        C2G_CUDA(cudaMalloc(&pi, sizeof(float) * V));
-        C2G_CUDA(cudaMalloc(&pc, sizeof(float) * V));
-    }
-    cudaGraph_t graph = nullptr;
-    cudaGraphExec_t exec = nullptr;
+    const cudaMemcpyKind in_kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
     float ms = 0.f;
-    cudaError_t e = cudaMemcpyAsync(sm, seedmask.data(), sizeof(unsigned) * V, cudaMemcpyHostToDevice, g->stream);
-    if (e == cudaSuccess && !on_device) e = cudaMemcpyAsync(pi, p_inj, sizeof(float) * V, cudaMemcpyHostToDevice, g->stream);
-    if (e == cudaSuccess && !on_device) e = cudaMemcpyAsync(pc, p_cont, sizeof(float) * V, cudaMemcpyHostToDevice, g->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
-    // Capture the whole propagation (init + iterations) once; replay it.
-    if (e == cudaSuccess) e = cudaStreamBeginCapture(g->stream, cudaStreamCaptureModeThreadLocal);
+    cudaError_t e = cudaMemcpyAsync(w->seeds, seed_vertices, sizeof(int) * kAdsL, cudaMemcpyHostToDevice, g->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(w->pi, p_inj, sizeof(float) * V, in_kind, g->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(w->pc, p_cont, sizeof(float) * V, in_kind, g->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(w->mask, 0, sizeof(unsigned) * V, g->stream);
     if (e == cudaSuccess) {
-        const int eb = g->num_sms * 8, vb = g->num_sms * 8;
-        ads_init<<<vb, 256, 0, g->stream>>>(g->V, sm, acc, Y);
-        for (int it = 0; it < iterations; ++it) {
-            if (g->E) ads_edge_pass<<<eb, 256, 0, g->stream>>>(g->row_r, g->adj_r, g->V, (long long)g->E, Y, acc);
-            ads_vertex_pass<<<vb, 256, 0, g->stream>>>(g->V, pi, pc, sm, acc, Y);
-        }
-        cudaError_t ce = cudaStreamEndCapture(g->stream, &graph);
-        e = ce;
+        ads_seed_mask<<<1, 32, 0, g->stream>>>(w->seeds, kAdsL, w->mask);
+        e = cudaGetLastError();
     }
-    if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
-    if (e == cudaSuccess) e = cudaEventRecord(g->ev0, g->stream);
-    if (e == cudaSuccess) e = cudaGraphLaunch(exec, g->stream);
+    C2G_CUDA(e);
+    if ((rc = ads_capture(g, w, iterations))) return rc;
+    e = cudaEventRecord(g->ev0, g->stream);
+    if (e == cudaSuccess) e = cudaGraphLaunch(w->exec, g->stream);
     if (e == cudaSuccess) e = cudaEventRecord(g->ev1, g->stream);
-    if (e == cudaSuccess && !on_device)
-        e = cudaMemcpyAsync(Y_out, Y, sizeof(float) * V * kAdsL, cudaMemcpyDeviceToHost, g->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(Y_out, w->Y, sizeof(float) * V * kAdsL,
+                            on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, g->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
-    if (e == cudaSuccess) cudaEventElapsedTime(&ms, g->ev0, g->ev1);
-    if (exec) cudaGraphExecDestroy(exec);
-    if (graph) cudaGraphDestroy(graph);
-    cudaFree(acc);
-    cudaFree(sm);
-    if (!on_device) {
-        cudaFree(Y);
-        cudaFree(pi);
-        cudaFree(pc);
-    }
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, g->ev0, g->ev1);
     C2G_CUDA(e);
     if (stats) {
         std::memset(stats, 0, sizeof(*stats));

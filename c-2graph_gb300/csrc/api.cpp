@@ -26,6 +26,7 @@ static void graph_release(c2g_graph* g) {
     ppr_free(g);
     batch_free(g);
     ppr_batch_free(g);
+    ads_free(g);
     if (!g->borrowed) adjoint_free(g);
     if (!g->borrowed) {
         void* ptrs[] = {g->row, g->adj_w, g->adj_f, g->hv, g->he, g->hw, g->rec_of_vertex};

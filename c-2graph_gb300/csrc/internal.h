@@ -131,6 +131,7 @@ struct c2g_graph {
     std::vector<int32_t> h_he, h_hw;  // record targets / weights (bits)
     void* batch = nullptr;            // batched-query workspaces (batch.cu)
     void* ppr_batch = nullptr;
+    void* ads = nullptr;              // label-propagation workspace (adsorption.cu)
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -166,6 +167,7 @@ void ppr_free(c2g_graph* g);
 int graph_view(c2g_graph* base, c2g_graph** out);
 void batch_free(c2g_graph* g);
 void ppr_batch_free(c2g_graph* g);
+void ads_free(c2g_graph* g);
 int ppr_batch_launch(c2g_graph* g, int32_t nq, const int32_t* sources, const c2g_ppr_params& prm,
                      const std::vector<int32_t>* seed_off, const std::vector<int32_t>* seed_v,
                      const std::vector<float>* seed_w, float* pr_out, float* res_out, int on_device, int query_major,
