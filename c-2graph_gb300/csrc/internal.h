@@ -59,6 +59,7 @@ struct SsspWork {
     int2* q[2] = {nullptr, nullptr};
     int* mark[2] = {nullptr, nullptr};
     int* far = nullptr;  // three far piles of V ids each
+    unsigned* bits = nullptr;  // next-frontier bitmap of the Bellman-Ford kernel (V/32 words)
     TraversalCtl* ctl = nullptr;
     StampState* st = nullptr;
     unsigned mark_cap = 0;

@@ -284,6 +284,129 @@ __global__ void __launch_bounds__(512, 2) sssp_persistent(const SsspParams p) {
     }
 }
 
+// Bellman-Ford rounds (delta = 0) with a bitmap next frontier.  A relaxation that
+// improves a distance issues red.min on it and red.or of the vertex's bit into a
+// V-bit map; neither waits for a return value, so the relaxation path has no atomic
+// round trip (the list kernel above needs the atomicMin result and a round-tag exchange
+// per improved vertex).  A sweep over the V/32 map words then builds the next frontier
+// in vertex order (entries, edge-base prefix, tile markers) and clears the words:
+// two grid barriers per round instead of one.
+constexpr int kSweepGroup = 4;  // map words whose row bounds are loaded together
+
+__device__ __forceinline__ void bits_sweep(const SsspParams& p, unsigned* bits, const FrontierOut& out,
+                                           WarpStage& fst, unsigned gwarp, unsigned nwarps, int lane) {
+    const unsigned V = (unsigned)p.V;
+    const unsigned nw = (V + 31u) >> 5;
+    for (unsigned b = gwarp * 32u; b < nw; b += nwarps * 32u) {
+        const unsigned wi = b + (unsigned)lane;
+        const unsigned m = wi < nw ? ldcg(bits + wi) : 0u;
+        if (m) bits[wi] = 0u;
+        unsigned nz = __ballot_sync(kFull, m != 0u);
+        while (nz) {
+            int ks[kSweepGroup], deg[kSweepGroup];
+            bool set[kSweepGroup];
+#pragma unroll
+            for (int u = 0; u < kSweepGroup; ++u) {
+                ks[u] = nz ? __ffs(nz) - 1 : -1;
+                nz &= nz - 1u;
+            }
+#pragma unroll
+            for (int u = 0; u < kSweepGroup; ++u) {
+                const unsigned mk = ks[u] < 0 ? 0u : (unsigned)__shfl_sync(kFull, (int)m, ks[u] < 0 ? 0 : ks[u]);
+                const unsigned v = ((b + (unsigned)(ks[u] < 0 ? 0 : ks[u])) << 5) + (unsigned)lane;
+                set[u] = (mk >> lane) & 1u;
+                deg[u] = set[u] ? __ldg(p.row + v + 1) - __ldg(p.row + v) : 0;
+            }
+#pragma unroll
+            for (int u = 0; u < kSweepGroup; ++u) {
+                if (ks[u] < 0) break;  // warp-uniform
+                const unsigned v = ((b + (unsigned)ks[u]) << 5) + (unsigned)lane;
+                stage_push(fst, out, set[u] && deg[u] > 0, (int)v, deg[u], 0.f);
+            }
+        }
+    }
+    stage_flush(fst, out);
+}
+
+__global__ void __launch_bounds__(512, 2) sssp_bits_persistent(const SsspParams p, unsigned* bits) {
+    TraversalCtl* ctl = p.ctl;
+    GridBarrier* bar = reinterpret_cast<GridBarrier*>(&ctl->bar_count);
+    int* flags = &ctl->flags;
+    const int lane = threadIdx.x & 31;
+    const unsigned gtid = blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned nthreads = gridDim.x * blockDim.x;
+    const unsigned gwarp = gtid >> 5, nwarps = nthreads >> 5;
+    const unsigned V = (unsigned)p.V;
+    __shared__ StageSmem sm;
+    const int wib = threadIdx.x >> 5;
+    WarpStage fst{sm.v0[wib], sm.d0[wib], nullptr, 0};
+    unsigned long long tph = globaltimer_ns();
+
+    // Init: dis = INF (src/sssp/purn/Main.cu:144-156), empty map.
+    for (unsigned v = gtid; v < V; v += nthreads) p.dist[v] = kInfDist;
+    for (unsigned i = gtid; i < ((V + 31u) >> 5); i += nthreads) bits[i] = 0u;
+    if (!grid_sync(bar, flags, p.barrier_ns, p.bar_extra)) return;
+    // Source and pruned-record seeds (src/sssp/purn/Main.cu:160-181) form round 1.
+    if (gtid == 0) {
+        atomicMin(p.dist + p.source, 0);
+        atomicOr(bits + ((unsigned)p.source >> 5), 1u << (p.source & 31));
+        ctl->seeds = p.n_seeds;
+    }
+    for (unsigned i = gtid; i < (unsigned)p.n_seeds; i += nthreads) {
+        const int v = p.seed_v[i];
+        atomicMin(p.dist + v, p.seed_w[i]);
+        atomicOr(bits + ((unsigned)v >> 5), 1u << (v & 31));
+    }
+    if (!grid_sync(bar, flags, p.barrier_ns, p.bar_extra)) return;
+    phase_mark(ctl->phase_ns, tph, 0);
+
+    int cur = 1, iters = 0;
+    for (;;) {
+        const int buf = cur & 1, slot = cur % 3;
+        if (gtid == 0) ctl->qctr[(cur + 1) % 3] = 0ull;
+        bits_sweep(p, bits, sssp_out(p, buf, slot), fst, gwarp, nwarps, lane);
+        if (!grid_sync(bar, flags, p.barrier_ns, p.bar_extra)) return;
+        phase_mark(ctl->phase_ns, tph, 1);
+        const unsigned long long c = ldcg(&ctl->qctr[slot]);
+        const unsigned F = (unsigned)(c >> 32), T = (unsigned)c;
+        if (F == 0) break;
+        if (++iters > p.max_iter) {
+            if (gtid == 0) atomicOr(flags, C2G_FLAG_ITER_CAP);
+            break;
+        }
+        if (gtid == 0) {
+            ctl->popped += F;
+            ctl->relaxed += T;
+        }
+        constexpr int U = kSsspUnroll;
+        walk_frontier_edges<U>(
+            p.q[buf], p.mark[buf], p.row, F, T, p.log_tile, p.mark_cap, V, p.E, flags,
+            [&](int v, unsigned) { return ldcg(p.dist + v); },  // the owner's current distance
+            [&](const bool* ok, const unsigned* idx, const int* du) {
+                int c2[U], nd[U], cd[U];
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    const int2 ew = ok[u] ? __ldg(p.adj + idx[u]) : make_int2(0, 0);
+                    c2[u] = ew.x;
+                    nd[u] = du[u] + ew.y;
+                }
+#pragma unroll
+                for (int u = 0; u < U; ++u) cd[u] = ok[u] ? ldcg(p.dist + c2[u]) : INT_MIN;
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    if (nd[u] < cd[u]) {  // an L2 read guards the update
+                        atomicMin(p.dist + c2[u], nd[u]);
+                        atomicOr(bits + ((unsigned)c2[u] >> 5), 1u << (c2[u] & 31));
+                    }
+                }
+            });
+        if (!grid_sync(bar, flags, p.barrier_ns, p.bar_extra)) return;
+        phase_mark(ctl->phase_ns, tph, 2);
+        ++cur;
+    }
+    if (gtid == 0) ctl->iterations = iters;
+}
+
 // ---------------------------------------------------------------------------------------
 // host side
 
@@ -292,10 +415,12 @@ static int sssp_geometry(c2g_graph* g) {
     int coop = 0;
     C2G_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, g->device));
     if (!coop) return fail(C2G_ERR_UNSUPPORTED, "device %d lacks cooperative launch", g->device);
-    int per_sm_a = 0, per_sm_b = 0;
+    int per_sm_a = 0, per_sm_b = 0, per_sm_c = 0;
     C2G_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_a, sssp_persistent<false>, 512, 0));
     C2G_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_b, sssp_persistent<true>, 512, 0));
+    C2G_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_c, sssp_bits_persistent, 512, 0));
     int per_sm = per_sm_a < per_sm_b ? per_sm_a : per_sm_b;
+    if (per_sm_c < per_sm) per_sm = per_sm_c;
     if (per_sm < 1) return fail(C2G_ERR_CUDA, "SSSP kernel cannot be resident (occupancy 0)");
     g->geom_sssp.blocks = per_sm * g->num_sms;
     g->geom_sssp.threads = 512;
@@ -305,7 +430,7 @@ static int sssp_geometry(c2g_graph* g) {
 void sssp_free(c2g_graph* g) {
     SsspWork& w = g->sssp;
     void* ptrs[] = {w.dist, w.stamp, w.farstamp, w.q[0], w.q[1], w.mark[0], w.mark[1],
-                    w.far, w.ctl, w.st};
+                    w.far, w.bits, w.ctl, w.st};
     for (void* ptr : ptrs)
         if (ptr) cudaFree(ptr);
     w = SsspWork();
@@ -327,6 +452,7 @@ static int sssp_alloc(c2g_graph* g) {
         C2G_CUDA(cudaMalloc(&w.mark[b], sizeof(int) * mark_cap));
     }
     C2G_CUDA(cudaMalloc(&w.far, sizeof(int) * nv * 3));
+    C2G_CUDA(cudaMalloc(&w.bits, sizeof(unsigned) * ((nv + 31) / 32)));
     C2G_CUDA(cudaMalloc(&w.ctl, sizeof(TraversalCtl)));
     C2G_CUDA(cudaMalloc(&w.st, sizeof(StampState)));
     C2G_CUDA(cudaMemsetAsync(w.stamp, 0xff, sizeof(int) * nv, g->stream));
@@ -374,10 +500,12 @@ int sssp_launch(c2g_graph* g, int32_t source, const int32_t* seed_v, const int32
     p.bar_extra = g->stall_next_sssp ? 1u : 0u;
     g->stall_next_sssp = 0;
     C2G_CUDA(cudaMemsetAsync(w.ctl, 0, sizeof(TraversalCtl), g->stream));
-    void* args[] = {&p};
+    unsigned* bits = w.bits;
+    void* args[] = {&p, &bits};
     const bool delta = p.delta > 0;
+    // delta = 0: Bellman-Ford rounds with the bitmap frontier; delta > 0: near/far buckets
     C2G_CUDA(cudaEventRecord(g->ev0, g->stream));
-    C2G_CUDA(cudaLaunchCooperativeKernel(delta ? (const void*)sssp_persistent<true> : (const void*)sssp_persistent<false>,
+    C2G_CUDA(cudaLaunchCooperativeKernel(delta ? (const void*)sssp_persistent<true> : (const void*)sssp_bits_persistent,
                                          dim3(g->geom_sssp.blocks), dim3(g->geom_sssp.threads), args, 0, g->stream));
     C2G_CUDA(cudaEventRecord(g->ev1, g->stream));
     if (ms) {
