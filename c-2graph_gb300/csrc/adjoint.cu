@@ -104,7 +104,7 @@ int build_reverse_graph(c2g_graph* g) {
     cudaFree(indeg);
     C2G_CUDA(e);
     int rc = build_markers(g, g->row_r, &g->mark_r);
-    if (!rc && !g->mark_f) rc = build_markers(g, g->row, &g->mark_f);  // may exist already (PPR)
+    if (!rc) rc = build_markers(g, g->row, &g->mark_f);
     return rc;
 }
 
@@ -193,7 +193,7 @@ extern "C" int c2g_ppr_adjoint(c2g_graph* g, int32_t source, const c2g_ppr_param
     c2g_ppr_params fp = *params;
     fp.r0 = 1.0f;
     fp.pr0 = fp.alpha;
-    rc = ppr_launch_view(g, g->row, g->adj_f, g->row_r, g->adj_r, g->mark_r, g->mark_f, source, fp, fp.alpha, 0, nullptr,
+    rc = ppr_launch_view(g, g->row, g->adj_f, g->row_r, g->adj_r, g->mark_r, source, fp, fp.alpha, 0, nullptr,
                          nullptr, nullptr, nullptr, 0, pi, nullptr, &ms_f);
     if (!rc && (cudaMemcpyAsync(&cf, g->ppr.ctl, sizeof(cf), cudaMemcpyDeviceToHost, g->stream) != cudaSuccess ||
                 cudaStreamSynchronize(g->stream) != cudaSuccess))
@@ -202,8 +202,7 @@ extern "C" int c2g_ppr_adjoint(c2g_graph* g, int32_t source, const c2g_ppr_param
     c2g_ppr_params bp = *params;
     bp.rmax = rmax_backward;
     if (!rc)
-        rc = ppr_launch_view(g, g->row_r, g->adj_r, g->row, g->adj_f, g->mark_f, g->mark_r, tv[0], bp, 1.0f,
-                             (int32_t)tv.size(),
+        rc = ppr_launch_view(g, g->row_r, g->adj_r, g->row, g->adj_f, g->mark_f, tv[0], bp, 1.0f, (int32_t)tv.size(),
                              dtv, dtr, nullptr, nullptr, 0, lam, nullptr, &ms_b);
     if (!rc && (cudaMemcpyAsync(&cb, g->ppr.ctl, sizeof(cb), cudaMemcpyDeviceToHost, g->stream) != cudaSuccess ||
                 cudaStreamSynchronize(g->stream) != cudaSuccess))

@@ -93,6 +93,14 @@ __device__ __forceinline__ void batch_sweep(const BatchParams& p, const Frontier
 
 constexpr int kBatchUnroll = 4;  // relaxation items in flight per lane
 
+// Next tile of a round for this warp from the round's tile counter (lane 0 takes it, the
+// warp shares it).  Tiles differ in cost (active queries per step), so a dynamic queue
+// balances the warps better than a fixed round-robin.
+__device__ __forceinline__ unsigned next_tile(unsigned* ctr, int lane) {
+    unsigned t = 0;
+    if (lane == 0) t = atomicAdd(ctr, 1u);
+    return (unsigned)__shfl_sync(kFull, (int)t, 0);
+}
 
 // Lane compaction of one owner run: the run's work is the items (edge ei, active-query
 // slot j) for ei in [0, len) and j in [0, cnt), numbered i = ei * cnt + j; lane l takes

@@ -98,15 +98,6 @@ __device__ __forceinline__ bool grid_sync(GridBarrier* b, int* flags, unsigned l
     return s_ok != 0;
 }
 
-// Next tile of a round for this warp from the round's tile counter (lane 0 takes it, the
-// warp shares it).  Where tiles differ in cost a dynamic queue balances the warps better
-// than a fixed round-robin.
-__device__ __forceinline__ unsigned next_tile(unsigned* ctr, int lane) {
-    unsigned t = 0;
-    if (lane == 0) t = atomicAdd(ctr, 1u);
-    return (unsigned)__shfl_sync(kFull, (int)t, 0);
-}
-
 // Phase timing of a persistent launch, read by c2g_graph_last_phases: block 0's
 // thread 0 adds the time since the previous mark to phase_ns[phase].  Called right
 // after a grid barrier, so each interval is one phase of the whole grid (wait included).

@@ -158,8 +158,7 @@ int sssp_launch(c2g_graph* g, int32_t source, const int32_t* seed_v, const int32
 int ppr_launch(c2g_graph* g, int32_t source, const c2g_ppr_params& p, const int32_t* seed_v,
                const float* seed_w, int32_t n_seeds, float* pr_dev, float* res_dev, float* ms);
 int ppr_launch_view(c2g_graph* g, const int32_t* row, const int2* adj, const int32_t* row_rev, const int2* adj_rev,
-                    const int32_t* mark_rev, const int32_t* mark_fw, int32_t source, const c2g_ppr_params& pp,
-                    float absorb, int32_t n_src,
+                    const int32_t* mark_rev, int32_t source, const c2g_ppr_params& pp, float absorb, int32_t n_src,
                     const int32_t* src_list, const float* src_r0, const int32_t* seed_v, const float* seed_w,
                     int32_t n_rec, float* pr_dev, float* res_dev, float* ms);
 int build_markers(c2g_graph* g, const int* row, int** out);

@@ -42,7 +42,6 @@ struct PprParams {
     const int* row_r;   // reverse CSR (in-edges carrying w(u,v)), or nullptr: push only
     const int2* adj_r;
     const int* mark_r;  // owner of in-edge t * 2^kPullTileLog
-    const int* mark_fw; // owner of edge t * 2^kPullTileLog of (row, adj), or nullptr: no streamed push
     int pull_div;       // pull when T * pull_div > E (0: never)
     int dense_div;      // dense push round (no touched list) when T * dense_div > E (0: never)
     float* pr;
@@ -194,93 +193,6 @@ __device__ __forceinline__ void ppr_pull(const PprParams& p) {
                 const bool vn = __shfl_down_sync(kFull, (int)valid, 1) != 0;
                 const bool tail = valid && (lane == 31 || !vn || kn != k);
                 if (tail && s != 0.0) atomicAdd(p.msg + o + (unsigned)k, s);
-            }
-            e0 = seg_end;
-            o += 32;
-        }
-    }
-}
-
-// Dense push round streamed over the whole CSR: every vertex v with qd[v] != 0 (the
-// frontier's pushed residuals (1-alpha)*r, zero elsewhere) adds qd[v]*w(v,t) to msg[t]
-// over its out-edges.  Edges are read in tiles of 2^kPullTileLog in CSR order (coalesced,
-// no frontier indirection: the frontier walk's entry -> row -> edge chain is gone); a
-// tile's owners come 32 at a time from the markers and each edge's owner from a shuffle
-// search.  Only active owners' edges are loaded and pushed (red.add).  The dense apply
-// that follows rewrites qd for every vertex.
-constexpr int kStreamUnroll = 4;
-
-__device__ __forceinline__ void ppr_stream_push(const PprParams& p, unsigned* tctr) {
-    constexpr int U = kStreamUnroll;
-    const int lane = threadIdx.x & 31;
-    const unsigned tw = 1u << kPullTileLog;
-    const unsigned ntiles = (p.E + tw - 1) >> kPullTileLog;
-    const unsigned V = (unsigned)p.V;
-    unsigned tn = next_tile(tctr, lane);
-    for (unsigned t = tn; t < ntiles; t = tn) {
-        tn = next_tile(tctr, lane);  // the next tile, fetched while this one runs
-        unsigned e0 = t << kPullTileLog;
-        const unsigned e1 = min(e0 + tw, p.E);
-        unsigned o = (unsigned)__ldg(p.mark_fw + t);
-        while (e0 < e1) {
-            const unsigned j = o + (unsigned)lane;
-            unsigned base = 0x7fffffffu, endv = 0xffffffffu;
-            double q = 0.0;
-            if (j < V) {
-                base = (unsigned)__ldg(p.row + j);
-                endv = (unsigned)__ldg(p.row + j + 1);
-                q = __ldcg(p.qd + j);
-            }
-            if (o >= V || (unsigned)__shfl_sync(kFull, (int)base, 0) > e0) {
-                if (lane == 0) atomicOr(&p.ctl->flags, C2G_FLAG_BOUNDS);
-                break;
-            }
-            const unsigned seg_end = min(e1, (unsigned)__shfl_sync(kFull, endv, 31));
-            if (seg_end <= e0) {  // 32 owners without edges here: move on (o grows to V at most)
-                o += 32;
-                continue;
-            }
-            const bool qnz = c2g_dbits(q) != 0ull;  // pushed residuals are positive
-            if (__any_sync(kFull, qnz)) {
-                const DSplit qs = c2g_dsplit(q);
-                // exponent and high significand in one word (0: inactive, or outside the
-                // integer product's range)
-                const unsigned qpk = (qnz && c2g_mul_q_ok(qs)) ? ((unsigned)qs.e << 21) | qs.hi : 0u;
-                const bool slowq = __any_sync(kFull, qnz && qpk == 0u);
-                for (unsigned eb = e0; eb < seg_end; eb += 32u * U) {
-                    int k[U];
-                    unsigned pk[U], lo[U];
-                    int2 ew[U];
-#pragma unroll
-                    for (int u = 0; u < U; ++u) {
-                        const unsigned e = eb + (unsigned)lane + 32u * u;
-                        k[u] = owner_lane(base, e);
-                        pk[u] = (unsigned)__shfl_sync(kFull, (int)qpk, k[u]);
-                        lo[u] = (unsigned)__shfl_sync(kFull, (int)qs.lo, k[u]);
-                        ew[u] = (e < seg_end && (pk[u] != 0u || slowq)) ? __ldg(p.adj + e) : make_int2(0, 0);
-                    }
-#pragma unroll
-                    for (int u = 0; u < U; ++u) {
-                        const bool in = eb + (unsigned)lane + 32u * u < seg_end;
-                        const unsigned wb = (unsigned)ew[u].y;
-                        DSplit sj;
-                        sj.lo = lo[u];
-                        sj.hi = pk[u] & 0x1fffffu;
-                        sj.e = (int)(pk[u] >> 21);
-                        const bool fast = in && pk[u] != 0u && c2g_mul_w_ok(wb);
-                        double m = c2g_mul(sj, wb);
-                        bool send = fast;
-                        // residual or weight outside the integer product's domain: FP64 pipe
-                        if (__any_sync(kFull, in && (slowq || (pk[u] != 0u && !c2g_mul_w_ok(wb) && (int)wb > 0)))) {
-                            const double qk = __shfl_sync(kFull, q, k[u]);
-                            if (in && !fast && c2g_dbits(qk) != 0ull && (int)wb > 0) {
-                                m = qk * (double)__int_as_float(ew[u].y);
-                                send = m > 0.0;
-                            }
-                        }
-                        if (send) atomicAdd(p.msg + ew[u].x, m);
-                    }
-                }
             }
             e0 = seg_end;
             o += 32;
@@ -453,8 +365,6 @@ __global__ void __launch_bounds__(512, 2) ppr_persistent(const PprParams p) {
         const FrontierOut out = ppr_out(p, (cur + 1) & 1, nslot);
         if (pull)
             ppr_pull(p);
-        else if (dense && p.mark_fw)
-            ppr_stream_push(p, &ctl->tilectr[slot]);
         else
             ppr_push(p, cur & 1, slot, F, T, tst, !dense);
         if (!grid_sync(bar, flags, p.barrier_ns)) return;
@@ -618,8 +528,7 @@ static int ppr_alloc(c2g_graph* g) {
 int build_reverse_graph(c2g_graph* g);
 
 int ppr_launch_view(c2g_graph* g, const int32_t* row, const int2* adj, const int32_t* row_rev, const int2* adj_rev,
-                    const int32_t* mark_rev, const int32_t* mark_fw, int32_t source, const c2g_ppr_params& pp,
-                    float absorb, int32_t n_src,
+                    const int32_t* mark_rev, int32_t source, const c2g_ppr_params& pp, float absorb, int32_t n_src,
                     const int32_t* src_list, const float* src_r0, const int32_t* seed_v, const float* seed_w,
                     int32_t n_rec, float* pr_dev, float* res_dev, float* ms) {
     int rc;
@@ -635,7 +544,6 @@ int ppr_launch_view(c2g_graph* g, const int32_t* row, const int2* adj, const int
     p.row_r = row_rev;
     p.adj_r = adj_rev;
     p.mark_r = mark_rev;
-    p.mark_fw = mark_fw;
     p.pull_div = row_rev ? g->ppr_cfg.pull_div : 0;
     p.dense_div = g->ppr_cfg.dense_div;
     p.pr = pr_dev ? pr_dev : w.pr;
@@ -697,14 +605,8 @@ int ppr_launch(c2g_graph* g, int32_t source, const c2g_ppr_params& pp, const int
         adj_r = g->adj_r;
         mark_r = g->mark_r;
     }
-    // Tile markers of the forward CSR for the streamed dense push (built once per handle;
-    // a view borrows its base's, or streams nothing).
-    if (!g->mark_f && !g->borrowed && g->E > 0) {
-        int rc = build_markers(g, g->row, &g->mark_f);
-        if (rc) return rc;
-    }
-    return ppr_launch_view(g, g->row, g->adj_f, row_r, adj_r, mark_r, g->mark_f, source, pp, pp.alpha, 0, nullptr,
-                           nullptr, seed_v, seed_w, n_rec, pr_dev, res_dev, ms);
+    return ppr_launch_view(g, g->row, g->adj_f, row_r, adj_r, mark_r, source, pp, pp.alpha, 0, nullptr, nullptr,
+                           seed_v, seed_w, n_rec, pr_dev, res_dev, ms);
 }
 
 }  // namespace c2g
