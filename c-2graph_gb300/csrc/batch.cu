@@ -92,6 +92,10 @@ __device__ __forceinline__ void batch_sweep(const BatchParams& p, const Frontier
 }
 
 constexpr int kBatchUnroll = 4;  // relaxation items in flight per lane
+// Launch shape of the batched SSSP: 3 blocks of 384 threads per SM (36 warps) measured
+// faster than 2 x 512 (32 warps) at the same 4 items per lane (132-135 vs 140 ms for 256
+// sources at scale 22), 1 x 512 with 8-12 items (220 ms) and 6 x 256 (192 ms).
+constexpr int kSsspBatchThreads = 384;
 
 // Next tile of a round for this warp from the round's tile counter (lane 0 takes it, the
 // warp shares it).  Tiles differ in cost (active queries per step), so a dynamic queue
@@ -132,7 +136,7 @@ __device__ __forceinline__ void owner_items(unsigned cnt, unsigned len, int lane
     }
 }
 
-__global__ void __launch_bounds__(512, 2) sssp_batch_persistent(const BatchParams p) {
+__global__ void __launch_bounds__(kSsspBatchThreads, 3) sssp_batch_persistent(const BatchParams p) {
     TraversalCtl* ctl = p.ctl;
     GridBarrier* bar = reinterpret_cast<GridBarrier*>(&ctl->bar_count);
     int* flags = &ctl->flags;
@@ -413,7 +417,7 @@ int sssp_batch_launch(c2g_graph* g, int32_t nq, const int32_t* sources, const st
     int coop = 0, per_sm = 0;
     C2G_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, g->device));
     if (!coop) return fail(C2G_ERR_UNSUPPORTED, "device lacks cooperative launch");
-    C2G_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sssp_batch_persistent, 512, 0));
+    C2G_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sssp_batch_persistent, kSsspBatchThreads, 0));
     if (per_sm < 1) return fail(C2G_ERR_CUDA, "batch kernel cannot be resident");
 
     C2G_CUDA(cudaMemcpyAsync(w->src, sources, sizeof(int) * (size_t)nq, cudaMemcpyHostToDevice, g->stream));
@@ -455,7 +459,7 @@ int sssp_batch_launch(c2g_graph* g, int32_t nq, const int32_t* sources, const st
     void* args[] = {&p};
     C2G_CUDA(cudaEventRecord(g->ev0, g->stream));
     const int blocks = grid_blocks(g, per_sm);
-    C2G_CUDA(cudaLaunchCooperativeKernel((const void*)sssp_batch_persistent, dim3(blocks), dim3(512),
+    C2G_CUDA(cudaLaunchCooperativeKernel((const void*)sssp_batch_persistent, dim3(blocks), dim3(kSsspBatchThreads),
                                          args, 0, g->stream));
     C2G_CUDA(cudaEventRecord(g->ev1, g->stream));
     // Results in the caller's layout.
