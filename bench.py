@@ -129,14 +129,9 @@ def make_dataset(d, scale, ef, seed):
 def pick_sources(vlist, n_each, seed=2024):
     """Config-3 selection: half uniform over vertices with out-edges, half from the top
     1% out-degree vertices."""
-    deg = np.diff(vlist)
-    rng = np.random.default_rng(seed)
-    cand = np.flatnonzero(deg > 0)
-    top = np.argsort(-deg, kind="stable")[:max(1, len(deg) // 100)]
-    top = top[deg[top] > 0]
-    half = n_each // 2
-    out = np.concatenate([rng.choice(cand, n_each - half, replace=False), rng.choice(top, half, replace=False)])
-    return out.astype(np.int32)
+    from c2g import replicas
+
+    return replicas.pick_sources(vlist, n_each, seed)
 
 
 def run_reference(args, rank, world):
@@ -196,8 +191,10 @@ def run_ours(args, rank, world, local_rank):
     po = {"vlist": c2g.read_array(os.path.join(work, "ppr", "vlist.bin"))}
     V = len(so["vlist"]) - 1
     nS, nP = args.sssp_per_step, args.ppr_per_step
-    ssrc = pick_sources(so["vlist"], nS, seed=2024 + rank)
-    psrc = pick_sources(po["vlist"], nP, seed=2025 + rank)
+    from c2g import replicas
+
+    ssrc = replicas.rank_sources(so["vlist"], nS, rank, 2024)
+    psrc = replicas.rank_sources(po["vlist"], nP, rank, 2025)
 
     gs = c2g.Graph.load(work, "sssp", device=dev)
     gp = c2g.Graph.load(work, "ppr", device=dev)
@@ -249,20 +246,15 @@ def run_ours(args, rank, world, local_rank):
         e1.record(stream)
         barrier()
         wall = time.time() - t0
-        ms = e0.elapsed_time(e1)
-        if dist_on:
-            t = torch.tensor([ms], device=dev)
-            tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
-            ms = float(t.item())
+        ms = replicas.max_over_ranks(e0.elapsed_time(e1), device=dev)
         return ms, wall, acc
 
     with ClockSampler(dev) as clk:
         ms_dev, wall_dev, tot = timed(False)
     ms_e2e, wall_e2e, _ = timed(True)
     q_step = nS + nP
-    q_all = q_step * args.steps * world
-    value = q_all / (ms_dev / 1000.0)
-    e2e = q_all / (ms_e2e / 1000.0)
+    value = replicas.job_rate(q_step * args.steps, world, ms_dev)
+    e2e = replicas.job_rate(q_step * args.steps, world, ms_e2e)
 
     # The plain per-query GPU path on a sample of the same mix (same kernels' single-
     # query form): the batched-vs-per-query ratio of the metric.
