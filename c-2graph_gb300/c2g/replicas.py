@@ -18,7 +18,9 @@ def pick_sources(vlist, n, seed):
     top = np.argsort(-deg, kind="stable")[:max(1, len(deg) // 100)]
     top = top[deg[top] > 0]
     half = n // 2
-    out = np.concatenate([rng.choice(cand, n - half, replace=False), rng.choice(top, half, replace=False)])
+    # small graphs: draw with replacement when a set is smaller than its share
+    out = np.concatenate([rng.choice(cand, n - half, replace=len(cand) < n - half),
+                          rng.choice(top, half, replace=len(top) < half)])
     return out.astype(np.int32)
 
 
