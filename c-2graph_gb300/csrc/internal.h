@@ -141,7 +141,7 @@ struct c2g_graph {
     c2g::PprConfig ppr_cfg;
     c2g::SsspWork sssp;
     c2g::PprWork ppr;
-    c2g::LaunchGeom geom_sssp, geom_ppr;
+    c2g::LaunchGeom geom_sssp, geom_ppr, geom_bits;
     int num_sms = 0;
     float grid_scale = 1.0f;  // fraction of the GPU a batched launch may occupy
     unsigned long long barrier_ns = 0;  // grid-barrier wait limit (0: per-kernel default)

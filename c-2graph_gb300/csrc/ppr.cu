@@ -87,6 +87,8 @@ __device__ __forceinline__ FrontierOut ppr_out(const PprParams& p, int buf, int 
 }
 
 constexpr int kPprUnroll = 4;  // edges in flight per lane
+constexpr int kPprThreads = 512;  // launch shape of the persistent push
+constexpr int kPprBlocksPerSm = 2;
 
 // Push round, phase A.  The first message a vertex gets in a round is the one whose
 // atomicAdd returns 0 (msg[v] is 0 between rounds and every message is positive), so no
@@ -200,7 +202,7 @@ __device__ __forceinline__ void ppr_pull(const PprParams& p) {
     }
 }
 
-__global__ void __launch_bounds__(512, 2) ppr_persistent(const PprParams p) {
+__global__ void __launch_bounds__(kPprThreads, kPprBlocksPerSm) ppr_persistent(const PprParams p) {
     TraversalCtl* ctl = p.ctl;
     GridBarrier* bar = reinterpret_cast<GridBarrier*>(&ctl->bar_count);
     int* flags = &ctl->flags;
@@ -480,10 +482,10 @@ static int ppr_geometry(c2g_graph* g) {
     C2G_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, g->device));
     if (!coop) return fail(C2G_ERR_UNSUPPORTED, "device %d lacks cooperative launch", g->device);
     int per_sm = 0;
-    C2G_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ppr_persistent, 512, 0));
+    C2G_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ppr_persistent, kPprThreads, 0));
     if (per_sm < 1) return fail(C2G_ERR_CUDA, "PPR kernel cannot be resident (occupancy 0)");
     g->geom_ppr.blocks = per_sm * g->num_sms;
-    g->geom_ppr.threads = 512;
+    g->geom_ppr.threads = kPprThreads;
     return C2G_OK;
 }
 

@@ -292,6 +292,8 @@ __global__ void __launch_bounds__(512, 2) sssp_persistent(const SsspParams p) {
 // in vertex order (entries, edge-base prefix, tile markers) and clears the words:
 // two grid barriers per round instead of one.
 constexpr int kSweepGroup = 4;  // map words whose row bounds are loaded together
+constexpr int kBitsThreads = 512;  // block size of the bitmap kernel (its own launch geometry)
+constexpr int kBitsBlocksPerSm = 2;
 
 __device__ __forceinline__ void bits_sweep(const SsspParams& p, unsigned* bits, const FrontierOut& out,
                                            WarpStage& fst, unsigned gwarp, unsigned nwarps, int lane) {
@@ -328,7 +330,8 @@ __device__ __forceinline__ void bits_sweep(const SsspParams& p, unsigned* bits, 
     stage_flush(fst, out);
 }
 
-__global__ void __launch_bounds__(512, 2) sssp_bits_persistent(const SsspParams p, unsigned* bits) {
+__global__ void __launch_bounds__(kBitsThreads, kBitsBlocksPerSm) sssp_bits_persistent(const SsspParams p,
+                                                                                       unsigned* bits) {
     TraversalCtl* ctl = p.ctl;
     GridBarrier* bar = reinterpret_cast<GridBarrier*>(&ctl->bar_count);
     int* flags = &ctl->flags;
@@ -418,12 +421,13 @@ static int sssp_geometry(c2g_graph* g) {
     int per_sm_a = 0, per_sm_b = 0, per_sm_c = 0;
     C2G_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_a, sssp_persistent<false>, 512, 0));
     C2G_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_b, sssp_persistent<true>, 512, 0));
-    C2G_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_c, sssp_bits_persistent, 512, 0));
-    int per_sm = per_sm_a < per_sm_b ? per_sm_a : per_sm_b;
-    if (per_sm_c < per_sm) per_sm = per_sm_c;
-    if (per_sm < 1) return fail(C2G_ERR_CUDA, "SSSP kernel cannot be resident (occupancy 0)");
+    C2G_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_c, sssp_bits_persistent, kBitsThreads, 0));
+    const int per_sm = per_sm_a < per_sm_b ? per_sm_a : per_sm_b;
+    if (per_sm < 1 || per_sm_c < 1) return fail(C2G_ERR_CUDA, "SSSP kernel cannot be resident (occupancy 0)");
     g->geom_sssp.blocks = per_sm * g->num_sms;
     g->geom_sssp.threads = 512;
+    g->geom_bits.blocks = per_sm_c * g->num_sms;
+    g->geom_bits.threads = kBitsThreads;
     return C2G_OK;
 }
 
@@ -506,7 +510,8 @@ int sssp_launch(c2g_graph* g, int32_t source, const int32_t* seed_v, const int32
     // delta = 0: Bellman-Ford rounds with the bitmap frontier; delta > 0: near/far buckets
     C2G_CUDA(cudaEventRecord(g->ev0, g->stream));
     C2G_CUDA(cudaLaunchCooperativeKernel(delta ? (const void*)sssp_persistent<true> : (const void*)sssp_bits_persistent,
-                                         dim3(g->geom_sssp.blocks), dim3(g->geom_sssp.threads), args, 0, g->stream));
+                                         dim3(delta ? g->geom_sssp.blocks : g->geom_bits.blocks),
+                                         dim3(delta ? g->geom_sssp.threads : g->geom_bits.threads), args, 0, g->stream));
     C2G_CUDA(cudaEventRecord(g->ev1, g->stream));
     if (ms) {
         C2G_CUDA(cudaEventSynchronize(g->ev1));
