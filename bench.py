@@ -283,7 +283,7 @@ def run_ours(args, rank, world, local_rank):
     # size (profiles/ppr_batch_persistent_rmat-s20-ef16_32q.md,
     # profiles/sssp_batch_persistent_rmat-s20-ef16_32q.md), expressed per unit processed
     # and scaled to this run's average launch.
-    traffic_per_unit = {"p": 5.8214e12 / 371.88e9, "s": 315.08e9 / 61.15e9}[dominant]
+    traffic_per_unit = {"p": 5.8424e12 / 371.90e9, "s": 318.54e9 / 61.20e9}[dominant]
     units = tot["p_push"] if dominant == "p" else tot["s_rel"]
     traffic = traffic_per_unit * units / args.steps
 
