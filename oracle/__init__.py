@@ -36,6 +36,9 @@ def lib():
             fn.restype = ctypes.c_int
             fn.argtypes = [_I32, _P, _P, _P, _I32, ctypes.c_double, ctypes.c_double, ctypes.c_double,
                            ctypes.c_double, _I32, _I32, _I32, _I32, _P, _P, _P, _P, _P]
+        L.orc_sssp_certificate.restype = ctypes.c_int64
+        L.orc_sssp_certificate.argtypes = [_I32, _P, _P, _P, _I32, _P, _I32, _P, _P, _P,
+                                           ctypes.POINTER(ctypes.c_int32)]
         L.orc_batch.restype = ctypes.c_int64
         L.orc_batch.argtypes = [ctypes.c_int, _I32, _P, _P, _P, _P, _I32, _P, ctypes.c_double,
                                 ctypes.c_double, _I32, _I32, _P, _P]
@@ -111,6 +114,19 @@ def ppr_push(row, col, f, source, alpha, rmax, r0=1.0, pr0=None, max_iter=500, s
                 int(degree_scaled), len(sv), _p(sv) if len(sv) else None, _p(sw) if len(sw) else None,
                 _p(pr), _p(res), _p(cnt))
     return pr, res, rounds, cnt
+
+
+def sssp_certificate(row, col, w, dist, sources, seed_v=(), seed_w=()):
+    """Check a distance vector against the Bellman conditions (orc_sssp_certificate);
+    returns (number of violating vertices, first violating vertex or -1)."""
+    row, col, w = _c(row, np.int32), _c(col, np.int32), _c(w, np.int32)
+    src, sv, sw = _c(sources, np.int32), _c(seed_v, np.int32), _c(seed_w, np.int32)
+    d = _c(dist, np.int32)
+    bv = ctypes.c_int32()
+    bad = lib().orc_sssp_certificate(len(row) - 1, _p(row), _p(col), _p(w), len(src), _p(src), len(sv),
+                                     _p(sv) if len(sv) else None, _p(sw) if len(sw) else None, _p(d),
+                                     ctypes.byref(bv))
+    return int(bad), int(bv.value)
 
 
 def batch(kind, row, col, w, f, sources, alpha=0.15, rmax=1e-7, max_iter=500, threads=1,

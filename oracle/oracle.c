@@ -18,6 +18,9 @@
  *                      src/ppr/purn/Main.cu:156-198 init/seeds, :248-360 push,
  *                      :379-407 frontier rule) in double or float
  *   orc_*_batch        one independent query per host thread (CPU baseline)
+ *   orc_sssp_certificate
+ *                      size-independent exactness check of a distance vector: the
+ *                      Bellman conditions of the fixed point CalcuSSSP computes
  *
  * Parity is pinned by tests/test_oracle_golden.py against fixtures made by the
  * reference's own code built from source (oracle/build.py, tests/golden/).
@@ -147,6 +150,53 @@ int orc_sssp_seeded(int32_t V, const int32_t* row, const int32_t* col, const int
     int r = orc_bellman_ford(V, row, col, w, dist, fr, n_seeds + 1);
     free(fr);
     return r;
+}
+
+/* Optimality certificate of a distance vector for sources S (dist 0) and seeds (v, w):
+ *   (a) dist[s] = 0 for s in S, dist[v] <= w for each seed;
+ *   (b) no edge improves a distance: dist[v] <= dist[u] + w(u,v) whenever dist[u] is finite;
+ *   (c) every other finite dist[v] is achieved by a tight in-edge (dist[u] + w(u,v) ==
+ *       dist[v]) or by a seed (w == dist[v]);
+ *   (d) unreachable vertices hold exactly ORC_INF.
+ * With positive weights (a)-(c) pin dist to the shortest distances (tight in-edges lead
+ * back, strictly decreasing, to a source or seed; no edge shortens any of them), so the
+ * check replaces an oracle run on graphs too large for one.  Returns the number of
+ * violating vertices (0: certified); bad_vertex gets the first one. */
+int64_t orc_sssp_certificate(int32_t V, const int32_t* row, const int32_t* col, const int32_t* w,
+                             int32_t n_src, const int32_t* src, int32_t n_seeds, const int32_t* seed_v,
+                             const int32_t* seed_w, const int32_t* dist, int32_t* bad_vertex) {
+    char* tight = (char*)calloc((size_t)(V > 0 ? V : 1), 1);
+    int64_t bad = 0;
+    *bad_vertex = -1;
+#define ORC_BAD(v)                              \
+    do {                                        \
+        if (*bad_vertex < 0) *bad_vertex = (v); \
+        ++bad;                                  \
+    } while (0)
+    for (int32_t k = 0; k < n_src; ++k) {
+        if (dist[src[k]] != 0) ORC_BAD(src[k]);
+        tight[src[k]] = 1;
+    }
+    for (int32_t k = 0; k < n_seeds; ++k) {
+        if (dist[seed_v[k]] > seed_w[k]) ORC_BAD(seed_v[k]);
+        if (dist[seed_v[k]] == seed_w[k]) tight[seed_v[k]] = 1;
+    }
+    for (int32_t u = 0; u < V; ++u) {
+        const int32_t du = dist[u];
+        if (du < 0 || du > ORC_INF) ORC_BAD(u);
+        if (du >= ORC_INF) continue;
+        for (int32_t j = row[u]; j < row[u + 1]; ++j) {
+            const int64_t nd = (int64_t)du + w[j];
+            const int32_t v = col[j];
+            if ((int64_t)dist[v] > nd) ORC_BAD(v);
+            if ((int64_t)dist[v] == nd) tight[v] = 1;
+        }
+    }
+    for (int32_t v = 0; v < V; ++v)
+        if (dist[v] < ORC_INF && !tight[v]) ORC_BAD(v);
+#undef ORC_BAD
+    free(tight);
+    return bad;
 }
 
 /* ---- PPR forward push -------------------------------------------------------------- */

@@ -169,3 +169,26 @@ def test_oracle_push_seeded_first_hop(built):
     ps, rs, ns, _ = oracle.ppr_push(vl, el, f, s, 0.2, 1e-9, seeded=True, seed_v=sv, seed_w=sw)
     assert ns == nb - 1
     assert np.abs(ps - pb).sum() < 1e-12
+
+
+def test_sssp_certificate_accepts_exact_and_rejects_planted_errors(tmp_path):
+    """The Bellman-conditions certificate used by the full-size GPU tests: Dijkstra's
+    distances pass; a distance raised or lowered by one (planted on the CPU) fails."""
+    import c2g
+    import oracle
+
+    d = str(tmp_path)
+    c2g.rmat_write(d, 12, 8, 5, 1, 1000)
+    o = oracle.load_dataset(d, "origin")
+    s = int(np.argmax(np.diff(o["vlist"])))
+    ref = oracle.dijkstra(o["vlist"], o["elist"], o["wlist"], [s], [0])
+    assert oracle.sssp_certificate(o["vlist"], o["elist"], o["wlist"], ref, [s]) == (0, -1)
+    reached = np.flatnonzero((ref < c2g.INF_DIST) & (ref > 0))
+    for delta in (1, -1):
+        bad = ref.copy()
+        bad[reached[5]] += delta
+        n, first = oracle.sssp_certificate(o["vlist"], o["elist"], o["wlist"], bad, [s])
+        assert n > 0 and first >= 0
+    unreached = ref.copy()
+    unreached[reached[3]] = c2g.INF_DIST  # a reachable vertex reported unreachable
+    assert oracle.sssp_certificate(o["vlist"], o["elist"], o["wlist"], unreached, [s])[0] > 0
