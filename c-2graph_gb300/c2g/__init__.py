@@ -128,6 +128,7 @@ SIGNATURES = {
                                       ctypes.c_double]),
     "c2g_prune_sssp": (ctypes.c_int, [ctypes.c_char_p]),
     "c2g_prune_ppr": (ctypes.c_int, [ctypes.c_char_p]),
+    "c2g_prune_ppr_alpha": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_double]),
 }
 
 
@@ -172,8 +173,12 @@ def prune_sssp(dir):
     _check(lib().c2g_prune_sssp(os.fsencode(dir)))
 
 
-def prune_ppr(dir):
-    _check(lib().c2g_prune_ppr(os.fsencode(dir)))
+def prune_ppr(dir, alpha=None):
+    """purn-ppr; with alpha, folded edges carry 1 - alpha instead of the baked 0.8."""
+    if alpha is None:
+        _check(lib().c2g_prune_ppr(os.fsencode(dir)))
+    else:
+        _check(lib().c2g_prune_ppr_alpha(os.fsencode(dir), float(alpha)))
 
 
 def read_array(path, dtype=np.int32):

@@ -72,13 +72,17 @@ struct SsspRule {
     static W combine_hit(W old, W d3, W dis) { return std::min(old, d3 + dis); }
     static constexpr bool skip_root_target = true;  // src/purn-sssp.cpp:244,263
 };
+// Factor of a folded PPR edge: the continuation probability 1 - alpha of the push the
+// pruned graph is built for.  The reference bakes 0.8 (alpha 0.2) into it.
+thread_local double g_ppr_keep = 0.8;
+
 struct PprRule {
     using W = float;
-    // (float * 0.8) * float evaluated in double, then rounded to float
-    // (src/purn-ppr.cpp:244,255,259).
-    static W combine_new(W d3, W dis) { return (float)((double)d3 * 0.8 * (double)dis); }
+    // (float * keep) * float evaluated in double, then rounded to float, keep = 0.8 in
+    // the reference (src/purn-ppr.cpp:244,255,259).
+    static W combine_new(W d3, W dis) { return (float)((double)d3 * g_ppr_keep * (double)dis); }
     static W combine_hit(W old, W d3, W dis) {
-        return (float)((double)old + (double)d3 * 0.8 * (double)dis);
+        return (float)((double)old + (double)d3 * g_ppr_keep * (double)dis);
     }
     static constexpr bool skip_root_target = false;
 };
@@ -276,7 +280,8 @@ int prune_sssp_dir(const std::string& dir) {
     return C2G_OK;
 }
 
-int prune_ppr_dir(const std::string& dir) {
+int prune_ppr_dir(const std::string& dir, double keep) {
+    g_ppr_keep = keep;
     std::vector<int32_t> vlist, elist;
     std::vector<float> flist;
     int rc;
@@ -332,5 +337,11 @@ extern "C" int c2g_prune_sssp(const char* dir) {
 
 extern "C" int c2g_prune_ppr(const char* dir) {
     if (!dir) return c2g::fail(C2G_ERR_ARG, "prune: dir is NULL");
-    return c2g::prune_ppr_dir(dir);
+    return c2g::prune_ppr_dir(dir, 0.8);
+}
+
+extern "C" int c2g_prune_ppr_alpha(const char* dir, double alpha) {
+    if (!dir) return c2g::fail(C2G_ERR_ARG, "prune: dir is NULL");
+    if (!(alpha > 0.0 && alpha < 1.0)) return c2g::fail(C2G_ERR_ARG, "prune: alpha must be in (0, 1)");
+    return c2g::prune_ppr_dir(dir, 1.0 - alpha);
 }

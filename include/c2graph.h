@@ -323,6 +323,11 @@ int c2g_rmat_write(const char* dir, int scale, int edge_factor, uint64_t seed,
  * record->vertex sidecar <dir>/sssp/hvmap.bin. */
 int c2g_prune_sssp(const char* dir);
 int c2g_prune_ppr(const char* dir);
+/* purn-ppr for another teleport probability: a folded edge carries (1 - alpha) instead
+ * of the reference's baked 0.8 (src/purn-ppr.cpp:244), so a seeded push with that alpha
+ * on the pruned graph follows the unpruned push.  alpha = 0.2 writes exactly what
+ * c2g_prune_ppr writes (1 - 0.2 and 0.8 are the same double). */
+int c2g_prune_ppr_alpha(const char* dir, double alpha);
 
 #ifdef __cplusplus
 }

@@ -192,3 +192,35 @@ def test_sssp_certificate_accepts_exact_and_rejects_planted_errors(tmp_path):
     unreached = ref.copy()
     unreached[reached[3]] = c2g.INF_DIST  # a reachable vertex reported unreachable
     assert oracle.sssp_certificate(o["vlist"], o["elist"], o["wlist"], unreached, [s])[0] > 0
+
+
+def test_prune_ppr_alpha(tmp_path):
+    """The alpha-parameterised PPR pruner: alpha 0.2 writes the reference's bytes; another
+    alpha keeps the pruned structure and scales every folded weight by powers of
+    (1 - alpha) / 0.8."""
+    import c2g
+
+    d = str(tmp_path)
+    c2g.rmat_write(d, 12, 8, 5, 1, 1000)
+    names = ("vlist", "elist", "wlist", "hvlist", "helist", "hwlist")
+
+    def snap():
+        return {n: open(os.path.join(d, "ppr", n + ".bin"), "rb").read() for n in names}
+
+    c2g.prune_ppr(d)
+    ref = snap()
+    c2g.prune_ppr(d, alpha=0.2)
+    assert snap() == ref
+    c2g.prune_ppr(d, alpha=0.15)
+    alt = snap()
+    for n in ("vlist", "elist", "hvlist", "helist"):
+        assert alt[n] == ref[n]
+    for n in ("wlist", "hwlist"):
+        a = np.frombuffer(alt[n], dtype=np.float32).astype(np.float64)
+        r = np.frombuffer(ref[n], dtype=np.float32).astype(np.float64)
+        changed = a != r
+        assert changed.any()  # folded edges exist and carry the new factor
+        ratio = a[changed] / r[changed]
+        assert ratio.min() >= 1.0 - 1e-6 and ratio.max() <= (0.85 / 0.8) ** 8 + 1e-6
+    with pytest.raises(c2g.C2GError):
+        c2g.prune_ppr(d, alpha=1.5)
