@@ -357,6 +357,15 @@ class Graph:
                                      _ptr(pi), _ptr(lam), ctypes.byref(loss), 0, ctypes.byref(st)))
         return grad, pi, lam, loss.value, st
 
+    def adsorption_device(self, seeds, p_inj_ptr, p_cont_ptr, p_abnd_ptr, Y_ptr, iterations=30):
+        """Label propagation with p_* and Y[V,16] in device memory (pointers); returns stats."""
+        sv = np.ascontiguousarray(seeds, dtype=np.int32)
+        st = Stats()
+        _check(lib().c2g_adsorption(self._h, len(sv), _ptr(sv), ctypes.c_void_p(p_inj_ptr), ctypes.c_void_p(p_cont_ptr),
+                                    ctypes.c_void_p(p_abnd_ptr), iterations, ctypes.c_void_p(Y_ptr), 1,
+                                    ctypes.byref(st)))
+        return st
+
     def adsorption(self, seeds, p_inj, p_cont, p_abnd, iterations=30):
         """Label propagation: (Y[V,16] float32, stats)."""
         sv = np.ascontiguousarray(seeds, dtype=np.int32)
