@@ -41,37 +41,60 @@ __global__ void scatter_in_kernel(const int* __restrict__ row, const int2* __res
 }
 
 // grad[e] = c * pi[u] * lambda[col[e]] for every forward edge e = (u -> col[e]).  Warps
-// take 256-edge tiles; each lane finds its edge's row by walking forward from the
-// tile's first row (found by a binary search over the row pointer).
-__global__ void adjoint_grad_kernel(const int* __restrict__ row, const int2* __restrict__ adj, int V, long long E,
-                                    const float* __restrict__ pi, const float* __restrict__ lam, float c,
-                                    float* __restrict__ grad) {
+// take tiles of 2^kPullTileLog edges; a tile's first owner comes from the forward tile
+// markers (one load), the next 32 owners' row bounds and pi values one per lane, and each
+// edge's owner from a shuffle search.  Edges are read 32 at a time, kGradUnroll batches in
+// flight, so the lambda gathers of a warp overlap.
+constexpr int kGradUnroll = 4;
+
+__global__ void adjoint_grad_kernel(const int* __restrict__ row, const int2* __restrict__ adj,
+                                    const int* __restrict__ mark, int V, unsigned E, const float* __restrict__ pi,
+                                    const float* __restrict__ lam, float c, float* __restrict__ grad,
+                                    int* __restrict__ flags) {
     const int lane = threadIdx.x & 31;
-    const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
-    const long long ntiles = (E + 255) >> 8;
-    for (long long t = warp; t < ntiles; t += nwarps) {
-        const long long e0 = t << 8;
-        // owner of e0: the largest u with row[u] <= e0 (binary search by one lane)
-        int lo = 0;
-        if (lane == 0) {
-            int hi = V;  // row[lo] <= e0 < row[hi] (row[V] = E > e0)
-            while (hi - lo > 1) {
-                const int mid = lo + ((hi - lo) >> 1);
-                if (row[mid] <= e0)
-                    lo = mid;
-                else
-                    hi = mid;
+    const unsigned warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const unsigned nwarps = (gridDim.x * blockDim.x) >> 5;
+    const unsigned tw = 1u << kPullTileLog;
+    const unsigned ntiles = (E + tw - 1) >> kPullTileLog;
+    for (unsigned t = warp; t < ntiles; t += nwarps) {
+        unsigned e0 = t << kPullTileLog;
+        const unsigned e1 = min(e0 + tw, E);
+        unsigned o = (unsigned)__ldg(mark + t);
+        while (e0 < e1) {
+            const unsigned j = o + (unsigned)lane;
+            unsigned base = 0x7fffffffu, endv = 0xffffffffu;
+            float pj = 0.f;
+            if (j < (unsigned)V) {
+                base = (unsigned)__ldg(row + j);
+                endv = (unsigned)__ldg(row + j + 1);
+                pj = __ldg(pi + j);
             }
-        }
-        lo = __shfl_sync(kFull, lo, 0);
-        int u = lo;
-        for (int k = 0; k < 8; ++k) {
-            const long long e = e0 + lane + 32 * k;
-            if (e >= E) break;
-            while (row[u + 1] <= e) ++u;
-            const int2 ew = adj[e];
-            grad[e] = c * pi[u] * lam[ew.x];
+            if (o >= (unsigned)V || (unsigned)__shfl_sync(kFull, (int)base, 0) > e0) {
+                if (lane == 0) atomicOr(flags, C2G_FLAG_BOUNDS);
+                break;
+            }
+            const unsigned seg_end = min(e1, (unsigned)__shfl_sync(kFull, endv, 31));
+            if (seg_end <= e0) {  // 32 owners without edges here (o grows to V at most)
+                o += 32;
+                continue;
+            }
+            for (unsigned eb = e0; eb < seg_end; eb += 32u * kGradUnroll) {
+                int2 ew[kGradUnroll];
+                float pk[kGradUnroll];
+#pragma unroll
+                for (int u = 0; u < kGradUnroll; ++u) {
+                    const unsigned e = eb + (unsigned)lane + 32u * u;
+                    pk[u] = __shfl_sync(kFull, pj, owner_lane(base, e));
+                    ew[u] = e < seg_end ? __ldg(adj + e) : make_int2(0, 0);
+                }
+#pragma unroll
+                for (int u = 0; u < kGradUnroll; ++u) {
+                    const unsigned e = eb + (unsigned)lane + 32u * u;
+                    if (e < seg_end) grad[e] = c * pk[u] * __ldg(lam + ew[u].x);
+                }
+            }
+            e0 = seg_end;
+            o += 32;
         }
     }
 }
@@ -217,8 +240,10 @@ extern "C" int c2g_ppr_adjoint(c2g_graph* g, int32_t source, const c2g_ppr_param
     }
     // gradient pass
     cudaEventRecord(g->ev0, g->stream);
-    if (E) adjoint_grad_kernel<<<g->num_sms * 8, 256, 0, g->stream>>>(g->row, g->adj_f, g->V, (long long)E, pi, lam,
-                                                                         1.0f - params->alpha, dgrad);
+    if (E)
+        adjoint_grad_kernel<<<g->num_sms * 8, 256, 0, g->stream>>>(g->row, g->adj_f, g->mark_f, g->V, (unsigned)E, pi,
+                                                                   lam, 1.0f - params->alpha, dgrad,
+                                                                   &g->ppr.ctl->flags);
     cudaEventRecord(g->ev1, g->stream);
     e = cudaGetLastError();
     if (e == cudaSuccess && !on_device)
@@ -231,10 +256,14 @@ extern "C" int c2g_ppr_adjoint(c2g_graph* g, int32_t source, const c2g_ppr_param
     if (e == cudaSuccess && lambda_out)
         e = cudaMemcpyAsync(lambda_out, lam, sizeof(float) * V,
                             on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, g->stream);
+    int gflags = 0;  // the gradient pass's bounds checks report into the push's control block
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(&gflags, &g->ppr.ctl->flags, sizeof(int), cudaMemcpyDeviceToHost, g->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
     if (e == cudaSuccess) cudaEventElapsedTime(&ms_g, g->ev0, g->ev1);
     cleanup();
     C2G_CUDA(e);
+    if (gflags & C2G_FLAG_BOUNDS) return fail(C2G_ERR_OVERFLOW, "adjoint gradient pass: device index check failed");
     if (loss) {
         double L = 0.0;
         for (int32_t t = 0; t < n_targets; ++t) L += (double)hpi[targets[t]];

@@ -56,27 +56,36 @@ __global__ void ads_edge_pass(const int* __restrict__ row_r, const int2* __restr
         bool whole = row_r[v] >= c0;
         float s = 0.f;
         for (long long b = c0; b < c1; b += 16) {
-            // 16 in-edges loaded one per lane, then consumed in order
+            // 16 in-edges loaded one per lane; their 16 label rows are gathered together
+            // (all loads in flight before the first is used), then consumed in edge order
             const long long my = b + l;
             int2 ew = make_int2(0, 0);
             if (my < c1) ew = __ldg(adj_r + my);
             const int n = (int)min(16ll, c1 - b);
-            for (int k = 0; k < n; ++k) {
-                const long long e = b + k;
-                while (e >= vend) {  // owner changes: write the finished owner
-                    const size_t o = (size_t)v * kAdsL + l;
-                    if (whole)
-                        acc[o] = s;
-                    else
-                        atomicAdd(acc + o, s);
-                    s = 0.f;
-                    ++v;
-                    whole = true;  // rows starting inside the chunk
-                    vend = row_r[v + 1];
-                }
+            float yv[16];
+#pragma unroll
+            for (int k = 0; k < 16; ++k) {
                 const int u = __shfl_sync(hmask, ew.x, (lane & 16) + k);
+                yv[k] = k < n ? __ldg(Y + (size_t)u * kAdsL + l) : 0.f;
+            }
+#pragma unroll
+            for (int k = 0; k < 16; ++k) {
+                if (k < n) {
+                    const long long e = b + k;
+                    while (e >= vend) {  // owner changes: write the finished owner
+                        const size_t o = (size_t)v * kAdsL + l;
+                        if (whole)
+                            acc[o] = s;
+                        else
+                            atomicAdd(acc + o, s);
+                        s = 0.f;
+                        ++v;
+                        whole = true;  // rows starting inside the chunk
+                        vend = row_r[v + 1];
+                    }
+                }
                 const float w = __int_as_float(__shfl_sync(hmask, ew.y, (lane & 16) + k));
-                s = fmaf(w, __ldg(Y + (size_t)u * kAdsL + l), s);
+                if (k < n) s = fmaf(w, yv[k], s);
             }
         }
         const size_t o = (size_t)v * kAdsL + l;
