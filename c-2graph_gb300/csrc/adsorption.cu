@@ -10,10 +10,11 @@
 // "none" label, which is not stored.
 //
 // One iteration is a pull over the reverse CSR: the in-edges of all vertices form one
-// range [0, E) cut into 512-edge chunks; a half-warp (16 lanes = 16 labels) walks a
-// chunk, accumulating per-owner sums in registers, and writes each owner's sum with a
-// plain store when the owner's in-edges lie inside the chunk, otherwise with atomicAdd
-// (only owners straddling a chunk boundary).  A vertex pass then applies p_inj / p_cont.
+// range [0, E) cut into tiles of 2^kPullTileLog edges; a group of 4 lanes (each holding 4
+// of the 16 labels as a float4) walks a tile from its marker's owner, accumulating
+// per-owner sums in registers, and writes each owner's row with a plain store when the
+// owner's in-edges lie inside the tile, otherwise with atomicAdd (only owners straddling
+// a tile boundary).  8 label rows are gathered before they are used.  A vertex pass then applies p_inj / p_cont.
 // Per iteration: (8 + 64) bytes per edge (in-edge record + source label row) and
 // 64 + 64 + 12 bytes per vertex.  The iteration sequence is captured once per handle
 // (and iteration count) into a CUDA graph and replayed; its buffers stay with the handle.
@@ -26,73 +27,72 @@
 namespace c2g {
 
 constexpr int kAdsL = 16;          // labels per query
-constexpr int kAdsChunkLog = 9;    // 512 in-edges per half-warp chunk
 
-__global__ void ads_edge_pass(const int* __restrict__ row_r, const int2* __restrict__ adj_r, int V, long long E,
-                              const float* __restrict__ Y, float* __restrict__ acc) {
+__global__ void ads_edge_pass(const int* __restrict__ row_r, const int2* __restrict__ adj_r,
+                              const int* __restrict__ mark_r, int V, unsigned E, const float4* __restrict__ Y,
+                              float* __restrict__ acc) {
     const int lane = threadIdx.x & 31;
-    const int l = lane & 15;
-    const unsigned hmask = (lane < 16) ? 0x0000ffffu : 0xffff0000u;
-    const long long half = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 4;
-    const long long nhalf = ((long long)gridDim.x * blockDim.x) >> 4;
-    const long long nchunks = (E + (1 << kAdsChunkLog) - 1) >> kAdsChunkLog;
-    for (long long ch = half; ch < nchunks; ch += nhalf) {
-        const long long c0 = ch << kAdsChunkLog;
-        const long long c1 = min(c0 + (1ll << kAdsChunkLog), E);
-        // owner of c0 (largest v with row_r[v] <= c0), searched by lane l == 0
-        int v = 0;
-        if (l == 0) {
-            int hi = V;
-            while (hi - v > 1) {
-                const int mid = v + ((hi - v) >> 1);
-                if (row_r[mid] <= c0)
-                    v = mid;
-                else
-                    hi = mid;
-            }
-        }
-        v = __shfl_sync(hmask, v, lane & 16);
-        long long vend = row_r[v + 1];
-        bool whole = row_r[v] >= c0;
-        float s = 0.f;
-        for (long long b = c0; b < c1; b += 16) {
-            // 16 in-edges loaded one per lane; their 16 label rows are gathered together
-            // (all loads in flight before the first is used), then consumed in edge order
-            const long long my = b + l;
-            int2 ew = make_int2(0, 0);
-            if (my < c1) ew = __ldg(adj_r + my);
-            const int n = (int)min(16ll, c1 - b);
-            float yv[16];
+    const int part = lane & 3;                   // labels 4*part .. 4*part+3 of every row
+    const int g0 = lane & ~3;                    // first lane of this 4-lane group
+    const unsigned gmask = 0xfu << g0;           // the group's lanes (groups diverge)
+    const unsigned ngroups = (gridDim.x * blockDim.x) >> 2;
+    const unsigned tw = 1u << kPullTileLog;
+    const unsigned ntiles = (E + tw - 1) >> kPullTileLog;
+    for (unsigned t = (blockIdx.x * blockDim.x + threadIdx.x) >> 2; t < ntiles; t += ngroups) {
+        const unsigned e0 = t << kPullTileLog;
+        const unsigned e1 = min(e0 + tw, E);
+        int v = __ldg(mark_r + t);               // owner of in-edge e0
+        unsigned vend = (unsigned)__ldg(row_r + v + 1);
+        bool whole = (unsigned)__ldg(row_r + v) >= e0;
+        float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
+        for (unsigned b = e0; b < e1; b += 8) {
+            // 8 in-edges, 2 per lane; their label rows gathered together, then consumed in order
+            int2 ea = make_int2(0, 0), eb = make_int2(0, 0);
+            if (b + part < e1) ea = __ldg(adj_r + b + part);
+            if (b + 4 + part < e1) eb = __ldg(adj_r + b + 4 + part);
+            float4 y[8];
+            float wt[8];
 #pragma unroll
-            for (int k = 0; k < 16; ++k) {
-                const int u = __shfl_sync(hmask, ew.x, (lane & 16) + k);
-                yv[k] = k < n ? __ldg(Y + (size_t)u * kAdsL + l) : 0.f;
+            for (int k = 0; k < 8; ++k) {
+                const int2 ek = k < 4 ? ea : eb;
+                const int u = __shfl_sync(gmask, ek.x, g0 + (k & 3));
+                wt[k] = __int_as_float(__shfl_sync(gmask, ek.y, g0 + (k & 3)));
+                y[k] = b + k < e1 ? __ldg(Y + (size_t)u * (kAdsL / 4) + part) : make_float4(0.f, 0.f, 0.f, 0.f);
             }
 #pragma unroll
-            for (int k = 0; k < 16; ++k) {
-                if (k < n) {
-                    const long long e = b + k;
-                    while (e >= vend) {  // owner changes: write the finished owner
-                        const size_t o = (size_t)v * kAdsL + l;
-                        if (whole)
-                            acc[o] = s;
-                        else
-                            atomicAdd(acc + o, s);
-                        s = 0.f;
-                        ++v;
-                        whole = true;  // rows starting inside the chunk
-                        vend = row_r[v + 1];
+            for (int k = 0; k < 8; ++k) {
+                const unsigned e = b + k;
+                if (e >= e1) break;  // group-uniform
+                while (e >= vend) {  // owner changes: write the finished owner's row part
+                    float* o = acc + (size_t)v * kAdsL + 4 * part;
+                    if (whole) {
+                        *reinterpret_cast<float4*>(o) = s;
+                    } else {
+                        atomicAdd(o, s.x);
+                        atomicAdd(o + 1, s.y);
+                        atomicAdd(o + 2, s.z);
+                        atomicAdd(o + 3, s.w);
                     }
+                    s = make_float4(0.f, 0.f, 0.f, 0.f);
+                    ++v;
+                    whole = true;  // rows starting inside the tile
+                    vend = (unsigned)__ldg(row_r + v + 1);
                 }
-                const float w = __int_as_float(__shfl_sync(hmask, ew.y, (lane & 16) + k));
-                if (k < n) s = fmaf(w, yv[k], s);
+                s.x = fmaf(wt[k], y[k].x, s.x);
+                s.y = fmaf(wt[k], y[k].y, s.y);
+                s.z = fmaf(wt[k], y[k].z, s.z);
+                s.w = fmaf(wt[k], y[k].w, s.w);
             }
         }
-        const size_t o = (size_t)v * kAdsL + l;
-        if (whole && vend <= c1)
-            acc[o] = s;
-        else
-            atomicAdd(acc + o, s);
+        float* o = acc + (size_t)v * kAdsL + 4 * part;
+        if (whole && vend <= e1) {
+            *reinterpret_cast<float4*>(o) = s;
+        } else {
+            atomicAdd(o, s.x);
+            atomicAdd(o + 1, s.y);
+            atomicAdd(o + 2, s.z);
+            atomicAdd(o + 3, s.w);
+        }
     }
 }
 
@@ -182,7 +182,9 @@ static int ads_capture(c2g_graph* g, AdsWork* w, int iterations) {
         const int eb = g->num_sms * 8, vb = g->num_sms * 8;
         ads_init<<<vb, 256, 0, g->stream>>>(g->V, w->mask, w->acc, w->Y);
         for (int it = 0; it < iterations; ++it) {
-            if (g->E) ads_edge_pass<<<eb, 256, 0, g->stream>>>(g->row_r, g->adj_r, g->V, (long long)g->E, w->Y, w->acc);
+            if (g->E)
+                ads_edge_pass<<<eb, 256, 0, g->stream>>>(g->row_r, g->adj_r, g->mark_r, g->V, (unsigned)g->E,
+                                                          reinterpret_cast<const float4*>(w->Y), w->acc);
             ads_vertex_pass<<<vb, 256, 0, g->stream>>>(g->V, w->pi, w->pc, w->mask, w->acc, w->Y);
         }
         e = cudaStreamEndCapture(g->stream, &graph);

@@ -97,14 +97,6 @@ constexpr int kBatchUnroll = 4;  // relaxation items in flight per lane
 // sources at scale 22), 1 x 512 with 8-12 items (220 ms) and 6 x 256 (192 ms).
 constexpr int kSsspBatchThreads = 384;
 
-// Next tile of a round for this warp from the round's tile counter (lane 0 takes it, the
-// warp shares it).  Tiles differ in cost (active queries per step), so a dynamic queue
-// balances the warps better than a fixed round-robin.
-__device__ __forceinline__ unsigned next_tile(unsigned* ctr, int lane) {
-    unsigned t = 0;
-    if (lane == 0) t = atomicAdd(ctr, 1u);
-    return (unsigned)__shfl_sync(kFull, (int)t, 0);
-}
 
 // Lane compaction of one owner run: the run's work is the items (edge ei, active-query
 // slot j) for ei in [0, len) and j in [0, cnt), numbered i = ei * cnt + j; lane l takes

@@ -321,6 +321,15 @@ struct StageSmemD {
     int v1[16][kStageCap];
 };
 
+// Next tile of a round for this warp from the round's tile counter (lane 0 takes it, the
+// warp shares it).  Where tiles differ in cost, or are few, a dynamic queue balances the
+// warps better than a fixed round-robin.
+__device__ __forceinline__ unsigned next_tile(unsigned* ctr, int lane) {
+    unsigned t = 0;
+    if (lane == 0) t = atomicAdd(ctr, 1u);
+    return (unsigned)__shfl_sync(kFull, (int)t, 0);
+}
+
 // Warp-cooperative walk over the edges of a frontier, in tiles of 2^log_tile edges
 // assigned to warps round-robin (tile t goes to warp t mod nwarps, no shared counter).
 // For each group of 32*U edges every lane gets U edges (stride 32, so the warp reads
@@ -333,7 +342,8 @@ template <int U, typename OwnerVal, typename Body>
 __device__ __forceinline__ void walk_frontier_edges(const int2* __restrict__ q, const int* __restrict__ mark,
                                                     const int* __restrict__ row, unsigned F, unsigned T,
                                                     int log_tile, unsigned mark_cap, unsigned qcap, unsigned E,
-                                                    int* flags, OwnerVal owner_val, Body body) {
+                                                    int* flags, OwnerVal owner_val, Body body,
+                                                    unsigned* tctr = nullptr) {
     using VT = decltype(owner_val(0, 0u));  // int or double
     const int lane = threadIdx.x & 31;
     const unsigned gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -344,7 +354,11 @@ __device__ __forceinline__ void walk_frontier_edges(const int2* __restrict__ q, 
         if (lane == 0) atomicOr(flags, C2G_FLAG_BOUNDS);
         return;
     }
-    for (unsigned t = gwarp; t < ntiles; t += nwarps) {
+    // tctr: a round's tile counter (zero at the round's start) for a dynamic queue of
+    // tiles, the next one fetched while the current one runs; nullptr: round-robin.
+    unsigned tn = tctr ? next_tile(tctr, lane) : gwarp;
+    for (unsigned t = tn; t < ntiles; t = tn) {
+        tn = tctr ? next_tile(tctr, lane) : t + nwarps;
         unsigned e0 = t << log_tile;
         const unsigned e1 = min(e0 + tw, T);
         unsigned o = (unsigned)ldcg(mark + t);

@@ -56,7 +56,10 @@ def test_noalloc_matches_regular_entry_point(gpu_available, graph16):
             assert rc == 0, L.c2g_last_error()
             ref, rst = g.sssp(s)
             assert np.array_equal(dist.cpu().numpy(), ref), s
-            assert st.status_flags == 0 and st.iterations == rst.iterations
+            # round counts are not compared: they depend on the schedule (an improvement
+            # seen early in a round can save a round), and the two entry points run
+            # different kernels
+            assert st.status_flags == 0 and rst.status_flags == 0 and st.iterations > 0
 
 
 def test_noalloc_rejects_sizes_beyond_scratch(gpu_available):
