@@ -642,7 +642,7 @@ __global__ void __launch_bounds__(kPprBatchThreads, 3) ppr_batch_persistent(cons
     const double one_m_a = 1.0 - (double)p.alpha;
     unsigned long long tph = globaltimer_ns();
 
-    // Init: pr = res = 0 (msg and tmask are zero between launches).
+    // Init: pr = res = 0 (msg and tmask are zero between launches: phase B clears them).
     {
         const size_t n4 = ((size_t)p.V * (size_t)p.Q) >> 2;
         float4* a4 = reinterpret_cast<float4*>(p.pr);

@@ -127,41 +127,6 @@ struct FrontierOut {
     int* flags;
 };
 
-// Warp-collective: every lane calls it; lanes with `want` append (v, deg, val).
-// deg must be > 0 for appended entries.
-__device__ __forceinline__ void frontier_push(const FrontierOut& out, bool want, int v, int deg, float val) {
-    const int lane = threadIdx.x & 31;
-    const unsigned m = __ballot_sync(kFull, want);
-    if (m == 0) return;
-    const int d = want ? deg : 0;
-    int incl = d;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const int t = __shfl_up_sync(kFull, incl, o);
-        if (lane >= o) incl += t;
-    }
-    const unsigned total = (unsigned)__shfl_sync(kFull, incl, 31);
-    const int leader = __ffs(m) - 1;
-    unsigned long long old = 0;
-    if (lane == leader)
-        old = atomicAdd(out.ctr, ((unsigned long long)__popc(m) << 32) | (unsigned long long)total);
-    old = __shfl_sync(kFull, old, leader);
-    if (want) {
-        const unsigned slot = (unsigned)(old >> 32) + (unsigned)__popc(m & ((1u << lane) - 1u));
-        const unsigned base = (unsigned)old + (unsigned)(incl - d);
-        if (slot < out.cap) {
-            out.q[slot] = make_int2(v, (int)base);
-            if (out.val) out.val[slot] = val;
-            const unsigned tile = 1u << out.log_tile;
-            unsigned t0 = (base + tile - 1) >> out.log_tile;
-            const unsigned t1 = (base + (unsigned)deg - 1) >> out.log_tile;
-            for (unsigned t = t0; t <= t1 && t < out.mark_cap; ++t) out.mark[t] = (int)slot;
-        } else {
-            atomicOr(out.flags, C2G_FLAG_QUEUE_OVERFLOW);
-        }
-    }
-}
-
 // Warp-collective count-only append of vertex ids.
 __device__ __forceinline__ void list_push(int* list, unsigned* ctr, unsigned cap, int* flags, bool want, int v) {
     const int lane = threadIdx.x & 31;
