@@ -106,6 +106,7 @@ SIGNATURES = {
     "c2g_ppr": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.POINTER(PprParams), _P, _P, ctypes.c_int,
                                ctypes.POINTER(Stats)]),
     "c2g_ppr_set_config": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int32]),
+    "c2g_ppr_batch_set_pull": (ctypes.c_int, [_P, ctypes.c_float]),
     "c2g_graph_set_watchdog": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int32]),
     "c2g_graph_last_phases": (ctypes.c_int, [_P, _P]),
     "c2g_ppr_default_params": (ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(PprParams)]),
@@ -298,6 +299,11 @@ class Graph:
 
     def ppr_config(self, pull_div=0, dense_div=16):
         _check(lib().c2g_ppr_set_config(self._h, pull_div, dense_div))
+
+    def ppr_batch_pull(self, ratio=8.0):
+        """Batched rounds with more than ratio * E pushes pull over the reverse CSR
+        (ratio < 0: push only; 0: every round)."""
+        _check(lib().c2g_ppr_batch_set_pull(self._h, float(ratio)))
 
     def ppr_params(self, adsorption=False, **kw):
         p = PprParams()

@@ -135,6 +135,7 @@ void adjoint_free(c2g_graph* g) {
     void* ptrs[] = {g->row_r, g->adj_r, g->mark_r, g->mark_f};
     for (void* p : ptrs)
         if (p) cudaFree(p);
+    g->wstat_valid = false;
     g->row_r = nullptr;
     g->adj_r = nullptr;
     g->mark_r = nullptr;

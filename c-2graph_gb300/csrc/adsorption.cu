@@ -14,7 +14,7 @@
 // of the 16 labels as a float4) walks a tile from its marker's owner, accumulating
 // per-owner sums in registers, and writes each owner's row with a plain store when the
 // owner's in-edges lie inside the tile, otherwise with atomicAdd (only owners straddling
-// a tile boundary).  8 label rows are gathered before they are used.  A vertex pass then applies p_inj / p_cont.
+// a tile boundary).  kAdsBatch label rows are gathered before they are used.  A vertex pass then applies p_inj / p_cont.
 // Per iteration: (8 + 64) bytes per edge (in-edge record + source label row) and
 // 64 + 64 + 12 bytes per vertex.  The iteration sequence is captured once per handle
 // (and iteration count) into a CUDA graph and replayed; its buffers stay with the handle.
@@ -28,7 +28,11 @@ namespace c2g {
 
 constexpr int kAdsL = 16;          // labels per query
 
-__global__ void ads_edge_pass(const int* __restrict__ row_r, const int2* __restrict__ adj_r,
+constexpr int kAdsBatch = 8;      // in-edges whose label rows a group gathers at once
+constexpr int kAdsMinBlocks = 3;  // launch bounds: resident 256-thread blocks per SM
+
+__global__ void __launch_bounds__(256, kAdsMinBlocks) ads_edge_pass(const int* __restrict__ row_r,
+                                                                    const int2* __restrict__ adj_r,
                               const int* __restrict__ mark_r, int V, unsigned E, const float4* __restrict__ Y,
                               float* __restrict__ acc) {
     const int lane = threadIdx.x & 31;
@@ -45,22 +49,23 @@ __global__ void ads_edge_pass(const int* __restrict__ row_r, const int2* __restr
         unsigned vend = (unsigned)__ldg(row_r + v + 1);
         bool whole = (unsigned)__ldg(row_r + v) >= e0;
         float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
-        for (unsigned b = e0; b < e1; b += 8) {
-            // 8 in-edges, 2 per lane; their label rows gathered together, then consumed in order
+        for (unsigned b = e0; b < e1; b += kAdsBatch) {
+            // kAdsBatch in-edges, kAdsBatch / 4 per lane; their label rows gathered together,
+            // then consumed in order
             int2 ea = make_int2(0, 0), eb = make_int2(0, 0);
             if (b + part < e1) ea = __ldg(adj_r + b + part);
-            if (b + 4 + part < e1) eb = __ldg(adj_r + b + 4 + part);
-            float4 y[8];
-            float wt[8];
+            if (kAdsBatch > 4 && b + 4 + part < e1) eb = __ldg(adj_r + b + 4 + part);
+            float4 y[kAdsBatch];
+            float wt[kAdsBatch];
 #pragma unroll
-            for (int k = 0; k < 8; ++k) {
+            for (int k = 0; k < kAdsBatch; ++k) {
                 const int2 ek = k < 4 ? ea : eb;
                 const int u = __shfl_sync(gmask, ek.x, g0 + (k & 3));
                 wt[k] = __int_as_float(__shfl_sync(gmask, ek.y, g0 + (k & 3)));
                 y[k] = b + k < e1 ? __ldg(Y + (size_t)u * (kAdsL / 4) + part) : make_float4(0.f, 0.f, 0.f, 0.f);
             }
 #pragma unroll
-            for (int k = 0; k < 8; ++k) {
+            for (int k = 0; k < kAdsBatch; ++k) {
                 const unsigned e = b + k;
                 if (e >= e1) break;  // group-uniform
                 while (e >= vend) {  // owner changes: write the finished owner's row part
@@ -195,8 +200,6 @@ static int ads_capture(c2g_graph* g, AdsWork* w, int iterations) {
     w->iterations = iterations;
     return C2G_OK;
 }
-
-int build_reverse_graph(c2g_graph* g);
 
 }  // namespace c2g
 

@@ -227,6 +227,8 @@ int graph_view(c2g_graph* base, c2g_graph** out) {
     g->h_hw = base->h_hw;
     g->sssp_cfg = base->sssp_cfg;
     g->ppr_cfg = base->ppr_cfg;
+    g->wstat_valid = base->wstat_valid;
+    g->wstat_wmax_bits = base->wstat_wmax_bits;
     g->borrowed = true;
     *out = g;
     return C2G_OK;
@@ -414,6 +416,14 @@ int c2g_ppr_set_config(c2g_graph* g, int32_t pull_div, int32_t dense_div) {
     std::lock_guard<std::mutex> lk(g->mu);
     g->ppr_cfg.pull_div = pull_div;
     g->ppr_cfg.dense_div = dense_div;
+    return C2G_OK;
+}
+
+int c2g_ppr_batch_set_pull(c2g_graph* g, float ratio) {
+    if (!g) return fail(C2G_ERR_ARG, "graph is NULL");
+    if (ratio != ratio) return fail(C2G_ERR_ARG, "ratio is NaN");
+    std::lock_guard<std::mutex> lk(g->mu);
+    g->ppr_cfg.batch_pull_ratio = ratio;
     return C2G_OK;
 }
 

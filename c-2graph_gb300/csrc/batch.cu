@@ -18,6 +18,9 @@
 //     edge-base prefix and tile markers), then the expansion.
 // Results are the same int32 fixed points as one c2g_sssp call per source.
 #include <climits>
+#include <cmath>
+#include <cstring>
+#include <algorithm>
 #include <vector>
 
 #include "device_common.cuh"
@@ -479,10 +482,12 @@ int sssp_batch_launch(c2g_graph* g, int32_t nq, const int32_t* sources, const st
 //
 // Same BSP semantics per query as c2g_ppr (src/ppr/purn/Main.cu:149-428): pop r, push
 // (1-alpha)*r*w into msg, then res += msg; if res > rmax: pr += alpha*res and activate.
-// State is vertex-major [V][Q]: pr float; res, msg and rq (the residual being pushed)
-// FP64.  A push marks the target's (vertex, word) touched mask with red.or; phase B
-// sweeps the touched masks, applies the messages and activates, building the frontier
-// entries (vertex, word) with the activated lanes as their mask.
+// State is vertex-major [V][Q]: pr float; res, msg and rq (the residual being pushed,
+// times 1-alpha) FP64.  A push round marks the target's (vertex, word) touched mask with
+// red.or; phase B sweeps the touched masks, applies the messages and activates, building
+// the frontier entries (vertex, word) with the activated lanes as their mask.  A round
+// with many pushes runs as a pull over the reverse CSR instead (pbatch_pull); both shapes
+// produce the same rounds.
 namespace c2g {
 
 struct PprBatchParams {
@@ -493,8 +498,10 @@ struct PprBatchParams {
     int logW, Q, nq;
     float* pr;        // [V][Q]
     double* res;      // [V][Q] FP64 residuals (see ppr.cu: threshold decisions)
-    double* msg;      // [V][Q], zero between launches
-    double* rq;       // [V][Q] residual being pushed
+    double* msg;      // [V][Q], zero between launches (pull rounds: 64-bit integer parts)
+    double* rq[2];    // [V][Q] (1-alpha) * residual being pushed, by frontier buffer
+    float2* rqf[2];   // the same as a float pair hi + lo (pull rounds)
+    unsigned* amask[2];  // [V][W] lanes activated with out-edges, by frontier buffer (pull lookup)
     unsigned* tmask;  // [V][W] touched lanes this round, zero between rounds
     int2* q[2];       // frontier entries (v*W + w, edge base)
     unsigned* qmask[2];
@@ -511,6 +518,13 @@ struct PprBatchParams {
     unsigned qcap, mark_cap;
     unsigned long long barrier_ns;
     long long* counters;  // [2] pushes (query, edge), edge-word steps
+    // pull rounds: reverse CSR (source, weight bits) with tile owners; a round pulls when
+    // its pushes exceed pull_min
+    const int* row_r;
+    const int2* adj_r;
+    const int* mark_r;
+    unsigned ntiles_r;
+    unsigned long long pull_min;
 };
 
 __device__ __forceinline__ FrontierOut pbatch_out(const PprBatchParams& p, int buf, int slot) {
@@ -532,31 +546,86 @@ __device__ __forceinline__ FrontierOut pbatch_out(const PprBatchParams& p, int b
 constexpr int kPprBatchThreads = 384;
 constexpr int kPprBatchUnroll = 3;  // push items in flight per lane
 
+// Apply of one (vertex, word) to the lanes that received messages: res += m; a lane whose
+// residual exceeds rmax adds alpha * res to pr and activates.  An activated lane with
+// out-edges stores (1-alpha) * res as the residual it pushes next round (in rq[ob]) and
+// zeroes res; one without out-edges keeps res until the next round pops it.  The word's
+// activated lanes go to the next frontier (and to amask[ob], the pull rounds' lookup),
+// or to the dangling list.  force = true: the seeded first hop (activate every touched
+// lane, no messages).  psum (lane 0) accumulates the next round's pushes.
+__device__ __forceinline__ void pbatch_apply_word(const PprBatchParams& p, bool force, int ob, int vw, int dg,
+                                                  size_t off, bool mine, double r, double m, float pv,
+                                                  unsigned long long rmax_bits, WarpStage& fst, const FrontierOut& out,
+                                                  unsigned* dctr, unsigned long long& psum, int lane) {
+    bool act = false;
+    if (mine) {
+        double rr = r;
+        if (!force) rr += m;
+        // rr and rmax are non-negative: compare their bit patterns
+        if (force || c2g_dbits(rr) > rmax_bits) {
+            if (!force) p.pr[off] = pv + (float)((double)p.alpha * rr);
+            act = true;
+            if (dg > 0) {
+                const double q = (1.0 - (double)p.alpha) * rr;  // (1-alpha)*r_u (src/ppr/purn/Main.cu:288)
+                p.rq[ob][off] = q;
+                if (c2g_split_ok(q)) {  // float pair for pull rounds (fp64_mul.h)
+                    const c2g_pair hl = c2g_split_pair(q);
+                    p.rqf[ob][off] = make_float2(c2g_bitsf(hl.hi), c2g_bitsf(hl.lo));
+                } else {
+                    const float hi = __double2float_rz(q);
+                    p.rqf[ob][off] = make_float2(hi, __double2float_rz(q - (double)hi));
+                }
+                p.res[off] = 0.0;
+            } else {
+                p.res[off] = rr;  // popped (zeroed) at the top of the next round
+            }
+        } else {
+            p.res[off] = rr;
+        }
+    }
+    const unsigned bits = __ballot_sync(kFull, act);
+    if (bits && lane == 0) {
+        if (dg == 0) {
+            const unsigned slot = atomicAdd(dctr, 1u);
+            if (slot < p.qcap)
+                p.dangle[slot] = make_int2(vw, (int)bits);
+            else
+                atomicOr(&p.ctl->flags, C2G_FLAG_QUEUE_OVERFLOW);
+        } else {
+            p.amask[ob][vw] = bits;
+            psum += (unsigned long long)__popc(bits) * (unsigned long long)dg;
+        }
+    }
+    stage_push(fst, out, lane == 0 && bits != 0u && dg > 0, vw, dg, __int_as_float((int)bits));
+}
+
 // Apply sweep: every (vertex, word) whose touched mask is non-zero applies its messages
-// lane by lane (lane = query) and activates; the mask is cleared.  Pushes mark targets
-// with red.or, so the push never waits on an atomic's return; the sweep reads V * W mask
-// words per round.  A warp takes 32 words at a time (their degrees loaded lane-parallel)
-// and applies up to kApplyGroup touched words at once: all their residual, message and
-// pr loads are issued before any of them is used, so the words' memory latencies
-// overlap instead of adding up.  force = true: the seeded first hop (activate every
-// touched lane, no messages).
+// lane by lane (lane = query) and activates; the mask is cleared.  pulled: the messages
+// are a pull round's sums (see pbatch_pull_flush for their two forms).  Pushes
+// mark targets with red.or, so the push never waits on an atomic's return; the sweep
+// reads V * W mask words per round.  A warp takes 32 words at a time (their degrees
+// loaded lane-parallel) and applies up to kApplyGroup touched words at once: all their
+// residual, message and pr loads are issued before any of them is used, so the words'
+// memory latencies overlap instead of adding up.
 constexpr int kApplyGroup = 3;  // 4 spills at 64 registers
 
-__device__ __forceinline__ unsigned pbatch_sweep(const PprBatchParams& p, bool force, WarpStage& fst,
-                                                 const FrontierOut& out, unsigned* dctr, unsigned gwarp,
-                                                 unsigned nwarps, int lane) {
+__device__ __forceinline__ unsigned pbatch_sweep(const PprBatchParams& p, bool force, bool pulled, int ob,
+                                                 WarpStage& fst, const FrontierOut& out, unsigned* dctr,
+                                                 unsigned long long& psum, unsigned gwarp, unsigned nwarps, int lane) {
     const unsigned nm = (unsigned)p.V << p.logW;
     const unsigned long long rmax_bits = c2g_dbits((double)p.rmax);
-    const double alpha = (double)p.alpha;
     unsigned cnt = 0;
     for (unsigned b = gwarp * 32u; b < nm; b += nwarps * 32u) {
         const unsigned i = b + (unsigned)lane;
         const unsigned tm = i < nm ? ldcg(p.tmask + i) : 0u;
         int dg = 0;
+        bool split = false;  // pulled: the sums of v came in parts (FP64), not as a float pair
         if (tm) {
             p.tmask[i] = 0u;
             const int v = (int)(i >> p.logW);
             dg = __ldg(p.row + v + 1) - __ldg(p.row + v);
+            if (pulled)
+                split = (__ldg(p.row_r + v) >> kPullTileLog) != ((__ldg(p.row_r + v + 1) - 1) >> kPullTileLog);
         }
         unsigned nz = __ballot_sync(kFull, tm != 0u);
         cnt += (unsigned)__popc(tm);  // touched (vertex, query) lanes seen by this lane
@@ -577,7 +646,7 @@ __device__ __forceinline__ unsigned pbatch_sweep(const PprBatchParams& p, bool f
                 const size_t off = ((size_t)(b + (unsigned)k) << 5) + lane;
                 const bool mine = (ln >> lane) & 1u;
                 r[u] = mine ? ldcg(p.res + off) : 0.0;
-                m[u] = (mine && !force) ? ldcg(p.msg + off) : 0.0;
+                m[u] = (mine && !force) ? ldcg(p.msg + off) : 0.0;  // fixed: the integer sum's bits
                 pv[u] = (mine && !force) ? ldcg(p.pr + off) : 0.f;
             }
 #pragma unroll
@@ -588,41 +657,163 @@ __device__ __forceinline__ unsigned pbatch_sweep(const PprBatchParams& p, bool f
                 const int vw = (int)(b + (unsigned)ks[u]);
                 const size_t off = ((size_t)(unsigned)vw << 5) + lane;
                 const bool mine = (ln >> lane) & 1u;
-                bool act = false;
-                if (mine) {
-                    double rr = r[u];
-                    if (!force) {
-                        rr += m[u];
-                        p.msg[off] = 0.0;
-                    }
-                    // rr and rmax are non-negative: compare their bit patterns
-                    if (force || c2g_dbits(rr) > rmax_bits) {
-                        if (!force) p.pr[off] = pv[u] + (float)(alpha * rr);
-                        act = true;
-                        if (dgu > 0) {
-                            p.rq[off] = rr;
-                            p.res[off] = 0.0;
-                        } else {
-                            p.res[off] = rr;  // popped (zeroed) at the top of the next round
-                        }
-                    } else {
-                        p.res[off] = rr;
-                    }
+                if (mine && !force) p.msg[off] = 0.0;
+                double mu = m[u];
+                if (pulled && !__shfl_sync(kFull, (int)split, ks[u])) {  // a float pair hi + lo
+                    const unsigned long long b = c2g_dbits(m[u]);
+                    mu = c2g_float_bits_to_double((unsigned)b) + c2g_float_bits_to_double((unsigned)(b >> 32));
                 }
-                const unsigned bits = __ballot_sync(kFull, act);
-                if (bits && dgu == 0 && lane == 0) {
-                    const unsigned slot = atomicAdd(dctr, 1u);
-                    if (slot < p.qcap)
-                        p.dangle[slot] = make_int2(vw, (int)bits);
-                    else
-                        atomicOr(&p.ctl->flags, C2G_FLAG_QUEUE_OVERFLOW);
-                }
-                stage_push(fst, out, lane == 0 && bits != 0u && dgu > 0, vw, dgu, __int_as_float((int)bits));
+                pbatch_apply_word(p, force, ob, vw, dgu, off, mine, r[u], mu, pv[u], rmax_bits, fst, out, dctr,
+                                  psum, lane);
             }
         }
     }
     stage_flush(fst, out);
     return cnt;
+}
+
+// ---------------------------------------------------------------------------------------
+// Pull round.  In the dense middle of a batch most (vertex, query) pairs are active, and a
+// push does one FP64 read-modify-write per (edge, query) on a message array far larger
+// than L2.  A pull round instead walks the reverse CSR: for each target v and query word,
+// the warp reads v's in-edges (u, w(u,v)), looks up u's active lanes (amask) and gathers
+// the pushed residuals of those lanes (one coalesced 256-byte row segment per edge and
+// word), summing the messages rq * w in registers.  The sums are float pairs hi + lo
+// (about 47 bits of relative precision): the product is hi*w + lo*w with its rounding
+// error recovered by an FMA, and each add is an error-free two-sum whose error joins lo.
+// Relative precision matters here, not absolute: a message sum decides res > rmax at the
+// scale of rmax, far below the largest sums.  Each target's sums are written once to msg
+// with its touched lanes in tmask; only targets whose in-edges cross a tile boundary add
+// their parts atomically (in FP64).  The apply sweep that follows is the push round's.
+// In-edges are cut into tiles of 2^kPullTileLog; warps take (tile, word group) items from
+// the round's queue, kPullWords query words per item.
+constexpr int kPullWords = 4;  // query words per pull item
+constexpr int kPullEdges = 2;  // in-edges whose rq rows are gathered before they are summed
+
+// Owner v's message sums of the item's words (hi + lo per lane) and its touched lanes
+// (tmask).  An owner whose in-edges lie in this tile is the only writer: a plain store of
+// the float pair.  Otherwise its parts are added in FP64 (atomics); the apply tells the
+// two forms apart by whether v's in-edges cross a tile boundary.
+__device__ __forceinline__ void pbatch_pull_flush(const PprBatchParams& p, int v, unsigned w0, bool whole,
+                                                  float (&sh)[kPullWords], float (&sl)[kPullWords], int lane) {
+    const unsigned W = 1u << p.logW;
+#pragma unroll
+    for (int j = 0; j < kPullWords; ++j) {
+        if (w0 + j >= W) break;  // warp-uniform
+        const bool nz = sh[j] != 0.f;
+        const unsigned bits = __ballot_sync(kFull, nz);
+        if (bits) {
+            const size_t vw = ((size_t)(unsigned)v << p.logW) + w0 + j;
+            const size_t off = (vw << 5) + lane;
+            if (whole) {
+                if (nz) reinterpret_cast<float2*>(p.msg)[off] = make_float2(sh[j], sl[j]);
+                if (lane == 0) p.tmask[vw] = bits;
+            } else {
+                if (nz) atomicAdd(p.msg + off, (double)sh[j] + (double)sl[j]);
+                if (lane == 0) atomicOr(p.tmask + vw, bits);
+            }
+        }
+        sh[j] = 0.f;
+        sl[j] = 0.f;
+    }
+}
+
+__device__ __forceinline__ void pbatch_pull(const PprBatchParams& p, int buf, unsigned* qctr, int lane, bool& bad) {
+    const unsigned W = 1u << p.logW;
+    const int lg = p.logW >= 2 ? p.logW - 2 : 0;  // word groups per tile = 2^lg (kPullWords = 4)
+    const unsigned nitems = p.ntiles_r << lg;
+    const unsigned* am = p.amask[buf];
+    const float2* rqb = p.rqf[buf];
+    const unsigned tw = 1u << kPullTileLog;
+    unsigned itn = next_tile(qctr, lane);
+    for (unsigned it = itn; it < nitems; it = itn) {
+        itn = next_tile(qctr, lane);  // the next item, fetched while this one runs
+        const unsigned t = it >> lg;
+        const unsigned w0 = (it & ((1u << lg) - 1u)) * (unsigned)kPullWords;
+        const unsigned e0 = t << kPullTileLog;
+        const unsigned e1 = min(e0 + tw, p.E);
+        int v = __ldg(p.mark_r + t);  // owner of in-edge e0
+        unsigned vend = (unsigned)__ldg(p.row_r + v + 1);
+        bool whole = (unsigned)__ldg(p.row_r + v) >= e0;
+        float sh[kPullWords], sl[kPullWords];
+#pragma unroll
+        for (int j = 0; j < kPullWords; ++j) sh[j] = sl[j] = 0.f;
+        for (unsigned b = e0; b < e1; b += 32u) {
+            // 32 in-edges, one per lane: source, weight and the source's active lanes for
+            // the item's words
+            const unsigned e = b + (unsigned)lane;
+            int src = 0;
+            float wt = 0.f;
+            unsigned mk[kPullWords];
+#pragma unroll
+            for (int j = 0; j < kPullWords; ++j) mk[j] = 0u;
+            if (e < e1) {
+                const int2 ed = __ldg(p.adj_r + e);
+                if ((unsigned)ed.x >= (unsigned)p.V) {
+                    bad = true;
+                } else if (ed.y > 0) {  // positive weights only, as the push
+                    src = ed.x;
+                    wt = __int_as_float(ed.y);
+                    const unsigned* ms = am + ((size_t)(unsigned)src << p.logW) + w0;
+                    if (W >= 4u) {  // four words, 16-byte aligned
+                        const uint4 m4 = ldcg(reinterpret_cast<const uint4*>(ms));
+                        mk[0] = m4.x;
+                        mk[1] = m4.y;
+                        mk[2] = m4.z;
+                        mk[3] = m4.w;
+                    } else {
+#pragma unroll
+                        for (int j = 0; j < kPullWords; ++j)
+                            if ((unsigned)j < W) mk[j] = ldcg(ms + j);
+                    }
+                }
+            }
+            const unsigned n = min(32u, e1 - b);
+            for (unsigned k0 = 0; k0 < n; k0 += kPullEdges) {
+                // gather the pushed residuals of kPullEdges in-edges, then add them in edge order
+                float2 qb[kPullEdges][kPullWords];
+                float wk[kPullEdges];
+#pragma unroll
+                for (int h = 0; h < kPullEdges; ++h) {
+                    const unsigned k = k0 + h < n ? k0 + h : n - 1u;
+                    wk[h] = __shfl_sync(kFull, wt, (int)k);
+                    const int u = __shfl_sync(kFull, src, (int)k);
+#pragma unroll
+                    for (int j = 0; j < kPullWords; ++j) {
+                        const unsigned mj = (unsigned)__shfl_sync(kFull, (int)mk[j], (int)k);
+                        const bool on = k0 + h < n && ((mj >> lane) & 1u);
+                        qb[h][j] = on ? ldcg(rqb + ((size_t)(unsigned)u << (p.logW + 5)) + ((w0 + j) << 5) + lane)
+                                      : make_float2(0.f, 0.f);
+                    }
+                }
+#pragma unroll
+                for (int h = 0; h < kPullEdges; ++h) {
+                    if (k0 + h >= n) break;  // warp-uniform
+                    const unsigned e = b + k0 + h;
+                    while (e >= vend) {  // owner changes: its sums are complete
+                        pbatch_pull_flush(p, v, w0, whole, sh, sl, lane);
+                        ++v;
+                        whole = true;  // owners starting inside the tile
+                        vend = (unsigned)__ldg(p.row_r + v + 1);
+                    }
+#pragma unroll
+                    for (int j = 0; j < kPullWords; ++j) {
+                        // message (hi + lo) * w = pm + pe; two-sum of sh + pm (explicit
+                        // roundings: nothing may be contracted into an FMA)
+                        const float pm = __fmul_rn(qb[h][j].x, wk[h]);
+                        const float pe = __fmaf_rn(qb[h][j].y, wk[h], __fmaf_rn(qb[h][j].x, wk[h], -pm));
+                        const float s = __fadd_rn(sh[j], pm);
+                        const float bv = __fadd_rn(s, -sh[j]);
+                        const float av = __fadd_rn(s, -bv);
+                        const float te = __fadd_rn(__fadd_rn(sh[j], -av), __fadd_rn(pm, -bv));
+                        sl[j] = __fadd_rn(sl[j], __fadd_rn(te, pe));
+                        sh[j] = s;
+                    }
+                }
+            }
+        }
+        pbatch_pull_flush(p, v, w0, whole && vend <= e1, sh, sl, lane);
+    }
 }
 
 __global__ void __launch_bounds__(kPprBatchThreads, 3) ppr_batch_persistent(const PprBatchParams p) {
@@ -641,8 +832,9 @@ __global__ void __launch_bounds__(kPprBatchThreads, 3) ppr_batch_persistent(cons
     int* qtab = sm.v1[wib];  // slot -> query position table of the owner being expanded
     const double one_m_a = 1.0 - (double)p.alpha;
     unsigned long long tph = globaltimer_ns();
+    unsigned long long psum = 0;  // next round's pushes counted by this warp (lane 0)
 
-    // Init: pr = res = 0 (msg and tmask are zero between launches: phase B clears them).
+    // Init: pr = res = 0 (msg, tmask and amask are zero between launches).
     {
         const size_t n4 = ((size_t)p.V * (size_t)p.Q) >> 2;
         float4* a4 = reinterpret_cast<float4*>(p.pr);
@@ -689,27 +881,33 @@ __global__ void __launch_bounds__(kPprBatchThreads, 3) ppr_batch_persistent(cons
     }
     if (!grid_sync(bar, flags, p.barrier_ns)) return;
     // Round-1 frontier: every touched (vertex, word) activates its touched lanes.
-    pbatch_sweep(p, true, fst, pbatch_out(p, 1, 1), &ctl->dctr[1], gwarp, nwarps, lane);
+    pbatch_sweep(p, true, false, 1, fst, pbatch_out(p, 1, 1), &ctl->dctr[1], psum, gwarp, nwarps, lane);
+    if (lane == 0 && psum) atomicAdd(&ctl->pcount[1], psum);
+    psum = 0;
     if (!grid_sync(bar, flags, p.barrier_ns)) return;
     phase_mark(ctl->phase_ns, tph, 0);
 
     long long pushes = 0, steps = 0;
     unsigned long long touched = 0;
     int cur = 1, iters = 0;
+    bool bad = false;
     for (;;) {
         const unsigned long long c = ldcg(&ctl->qctr[cur % 3]);
         const unsigned F = (unsigned)(c >> 32), T = (unsigned)c;
         const unsigned D = min(ldcg(&ctl->dctr[cur % 3]), p.qcap);
-        const int buf = cur & 1;
+        const unsigned long long P = ldcg(&ctl->pcount[cur % 3]);  // this round's (query, edge) pushes
+        const int buf = cur & 1, ob = (cur + 1) & 1;
         if (F == 0 && D == 0) break;
         if (++iters > p.max_iter) {
-            // Round cap: activated lanes keep their residual (never popped).
+            // Round cap: activated lanes keep their residual (never popped); their
+            // activity masks are cleared for the next launch.
             if (gtid == 0) atomicOr(flags, C2G_FLAG_ITER_CAP);
             for (unsigned j = gwarp; j < F; j += nwarps) {
                 const int vw = ldcg(p.q[buf] + j).x;
                 const unsigned lanes = ldcg(p.qmask[buf] + j);
                 const size_t off = (size_t)(vw >> p.logW) * p.Q + ((vw & (W - 1)) << 5) + lane;
-                if ((lanes >> lane) & 1u) p.res[off] = ldcg(p.rq + off);
+                if ((lanes >> lane) & 1u) p.res[off] = ldcg(p.rq[buf] + off) / one_m_a;
+                if (lane == 0) p.amask[buf][vw] = 0u;
             }
             break;
         }
@@ -729,16 +927,26 @@ __global__ void __launch_bounds__(kPprBatchThreads, 3) ppr_batch_persistent(cons
             ctl->qctr[fslot] = 0ull;
             ctl->dctr[fslot] = 0u;
             ctl->tilectr[fslot] = 0u;
+            ctl->pcount[fslot] = 0ull;
             ctl->popped += F;
             ctl->relaxed += T;
         }
-        // Phase A: push along the frontier's edges (owner runs, as in the SSSP batch):
-        // red.add of the FP64 message per active lane, red.or of the word's sending lanes
-        // into the target's touched mask.
-        {
+        const bool pull = P > p.pull_min;  // grid-uniform
+        if (pull) {
+            // Pull round, phase A: gather and sum the messages per target.
+            if (gtid == 0) {
+                pushes += (long long)P;
+                steps += T;
+            }
+            pbatch_pull(p, buf, &ctl->tilectr[cur % 3], lane, bad);
+        } else {
+            // Push round, phase A: push along the frontier's edges (owner runs, as in the
+            // SSSP batch): red.add of the FP64 message per active lane, red.or of the
+            // word's sending lanes into the target's touched mask.
             const int2* q = p.q[buf];
             const unsigned* qm = p.qmask[buf];
             const int* mark = p.mark[buf];
+            const double* rqb = p.rq[buf];
             const unsigned tile = 1u << kBatchTileLog;
             const unsigned ntiles = (T + tile - 1) >> kBatchTileLog;
             unsigned* tctr = &ctl->tilectr[cur % 3];
@@ -752,7 +960,7 @@ __global__ void __launch_bounds__(kPprBatchThreads, 3) ppr_batch_persistent(cons
                     const unsigned j = o + (unsigned)lane;
                     unsigned base = 0x7fffffffu, endv = 0xffffffffu, msk = 0u, rs = 0u;
                     int vw = 0;
-                    bool bad = false;
+                    bool badj = false;
                     if (j < F) {
                         const int2 qe = ldcg(q + j);
                         vw = qe.x;
@@ -761,11 +969,11 @@ __global__ void __launch_bounds__(kPprBatchThreads, 3) ppr_batch_persistent(cons
                         rs = (unsigned)__ldg(p.row + v);
                         const unsigned deg = (unsigned)__ldg(p.row + v + 1) - rs;
                         endv = base + deg;
-                        bad = rs + deg > p.E || deg == 0u;
+                        badj = rs + deg > p.E || deg == 0u;
                         msk = ldcg(qm + j);
                     }
                     const unsigned seg_end = min(e1, (unsigned)__shfl_sync(kFull, endv, 31));
-                    if (__any_sync(kFull, bad) || seg_end <= e0 || o >= F ||
+                    if (__any_sync(kFull, badj) || seg_end <= e0 || o >= F ||
                         (unsigned)__shfl_sync(kFull, (int)base, 0) > e0) {
                         if (lane == 0) atomicOr(flags, C2G_FLAG_BOUNDS);
                         break;
@@ -788,9 +996,10 @@ __global__ void __launch_bounds__(kPprBatchThreads, 3) ppr_batch_persistent(cons
                         __syncwarp();
                         double* mw = p.msg + (w << 5);  // + v * Q + query position
                         unsigned* trow = p.tmask + w;   // + (v << logW): touched word of v
-                        // (1-alpha)*r_u of slot `lane`'s query (src/ppr/purn/Main.cu:288)
+                        // (1-alpha)*r_u of slot `lane`'s query, stored by the apply that
+                        // activated it (src/ppr/purn/Main.cu:288)
                         const double qu = (unsigned)lane < cnt
-                                              ? one_m_a * ldcg(p.rq + (size_t)((unsigned)kvw >> p.logW) * Qu + (w << 5) + qp)
+                                              ? ldcg(rqb + (size_t)((unsigned)kvw >> p.logW) * Qu + (w << 5) + qp)
                                               : 0.0;
                         const DSplit qs = c2g_dsplit(qu);
                         // exponent and high significand in one word (0: residual outside the
@@ -846,13 +1055,18 @@ __global__ void __launch_bounds__(kPprBatchThreads, 3) ppr_batch_persistent(cons
         }
         if (!grid_sync(bar, flags, p.barrier_ns)) return;
         phase_mark(ctl->phase_ns, tph, 2);
+        // The frontier just consumed leaves the pull lookup.
+        for (unsigned j = gtid; j < F; j += nthreads) p.amask[buf][ldcg(p.q[buf] + j).x] = 0u;
         // Phase B: apply the messages of the touched pairs and activate.
-        touched += pbatch_sweep(p, false, fst, pbatch_out(p, (cur + 1) & 1, nslot), &ctl->dctr[nslot], gwarp,
+        touched += pbatch_sweep(p, false, pull, ob, fst, pbatch_out(p, ob, nslot), &ctl->dctr[nslot], psum, gwarp,
                                 nwarps, lane);
+        if (lane == 0 && psum) atomicAdd(&ctl->pcount[nslot], psum);
+        psum = 0;
         if (!grid_sync(bar, flags, p.barrier_ns)) return;
         phase_mark(ctl->phase_ns, tph, 1);
         ++cur;
     }
+    if (bad) atomicOr(flags, C2G_FLAG_BOUNDS);
     // pushes are counted by lane 0 of each warp; touched lanes by every lane
     unsigned long long tl = touched;
     for (int o = 16; o >= 1; o >>= 1) tl += __shfl_xor_sync(kFull, tl, o);
@@ -901,6 +1115,9 @@ struct PprBatchWork {
     double* res = nullptr;
     double* msg = nullptr;
     double* rq = nullptr;
+    double* rq2 = nullptr;
+    float2* rqf[2] = {nullptr, nullptr};
+    unsigned* amask[2] = {nullptr, nullptr};
     unsigned* tmask = nullptr;
     int2* q[2] = {nullptr, nullptr};
     unsigned* qmask[2] = {nullptr, nullptr};
@@ -915,13 +1132,14 @@ struct PprBatchWork {
     float* stage = nullptr;
     size_t seed_cap = 0;
     int Q = 0;
-    bool clean = false;  // msg and tmask are zero
+    bool clean = false;  // msg, tmask and amask are zero
 };
 
 void ppr_batch_free(c2g_graph* g) {
     PprBatchWork* w = reinterpret_cast<PprBatchWork*>(g->ppr_batch);
     if (!w) return;
-    void* ptrs[] = {w->pr, w->res, w->msg, w->rq, w->tmask, w->q[0], w->q[1], w->qmask[0], w->qmask[1],
+    void* ptrs[] = {w->pr, w->res, w->msg, w->rq, w->rq2, w->rqf[0], w->rqf[1], w->amask[0], w->amask[1], w->tmask, w->q[0], w->q[1],
+                    w->qmask[0], w->qmask[1],
                     w->mark[0], w->mark[1], w->dangle, w->ctl, w->counters, w->src, w->seed_off,
                     w->seed_v, w->seed_w, w->stage};
     for (void* p : ptrs)
@@ -944,7 +1162,12 @@ static int ppr_batch_alloc(c2g_graph* g, int Q, size_t n_seeds) {
     C2G_CUDA(cudaMalloc(&w->res, sizeof(double) * VQ));
     C2G_CUDA(cudaMalloc(&w->msg, sizeof(double) * VQ));
     C2G_CUDA(cudaMalloc(&w->rq, sizeof(double) * VQ));
+    C2G_CUDA(cudaMalloc(&w->rq2, sizeof(double) * VQ));
+    C2G_CUDA(cudaMalloc(&w->rqf[0], sizeof(float2) * VQ));
+    C2G_CUDA(cudaMalloc(&w->rqf[1], sizeof(float2) * VQ));
     C2G_CUDA(cudaMalloc(&w->tmask, sizeof(unsigned) * qcap));
+    C2G_CUDA(cudaMalloc(&w->amask[0], sizeof(unsigned) * qcap));
+    C2G_CUDA(cudaMalloc(&w->amask[1], sizeof(unsigned) * qcap));
     for (int b = 0; b < 2; ++b) {
         C2G_CUDA(cudaMalloc(&w->q[b], sizeof(int2) * qcap));
         C2G_CUDA(cudaMalloc(&w->qmask[b], sizeof(unsigned) * qcap));
@@ -963,6 +1186,39 @@ static int ppr_batch_alloc(c2g_graph* g, int Q, size_t n_seeds) {
     return C2G_OK;
 }
 
+// Largest positive weight of the reverse CSR (its bits: positive floats order as
+// integers).  A non-finite weight makes it non-finite, which disables pull rounds.
+__global__ void weight_stats_kernel(const int2* __restrict__ adj_r, long long E, unsigned* wmax_bits) {
+    unsigned wm = 0;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < E; e += (long long)gridDim.x * blockDim.x) {
+        const int wb = __ldg(adj_r + e).y;
+        if (wb > 0) wm = max(wm, (unsigned)wb);
+    }
+    for (int o = 16; o >= 1; o >>= 1) wm = max(wm, (unsigned)__shfl_xor_sync(kFull, (int)wm, o));
+    if ((threadIdx.x & 31) == 0 && wm) atomicMax(wmax_bits, wm);
+}
+
+// Reverse CSR and weight statistics for pull rounds (once per graph and weights).
+int ppr_pull_prepare(c2g_graph* g) {
+    int rc = build_reverse_graph(g);
+    if (rc || g->wstat_valid) return rc;
+    unsigned* d = nullptr;
+    C2G_CUDA(cudaMalloc(&d, sizeof(unsigned)));
+    cudaError_t e = cudaMemsetAsync(d, 0, sizeof(unsigned), g->stream);
+    if (e == cudaSuccess && g->E > 0) {
+        weight_stats_kernel<<<g->num_sms * 8, 256, 0, g->stream>>>(g->adj_r, (long long)g->E, d);
+        e = cudaGetLastError();
+    }
+    unsigned h = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&h, d, sizeof(unsigned), cudaMemcpyDeviceToHost, g->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+    cudaFree(d);
+    C2G_CUDA(e);
+    g->wstat_wmax_bits = h;
+    g->wstat_valid = true;
+    return C2G_OK;
+}
+
 int ppr_batch_launch(c2g_graph* g, int32_t nq, const int32_t* sources, const c2g_ppr_params& prm,
                      const std::vector<int32_t>* seed_off, const std::vector<int32_t>* seed_v,
                      const std::vector<float>* seed_w, float* pr_out, float* res_out, int on_device, int query_major,
@@ -977,6 +1233,17 @@ int ppr_batch_launch(c2g_graph* g, int32_t nq, const int32_t* sources, const c2g
         return fail(C2G_ERR_RANGE, "batch of %d queries too large for this graph", nq);
     int rc;
     const size_t ns = seed_v ? seed_v->size() : 0;
+    // Pull rounds need the reverse CSR (a view uses its base's, never builds it) and finite
+    // weights; with rmax below 1e-30 pushed residuals may leave the FP32 range of the pull's
+    // float pairs, so such launches push only.
+    unsigned long long pull_min = ~0ull;
+    const float ratio = g->ppr_cfg.batch_pull_ratio;
+    if (ratio >= 0.f && g->E > 0 && prm.rmax >= 1e-30f && (g->wstat_valid || !g->borrowed)) {
+        if (!g->borrowed && (rc = ppr_pull_prepare(g))) return rc;
+        float wmax;
+        std::memcpy(&wmax, &g->wstat_wmax_bits, sizeof(float));
+        if (std::isfinite(wmax)) pull_min = (unsigned long long)((double)ratio * (double)g->E);
+    }
     if ((rc = ppr_batch_alloc(g, Q, ns))) return rc;
     PprBatchWork* w = reinterpret_cast<PprBatchWork*>(g->ppr_batch);
     int coop = 0, per_sm = 0;
@@ -987,7 +1254,8 @@ int ppr_batch_launch(c2g_graph* g, int32_t nq, const int32_t* sources, const c2g
     const size_t VQ = (size_t)g->V * (size_t)w->Q;
     if (!w->clean) {
         C2G_CUDA(cudaMemsetAsync(w->msg, 0, sizeof(double) * VQ, g->stream));
-        C2G_CUDA(cudaMemsetAsync(w->tmask, 0, sizeof(unsigned) * (size_t)g->V * (size_t)(w->Q / 32), g->stream));
+        for (unsigned* m : {w->tmask, w->amask[0], w->amask[1]})
+            C2G_CUDA(cudaMemsetAsync(m, 0, sizeof(unsigned) * (size_t)g->V * (size_t)(w->Q / 32), g->stream));
         w->clean = true;
     }
     C2G_CUDA(cudaMemcpyAsync(w->src, sources, sizeof(int) * (size_t)nq, cudaMemcpyHostToDevice, g->stream));
@@ -1010,7 +1278,12 @@ int ppr_batch_launch(c2g_graph* g, int32_t nq, const int32_t* sources, const c2g
     p.pr = w->pr;
     p.res = w->res;
     p.msg = w->msg;
-    p.rq = w->rq;
+    p.rq[0] = w->rq;
+    p.rq[1] = w->rq2;
+    p.amask[0] = w->amask[0];
+    p.amask[1] = w->amask[1];
+    p.rqf[0] = w->rqf[0];
+    p.rqf[1] = w->rqf[1];
     p.tmask = w->tmask;
     for (int b = 0; b < 2; ++b) {
         p.q[b] = w->q[b];
@@ -1033,6 +1306,11 @@ int ppr_batch_launch(c2g_graph* g, int32_t nq, const int32_t* sources, const c2g
     p.mark_cap = (unsigned)((((size_t)g->E * (size_t)(p.Q / 32)) >> kBatchTileLog) + 2);
     p.barrier_ns = g->barrier_ns ? g->barrier_ns : 4000000000ull;
     p.counters = w->counters;
+    p.row_r = g->row_r;
+    p.adj_r = g->adj_r;
+    p.mark_r = g->mark_r;
+    p.ntiles_r = (unsigned)(((size_t)g->E + (1u << kPullTileLog) - 1) >> kPullTileLog);
+    p.pull_min = pull_min;
     C2G_CUDA(cudaMemsetAsync(w->ctl, 0, sizeof(TraversalCtl), g->stream));
     C2G_CUDA(cudaMemsetAsync(w->counters, 0, sizeof(long long) * 2, g->stream));
     void* args[] = {&p};

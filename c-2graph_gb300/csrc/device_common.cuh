@@ -52,6 +52,8 @@ __device__ __forceinline__ float ldcg(const float* p) { return __ldcg(p); }
 __device__ __forceinline__ int2 ldcg(const int2* p) { return __ldcg(p); }
 __device__ __forceinline__ unsigned long long ldcg(const unsigned long long* p) { return __ldcg(p); }
 __device__ __forceinline__ double ldcg(const double* p) { return __ldcg(p); }
+__device__ __forceinline__ float2 ldcg(const float2* p) { return __ldcg(p); }
+__device__ __forceinline__ uint4 ldcg(const uint4* p) { return __ldcg(p); }
 
 // Grid barrier with a time limit.  Every CTA of a cooperative launch calls it; it
 // returns false (and all later calls return false) once any CTA has given up, so the

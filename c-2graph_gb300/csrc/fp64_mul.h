@@ -108,4 +108,60 @@ C2G_HD bool c2g_mul_q_ok(const DSplit& q) { return q.e >= 128 && q.e <= 1916; }
 // Weight part: w positive, normal and finite (exponent field 1..254).
 C2G_HD bool c2g_mul_w_ok(uint32_t wb) { return wb - 0x00800000u < 0x7f000000u; }
 
+// ---------------------------------------------------------------------------------------
+// Float pairs (pull rounds of the batched push, which sum messages as hi + lo in FP32).
+// Both conversions are integer operations on the bits, since GB300's FP64 pipe is slow.
+
+C2G_HD float c2g_bitsf(uint32_t u) {
+#if defined(__CUDA_ARCH__)
+    return __uint_as_float(u);
+#else
+    union {
+        float f;
+        uint32_t u;
+    } c;
+    c.u = u;
+    return c.f;
+#endif
+}
+
+struct c2g_pair {
+    uint32_t hi, lo;  // float bits
+};
+
+// q > 0 with biased exponent in [949, 1150] (q in [2^-74, 2^127)): hi = q cut to 24
+// significant bits, lo = the remaining 29 bits cut to 24, so hi + lo <= q with relative
+// error below 2^-47.  hi's float exponent is q's rebiased; lo holds q's low 29 bits
+// r * 2^(eq - 1075), normalised so that its top bit is the float's implicit one.
+C2G_HD bool c2g_split_ok(double q) {
+    const uint32_t e = (uint32_t)(c2g_dbits(q) >> 52) & 0x7ffu;
+    return e >= 949u && e <= 1150u;
+}
+
+C2G_HD c2g_pair c2g_split_pair(double q) {
+    const uint64_t b = c2g_dbits(q);
+    const uint32_t e = (uint32_t)(b >> 52) & 0x7ffu;
+    c2g_pair p;
+    p.hi = ((e - 896u) << 23) | ((uint32_t)(b >> 29) & 0x7fffffu);
+    const uint32_t r = (uint32_t)b & 0x1fffffffu;
+    p.lo = 0u;
+    if (r) {
+#if defined(__CUDA_ARCH__)
+        const uint32_t lz = (uint32_t)__clz((int)r) - 3u;  // r << lz has its top bit at bit 28
+#else
+        const uint32_t lz = (uint32_t)__builtin_clz(r) - 3u;
+#endif
+        p.lo = ((e - 920u - lz) << 23) | (((r << lz) >> 5) & 0x7fffffu);
+    }
+    return p;
+}
+
+// A float (bits) as a double, exactly, for normal floats and zero (subnormals give 0).
+C2G_HD double c2g_float_bits_to_double(uint32_t u) {
+    const uint32_t e = (u >> 23) & 0xffu;
+    if (e == 0u) return 0.0;
+    return c2g_bitsd(((uint64_t)(u & 0x80000000u) << 32) | ((uint64_t)(e + 896u) << 52) |
+                     ((uint64_t)(u & 0x7fffffu) << 29));
+}
+
 }  // namespace c2g

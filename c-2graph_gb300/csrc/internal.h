@@ -43,6 +43,7 @@ struct TraversalCtl {
     long long popped, relaxed, touched, seeds;
     int pad[1];
     unsigned long long phase_ns[4];  // block 0's time per phase (see phase_mark)
+    unsigned long long pcount[3];    // batched PPR: (query, edge) pushes of the frontier per round slot
 };
 
 // Stamps survive across launches; the kernel advances the bases itself.
@@ -91,6 +92,7 @@ struct SsspConfig {
 };
 
 struct PprConfig {
+    float batch_pull_ratio = 8.0f;  // batched rounds with more than ratio * E pushes pull (< 0: never)
     int log_tile = 8;
     int pull_div = 0;   // pull round when frontier out-edges * pull_div > E; 0 = push only (default)
     int dense_div = 16;  // dense push round (red.add, apply sweep over V) when out-edges * dense_div > E
@@ -146,6 +148,10 @@ struct c2g_graph {
     float grid_scale = 1.0f;  // fraction of the GPU a batched launch may occupy
     unsigned long long barrier_ns = 0;  // grid-barrier wait limit (0: per-kernel default)
     unsigned long long last_phase_ns[4] = {0, 0, 0, 0};  // phases of the last launch
+    // float-weight statistics (batched pull rounds), valid = false until computed: the
+    // largest positive weight (bits)
+    bool wstat_valid = false;
+    uint32_t wstat_wmax_bits = 0;
     int stall_next_sssp = 0;            // failure-detection test: next SSSP barrier cannot complete
     bool borrowed = false;    // a view: graph arrays belong to another handle
 };
@@ -169,6 +175,9 @@ int graph_view(c2g_graph* base, c2g_graph** out);
 void batch_free(c2g_graph* g);
 void ppr_batch_free(c2g_graph* g);
 void ads_free(c2g_graph* g);
+int build_reverse_graph(c2g_graph* g);
+// Reverse CSR and the weight statistics of the batched pull rounds (once per weights).
+int ppr_pull_prepare(c2g_graph* g);
 int ppr_batch_launch(c2g_graph* g, int32_t nq, const int32_t* sources, const c2g_ppr_params& prm,
                      const std::vector<int32_t>* seed_off, const std::vector<int32_t>* seed_v,
                      const std::vector<float>* seed_w, float* pr_out, float* res_out, int on_device, int query_major,

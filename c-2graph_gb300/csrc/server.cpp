@@ -181,7 +181,7 @@ int c2g_server_create(c2g_graph* g, const float* p_inj, const float* p_cont, con
     int rc = C2G_OK;
     {
         std::lock_guard<std::mutex> lk(g->mu);
-        if (g->adj_f) rc = build_reverse_graph(g);
+        if (g->adj_f) rc = ppr_pull_prepare(g);
     }
     for (int k = 0; k < 3 && !rc; ++k) {
         rc = graph_view(g, &s->views[k]);
@@ -190,7 +190,7 @@ int c2g_server_create(c2g_graph* g, const float* p_inj, const float* p_cont, con
     // Per-query device state (bytes) and the admission budget.
     const int64_t W = 1;  // words per query amortise to 1/32 per query; counted per query
     s->bytes_per_query[C2G_REQ_SSSP] = (int64_t)V * (4 + 4) + (int64_t)V * 20 * W / 32;  // dist + staging + masks/queues
-    s->bytes_per_query[C2G_REQ_PPR] = (int64_t)V * (4 * 4 + 4);                           // pr,res,msg,rq + staging
+    s->bytes_per_query[C2G_REQ_PPR] = (int64_t)V * (4 + 8 * 6 + 4) + (int64_t)V * 12 / 32;  // pr,res,msg,rq x2,rq pairs x2,staging,masks
     s->bytes_per_query[C2G_REQ_ADSORPTION] = (int64_t)V * 16 * 4 * 3;                     // Y, acc, host-copy stage
     size_t free_b = 0, total_b = 0;
     if (!rc && cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) rc = fail(C2G_ERR_CUDA, "cudaMemGetInfo failed");

@@ -228,6 +228,15 @@ int c2g_ppr_batch(c2g_graph* g, int32_t n, const int32_t* sources, const c2g_ppr
  * the same BSP rounds either way. */
 int c2g_ppr_set_config(c2g_graph* g, int32_t pull_div, int32_t dense_div);
 
+/* Round shapes of the batched push (c2g_ppr_batch).  A round whose frontier makes more
+ * than ratio * E (query, edge) pushes pulls over the reverse CSR (built on first use):
+ * each target gathers its in-neighbours' pushed residuals and sums the messages as FP32
+ * pairs (about 47 bits of relative precision) before they meet the FP64 residual.
+ * ratio < 0: push only; 0: pull every round; default 8.  Pull rounds need finite weights
+ * and rmax >= 1e-30.  Results are the same BSP rounds either way, within summation
+ * order. */
+int c2g_ppr_batch_set_pull(c2g_graph* g, float ratio);
+
 /* Reference defaults: PPR (alpha 0.2, rmax 0.001/(V+1), cap 500), and the adsorption
  * program (alpha 0.2, r0 10, pr0 8, rmax 1/V, cap 2000). */
 int c2g_ppr_default_params(const c2g_graph* g, int adsorption, c2g_ppr_params* out);

@@ -66,6 +66,29 @@ int main(int argc, char** argv) {
             done += r2;
         }
     }
+    // float pairs: hi + lo <= q within 2^-47 relative, both parts exact as doubles
+    for (long i = 0; i < n; ++i) {
+        const uint64_t a = next_u64(), b = next_u64();
+        const uint64_t e = 949 + a % 202;
+        const double q = c2g::c2g_bitsd((e << 52) | (b & 0xfffffffffffffull));
+        if (!c2g::c2g_split_ok(q)) {
+            std::printf("split range rejects q=%a\n", q);
+            return 1;
+        }
+        const c2g::c2g_pair p = c2g::c2g_split_pair(q);
+        const float hi = c2g::c2g_bitsf(p.hi), lo = c2g::c2g_bitsf(p.lo);
+        const double hd = c2g::c2g_float_bits_to_double(p.hi), ld = c2g::c2g_float_bits_to_double(p.lo);
+        if (hd != (double)hi || ld != (double)lo) {
+            std::printf("float->double mismatch q=%a\n", q);
+            return 1;
+        }
+        const double rel = (q - (hd + ld)) / q;
+        if (!(rel >= 0.0 && rel < 0x1p-47)) {
+            std::printf("split error q=%a hi=%a lo=%a rel=%g\n", q, (double)hi, (double)lo, rel);
+            return 1;
+        }
+        ++done;
+    }
     std::printf("ok %ld\n", done);
     return 0;
 }

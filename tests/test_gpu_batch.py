@@ -166,3 +166,74 @@ def test_ppr_batch_matches_single_and_cap(gpu_available, g14p):
             rp, rr, rounds, _ = oracle.ppr_push(o["vlist"], o["elist"], o["flist"], int(src[i]), 0.2, 1e-6,
                                                 max_iter=3)
             assert _l1(pr[i], rp) <= 1e-6 and _l1(res[i], rr) <= 1e-6
+
+
+@pytest.mark.parametrize("ratio", [-1.0, 0.0, 8.0])
+def test_ppr_batch_pull_shapes_vs_fp64(gpu_available, g14p, ratio):
+    """Push-only, pull-every-round and the default mix: every query within L1 <= 1e-6 of
+    the FP64 oracle, base and seeded, with the pushes counted the same way."""
+    import c2g
+    import oracle
+
+    o = oracle.load_dataset(g14p, "origin")
+    src = _sources(o["vlist"], 48, 5)
+    with c2g.Graph.load(g14p, "origin") as gr:
+        gr.ppr_batch_pull(ratio)
+        prm = gr.ppr_params(alpha=0.15, rmax=1e-7, seeded=0, pr0=0.15, r0=1.0, max_iter=500)
+        pr, res, st = gr.ppr_batch(src, prm)
+        assert st.status_flags == 0
+        for i in (0, 7, 23, 24, 40, 47):
+            rp, rr, _, cnt = oracle.ppr_push(o["vlist"], o["elist"], o["flist"], int(src[i]), 0.15, 1e-7)
+            assert _l1(pr[i], rp) <= 1e-6, (ratio, i, _l1(pr[i], rp))
+            assert _l1(res[i], rr) <= 1e-6, (ratio, i, _l1(res[i], rr))
+    p = oracle.load_dataset(g14p, "ppr")
+    hv, he, hw = p["hvlist"], p["helist"], p["hwlist"]
+    src = _sources(p["vlist"], 40, 6)
+    with c2g.Graph.load(g14p, "ppr") as gr:
+        gr.ppr_batch_pull(ratio)
+        prm = gr.ppr_params(alpha=0.15, rmax=1e-7, seeded=1)
+        pr, res, st = gr.ppr_batch(src, prm)
+        assert st.status_flags == 0
+        for i in (0, 19, 20, 39):
+            s = int(src[i])
+            sv = np.concatenate([he[hv[s]:hv[s + 1]], p["elist"][p["vlist"][s]:p["vlist"][s + 1]]])
+            sw = np.concatenate([hw[hv[s]:hv[s + 1]], p["wlist"][p["vlist"][s]:p["vlist"][s + 1]]])
+            rp, rr, _, _ = oracle.ppr_push(p["vlist"], p["elist"], p["wlist"], s, 0.15, 1e-7, seeded=True,
+                                           seed_v=sv, seed_w=sw)
+            assert _l1(pr[i], rp) <= 1e-6, (ratio, i)
+            assert _l1(res[i], rr) <= 1e-6, (ratio, i)
+
+
+def test_ppr_batch_pull_cap_and_heavy_weights(gpu_available, g14p):
+    """Pull every round: a round cap keeps the activated residuals; weights whose
+    out-sums exceed 1 (the residual grows) narrow the fixed-point range and still match
+    the FP64 oracle."""
+    import c2g
+    import oracle
+
+    o = oracle.load_dataset(g14p, "origin")
+    src = _sources(o["vlist"], 36, 8)
+    with c2g.Graph.load(g14p, "origin") as gr:
+        gr.ppr_batch_pull(0.0)
+        prm = gr.ppr_params(alpha=0.2, rmax=1e-6, seeded=0, pr0=0.2, r0=1.0, max_iter=4)
+        pr, res, st = gr.ppr_batch(src, prm)
+        assert st.status_flags & c2g.FLAG_ITER_CAP
+        for i in (0, 35):
+            rp, rr, _, _ = oracle.ppr_push(o["vlist"], o["elist"], o["flist"], int(src[i]), 0.2, 1e-6, max_iter=4)
+            assert _l1(pr[i], rp) <= 1e-6 and _l1(res[i], rr) <= 1e-6
+        # a second launch after the cap starts from clean state
+        prm.max_iter = 500
+        pr, res, st = gr.ppr_batch(src, prm)
+        assert st.status_flags == 0
+        rp, rr, _, _ = oracle.ppr_push(o["vlist"], o["elist"], o["flist"], int(src[3]), 0.2, 1e-6)
+        assert _l1(pr[3], rp) <= 1e-6 and _l1(res[3], rr) <= 1e-6
+        heavy = (o["flist"].astype(np.float32) * np.float32(3.0)).astype(np.float32)
+        gr.set_weights(heavy)
+        prm = gr.ppr_params(alpha=0.2, rmax=1e-6, seeded=0, pr0=0.2, r0=1.0, max_iter=6)
+        pr, res, st = gr.ppr_batch(src, prm)
+        assert st.status_flags == c2g.FLAG_ITER_CAP or st.status_flags == 0
+        for i in (1, 30):
+            rp, rr, _, _ = oracle.ppr_push(o["vlist"], o["elist"], heavy, int(src[i]), 0.2, 1e-6, max_iter=6)
+            scale = max(1.0, float(np.abs(rp).sum()))
+            assert _l1(pr[i], rp) <= 1e-6 * scale, (i, _l1(pr[i], rp), scale)
+            assert _l1(res[i], rr) <= 1e-6 * max(1.0, float(np.abs(rr).sum())), i
