@@ -280,10 +280,9 @@ def run_ours(args, rank, world, local_rank):
     achieved = tot[dominant + "_bytes"] / (tot[dominant + "_ms"] / 1000.0) / 1e9
     kernel_name = "sssp_batch_persistent" if dominant == "s" else "ppr_batch_persistent"
     # DRAM bytes (read + write) per launch from a one-pass ncu capture of this step at full
-    # size (profiles/ppr_batch_persistent_rmat-s20-ef16_32q.md,
-    # profiles/sssp_batch_persistent_rmat-s20-ef16_32q.md), expressed per unit processed
-    # and scaled to this run's average launch.
-    traffic_per_unit = {"p": 5.8424e12 / 371.90e9, "s": 318.54e9 / 61.20e9}[dominant]
+    # size (profiles/launches_bench_default_rmat-s22-ef16_256sssp-256ppr.md), expressed per
+    # unit processed and scaled to this run's average launch.
+    traffic_per_unit = {"p": 3.3675e12 / 371.88e9, "s": 317.66e9 / 61.10e9}[dominant]
     units = tot["p_push"] if dominant == "p" else tot["s_rel"]
     traffic = traffic_per_unit * units / args.steps
 
