@@ -600,8 +600,8 @@ __device__ __forceinline__ void pbatch_apply_word(const PprBatchParams& p, bool 
 }
 
 // Apply sweep: every (vertex, word) whose touched mask is non-zero applies its messages
-// lane by lane (lane = query) and activates; the mask is cleared.  pulled: the messages
-// are a pull round's sums (see pbatch_pull_flush for their two forms).  Pushes
+// lane by lane (lane = query) and activates; the mask is cleared.  After a pull round only
+// the targets whose in-edges cross a tile boundary are left to it.  Pushes
 // mark targets with red.or, so the push never waits on an atomic's return; the sweep
 // reads V * W mask words per round.  A warp takes 32 words at a time (their degrees
 // loaded lane-parallel) and applies up to kApplyGroup touched words at once: all their
@@ -609,7 +609,7 @@ __device__ __forceinline__ void pbatch_apply_word(const PprBatchParams& p, bool 
 // memory latencies overlap instead of adding up.
 constexpr int kApplyGroup = 3;  // 4 spills at 64 registers
 
-__device__ __forceinline__ unsigned pbatch_sweep(const PprBatchParams& p, bool force, bool pulled, int ob,
+__device__ __forceinline__ unsigned pbatch_sweep(const PprBatchParams& p, bool force, int ob,
                                                  WarpStage& fst, const FrontierOut& out, unsigned* dctr,
                                                  unsigned long long& psum, unsigned gwarp, unsigned nwarps, int lane) {
     const unsigned nm = (unsigned)p.V << p.logW;
@@ -619,13 +619,10 @@ __device__ __forceinline__ unsigned pbatch_sweep(const PprBatchParams& p, bool f
         const unsigned i = b + (unsigned)lane;
         const unsigned tm = i < nm ? ldcg(p.tmask + i) : 0u;
         int dg = 0;
-        bool split = false;  // pulled: the sums of v came in parts (FP64), not as a float pair
         if (tm) {
             p.tmask[i] = 0u;
             const int v = (int)(i >> p.logW);
             dg = __ldg(p.row + v + 1) - __ldg(p.row + v);
-            if (pulled)
-                split = (__ldg(p.row_r + v) >> kPullTileLog) != ((__ldg(p.row_r + v + 1) - 1) >> kPullTileLog);
         }
         unsigned nz = __ballot_sync(kFull, tm != 0u);
         cnt += (unsigned)__popc(tm);  // touched (vertex, query) lanes seen by this lane
@@ -658,12 +655,7 @@ __device__ __forceinline__ unsigned pbatch_sweep(const PprBatchParams& p, bool f
                 const size_t off = ((size_t)(unsigned)vw << 5) + lane;
                 const bool mine = (ln >> lane) & 1u;
                 if (mine && !force) p.msg[off] = 0.0;
-                double mu = m[u];
-                if (pulled && !__shfl_sync(kFull, (int)split, ks[u])) {  // a float pair hi + lo
-                    const unsigned long long b = c2g_dbits(m[u]);
-                    mu = c2g_float_bits_to_double((unsigned)b) + c2g_float_bits_to_double((unsigned)(b >> 32));
-                }
-                pbatch_apply_word(p, force, ob, vw, dgu, off, mine, r[u], mu, pv[u], rmax_bits, fst, out, dctr,
+                pbatch_apply_word(p, force, ob, vw, dgu, off, mine, r[u], m[u], pv[u], rmax_bits, fst, out, dctr,
                                   psum, lane);
             }
         }
@@ -682,49 +674,82 @@ __device__ __forceinline__ unsigned pbatch_sweep(const PprBatchParams& p, bool f
 // (about 47 bits of relative precision): the product is hi*w + lo*w with its rounding
 // error recovered by an FMA, and each add is an error-free two-sum whose error joins lo.
 // Relative precision matters here, not absolute: a message sum decides res > rmax at the
-// scale of rmax, far below the largest sums.  Each target's sums are written once to msg
-// with its touched lanes in tmask; only targets whose in-edges cross a tile boundary add
-// their parts atomically (in FP64).  The apply sweep that follows is the push round's.
+// scale of rmax, far below the largest sums.  A target whose in-edges lie in one tile is
+// applied by the warp that summed them; only targets whose in-edges cross a tile boundary
+// add their parts to msg (FP64 atomics) for the apply sweep that follows, as after a push.
 // In-edges are cut into tiles of 2^kPullTileLog; warps take (tile, word group) items from
 // the round's queue, kPullWords query words per item.
 constexpr int kPullWords = 4;  // query words per pull item
 constexpr int kPullEdges = 2;  // in-edges whose rq rows are gathered before they are summed
 
-// Owner v's message sums of the item's words (hi + lo per lane) and its touched lanes
-// (tmask).  An owner whose in-edges lie in this tile is the only writer: a plain store of
-// the float pair.  Otherwise its parts are added in FP64 (atomics); the apply tells the
-// two forms apart by whether v's in-edges cross a tile boundary.
-__device__ __forceinline__ void pbatch_pull_flush(const PprBatchParams& p, int v, unsigned w0, bool whole,
-                                                  float (&sh)[kPullWords], float (&sl)[kPullWords], int lane) {
+// Owner v's message sums of the item's words are complete (hi + lo per lane).  An owner
+// whose in-edges lie in this tile has them all: it is applied here, by the pulling warp
+// (the pullers read the other round parity's rq pairs and activity masks, so this apply
+// does not disturb them).  An owner whose in-edges cross a tile boundary adds its part to
+// msg in FP64 (atomics) and marks tmask; the apply sweep after the barrier finishes it.
+__device__ __forceinline__ unsigned pbatch_pull_owner(const PprBatchParams& p, int v, unsigned w0, bool whole,
+                                                      const float (&sh)[kPullWords], const float (&sl)[kPullWords],
+                                                      int ob, unsigned long long rmax_bits, WarpStage& fst,
+                                                      const FrontierOut& out, unsigned* dctr,
+                                                      unsigned long long& psum, int lane) {
     const unsigned W = 1u << p.logW;
+    unsigned cnt = 0;
+    if (!whole) {
+#pragma unroll
+        for (int j = 0; j < kPullWords; ++j) {
+            if (w0 + j >= W) break;  // warp-uniform
+            const bool nz = sh[j] != 0.f;
+            const unsigned bits = __ballot_sync(kFull, nz);
+            if (bits) {
+                const size_t vw = ((size_t)(unsigned)v << p.logW) + w0 + j;
+                if (nz)
+                    atomicAdd(p.msg + (vw << 5) + lane, c2g_float_bits_to_double(__float_as_uint(sh[j])) +
+                                                            c2g_float_bits_to_double(__float_as_uint(sl[j])));
+                if (lane == 0) atomicOr(p.tmask + vw, bits);
+            }
+        }
+        return 0;
+    }
+    const int dg = __ldg(p.row + v + 1) - __ldg(p.row + v);
+    double r[kPullWords];
+    float pv[kPullWords];
+#pragma unroll
+    for (int j = 0; j < kPullWords; ++j) {
+        const size_t off = (size_t)v * (size_t)p.Q + ((w0 + j) << 5) + lane;
+        const bool nz = sh[j] != 0.f;
+        r[j] = nz ? ldcg(p.res + off) : 0.0;
+        pv[j] = nz ? ldcg(p.pr + off) : 0.f;
+    }
 #pragma unroll
     for (int j = 0; j < kPullWords; ++j) {
         if (w0 + j >= W) break;  // warp-uniform
         const bool nz = sh[j] != 0.f;
-        const unsigned bits = __ballot_sync(kFull, nz);
-        if (bits) {
-            const size_t vw = ((size_t)(unsigned)v << p.logW) + w0 + j;
-            const size_t off = (vw << 5) + lane;
-            if (whole) {
-                if (nz) reinterpret_cast<float2*>(p.msg)[off] = make_float2(sh[j], sl[j]);
-                if (lane == 0) p.tmask[vw] = bits;
-            } else {
-                if (nz) atomicAdd(p.msg + off, (double)sh[j] + (double)sl[j]);
-                if (lane == 0) atomicOr(p.tmask + vw, bits);
-            }
-        }
-        sh[j] = 0.f;
-        sl[j] = 0.f;
+        if (!__any_sync(kFull, nz)) continue;
+        cnt += nz ? 1u : 0u;
+        const size_t off = (size_t)v * (size_t)p.Q + ((w0 + j) << 5) + lane;
+        const double m = c2g_float_bits_to_double(__float_as_uint(sh[j])) +
+                         c2g_float_bits_to_double(__float_as_uint(sl[j]));
+        pbatch_apply_word(p, false, ob, (int)(((unsigned)v << p.logW) + w0 + j), dg, off, nz, r[j], m, pv[j],
+                          rmax_bits, fst, out, dctr, psum, lane);
     }
+    return cnt;
 }
 
-__device__ __forceinline__ void pbatch_pull(const PprBatchParams& p, int buf, unsigned* qctr, int lane, bool& bad) {
+// Phase A of a pull round.  A warp takes (tile, word group) items from the round's queue
+// and walks the tile's owners one by one: for each owner, its in-edges in the tile in
+// chunks of 32 (source, weight and the source's active lanes loaded lane-parallel), the
+// pushed residuals of kPullEdges in-edges gathered before they are summed.
+__device__ __forceinline__ unsigned pbatch_pull(const PprBatchParams& p, int buf, int ob, unsigned* qctr,
+                                                WarpStage& fst, const FrontierOut& out, unsigned* dctr,
+                                                unsigned long long& psum, int lane, bool& bad) {
     const unsigned W = 1u << p.logW;
     const int lg = p.logW >= 2 ? p.logW - 2 : 0;  // word groups per tile = 2^lg (kPullWords = 4)
     const unsigned nitems = p.ntiles_r << lg;
     const unsigned* am = p.amask[buf];
     const float2* rqb = p.rqf[buf];
     const unsigned tw = 1u << kPullTileLog;
+    const unsigned long long rmax_bits = c2g_dbits((double)p.rmax);
+    unsigned cnt = 0;
     unsigned itn = next_tile(qctr, lane);
     for (unsigned it = itn; it < nitems; it = itn) {
         itn = next_tile(qctr, lane);  // the next item, fetched while this one runs
@@ -733,87 +758,90 @@ __device__ __forceinline__ void pbatch_pull(const PprBatchParams& p, int buf, un
         const unsigned e0 = t << kPullTileLog;
         const unsigned e1 = min(e0 + tw, p.E);
         int v = __ldg(p.mark_r + t);  // owner of in-edge e0
-        unsigned vend = (unsigned)__ldg(p.row_r + v + 1);
-        bool whole = (unsigned)__ldg(p.row_r + v) >= e0;
-        float sh[kPullWords], sl[kPullWords];
+        unsigned vs = (unsigned)__ldg(p.row_r + v);
+        for (;;) {
+            const unsigned ve = (unsigned)__ldg(p.row_r + v + 1);
+            const unsigned ea = max(vs, e0), ez = min(ve, e1);
+            if (ea < ez) {  // warp-uniform: v has in-edges in this tile
+                float sh[kPullWords], sl[kPullWords];
 #pragma unroll
-        for (int j = 0; j < kPullWords; ++j) sh[j] = sl[j] = 0.f;
-        for (unsigned b = e0; b < e1; b += 32u) {
-            // 32 in-edges, one per lane: source, weight and the source's active lanes for
-            // the item's words
-            const unsigned e = b + (unsigned)lane;
-            int src = 0;
-            float wt = 0.f;
-            unsigned mk[kPullWords];
+                for (int j = 0; j < kPullWords; ++j) sh[j] = sl[j] = 0.f;
+                for (unsigned b = ea; b < ez; b += 32u) {
+                    const unsigned e = b + (unsigned)lane;
+                    int src = 0;
+                    float wt = 0.f;
+                    unsigned mk[kPullWords];
 #pragma unroll
-            for (int j = 0; j < kPullWords; ++j) mk[j] = 0u;
-            if (e < e1) {
-                const int2 ed = __ldg(p.adj_r + e);
-                if ((unsigned)ed.x >= (unsigned)p.V) {
-                    bad = true;
-                } else if (ed.y > 0) {  // positive weights only, as the push
-                    src = ed.x;
-                    wt = __int_as_float(ed.y);
-                    const unsigned* ms = am + ((size_t)(unsigned)src << p.logW) + w0;
-                    if (W >= 4u) {  // four words, 16-byte aligned
-                        const uint4 m4 = ldcg(reinterpret_cast<const uint4*>(ms));
-                        mk[0] = m4.x;
-                        mk[1] = m4.y;
-                        mk[2] = m4.z;
-                        mk[3] = m4.w;
-                    } else {
+                    for (int j = 0; j < kPullWords; ++j) mk[j] = 0u;
+                    if (e < ez) {
+                        const int2 ed = __ldg(p.adj_r + e);
+                        if ((unsigned)ed.x >= (unsigned)p.V) {
+                            bad = true;
+                        } else if (ed.y > 0) {  // positive weights only, as the push
+                            src = ed.x;
+                            wt = __int_as_float(ed.y);
+                            const unsigned* ms = am + ((size_t)(unsigned)src << p.logW) + w0;
+                            if (W >= 4u) {  // four words, 16-byte aligned
+                                const uint4 m4 = ldcg(reinterpret_cast<const uint4*>(ms));
+                                mk[0] = m4.x;
+                                mk[1] = m4.y;
+                                mk[2] = m4.z;
+                                mk[3] = m4.w;
+                            } else {
 #pragma unroll
-                        for (int j = 0; j < kPullWords; ++j)
-                            if ((unsigned)j < W) mk[j] = ldcg(ms + j);
+                                for (int j = 0; j < kPullWords; ++j)
+                                    if ((unsigned)j < W) mk[j] = ldcg(ms + j);
+                            }
+                        }
+                    }
+                    const unsigned n = min(32u, ez - b);
+                    for (unsigned k0 = 0; k0 < n; k0 += kPullEdges) {
+                        // gather the pushed residuals of kPullEdges in-edges, then add them
+                        float2 qb[kPullEdges][kPullWords];
+                        float wk[kPullEdges];
+#pragma unroll
+                        for (int h = 0; h < kPullEdges; ++h) {
+                            const unsigned k = k0 + h < n ? k0 + h : n - 1u;
+                            wk[h] = __shfl_sync(kFull, wt, (int)k);
+                            const int u = __shfl_sync(kFull, src, (int)k);
+#pragma unroll
+                            for (int j = 0; j < kPullWords; ++j) {
+                                const unsigned mj = (unsigned)__shfl_sync(kFull, (int)mk[j], (int)k);
+                                const bool on = k0 + h < n && ((mj >> lane) & 1u);
+                                qb[h][j] = on ? ldcg(rqb + ((size_t)(unsigned)u << (p.logW + 5)) + ((w0 + j) << 5) +
+                                                     lane)
+                                              : make_float2(0.f, 0.f);
+                            }
+                        }
+#pragma unroll
+                        for (int h = 0; h < kPullEdges; ++h) {
+#pragma unroll
+                            for (int j = 0; j < kPullWords; ++j) {
+                                // message (hi + lo) * w = pm + pe; two-sum of sh + pm
+                                // (explicit roundings: nothing may be contracted into an FMA)
+                                const float pm = __fmul_rn(qb[h][j].x, wk[h]);
+                                const float pe =
+                                    __fmaf_rn(qb[h][j].y, wk[h], __fmaf_rn(qb[h][j].x, wk[h], -pm));
+                                const float s = __fadd_rn(sh[j], pm);
+                                const float bv = __fadd_rn(s, -sh[j]);
+                                const float av = __fadd_rn(s, -bv);
+                                const float te = __fadd_rn(__fadd_rn(sh[j], -av), __fadd_rn(pm, -bv));
+                                sl[j] = __fadd_rn(sl[j], __fadd_rn(te, pe));
+                                sh[j] = s;
+                            }
+                        }
                     }
                 }
+                cnt += pbatch_pull_owner(p, v, w0, vs >= e0 && ve <= e1, sh, sl, ob, rmax_bits, fst, out, dctr,
+                                         psum, lane);
             }
-            const unsigned n = min(32u, e1 - b);
-            for (unsigned k0 = 0; k0 < n; k0 += kPullEdges) {
-                // gather the pushed residuals of kPullEdges in-edges, then add them in edge order
-                float2 qb[kPullEdges][kPullWords];
-                float wk[kPullEdges];
-#pragma unroll
-                for (int h = 0; h < kPullEdges; ++h) {
-                    const unsigned k = k0 + h < n ? k0 + h : n - 1u;
-                    wk[h] = __shfl_sync(kFull, wt, (int)k);
-                    const int u = __shfl_sync(kFull, src, (int)k);
-#pragma unroll
-                    for (int j = 0; j < kPullWords; ++j) {
-                        const unsigned mj = (unsigned)__shfl_sync(kFull, (int)mk[j], (int)k);
-                        const bool on = k0 + h < n && ((mj >> lane) & 1u);
-                        qb[h][j] = on ? ldcg(rqb + ((size_t)(unsigned)u << (p.logW + 5)) + ((w0 + j) << 5) + lane)
-                                      : make_float2(0.f, 0.f);
-                    }
-                }
-#pragma unroll
-                for (int h = 0; h < kPullEdges; ++h) {
-                    if (k0 + h >= n) break;  // warp-uniform
-                    const unsigned e = b + k0 + h;
-                    while (e >= vend) {  // owner changes: its sums are complete
-                        pbatch_pull_flush(p, v, w0, whole, sh, sl, lane);
-                        ++v;
-                        whole = true;  // owners starting inside the tile
-                        vend = (unsigned)__ldg(p.row_r + v + 1);
-                    }
-#pragma unroll
-                    for (int j = 0; j < kPullWords; ++j) {
-                        // message (hi + lo) * w = pm + pe; two-sum of sh + pm (explicit
-                        // roundings: nothing may be contracted into an FMA)
-                        const float pm = __fmul_rn(qb[h][j].x, wk[h]);
-                        const float pe = __fmaf_rn(qb[h][j].y, wk[h], __fmaf_rn(qb[h][j].x, wk[h], -pm));
-                        const float s = __fadd_rn(sh[j], pm);
-                        const float bv = __fadd_rn(s, -sh[j]);
-                        const float av = __fadd_rn(s, -bv);
-                        const float te = __fadd_rn(__fadd_rn(sh[j], -av), __fadd_rn(pm, -bv));
-                        sl[j] = __fadd_rn(sl[j], __fadd_rn(te, pe));
-                        sh[j] = s;
-                    }
-                }
-            }
+            if (ve >= e1) break;
+            ++v;
+            vs = ve;
         }
-        pbatch_pull_flush(p, v, w0, whole && vend <= e1, sh, sl, lane);
     }
+    stage_flush(fst, out);
+    return cnt;
 }
 
 __global__ void __launch_bounds__(kPprBatchThreads, 3) ppr_batch_persistent(const PprBatchParams p) {
@@ -881,7 +909,7 @@ __global__ void __launch_bounds__(kPprBatchThreads, 3) ppr_batch_persistent(cons
     }
     if (!grid_sync(bar, flags, p.barrier_ns)) return;
     // Round-1 frontier: every touched (vertex, word) activates its touched lanes.
-    pbatch_sweep(p, true, false, 1, fst, pbatch_out(p, 1, 1), &ctl->dctr[1], psum, gwarp, nwarps, lane);
+    pbatch_sweep(p, true, 1, fst, pbatch_out(p, 1, 1), &ctl->dctr[1], psum, gwarp, nwarps, lane);
     if (lane == 0 && psum) atomicAdd(&ctl->pcount[1], psum);
     psum = 0;
     if (!grid_sync(bar, flags, p.barrier_ns)) return;
@@ -933,12 +961,14 @@ __global__ void __launch_bounds__(kPprBatchThreads, 3) ppr_batch_persistent(cons
         }
         const bool pull = P > p.pull_min;  // grid-uniform
         if (pull) {
-            // Pull round, phase A: gather and sum the messages per target.
+            // Pull round, phase A: gather and sum the messages per target, and apply the
+            // targets whose in-edges lie in one tile.
             if (gtid == 0) {
                 pushes += (long long)P;
                 steps += T;
             }
-            pbatch_pull(p, buf, &ctl->tilectr[cur % 3], lane, bad);
+            touched += pbatch_pull(p, buf, ob, &ctl->tilectr[cur % 3], fst, pbatch_out(p, ob, nslot),
+                                   &ctl->dctr[nslot], psum, lane, bad);
         } else {
             // Push round, phase A: push along the frontier's edges (owner runs, as in the
             // SSSP batch): red.add of the FP64 message per active lane, red.or of the
@@ -1058,8 +1088,8 @@ __global__ void __launch_bounds__(kPprBatchThreads, 3) ppr_batch_persistent(cons
         // The frontier just consumed leaves the pull lookup.
         for (unsigned j = gtid; j < F; j += nthreads) p.amask[buf][ldcg(p.q[buf] + j).x] = 0u;
         // Phase B: apply the messages of the touched pairs and activate.
-        touched += pbatch_sweep(p, false, pull, ob, fst, pbatch_out(p, ob, nslot), &ctl->dctr[nslot], psum, gwarp,
-                                nwarps, lane);
+        touched += pbatch_sweep(p, false, ob, fst, pbatch_out(p, ob, nslot), &ctl->dctr[nslot], psum, gwarp, nwarps,
+                                lane);
         if (lane == 0 && psum) atomicAdd(&ctl->pcount[nslot], psum);
         psum = 0;
         if (!grid_sync(bar, flags, p.barrier_ns)) return;
