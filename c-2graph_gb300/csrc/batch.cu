@@ -946,6 +946,10 @@ __global__ void __launch_bounds__(kPprBatchThreads, 3) ppr_batch_persistent(cons
             if (((unsigned)dv.y >> lane) & 1u) p.res[off] = 0.0;
         }
         if (F == 0) break;
+        const bool pull = P > p.pull_min;  // grid-uniform
+        // A pull round applies targets while it pulls: the pops above (residuals) and the
+        // dangling list they read (which the applies refill) must be done first.
+        if (pull && D > 0 && !grid_sync(bar, flags, p.barrier_ns)) return;
         if (F > p.qcap || ((T + (1u << kBatchTileLog) - 1u) >> kBatchTileLog) > p.mark_cap) {
             if (gtid == 0) atomicOr(flags, C2G_FLAG_BOUNDS);
             break;
@@ -959,7 +963,6 @@ __global__ void __launch_bounds__(kPprBatchThreads, 3) ppr_batch_persistent(cons
             ctl->popped += F;
             ctl->relaxed += T;
         }
-        const bool pull = P > p.pull_min;  // grid-uniform
         if (pull) {
             // Pull round, phase A: gather and sum the messages per target, and apply the
             // targets whose in-edges lie in one tile.
