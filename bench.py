@@ -258,13 +258,15 @@ def run_ours(args, rank, world, local_rank):
 
     # The plain per-query GPU path on a sample of the same mix (same kernels' single-
     # query form): the batched-vs-per-query ratio of the metric.
-    pq_s = pq_p = 0.0
+    pq_s = pq_p = pq_sb = pq_pb = 0.0
     for s in ssrc[: args.per_query_sample]:
         _, st = gs.sssp(int(s), seeds=True, mode=c2g.SEEDS_EXACT, out_ptr=dist_d.data_ptr())
         pq_s += st.device_ms
+        pq_sb += st.alg_bytes
     for s in psrc[: max(1, args.per_query_sample // 2)]:
         _, _, st = gp.ppr(int(s), prm, pr_ptr=pr_d.data_ptr())
         pq_p += st.device_ms
+        pq_pb += st.alg_bytes
     ms_sssp_pq = pq_s / args.per_query_sample
     ms_ppr_pq = pq_p / max(1, args.per_query_sample // 2)
     per_query_qps = q_step / ((nS * ms_sssp_pq + nP * ms_ppr_pq) / 1000.0)
@@ -327,6 +329,11 @@ def run_ours(args, rank, world, local_rank):
                 "batched_vs_per_query": value / per_query_qps,
                 "per_query_qps": per_query_qps,
                 "per_query_sssp_ms": ms_sssp_pq, "per_query_ppr_ms": ms_ppr_pq,
+                # single-query relaxation against the HBM roofline (algorithmic bytes / time)
+                "per_query_sssp_alg_gbs": pq_sb / (pq_s / 1000.0) / 1e9 if pq_s else None,
+                "per_query_sssp_roofline_frac": pq_sb / (pq_s / 1000.0) / 1e9 / peak if pq_s else None,
+                "per_query_ppr_alg_gbs": pq_pb / (pq_p / 1000.0) / 1e9 if pq_p else None,
+                "per_query_ppr_roofline_frac": pq_pb / (pq_p / 1000.0) / 1e9 / peak if pq_p else None,
                 "batched_sssp_ms_per_step": tot["s_ms"] / args.steps,
                 "batched_ppr_ms_per_step": tot["p_ms"] / args.steps,
                 "sssp_batched_gteps_graph500": gteps_batched,
