@@ -323,6 +323,45 @@ __global__ void batch_transpose(const int* __restrict__ dist, int V, int Q, int 
     }
 }
 
+// [V][Q] state -> query-major [nq][V] output through a 32 x 32 shared-memory tile: the
+// reads cover one 128-byte line of 32 queries per vertex, the writes 32 consecutive
+// vertices per query, both coalesced.  (Element-wise, consecutive threads would read with
+// a stride of one vertex row.)  Block 32 x 8; grid (V / 32, nq / 32), rounded up.
+template <typename S, typename D>
+__global__ void __launch_bounds__(256) batch_transpose_qmajor(const S* __restrict__ src, int V, int Q, int nq,
+                                                             D* __restrict__ out) {
+    __shared__ D tile[32][33];
+    const int v0 = (int)blockIdx.x * 32, q0 = (int)blockIdx.y * 32;
+    for (int k = (int)threadIdx.y; k < 32; k += 8) {
+        const int v = v0 + k, q = q0 + (int)threadIdx.x;
+        if (v < V && q < nq) tile[k][threadIdx.x] = (D)src[(size_t)v * (size_t)Q + (size_t)q];
+    }
+    __syncthreads();
+    for (int k = (int)threadIdx.y; k < 32; k += 8) {
+        const int q = q0 + k, v = v0 + (int)threadIdx.x;
+        if (q < nq && v < V) out[(size_t)q * (size_t)V + (size_t)v] = tile[threadIdx.x][k];
+    }
+}
+
+// A host output buffer the kernels can write directly: page-locked host memory has a
+// device address (over NVLink-C2C on Grace machines), so the results skip the device
+// staging copy and the separate device-to-host copy.  nullptr for pageable memory.
+static void* mapped_host(void* p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();  // clear the error state of the query
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
+template <typename S, typename D>
+static void launch_transpose_qmajor(const S* src, int V, int Q, int nq, D* out, cudaStream_t st) {
+    if (V <= 0 || nq <= 0) return;
+    const dim3 grid((unsigned)((V + 31) / 32), (unsigned)((nq + 31) / 32));
+    batch_transpose_qmajor<S, D><<<grid, dim3(32, 8), 0, st>>>(src, V, Q, nq, out);
+}
+
 // ---------------------------------------------------------------------------------------
 // host side
 
@@ -457,15 +496,21 @@ int sssp_batch_launch(c2g_graph* g, int32_t nq, const int32_t* sources, const st
     C2G_CUDA(cudaLaunchCooperativeKernel((const void*)sssp_batch_persistent, dim3(blocks), dim3(kSsspBatchThreads),
                                          args, 0, g->stream));
     C2G_CUDA(cudaEventRecord(g->ev1, g->stream));
-    // Results in the caller's layout.
+    // Results in the caller's layout (pinned host memory is written directly).
     int* dst = out;
-    if (!out_on_device) {
+    int* direct = out_on_device ? nullptr : static_cast<int*>(mapped_host(out));
+    if (direct) {
+        dst = direct;
+    } else if (!out_on_device) {
         if (!w->stage) C2G_CUDA(cudaMalloc(&w->stage, sizeof(int) * (size_t)g->V * (size_t)Q));
         dst = w->stage;
     }
-    batch_transpose<<<g->num_sms * 8, 256, 0, g->stream>>>(w->dist, g->V, Q, nq, dst, query_major);
+    if (query_major)
+        launch_transpose_qmajor<int, int>(w->dist, g->V, Q, nq, dst, g->stream);
+    else
+        batch_transpose<<<g->num_sms * 8, 256, 0, g->stream>>>(w->dist, g->V, Q, nq, dst, query_major);
     cudaError_t e = cudaGetLastError();
-    if (e == cudaSuccess && !out_on_device)
+    if (e == cudaSuccess && !out_on_device && !direct)
         e = cudaMemcpyAsync(out, dst, sizeof(int) * (size_t)g->V * (size_t)nq, cudaMemcpyDeviceToHost, g->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(ctl_out, w->ctl, sizeof(TraversalCtl), cudaMemcpyDeviceToHost, g->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(counters, w->counters, sizeof(long long) * 2, cudaMemcpyDeviceToHost, g->stream);
@@ -1357,17 +1402,26 @@ int ppr_batch_launch(c2g_graph* g, int32_t nq, const int32_t* sources, const c2g
     for (int k = 0; k < 2 && e == cudaSuccess; ++k) {
         if (!outs[k]) continue;
         float* dst = outs[k];
-        if (!on_device) {
+        float* direct = on_device ? nullptr : static_cast<float*>(mapped_host(outs[k]));
+        if (direct) {
+            dst = direct;
+        } else if (!on_device) {
             if (!w->stage) e = cudaMalloc(&w->stage, sizeof(float) * VQ);
             dst = w->stage;
         }
         if (e != cudaSuccess) break;
         if (k == 0)
-            batch_transpose_f<<<g->num_sms * 8, 256, 0, g->stream>>>(w->pr, g->V, p.Q, nq, dst, query_major);
+            if (query_major)
+                launch_transpose_qmajor<float, float>(w->pr, g->V, p.Q, nq, dst, g->stream);
+            else
+                batch_transpose_f<<<g->num_sms * 8, 256, 0, g->stream>>>(w->pr, g->V, p.Q, nq, dst, query_major);
         else
-            batch_transpose_d2f<<<g->num_sms * 8, 256, 0, g->stream>>>(w->res, g->V, p.Q, nq, dst, query_major);
+            if (query_major)
+                launch_transpose_qmajor<double, float>(w->res, g->V, p.Q, nq, dst, g->stream);
+            else
+                batch_transpose_d2f<<<g->num_sms * 8, 256, 0, g->stream>>>(w->res, g->V, p.Q, nq, dst, query_major);
         e = cudaGetLastError();
-        if (e == cudaSuccess && !on_device)
+        if (e == cudaSuccess && !on_device && !direct)
             e = cudaMemcpyAsync(outs[k], dst, sizeof(float) * (size_t)g->V * (size_t)nq, cudaMemcpyDeviceToHost,
                                 g->stream);
     }

@@ -237,3 +237,32 @@ def test_ppr_batch_pull_cap_and_heavy_weights(gpu_available, g14p):
             scale = max(1.0, float(np.abs(rp).sum()))
             assert _l1(pr[i], rp) <= 1e-6 * scale, (i, _l1(pr[i], rp), scale)
             assert _l1(res[i], rr) <= 1e-6 * max(1.0, float(np.abs(rr).sum())), i
+
+
+def test_batch_outputs_into_pinned_host_memory(gpu_available, g16):
+    """Page-locked host outputs are written by the kernels directly; pageable ones go
+    through a device stage and a copy.  Both give the same arrays, in both layouts."""
+    import ctypes
+
+    import torch
+
+    import c2g
+
+    with c2g.Graph.load(g16, "origin") as gr:
+        src = _sources(np.fromfile(g16 + "/origin/vlist.bin", dtype=np.int32), 45, 21)
+        for vm in (False, True):
+            ref, _ = gr.sssp_batch(src, vertex_major=vm)
+            pinned = torch.empty(ref.shape, dtype=torch.int32).pin_memory().numpy()
+            pinned.fill(-7)
+            got, st = gr.sssp_batch(src, out=pinned, vertex_major=vm)
+            assert st.status_flags == 0 and np.array_equal(pinned, ref), vm
+        prm = gr.ppr_params(alpha=0.15, rmax=1e-6, seeded=0, pr0=0.15, r0=1.0)
+        pr_ref, _, _ = gr.ppr_batch(src, prm, want_res=False)
+        pinned = torch.empty(pr_ref.shape, dtype=torch.float32).pin_memory().numpy()
+        pinned.fill(-1.0)
+        st = c2g.Stats()
+        s = np.ascontiguousarray(src, dtype=np.int32)
+        c2g._check(c2g.lib().c2g_ppr_batch(gr._h, len(s), c2g._ptr(s), ctypes.byref(prm), c2g._ptr(pinned), None,
+                                           0, 0, ctypes.byref(st)))
+        assert st.status_flags == 0
+        assert np.abs(pinned.astype(np.float64) - pr_ref).sum(axis=1).max() <= 1e-9
