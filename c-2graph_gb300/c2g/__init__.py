@@ -107,6 +107,8 @@ SIGNATURES = {
                                ctypes.POINTER(Stats)]),
     "c2g_ppr_set_config": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int32]),
     "c2g_ppr_batch_set_pull": (ctypes.c_int, [_P, ctypes.c_float]),
+    "c2g_ppr_batch_autotune": (ctypes.c_int, [_P, ctypes.c_int32, _P, ctypes.POINTER(PprParams), ctypes.c_int32,
+                                              ctypes.c_char_p, _P]),
     "c2g_graph_set_watchdog": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int32]),
     "c2g_graph_last_phases": (ctypes.c_int, [_P, _P]),
     "c2g_ppr_default_params": (ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(PprParams)]),
@@ -304,6 +306,14 @@ class Graph:
         """Batched rounds with more than ratio * E pushes pull over the reverse CSR
         (ratio < 0: push only; 0: every round)."""
         _check(lib().c2g_ppr_batch_set_pull(self._h, float(ratio)))
+
+    def ppr_batch_autotune(self, sources, params, reps=1, json_path=None):
+        """Time the pull ratios on this batch, apply the fastest valid one and return it."""
+        src = np.ascontiguousarray(sources, dtype=np.int32)
+        best = ctypes.c_float(0.0)
+        _check(lib().c2g_ppr_batch_autotune(self._h, len(src), _ptr(src), ctypes.byref(params), int(reps),
+                                            json_path.encode() if json_path else None, ctypes.byref(best)))
+        return float(best.value)
 
     def ppr_params(self, adsorption=False, **kw):
         p = PprParams()

@@ -6,10 +6,13 @@
 // distances differ from the first candidate's is rejected (all must be the same
 // fixed point).  The winner is applied to the handle and, when a path is given, written
 // as a JSON record of every timing.
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <string>
 #include <vector>
+
+#include <cuda_runtime.h>
 
 #include "../../include/c2graph.h"
 #include "host_io.h"
@@ -70,5 +73,89 @@ extern "C" int c2g_sssp_autotune(c2g_graph* g, int32_t n, const int32_t* sources
     }
     if (best_delta) *best_delta = bd;
     if (best_tile) *best_tile = bt;
+    return C2G_OK;
+}
+
+// Autotuner of the batched push's round shape: the push-count ratio above which a round
+// pulls over the reverse CSR (c2g_ppr_batch_set_pull).  The best ratio depends on how
+// dense the batch's rounds get (queries, graph, rmax), so c2g_ppr_batch_autotune times
+// each candidate on the caller's batch (one warm-up launch, then `reps` timed ones; the
+// batch kernel's device time).  The first candidate is push only; a candidate whose pr
+// differs from it by more than the parity bar (L1 1e-6 per query, on the first 8
+// queries) is rejected.  The winner is applied to the handle and, when a path is given,
+// written as a JSON record of every timing.
+extern "C" int c2g_ppr_batch_autotune(c2g_graph* g, int32_t n, const int32_t* sources,
+                                      const c2g_ppr_params* params, int32_t reps, const char* json_path,
+                                      float* best_ratio) {
+    using namespace c2g;
+    if (!g || !sources || !params || n < 1) return fail(C2G_ERR_ARG, "autotune: need a batch of sources");
+    if (reps < 1) reps = 1;
+    const float ratios[] = {-1.f, 1.f, 2.f, 4.f, 8.f, 16.f, 32.f};
+    const size_t V = (size_t)g->V, rows = (size_t)(n < 8 ? n : 8);
+    float* dpr = nullptr;
+    {
+        int prev = -1;
+        cudaGetDevice(&prev);
+        cudaSetDevice(g->device);
+        const cudaError_t e = cudaMalloc(&dpr, sizeof(float) * V * (size_t)n);
+        if (prev >= 0) cudaSetDevice(prev);
+        if (e != cudaSuccess) return fail(C2G_ERR_CUDA, "autotune: %s", cudaGetErrorString(e));
+    }
+    std::vector<float> ref(rows * V), got(rows * V);
+    const float saved = g->ppr_cfg.batch_pull_ratio;
+    double best_ms = 1e300;
+    float best = saved;
+    std::string json = "{\"candidates\": [";
+    int rc = C2G_OK;
+    bool first = true;
+    for (float r : ratios) {
+        if ((rc = c2g_ppr_batch_set_pull(g, r))) break;
+        c2g_stats st;
+        double ms = 0.0;
+        for (int k = 0; k <= reps && !rc; ++k) {
+            rc = c2g_ppr_batch(g, n, sources, params, dpr, nullptr, 1, C2G_LAYOUT_QUERY_MAJOR, &st);
+            if (k > 0) ms += st.device_ms;
+        }
+        if (rc) break;
+        ms /= reps;
+        float* dst = first ? ref.data() : got.data();
+        if (cudaMemcpy(dst, dpr, sizeof(float) * rows * V, cudaMemcpyDeviceToHost) != cudaSuccess) {
+            rc = fail(C2G_ERR_CUDA, "autotune: copying results failed");
+            break;
+        }
+        double worst = 0.0;
+        if (!first)
+            for (size_t q = 0; q < rows; ++q) {
+                double l1 = 0.0;
+                for (size_t v = 0; v < V; ++v) l1 += std::fabs((double)got[q * V + v] - (double)ref[q * V + v]);
+                worst = l1 > worst ? l1 : worst;
+            }
+        const bool valid = worst <= 1e-6 && st.status_flags == 0;
+        char buf[192];
+        snprintf(buf, sizeof(buf), "%s{\"ratio\": %g, \"ms_per_batch\": %.3f, \"l1_vs_push\": %.3g, \"valid\": %s}",
+                 first ? "" : ", ", (double)r, ms, worst, valid ? "true" : "false");
+        json += buf;
+        if (valid && ms < best_ms) {
+            best_ms = ms;
+            best = r;
+        }
+        first = false;
+    }
+    cudaFree(dpr);
+    if (rc) {
+        c2g_ppr_batch_set_pull(g, saved);
+        return rc;
+    }
+    char tail[128];
+    snprintf(tail, sizeof(tail), "], \"best\": {\"ratio\": %g, \"ms_per_batch\": %.3f}}\n", (double)best, best_ms);
+    json += tail;
+    if ((rc = c2g_ppr_batch_set_pull(g, best))) return rc;
+    if (json_path) {
+        FILE* f = fopen(json_path, "w");
+        if (!f) return fail(C2G_ERR_IO, "cannot write %s", json_path);
+        fputs(json.c_str(), f);
+        fclose(f);
+    }
+    if (best_ratio) *best_ratio = best;
     return C2G_OK;
 }

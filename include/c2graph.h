@@ -237,6 +237,13 @@ int c2g_ppr_set_config(c2g_graph* g, int32_t pull_div, int32_t dense_div);
  * order. */
 int c2g_ppr_batch_set_pull(c2g_graph* g, float ratio);
 
+/* Autotuner of that round shape: times ratios {push only, 1, 2, 4, 8, 16, 32} on this
+ * batch (one warm-up launch, then `reps` timed), rejects any whose pr differs from the
+ * push-only run by more than L1 1e-6 per query (first 8 queries), applies the fastest
+ * and writes every timing as JSON to json_path (may be NULL). */
+int c2g_ppr_batch_autotune(c2g_graph* g, int32_t n, const int32_t* sources, const c2g_ppr_params* params,
+                           int32_t reps, const char* json_path, float* best_ratio);
+
 /* Reference defaults: PPR (alpha 0.2, rmax 0.001/(V+1), cap 500), and the adsorption
  * program (alpha 0.2, r0 10, pr0 8, rmax 1/V, cap 2000). */
 int c2g_ppr_default_params(const c2g_graph* g, int adsorption, c2g_ppr_params* out);

@@ -266,3 +266,26 @@ def test_batch_outputs_into_pinned_host_memory(gpu_available, g16):
                                            0, 0, ctypes.byref(st)))
         assert st.status_flags == 0
         assert np.abs(pinned.astype(np.float64) - pr_ref).sum(axis=1).max() <= 1e-9
+
+
+def test_ppr_batch_autotune(gpu_available, g14p, tmp_path):
+    """The pull-ratio autotuner times its candidates on the batch, records them, applies
+    a valid one, and the batch under it still matches the FP64 oracle."""
+    import json
+
+    import c2g
+    import oracle
+
+    o = oracle.load_dataset(g14p, "origin")
+    src = _sources(o["vlist"], 64, 12)
+    path = str(tmp_path / "pull.json")
+    with c2g.Graph.load(g14p, "origin") as gr:
+        prm = gr.ppr_params(alpha=0.15, rmax=1e-7, seeded=0, pr0=0.15, r0=1.0)
+        best = gr.ppr_batch_autotune(src, prm, reps=1, json_path=path)
+        rec = json.load(open(path))
+        assert len(rec["candidates"]) == 7 and rec["candidates"][0]["ratio"] == -1
+        assert rec["best"]["ratio"] == best and any(c["ratio"] == best and c["valid"] for c in rec["candidates"])
+        pr, res, st = gr.ppr_batch(src, prm)
+        assert st.status_flags == 0
+        rp, rr, _, _ = oracle.ppr_push(o["vlist"], o["elist"], o["flist"], int(src[5]), 0.15, 1e-7)
+        assert _l1(pr[5], rp) <= 1e-6 and _l1(res[5], rr) <= 1e-6
