@@ -85,20 +85,24 @@ void run_batch(c2g_server* s, int kind, std::vector<Pending>& batch) {
     const int n = (int)batch.size();
     const size_t V = (size_t)g->V;
     std::vector<int> status(n, C2G_OK);
+    std::vector<Clock::time_point> t_done(n);  // when each request's result was complete
     if (kind == C2G_REQ_SSSP) {
         std::vector<int32_t> src(n);
         for (int i = 0; i < n; ++i) src[i] = batch[i].req.source;
-        std::vector<int32_t> out((size_t)n * V);
+        std::vector<int32_t> outv((size_t)n * V);
+        int32_t* out = outv.data();
         c2g_stats st;
-        const int rc = c2g_sssp_batch(g, n, src.data(), 0, C2G_SEEDS_COMPAT, out.data(), 0, C2G_LAYOUT_QUERY_MAJOR, &st);
+        const int rc = c2g_sssp_batch(g, n, src.data(), 0, C2G_SEEDS_COMPAT, out, 0, C2G_LAYOUT_QUERY_MAJOR, &st);
         for (int i = 0; i < n; ++i) {
             status[i] = rc;
-            if (!rc && batch[i].req.out) std::memcpy(batch[i].req.out, out.data() + (size_t)i * V, sizeof(int32_t) * V);
+            if (!rc && batch[i].req.out) std::memcpy(batch[i].req.out, out + (size_t)i * V, sizeof(int32_t) * V);
         }
+        std::fill(t_done.begin(), t_done.end(), Clock::now());
     } else if (kind == C2G_REQ_PPR) {
         std::vector<int32_t> src(n);
         for (int i = 0; i < n; ++i) src[i] = batch[i].req.source;
-        std::vector<float> pr((size_t)n * V);
+        std::vector<float> prv((size_t)n * V);
+        float* pr = prv.data();
         c2g_ppr_params p;
         c2g_ppr_default_params(g, 0, &p);
         p.alpha = s->cfg.alpha;
@@ -107,25 +111,39 @@ void run_batch(c2g_server* s, int kind, std::vector<Pending>& batch) {
         p.pr0 = s->cfg.alpha;
         p.seeded = 0;
         c2g_stats st;
-        const int rc = c2g_ppr_batch(g, n, src.data(), &p, pr.data(), nullptr, 0, C2G_LAYOUT_QUERY_MAJOR, &st);
+        const int rc = c2g_ppr_batch(g, n, src.data(), &p, pr, nullptr, 0, C2G_LAYOUT_QUERY_MAJOR, &st);
         for (int i = 0; i < n; ++i) {
             status[i] = rc;
-            if (!rc && batch[i].req.out) std::memcpy(batch[i].req.out, pr.data() + (size_t)i * V, sizeof(float) * V);
+            if (!rc && batch[i].req.out) std::memcpy(batch[i].req.out, pr + (size_t)i * V, sizeof(float) * V);
         }
+        std::fill(t_done.begin(), t_done.end(), Clock::now());
     } else {
+        // Label propagation runs request by request: each result is published as soon as
+        // it is complete, so a waiter does not wait for the rest of the batch.
         std::vector<float> Y(V * 16);
         for (int i = 0; i < n; ++i) {
             c2g_stats st;
             const int rc = c2g_adsorption(g, 16, batch[i].seeds.data(), s->p_inj.data(), s->p_cont.data(),
                                           s->p_abnd.data(), s->cfg.ads_iterations,
                                           batch[i].req.out ? static_cast<float*>(batch[i].req.out) : Y.data(), 0, &st);
-            status[i] = rc;
+            const auto ti = Clock::now();
+            std::lock_guard<std::mutex> lk(s->mu);
+            const double ms = std::chrono::duration<double, std::milli>(ti - batch[i].t_submit).count();
+            s->done[batch[i].ticket] = Done{rc, ms};
+            s->latencies.push_back(ms);
+            s->completed += 1;
+            s->t_last_done = ti;
+            s->cv_done.notify_all();
         }
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->batches[kind] += 1;
+        s->max_batch_seen = std::max<int64_t>(s->max_batch_seen, n);
+        return;
     }
     const auto t = Clock::now();
     std::lock_guard<std::mutex> lk(s->mu);
     for (int i = 0; i < n; ++i) {
-        const double ms = std::chrono::duration<double, std::milli>(t - batch[i].t_submit).count();
+        const double ms = std::chrono::duration<double, std::milli>(t_done[i] - batch[i].t_submit).count();
         s->done[batch[i].ticket] = Done{status[i], ms};
         s->latencies.push_back(ms);
     }
