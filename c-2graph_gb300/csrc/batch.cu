@@ -543,7 +543,7 @@ struct PprBatchParams {
     int logW, Q, nq;
     float* pr;        // [V][Q]
     double* res;      // [V][Q] FP64 residuals (see ppr.cu: threshold decisions)
-    double* msg;      // [V][Q], zero between launches (pull rounds: 64-bit integer parts)
+    double* msg;      // [V][Q], zero between launches (pull rounds: parts of tile-straddling targets)
     double* rq[2];    // [V][Q] (1-alpha) * residual being pushed, by frontier buffer
     float2* rqf[2];   // the same as a float pair hi + lo (pull rounds)
     unsigned* amask[2];  // [V][W] lanes activated with out-edges, by frontier buffer (pull lookup)
@@ -688,7 +688,7 @@ __device__ __forceinline__ unsigned pbatch_sweep(const PprBatchParams& p, bool f
                 const size_t off = ((size_t)(b + (unsigned)k) << 5) + lane;
                 const bool mine = (ln >> lane) & 1u;
                 r[u] = mine ? ldcg(p.res + off) : 0.0;
-                m[u] = (mine && !force) ? ldcg(p.msg + off) : 0.0;  // fixed: the integer sum's bits
+                m[u] = (mine && !force) ? ldcg(p.msg + off) : 0.0;
                 pv[u] = (mine && !force) ? ldcg(p.pr + off) : 0.f;
             }
 #pragma unroll
