@@ -287,7 +287,7 @@ def run_ours(args, rank, world, local_rank):
     # DRAM bytes (read + write) per launch from a one-pass ncu capture of this step at full
     # size (profiles/launches_bench_default_rmat-s22-ef16_256sssp-256ppr.md), expressed per
     # unit processed and scaled to this run's average launch.
-    traffic_per_unit = {"p": 3.0350e12 / 371.88e9, "s": 315.75e9 / 61.13e9}[dominant]
+    traffic_per_unit = {"p": 3.0992e12 / 371.88e9, "s": 326.22e9 / 61.33e9}[dominant]
     units = tot["p_push"] if dominant == "p" else tot["s_rel"]
     traffic = traffic_per_unit * units / args.steps
 
