@@ -54,7 +54,18 @@ struct BatchParams {
     long long* counters;  // [2]: relaxations (query, edge), edge-word steps
 };
 
-constexpr int kBatchTileLog = 9;  // 512 edge-word steps per warp tile (128: 132 ms, 512: 121 ms per 256-source SSSP batch at scale 22)
+// Warp tiles of the expansion: markers are laid every 2^kBatchTileLog edge-word steps; a
+// round with enough work (at least 16 big tiles per warp) walks tiles of 2^kBatchTileBig
+// steps (every 4th marker), a smaller one tiles of 2^kBatchTileLog.  256 sources at
+// scale 22: 132 ms per SSSP batch with 128-step tiles, 121 ms with 512; 32 sources at
+// scale 20: 4.6 ms with 128, 5.4 ms with 512 (too few tiles per warp).
+constexpr int kBatchTileLog = 7;
+constexpr int kBatchTileBig = 9;
+
+__device__ __forceinline__ int batch_tile_log(unsigned T, unsigned nwarps) {
+    return (unsigned long long)T >= ((unsigned long long)nwarps << (kBatchTileBig + 4)) ? kBatchTileBig
+                                                                                         : kBatchTileLog;
+}
 
 __device__ __forceinline__ FrontierOut batch_out(const BatchParams& p, int buf, int slot) {
     FrontierOut o;
@@ -209,15 +220,16 @@ __global__ void __launch_bounds__(kSsspBatchThreads, 3) sssp_batch_persistent(co
         const int2* q = p.q[buf];
         const unsigned* qm = p.qmask[buf];
         const int* mark = p.mark[buf];
-        const unsigned tile = 1u << kBatchTileLog;
-        const unsigned ntiles = (T + tile - 1) >> kBatchTileLog;
+        const int tl = batch_tile_log(T, nwarps);
+        const unsigned tile = 1u << tl;
+        const unsigned ntiles = (T + tile - 1) >> tl;
         unsigned* tctr = &ctl->tilectr[slot];
         unsigned tn = next_tile(tctr, lane);
         for (unsigned t = tn; t < ntiles; t = tn) {
             tn = next_tile(tctr, lane);  // the next tile, fetched while this one runs
-            unsigned e0 = t << kBatchTileLog;
+            unsigned e0 = t << tl;
             const unsigned e1 = min(e0 + tile, T);
-            unsigned o = (unsigned)ldcg(mark + t);
+            unsigned o = (unsigned)ldcg(mark + (t << (tl - kBatchTileLog)));
             while (e0 < e1) {
                 const unsigned j = o + (unsigned)lane;
                 unsigned base = 0x7fffffffu, endv = 0xffffffffu, msk = 0u, rs = 0u;
@@ -1025,15 +1037,16 @@ __global__ void __launch_bounds__(kPprBatchThreads, 3) ppr_batch_persistent(cons
             const unsigned* qm = p.qmask[buf];
             const int* mark = p.mark[buf];
             const double* rqb = p.rq[buf];
-            const unsigned tile = 1u << kBatchTileLog;
-            const unsigned ntiles = (T + tile - 1) >> kBatchTileLog;
+            const int tl = batch_tile_log(T, nwarps);
+            const unsigned tile = 1u << tl;
+            const unsigned ntiles = (T + tile - 1) >> tl;
             unsigned* tctr = &ctl->tilectr[cur % 3];
             unsigned tn = next_tile(tctr, lane);
             for (unsigned t = tn; t < ntiles; t = tn) {
                 tn = next_tile(tctr, lane);  // the next tile, fetched while this one runs
-                unsigned e0 = t << kBatchTileLog;
+                unsigned e0 = t << tl;
                 const unsigned e1 = min(e0 + tile, T);
-                unsigned o = (unsigned)ldcg(mark + t);
+                unsigned o = (unsigned)ldcg(mark + (t << (tl - kBatchTileLog)));
                 while (e0 < e1) {
                     const unsigned j = o + (unsigned)lane;
                     unsigned base = 0x7fffffffu, endv = 0xffffffffu, msk = 0u, rs = 0u;
