@@ -289,3 +289,24 @@ def test_ppr_batch_autotune(gpu_available, g14p, tmp_path):
         assert st.status_flags == 0
         rp, rr, _, _ = oracle.ppr_push(o["vlist"], o["elist"], o["flist"], int(src[5]), 0.15, 1e-7)
         assert _l1(pr[5], rp) <= 1e-6 and _l1(res[5], rr) <= 1e-6
+
+
+@pytest.mark.parametrize("n", [20, 100, 200])
+def test_ppr_batch_pull_word_counts_vs_fp64(gpu_available, g14p, n):
+    """Pull every round with 1, 4 and 8 query words per vertex (scalar and vector mask
+    loads, one or two word groups per tile): each checked query within L1 <= 1e-6 of the
+    FP64 oracle."""
+    import c2g
+    import oracle
+
+    o = oracle.load_dataset(g14p, "origin")
+    src = _sources(o["vlist"], n, 300 + n)
+    with c2g.Graph.load(g14p, "origin") as gr:
+        gr.ppr_batch_pull(0.0)
+        prm = gr.ppr_params(alpha=0.15, rmax=1e-7, seeded=0, pr0=0.15, r0=1.0)
+        pr, res, st = gr.ppr_batch(src, prm)
+        assert st.status_flags == 0
+        for i in sorted({0, n // 3, n // 2, n - 1}):
+            rp, rr, _, _ = oracle.ppr_push(o["vlist"], o["elist"], o["flist"], int(src[i]), 0.15, 1e-7)
+            assert _l1(pr[i], rp) <= 1e-6, (n, i, _l1(pr[i], rp))
+            assert _l1(res[i], rr) <= 1e-6, (n, i)
