@@ -129,6 +129,9 @@ SIGNATURES = {
     "c2g_rmat_write": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, ctypes.c_uint64,
                                       ctypes.c_int32, ctypes.c_int32, ctypes.c_double, ctypes.c_double,
                                       ctypes.c_double]),
+    "c2g_rmat_write_gpu": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, ctypes.c_uint64,
+                                          ctypes.c_int32, ctypes.c_int32, ctypes.c_double, ctypes.c_double,
+                                          ctypes.c_double, ctypes.c_int]),
     "c2g_prune_sssp": (ctypes.c_int, [ctypes.c_char_p]),
     "c2g_prune_ppr": (ctypes.c_int, [ctypes.c_char_p]),
     "c2g_prune_ppr_alpha": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_double]),
@@ -168,8 +171,12 @@ def device_count():
     return n.value
 
 
-def rmat_write(dir, scale, edge_factor, seed, wmin=1, wmax=100, a=0.57, b=0.19, c=0.19):
-    _check(lib().c2g_rmat_write(os.fsencode(dir), scale, edge_factor, seed, wmin, wmax, a, b, c))
+def rmat_write(dir, scale, edge_factor, seed, wmin=1, wmax=100, a=0.57, b=0.19, c=0.19, gpu=False, device=0):
+    """Seeded R-MAT graph in the origin/ layout; gpu=True builds it on the device (same bytes)."""
+    if gpu:
+        _check(lib().c2g_rmat_write_gpu(os.fsencode(dir), scale, edge_factor, seed, wmin, wmax, a, b, c, device))
+    else:
+        _check(lib().c2g_rmat_write(os.fsencode(dir), scale, edge_factor, seed, wmin, wmax, a, b, c))
 
 
 def prune_sssp(dir):

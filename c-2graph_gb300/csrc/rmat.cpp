@@ -15,26 +15,11 @@
 
 #include "../../include/c2graph.h"
 #include "host_io.h"
+#include "rmat.h"
+#include "rmat_draw.h"
 
 namespace c2g {
 
-static inline uint64_t mix64(uint64_t x) {
-    x += 0x9e3779b97f4a7c15ULL;
-    x = (x ^ (x >> 30)) * 0xbf58476d1ce4e5b9ULL;
-    x = (x ^ (x >> 27)) * 0x94d049bb133111ebULL;
-    return x ^ (x >> 31);
-}
-
-// Keyed counter-based draw: stream separates edge endpoints, weights and flist.
-static inline uint64_t draw(uint64_t seed, uint64_t stream, uint64_t index, uint64_t k) {
-    return mix64(mix64(seed ^ (stream * 0xd1342543de82ef95ULL)) + index * 0x9e3779b97f4a7c15ULL + k);
-}
-
-struct RmatGraph {
-    int64_t V = 0;
-    std::vector<int32_t> row, col, wgt;
-    std::vector<float> fw;
-};
 
 // Generate an R-MAT graph in memory.
 int rmat_build(int scale, int edge_factor, uint64_t seed, int32_t wmin, int32_t wmax, double a,
@@ -56,21 +41,7 @@ int rmat_build(int scale, int edge_factor, uint64_t seed, int32_t wmin, int32_t 
 #pragma omp parallel for schedule(static)
     for (int64_t i = 0; i < M; ++i) {
         uint64_t s = 0, d = 0;
-        uint64_t r = 0;
-        for (int lvl = 0; lvl < scale; ++lvl) {
-            if ((lvl & 1) == 0) r = draw(seed, 1, (uint64_t)i, (uint64_t)(lvl >> 1));
-            uint64_t q = (lvl & 1) ? (r >> 32) : (r & 0xffffffffULL);
-            const int bit = scale - 1 - lvl;
-            if (q < ta) {
-            } else if (q < tb) {
-                d |= uint64_t(1) << bit;
-            } else if (q < tc) {
-                s |= uint64_t(1) << bit;
-            } else {
-                s |= uint64_t(1) << bit;
-                d |= uint64_t(1) << bit;
-            }
-        }
+        rmat_endpoints(seed, (uint64_t)i, scale, ta, tb, tc, &s, &d);
         src[i] = (int32_t)s;
         dst[i] = (int32_t)d;
     }
@@ -113,9 +84,8 @@ int rmat_build(int scale, int edge_factor, uint64_t seed, int32_t wmin, int32_t 
     for (int64_t v = 0; v < V; ++v) {
         double sum = 0.0;
         for (int64_t e = g.row[v]; e < g.row[v + 1]; ++e) {
-            g.wgt[e] = (int32_t)((int64_t)wmin + (int64_t)(draw(seed, 2, (uint64_t)e, 0) % range));
-            // uniform(0,1) with 24 random bits: exactly representable as float.
-            const float u = (float)(((double)(draw(seed, 3, (uint64_t)e, 0) >> 40) + 0.5) / 16777216.0);
+            g.wgt[e] = rmat_weight(seed, (uint64_t)e, wmin, range);
+            const float u = rmat_fvalue(seed, (uint64_t)e);
             g.fw[e] = u;
             sum += (double)u;
         }

@@ -334,6 +334,11 @@ int c2g_server_destroy(c2g_server* s);
 int c2g_rmat_write(const char* dir, int scale, int edge_factor, uint64_t seed,
                    int32_t wmin, int32_t wmax, double a, double b, double c);
 
+/* The same graph generated on GPU `device` (endpoint draws, sort and dedup, weights on the
+ * device; the files are byte-identical to c2g_rmat_write's). */
+int c2g_rmat_write_gpu(const char* dir, int scale, int edge_factor, uint64_t seed, int32_t wmin, int32_t wmax,
+                       double a, double b, double c, int device);
+
 /* C^2graph-P pruners.  Byte-identical outputs to purn-sssp (src/purn-sssp.cpp:61-352)
  * and purn-ppr (src/purn-ppr.cpp:63-344); purn-sssp additionally writes the
  * record->vertex sidecar <dir>/sssp/hvmap.bin. */

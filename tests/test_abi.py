@@ -63,6 +63,7 @@ def test_bad_variant_and_args(built, tmp_path):
     prm = c2g.PprParams()
     assert c2g.lib().c2g_ppr_batch_autotune(None, 4, c2g._ptr(src), ctypes.byref(prm), 1, None, None) == c2g.ERR_ARG
     assert c2g.lib().c2g_sssp_autotune(None, 4, c2g._ptr(src), 0, 0, None, None, None) == c2g.ERR_ARG
+    assert c2g.lib().c2g_rmat_write_gpu(None, 10, 8, 1, 1, 10, 0.57, 0.19, 0.19, 0) == c2g.ERR_ARG
 
 
 def test_corrupt_dataset_is_format_error(built, tmp_path):
