@@ -228,7 +228,8 @@ int c2g_ppr_batch(c2g_graph* g, int32_t n, const int32_t* sources, const c2g_ppr
  * the same BSP rounds either way. */
 int c2g_ppr_set_config(c2g_graph* g, int32_t pull_div, int32_t dense_div);
 
-/* Round shapes of the batched push (c2g_ppr_batch).  A round whose frontier makes more
+/* Round shapes of the batched push (c2g_ppr_batch; no counterpart in the reference, which
+ * runs one query per launch).  A round whose frontier makes more
  * than ratio * E (query, edge) pushes pulls over the reverse CSR (built on first use):
  * each target gathers its in-neighbours' pushed residuals and sums the messages as FP32
  * pairs (about 47 bits of relative precision) before they meet the FP64 residual.
@@ -237,7 +238,7 @@ int c2g_ppr_set_config(c2g_graph* g, int32_t pull_div, int32_t dense_div);
  * order. */
 int c2g_ppr_batch_set_pull(c2g_graph* g, float ratio);
 
-/* Autotuner of that round shape: times ratios {push only, 1, 2, 4, 8, 16, 32} on this
+/* Autotuner of that round shape (no counterpart in the reference): times ratios {push only, 1, 2, 4, 8, 16, 32} on this
  * batch (one warm-up launch, then `reps` timed), rejects any whose pr differs from the
  * push-only run by more than L1 1e-6 per query (first 8 queries), applies the fastest
  * and writes every timing as JSON to json_path (may be NULL). */
@@ -335,7 +336,8 @@ int c2g_rmat_write(const char* dir, int scale, int edge_factor, uint64_t seed,
                    int32_t wmin, int32_t wmax, double a, double b, double c);
 
 /* The same graph generated on GPU `device` (endpoint draws, sort and dedup, weights on the
- * device; the files are byte-identical to c2g_rmat_write's). */
+ * device; the files are byte-identical to c2g_rmat_write's).  Like c2g_rmat_write it
+ * stands in for the reference's text converter (utils/convert2binary.cpp:10-114). */
 int c2g_rmat_write_gpu(const char* dir, int scale, int edge_factor, uint64_t seed, int32_t wmin, int32_t wmax,
                        double a, double b, double c, int device);
 
