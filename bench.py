@@ -115,60 +115,109 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def make_dataset(d, scale, ef, seed):
-    import c2g
-
+def make_dataset(tools, d, scale, ef, seed):
+    """The step's inputs in <d>: the R-MAT graph (int32 weights in [1, 1000], flist),
+    pruned by purn-sssp and by purn-ppr for the step's alpha (folded edges carry
+    1 - alpha).  `tools` is the library (c2g) for our arm and the oracle's restatement for
+    the reference arm; both write the same bytes (tests/test_oracle_golden.py)."""
     t0 = time.time()
-    c2g.rmat_write(d, scale, ef, seed, 1, 1000)
+    tools.rmat_write(d, scale, ef, seed, 1, 1000)
     t1 = time.time()
-    c2g.prune_sssp(d)
-    c2g.prune_ppr(d)
+    tools.prune_sssp(d)
+    tools.prune_ppr(d, alpha=ALPHA)
     return t1 - t0, time.time() - t1
 
 
-def pick_sources(vlist, n_each, seed=2024):
-    """Config-3 selection: half uniform over vertices with out-edges, half from the top
-    1% out-degree vertices."""
-    from c2g import replicas
+def workload_sources(vlist, n, seed):
+    """The batched configuration's selection: half uniform over vertices with out-edges,
+    half from the top 1% out-degree vertices (seeded; SSSP seed 2024, PPR 2025, plus the
+    rank under torchrun).  The same rule as c2g.replicas.pick_sources, restated here so
+    the reference arm needs nothing from the library."""
+    deg = np.diff(vlist)
+    rng = np.random.default_rng(seed)
+    cand = np.flatnonzero(deg > 0)
+    top = np.argsort(-deg, kind="stable")[:max(1, len(deg) // 100)]
+    top = top[deg[top] > 0]
+    half = n // 2
+    out = np.concatenate([rng.choice(cand, n - half, replace=len(cand) < n - half),
+                          rng.choice(top, half, replace=len(top) < half)])
+    return out.astype(np.int32)
 
-    return replicas.pick_sources(vlist, n_each, seed)
+
+def step_config(args, V, e_sssp, e_ppr, nS, nP, world):
+    return {"workload": "rmat-s%d-ef%d pruned, batched multi-tenant mix: %d SSSP + %d PPR sources per step"
+                        % (args.scale, args.edge_factor, nS, nP),
+            "vertices": V, "edges_sssp": e_sssp, "edges_ppr": e_ppr,
+            "sssp": "sssp-purn on sssp/, each source's own record as seeds (EXACT), int32 distances",
+            "ppr": "ppr-purn on ppr/ pruned for alpha %.2f, seeded first hop, alpha %.2f, rmax %g" % (ALPHA, ALPHA,
+                                                                                                  RMAX),
+            "alpha": ALPHA, "rmax": RMAX,
+            "sources": "half uniform over vertices with out-edges, half from the top 1% out-degree",
+            "l2": "graph and state larger than L2 (no flush needed)",
+            "parallelism": "replicas (query-sharded)" if world > 1 else "single GPU"}
+
+
+def step_ppr_params(g):
+    """The step's PPR parameters: alpha 0.15, rmax 1e-7, seeded first hop (ppr-purn),
+    the reference's 500-round cap."""
+    return g.ppr_params(alpha=ALPHA, rmax=RMAX, seeded=1, max_iter=500)
+
+
+def cpu_queries(s_ds, p_ds, ssrc, psrc, threads):
+    """The reference's CPU implementation of the step's queries (oracle restatement):
+    the reference CPU Bellman-Ford from each SSSP source and its record seeds on sssp/,
+    and the BSP push in FP32 from each PPR source's first hop on ppr/; one query per
+    host thread.  s_ds / p_ds are the sssp/ and ppr/ arrays (oracle.load_dataset).
+    Returns the elapsed seconds."""
+    import oracle
+
+    ss, ps = oracle.query_seeds(s_ds, ssrc, "sssp"), oracle.query_seeds(p_ds, psrc, "ppr")
+    t0 = time.time()
+    oracle.batch("sssp", s_ds["vlist"], s_ds["elist"], s_ds["wlist"], None, ssrc, threads=threads, seeds=ss)
+    oracle.batch("ppr", p_ds["vlist"], p_ds["elist"], None, p_ds["wlist"], psrc, alpha=ALPHA, rmax=RMAX,
+                 max_iter=500, threads=threads, seeds=ps)
+    return time.time() - t0
 
 
 def run_reference(args, rank, world):
-    """CPU arm: the reference's CPU implementation (oracle restatement), all threads."""
+    """Reference arm: the reference's CPU implementation of the path (the oracle's
+    restatement of its CPU Bellman-Ford and of the push), all host threads, one query
+    per thread and kind, on the same inputs and sources as our arm.  Inputs are written
+    by the oracle's own R-MAT writer and pruners; nothing here loads the library."""
     if rank != 0:
         return
-    import c2g
     import oracle
 
     threads = os.cpu_count() or 1
     with tempfile.TemporaryDirectory(dir=args.workdir) as d:
-        c2g.rmat_write(d, args.scale, args.edge_factor, args.seed, 1, 1000)
-        o = oracle.load_dataset(d, "origin")
-        ssrc = pick_sources(o["vlist"], 256)
-        psrc = pick_sources(o["vlist"], 256, seed=2025)
-        # one query per host thread and kind, so every thread works in each kind's pass
-        ns = npq = min(max(args.cpu_sample, threads), 256)
+        make_dataset(oracle, d, args.scale, args.edge_factor, args.seed)
+        s_ds, p_ds = oracle.load_dataset(d, "sssp"), oracle.load_dataset(d, "ppr")
+        svl, pvl = s_ds["vlist"], p_ds["vlist"]
+        V = len(svl) - 1
+        nS, nP = args.sssp_per_step, args.ppr_per_step
+        ssrc = workload_sources(svl, nS, 2024)
+        psrc = workload_sources(pvl, nP, 2025)
+        # a bounded sample per step: one query per host thread and kind, rotating
+        # through the step's sources
+        ns = min(threads, nS)
+        npq = min(threads, nP)
         times, q_total = [], 0
         for step in range(args.warmup + args.steps):
-            k = (step * ns) % 256
-            t0 = time.time()
-            oracle.batch("sssp", o["vlist"], o["elist"], o["wlist"], None, np.roll(ssrc, -k)[:ns], threads=threads)
-            oracle.batch("ppr", o["vlist"], o["elist"], None, o["flist"], np.roll(psrc, -k)[:npq], alpha=ALPHA,
-                         rmax=RMAX, threads=threads)
-            dt = time.time() - t0
+            dt = cpu_queries(s_ds, p_ds, np.roll(ssrc, -(step * ns) % nS)[:ns], np.roll(psrc, -(step * npq) % nP)[:npq],
+                             threads)
             if step >= args.warmup:
                 times.append(dt)
                 q_total += ns + npq
+        cfg = step_config(args, V, int(svl[-1]), int(pvl[-1]), nS, nP, world)
     v = q_total / sum(times)
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "queries/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * float(np.mean(times)),
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32+f32",
-            "data": "synthetic R-MAT (seeded), no public dataset",
-            "config": {"workload": "rmat-s%d-ef%d query mix 50%% SSSP / 50%% PPR" % (args.scale, args.edge_factor),
-                       "graph": "origin (reference CPU Bellman-Ford runs unpruned)", "alpha": ALPHA, "rmax": RMAX},
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "int32 (SSSP) + f32 (PPR)", "data": "synthetic R-MAT (seeded); no public dataset",
+            "config": cfg,
             "cpu_baseline": {"value": v, "unit": "queries/s", "cores": threads, "kind": "port",
-                             "sample": "%d SSSP + %d PPR queries per step, one per thread" % (ns, npq)},
+                             "sample": "%d SSSP + %d PPR queries of the step's sources per step, one per host "
+                                       "thread" % (ns, npq)},
             "e2e": {"value": v, "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -186,15 +235,16 @@ def run_ours(args, rank, world, local_rank):
 
         tdist.init_process_group("nccl", device_id=torch.device("cuda", dev))
     work = tempfile.mkdtemp(dir=args.workdir)
-    gen_s, prune_s = make_dataset(work, args.scale, args.edge_factor, args.seed)
+    gen_s, prune_s = make_dataset(c2g, work, args.scale, args.edge_factor, args.seed)
     so = {"vlist": c2g.read_array(os.path.join(work, "sssp", "vlist.bin"))}
     po = {"vlist": c2g.read_array(os.path.join(work, "ppr", "vlist.bin"))}
     V = len(so["vlist"]) - 1
     nS, nP = args.sssp_per_step, args.ppr_per_step
     from c2g import replicas
 
-    ssrc = replicas.rank_sources(so["vlist"], nS, rank, 2024)
-    psrc = replicas.rank_sources(po["vlist"], nP, rank, 2025)
+    # every rank runs a full batch of its own draw (weak scaling)
+    ssrc = workload_sources(so["vlist"], nS, 2024 + rank)
+    psrc = workload_sources(po["vlist"], nP, 2025 + rank)
 
     gs = c2g.Graph.load(work, "sssp", device=dev)
     gp = c2g.Graph.load(work, "ppr", device=dev)
@@ -202,10 +252,11 @@ def run_ours(args, rank, world, local_rank):
     gs.set_stream(stream.cuda_stream)
     gp.set_stream(stream.cuda_stream)
     gs.sssp_config(delta=args.delta, tile=args.tile)
-    prm = gp.ppr_params(alpha=ALPHA, rmax=RMAX, seeded=1, max_iter=500)
+    prm = step_ppr_params(gp)
     # Round shape of the batched push from the project's autotuner, on this step's batch
     # (outside the timed region).
     pull_ratio = gp.ppr_batch_autotune(psrc, prm, reps=1)
+    sssp_tile = "per round: 512 edge-word steps with >= 16 per warp, else 128"
     dist_d = torch.empty((nS, V), dtype=torch.int32, device=dev)
     pr_d = torch.empty((nP, V), dtype=torch.float32, device=dev)
     dist_h = torch.empty((nS, V), dtype=torch.int32).pin_memory().numpy()
@@ -284,9 +335,8 @@ def run_ours(args, rank, world, local_rank):
     peak, peak_kind = measured_peak()
     achieved = tot[dominant + "_bytes"] / (tot[dominant + "_ms"] / 1000.0) / 1e9
     kernel_name = "sssp_batch_persistent" if dominant == "s" else "ppr_batch_persistent"
-    # DRAM bytes (read + write) per launch from a one-pass ncu capture of this step at full
-    # size (profiles/launches_bench_default_rmat-s22-ef16_256sssp-256ppr.md), expressed per
-    # unit processed and scaled to this run's average launch.
+    # DRAM bytes (read + write) per unit processed (push or relaxation), from an ncu
+    # capture of the kernel, scaled to this run's average launch.
     traffic_per_unit = {"p": 3.0992e12 / 371.88e9, "s": 326.22e9 / 61.33e9}[dominant]
     units = tot["p_push"] if dominant == "p" else tot["s_rel"]
     traffic = traffic_per_unit * units / args.steps
@@ -295,38 +345,37 @@ def run_ours(args, rank, world, local_rank):
     if rank == 0 and not args.no_cpu_baseline:
         import oracle  # CPU-baseline leg only
 
-        threads = 1
-        o = oracle.load_dataset(work, "origin")
-        k = args.cpu_sample
-        t0 = time.time()
-        oracle.batch("sssp", o["vlist"], o["elist"], o["wlist"], None, ssrc[:k], threads=threads)
-        oracle.batch("ppr", o["vlist"], o["elist"], None, o["flist"], psrc[:k], alpha=ALPHA, rmax=RMAX,
-                     threads=threads)
-        dt = time.time() - t0
+        # the same inputs and sources, one query per host thread and kind
+        threads = os.cpu_count() or 1
+        s_ds, p_ds = oracle.load_dataset(work, "sssp"), oracle.load_dataset(work, "ppr")
+        k = min(threads, nS, nP) if args.cpu_sample <= 0 else args.cpu_sample
+        dt = cpu_queries(s_ds, p_ds, ssrc[:k], psrc[:k], threads)
         cpu = {"value": 2 * k / dt, "unit": "queries/s", "cores": threads, "kind": "port",
-               "sample": "%d SSSP (reference CPU Bellman-Ford restated, origin/) + %d PPR (FP32 BSP push) "
-                         "queries on one core" % (k, k)}
+               "sample": "%d SSSP (reference CPU Bellman-Ford restated, EXACT seeds on sssp/) + %d PPR (BSP push "
+                         "in FP32, seeded on ppr/) queries of the step's sources, one per host thread" % (k, k)}
+        del s_ds, p_ds
 
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "queries/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_dev / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "int32 (SSSP) + f32 (PPR)",
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "int32 (SSSP); PPR: f64 residual state (res, msg, pushed residual), f32 weights and pr",
             "data": "synthetic R-MAT (seeded); no public dataset",
-            "config": {"workload": "rmat-s%d-ef%d pruned, batched multi-tenant mix: %d SSSP + %d PPR sources per "
-                                   "step, one launch per kind" % (args.scale, args.edge_factor, nS, nP),
-                       "path": "batched", "vertices": V, "edges_sssp": int(so["vlist"][-1]),
-                       "edges_ppr": int(po["vlist"][-1]), "alpha": ALPHA, "rmax": RMAX,
-                       "sources": "half uniform over vertices with out-edges, half from the top 1% out-degree",
-                       "l2": "graph and state larger than L2 (no flush needed)",
-                       "ppr_pull_ratio": pull_ratio,
-                       "parallelism": "replicas (query-sharded)" if world > 1 else "single GPU"},
+            "config": dict(step_config(args, V, int(so["vlist"][-1]), int(po["vlist"][-1]), nS, nP, world),
+                           path="batched, one persistent launch per kind", ppr_pull_ratio=pull_ratio,
+                           sssp_tile_steps=sssp_tile),
             "e2e": {"value": e2e, "unit": "queries/s", "h2d_bytes_per_step": 4 * q_step,
                     "d2h_bytes_per_step": 4 * V * q_step},
             "gpu_launches": 4 * args.steps,
             "roofline": {"bound": "hbm", "kernel": kernel_name, "achieved": achieved, "peak": peak,
                          "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
-                         "traffic_note": "DRAM bytes per launch, full-size one-pass ncu capture scaled by units"},
+                         "traffic_note": "DRAM bytes per launch: an ncu capture's bytes per unit, scaled by units",
+                         "byte_model": {"p": "FP64 residual layout: 12 B x V x Q init, 40 B per (vertex, word) "
+                                             "entry, 8 B per edge-word step, 8 B per (query, edge) push (FP64 "
+                                             "message add), 32 B per touched lane (res and msg read + write)",
+                                        "s": "4 B x V x Q init, 40 B per entry, 8 B per edge-word step, 8 B per "
+                                             "(query, edge) relaxation"}[dominant]},
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
             "detail": {
@@ -513,7 +562,8 @@ def main():
     ap.add_argument("--per-query-sample", type=int, default=8)
     ap.add_argument("--delta", type=int, default=0)
     ap.add_argument("--tile", type=int, default=256)
-    ap.add_argument("--cpu-sample", type=int, default=2)
+    ap.add_argument("--cpu-sample", type=int, default=0,
+                    help="queries per kind in the CPU-baseline leg (0: one per host thread)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workdir", default=None)
     ap.add_argument("--mode", default="step", choices=["step", "serve", "adjoint", "adsorption"],

@@ -25,6 +25,7 @@ OK = 0
 ERR_ARG, ERR_IO, ERR_FORMAT, ERR_CUDA, ERR_OOM = -1, -2, -3, -4, -5
 ERR_RANGE, ERR_TIMEOUT, ERR_OVERFLOW, ERR_UNSUPPORTED, ERR_NODEVICE = -6, -7, -8, -9, -10
 FLAG_BARRIER_TIMEOUT, FLAG_ITER_CAP, FLAG_QUEUE_OVERFLOW, FLAG_BOUNDS = 0x1, 0x2, 0x4, 0x8
+NOALLOC_MAX_V, NOALLOC_MAX_E = 262144, 4194304  # size of c2g_sssp_noalloc's static scratch
 
 VARIANTS = {"origin": 0, "sssp": 1, "ppr": 2}
 SEEDS_COMPAT, SEEDS_EXACT = 0, 1

@@ -32,6 +32,7 @@ struct SsspParams {
     int* dist;
     int* stamp;
     int* farstamp;
+    int stamp_extent;  // entries of stamp/farstamp cleared when the round tags restart (>= V)
     int2* q[2];
     int* mark[2];
     int* far[3];
@@ -165,13 +166,15 @@ __global__ void __launch_bounds__(512, 2) sssp_persistent(const SsspParams p) {
     if (reset) sbase = ebase = 0;
 
     // Init: dis = INF (src/sssp/purn/Main.cu:144-156).
-    for (unsigned v = gtid; v < V; v += nthreads) {
-        p.dist[v] = kInfDist;
-        if (reset) {
+    for (unsigned v = gtid; v < V; v += nthreads) p.dist[v] = kInfDist;
+    // Restarting tags clear every stamp the array holds, not only this graph's V: an
+    // array shared by calls on graphs of different sizes keeps older tags beyond V,
+    // which a later, larger graph would read as current.
+    if (reset)
+        for (unsigned v = gtid; v < (unsigned)p.stamp_extent; v += nthreads) {
             p.stamp[v] = -1;
             p.farstamp[v] = -1;
         }
-    }
     if (gtid == 0) ctl->farmin[0] = ctl->farmin[1] = ctl->farmin[2] = INT_MAX;
     if (!grid_sync(bar, flags, p.barrier_ns, p.bar_extra)) return;
 
@@ -489,6 +492,7 @@ int sssp_launch(c2g_graph* g, int32_t source, const int32_t* seed_v, const int32
     p.dist = dist_dev ? dist_dev : w.dist;
     p.stamp = w.stamp;
     p.farstamp = w.farstamp;
+    p.stamp_extent = g->V;
     p.q[0] = w.q[0];
     p.q[1] = w.q[1];
     p.mark[0] = w.mark[0];
@@ -560,9 +564,8 @@ constexpr size_t kOffSt = kOffCtl + align256(sizeof(TraversalCtl));
 constexpr size_t kNoAllocScratchBytes = kOffSt + align256(sizeof(StampState));
 
 constexpr int kNoAllocMaxDevices = 64;
-void* g_noalloc_base[kNoAllocMaxDevices];           // device address of the scratch, per device
-cudaError_t g_noalloc_setup_err[kNoAllocMaxDevices];
-std::once_flag g_noalloc_once[kNoAllocMaxDevices];
+void* g_noalloc_base[kNoAllocMaxDevices];  // device address of the scratch, per device (null: not looked up)
+std::mutex g_noalloc_mu;
 
 }  // namespace
 
@@ -588,14 +591,23 @@ extern "C" int c2g_sssp_noalloc(const int32_t* row, const void* adj, int32_t V, 
     C2G_CUDA(cudaGetDevice(&dev));
     if (dev < 0 || dev >= kNoAllocMaxDevices) return fail(C2G_ERR_UNSUPPORTED, "device index %d too large", dev);
     // Once per device, with that device current: the device address of the scratch.
-    // The host-side name of a __device__ array is not a device address.
-    std::call_once(g_noalloc_once[dev], [dev] {
-        g_noalloc_setup_err[dev] = cudaGetSymbolAddress(&g_noalloc_base[dev], g_sssp_noalloc_scratch);
-    });
-    if (g_noalloc_setup_err[dev] != cudaSuccess)
-        return fail(C2G_ERR_CUDA, "noalloc SSSP: cudaGetSymbolAddress failed: %s",
-                    cudaGetErrorString(g_noalloc_setup_err[dev]));
-    unsigned char* base = static_cast<unsigned char*>(g_noalloc_base[dev]);
+    // The host-side name of a __device__ array is not a device address.  Only a
+    // successful lookup is kept; a failed one (say, made during a stream capture) is
+    // retried by the next call.
+    unsigned char* base = nullptr;
+    {
+        std::lock_guard<std::mutex> lk(g_noalloc_mu);
+        if (!g_noalloc_base[dev]) {
+            void* addr = nullptr;
+            const cudaError_t e = cudaGetSymbolAddress(&addr, g_sssp_noalloc_scratch);
+            if (e != cudaSuccess) {
+                cudaGetLastError();
+                return fail(C2G_ERR_CUDA, "noalloc SSSP: cudaGetSymbolAddress failed: %s", cudaGetErrorString(e));
+            }
+            g_noalloc_base[dev] = addr;
+        }
+        base = static_cast<unsigned char*>(g_noalloc_base[dev]);
+    }
     cudaStream_t s = static_cast<cudaStream_t>(stream);
 
     int coop = 0, per_sm = 0, sms = 0;
@@ -613,6 +625,7 @@ extern "C" int c2g_sssp_noalloc(const int32_t* row, const void* adj, int32_t V, 
     p.dist = dist;
     p.stamp = reinterpret_cast<int*>(base + kOffStamp);
     p.farstamp = reinterpret_cast<int*>(base + kOffFarstamp);
+    p.stamp_extent = C2G_NOALLOC_MAX_V;  // the array serves graphs of every size
     p.q[0] = reinterpret_cast<int2*>(base + kOffQ0);
     p.q[1] = reinterpret_cast<int2*>(base + kOffQ1);
     p.mark[0] = reinterpret_cast<int*>(base + kOffMark0);

@@ -40,8 +40,15 @@ def lib():
         L.orc_sssp_certificate.argtypes = [_I32, _P, _P, _P, _I32, _P, _I32, _P, _P, _P,
                                            ctypes.POINTER(ctypes.c_int32)]
         L.orc_batch.restype = ctypes.c_int64
-        L.orc_batch.argtypes = [ctypes.c_int, _I32, _P, _P, _P, _P, _I32, _P, ctypes.c_double,
-                                ctypes.c_double, _I32, _I32, _P, _P]
+        L.orc_batch.argtypes = [ctypes.c_int, _I32, _P, _P, _P, _P, _I32, _P, _P, _P, _P, ctypes.c_double,
+                                ctypes.c_double, _I32, _I32, _P, _P, _P, _P]
+        L.orc_rmat_write.restype = ctypes.c_int
+        L.orc_rmat_write.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, ctypes.c_uint64, _I32, _I32,
+                                     ctypes.c_double, ctypes.c_double, ctypes.c_double]
+        L.orc_prune_sssp.restype = ctypes.c_int
+        L.orc_prune_sssp.argtypes = [ctypes.c_char_p]
+        L.orc_prune_ppr.restype = ctypes.c_int
+        L.orc_prune_ppr.argtypes = [ctypes.c_char_p, ctypes.c_double]
         _lib = L
     return _lib
 
@@ -130,22 +137,90 @@ def sssp_certificate(row, col, w, dist, sources, seed_v=(), seed_w=()):
 
 
 def batch(kind, row, col, w, f, sources, alpha=0.15, rmax=1e-7, max_iter=500, threads=1,
-          keep=False):
-    """Independent queries on `threads` host threads (CPU baseline).  kind 'sssp' or 'ppr'.
-    Returns (edges, outputs-or-None)."""
+          keep=False, seeds=None, f64=False):
+    """Independent queries on `threads` host threads (CPU baseline, parallel checks).
+    kind 'sssp' (reference CPU Bellman-Ford) or 'ppr' (BSP push, float; double with
+    f64).  seeds = (offsets[n+1], vertices, weights) gives each query its first hop
+    (sssp-purn / ppr-purn), see query_seeds.  Returns (edges, outputs-or-None); the PPR
+    outputs in double are (pr, res)."""
     row, col = _c(row, np.int32), _c(col, np.int32)
     w = None if w is None else _c(w, np.int32)
     f = None if f is None else _c(f, np.float32)
     src = _c(sources, np.int32)
     V = len(row) - 1
-    k = 0 if kind == "sssp" else 1
-    out = None
+    k = 0 if kind == "sssp" else (2 if f64 else 1)
+    so = sv = sw = None
+    if seeds is not None:
+        so, sv = _c(seeds[0], np.int32), _c(seeds[1], np.int32)
+        sw = _c(seeds[2], np.int32 if k == 0 else np.float32)
+        assert len(so) == len(src) + 1
+    # the reference holds alpha and rmax as float (ppr_push's params_f32)
+    alpha, rmax = float(np.float32(alpha)), float(np.float32(rmax))
+    dist = pr = pr64 = res64 = None
     if keep:
-        out = np.empty((len(src), V), dtype=np.int32 if k == 0 else np.float32)
-    edges = lib().orc_batch(k, V, _p(row), _p(col), _p(w), _p(f), len(src), _p(src), alpha, rmax,
-                            max_iter, threads, _p(out) if (keep and k == 0) else None,
-                            _p(out) if (keep and k == 1) else None)
-    return edges, out
+        if k == 0:
+            dist = np.empty((len(src), V), dtype=np.int32)
+        elif k == 1:
+            pr = np.empty((len(src), V), dtype=np.float32)
+        else:
+            pr64 = np.empty((len(src), V), dtype=np.float64)
+            res64 = np.empty((len(src), V), dtype=np.float64)
+    edges = lib().orc_batch(k, V, _p(row), _p(col), _p(w), _p(f), len(src), _p(src), _p(so), _p(sv), _p(sw),
+                            alpha, rmax, max_iter, threads, _p(dist), _p(pr), _p(pr64), _p(res64))
+    out = dist if k == 0 else (pr if k == 1 else (pr64, res64))
+    return edges, (out if keep else None)
+
+
+def query_seeds(ds, sources, kind):
+    """First-hop seeds of each source as (offsets, vertices, weights).
+    kind 'sssp': the source's own pruned record, found through the record->vertex
+    sidecar (EXACT mode; sources without a record get none).  kind 'ppr': the source's
+    record (hvlist indexed by vertex, src/ppr/purn/Main.cu:78-86) followed by its kept
+    out-edges (:87-93)."""
+    hv, he, hw = ds["hvlist"], ds["helist"], ds["hwlist"]
+    rec_of = None
+    if kind == "sssp":
+        rec_of = np.full(len(ds["vlist"]) - 1, -1, dtype=np.int64)
+        rec_of[ds["hvmap"]] = np.arange(len(ds["hvmap"]))
+    off, vs, ws = [0], [], []
+    for s in np.asarray(sources, dtype=np.int64):
+        if kind == "sssp":
+            r = rec_of[s]
+            sv = he[hv[r]:hv[r + 1]] if r >= 0 else he[:0]
+            sw = hw[hv[r]:hv[r + 1]] if r >= 0 else hw[:0]
+        else:
+            vl = ds["vlist"]
+            sv = np.concatenate([he[hv[s]:hv[s + 1]], ds["elist"][vl[s]:vl[s + 1]]])
+            sw = np.concatenate([hw[hv[s]:hv[s + 1]], ds["wlist"][vl[s]:vl[s + 1]]])
+        vs.append(sv)
+        ws.append(sw)
+        off.append(off[-1] + len(sv))
+    wdt = np.int32 if kind == "sssp" else np.float32
+    v = np.concatenate(vs).astype(np.int32) if vs else np.zeros(0, np.int32)
+    w = np.concatenate(ws).astype(wdt) if ws else np.zeros(0, wdt)
+    return np.asarray(off, dtype=np.int32), v, w
+
+
+def rmat_write(dir, scale, edge_factor, seed, wmin=1, wmax=100, a=0.57, b=0.19, c=0.19):
+    """Seeded R-MAT graph in the origin/ layout (oracle/ingest.c orc_rmat_write)."""
+    rc = lib().orc_rmat_write(os.fsencode(dir), scale, edge_factor, seed, wmin, wmax, a, b, c)
+    if rc:
+        raise RuntimeError("orc_rmat_write failed: %d" % rc)
+
+
+def prune_sssp(dir):
+    """purn-sssp restated (oracle/ingest.c orc_prune_sssp), plus sssp/hvmap.bin."""
+    rc = lib().orc_prune_sssp(os.fsencode(dir))
+    if rc:
+        raise RuntimeError("orc_prune_sssp failed: %d" % rc)
+
+
+def prune_ppr(dir, alpha=None):
+    """purn-ppr restated (oracle/ingest.c orc_prune_ppr); alpha None keeps the
+    reference's baked 0.8, else folded edges carry 1 - alpha."""
+    rc = lib().orc_prune_ppr(os.fsencode(dir), 0.8 if alpha is None else 1.0 - alpha)
+    if rc:
+        raise RuntimeError("orc_prune_ppr failed: %d" % rc)
 
 
 def adsorption_labels(row, col, f, seeds, p_inj, p_cont, iterations):

@@ -1,7 +1,8 @@
 """Build recipe for the oracle (test infrastructure only).
 
-* ``build_oracle()`` compiles oracle/oracle.c (the CPU restatement) into
-  oracle/liboracle.so with gcc.  It builds on any host (x86 or Arm).
+* ``build_oracle()`` compiles oracle/oracle.c (the CPU restatement of the traversals)
+  and oracle/ingest.c (the R-MAT writer and the pruners) into oracle/liboracle.so with
+  gcc.  It builds on any host (x86 or Arm).
 * ``build_ref()`` compiles the reference's own CPU programs from their sources, where
   they lie in the reference tree, into oracle/_ref/ (git-ignored):
   purn-sssp (src/purn-sssp.cpp), purn-ppr (src/purn-ppr.cpp), convert2binary
@@ -39,10 +40,10 @@ def _stale(target, sources):
 
 
 def build_oracle(force=False):
-    src = os.path.join(HERE, "oracle.c")
-    if force or _stale(ORACLE_SO, [src]):
-        _run(["gcc", "-O2", "-std=c11", "-fPIC", "-shared", "-pthread", "-ffp-contract=off",
-              src, "-o", ORACLE_SO + ".tmp", "-lm"])
+    srcs = [os.path.join(HERE, "oracle.c"), os.path.join(HERE, "ingest.c")]
+    if force or _stale(ORACLE_SO, srcs):
+        _run(["gcc", "-O2", "-std=c11", "-D_DEFAULT_SOURCE", "-fPIC", "-shared", "-pthread", "-ffp-contract=off"]
+             + srcs + ["-o", ORACLE_SO + ".tmp", "-lm"])
         os.replace(ORACLE_SO + ".tmp", ORACLE_SO)
     return ORACLE_SO
 

@@ -17,7 +17,8 @@
  *                      BSP forward push of calcuatePPR (src/ppr/base/Main.cu:146-150,
  *                      src/ppr/purn/Main.cu:156-198 init/seeds, :248-360 push,
  *                      :379-407 frontier rule) in double or float
- *   orc_*_batch        one independent query per host thread (CPU baseline)
+ *   orc_batch          one independent query per host thread, with or without each
+ *                      query's first-hop seeds (CPU baseline, parallel checks)
  *   orc_sssp_certificate
  *                      size-independent exactness check of a distance vector: the
  *                      Bellman conditions of the fixed point CalcuSSSP computes
@@ -289,61 +290,91 @@ int orc_ppr_push_f32(int32_t V, const int32_t* row, const int32_t* col, const fl
     ORC_PPR_BODY(float)
 }
 
-/* ---- batched CPU baseline: one query per thread -------------------------------------- */
+/* ---- batched queries: one query per thread (CPU baseline and parallel checks) ------- */
 
 typedef struct {
-    int kind; /* 0 sssp (plain Bellman-Ford from the source), 1 ppr f32 base push */
+    int kind; /* 0 sssp (reference CPU Bellman-Ford from the source and its seeds),
+                 1 ppr BSP push in float, 2 the same push in double */
     int32_t V;
     const int32_t *row, *col, *w;
     const float* f;
     const int32_t* sources;
+    const int32_t* seed_off; /* NULL: no seeds; else seeds of query q in [seed_off[q], seed_off[q+1]) */
+    const int32_t* seed_v;
+    const void* seed_w; /* int32 (sssp) or float (ppr) */
     int32_t nq;
     int32_t* next; /* shared work counter */
     pthread_mutex_t* mu;
     double alpha, rmax;
     int32_t max_iter;
-    int64_t edges; /* per-thread edges relaxed */
+    int64_t edges;     /* per-thread edges relaxed */
     int32_t* dist_out; /* optional: nq*V */
-    float* pr_out;     /* optional: nq*V */
+    float* pr_out;     /* optional: nq*V (kind 1) */
+    double* pr64_out;  /* optional: nq*V (kind 2) */
+    double* res64_out; /* optional: nq*V (kind 2) */
 } orc_worker;
 
 static void* orc_worker_main(void* p) {
     orc_worker* wk = (orc_worker*)p;
     int32_t V = wk->V;
-    int32_t* dist = (int32_t*)malloc(sizeof(int32_t) * (size_t)V);
-    float* pr = (float*)malloc(sizeof(float) * (size_t)V);
-    float* res = (float*)malloc(sizeof(float) * (size_t)V);
+    const size_t nv = (size_t)(V > 0 ? V : 1);
+    int32_t* dist = (int32_t*)malloc(sizeof(int32_t) * nv);
+    float* pr = (float*)malloc(sizeof(float) * nv);
+    float* res = (float*)malloc(sizeof(float) * nv);
+    double* pr64 = wk->kind == 2 ? (double*)malloc(sizeof(double) * nv) : NULL;
+    double* res64 = wk->kind == 2 ? (double*)malloc(sizeof(double) * nv) : NULL;
     for (;;) {
         pthread_mutex_lock(wk->mu);
         int32_t q = (*wk->next)++;
         pthread_mutex_unlock(wk->mu);
         if (q >= wk->nq) break;
-        int32_t s = wk->sources[q];
+        const int32_t s = wk->sources[q];
+        int32_t ns = 0;
+        const int32_t* sv = NULL;
+        const void* sw = NULL;
+        if (wk->seed_off) {
+            ns = wk->seed_off[q + 1] - wk->seed_off[q];
+            sv = wk->seed_v + wk->seed_off[q];
+            sw = wk->kind == 0 ? (const void*)((const int32_t*)wk->seed_w + wk->seed_off[q])
+                               : (const void*)((const float*)wk->seed_w + wk->seed_off[q]);
+        }
         if (wk->kind == 0) {
-            orc_sssp_seeded(V, wk->row, wk->col, wk->w, s, 0, NULL, NULL, dist);
+            orc_sssp_seeded(V, wk->row, wk->col, wk->w, s, ns, sv, (const int32_t*)sw, dist);
             for (int32_t v = 0; v < V; ++v)
                 if (dist[v] != ORC_INF) wk->edges += wk->row[v + 1] - wk->row[v];
             if (wk->dist_out) memcpy(wk->dist_out + (size_t)q * V, dist, sizeof(int32_t) * (size_t)V);
-        } else {
+        } else if (wk->kind == 1) {
             int64_t c[3];
-            orc_ppr_push_f32(V, wk->row, wk->col, wk->f, s, wk->alpha, wk->rmax, 1.0, wk->alpha,
-                             wk->max_iter, 0, 0, 0, NULL, NULL, pr, res, c);
+            orc_ppr_push_f32(V, wk->row, wk->col, wk->f, s, wk->alpha, wk->rmax, 1.0, wk->alpha, wk->max_iter,
+                             wk->seed_off != NULL, 0, ns, sv, (const float*)sw, pr, res, c);
             wk->edges += c[1];
             if (wk->pr_out) memcpy(wk->pr_out + (size_t)q * V, pr, sizeof(float) * (size_t)V);
+        } else {
+            int64_t c[3];
+            orc_ppr_push_f64(V, wk->row, wk->col, wk->f, s, wk->alpha, wk->rmax, 1.0, wk->alpha, wk->max_iter,
+                             wk->seed_off != NULL, 0, ns, sv, (const float*)sw, pr64, res64, c);
+            wk->edges += c[1];
+            if (wk->pr64_out) memcpy(wk->pr64_out + (size_t)q * V, pr64, sizeof(double) * (size_t)V);
+            if (wk->res64_out) memcpy(wk->res64_out + (size_t)q * V, res64, sizeof(double) * (size_t)V);
         }
     }
     free(dist);
     free(pr);
     free(res);
+    free(pr64);
+    free(res64);
     return NULL;
 }
 
-/* Run nq independent queries on nthreads host threads.  kind 0: SSSP (edges =
- * out-edges of reached vertices); kind 1: PPR f32 push (edges = edges pushed).
- * Returns the total edge count. */
+/* Run nq independent queries on nthreads host threads.  kind 0: SSSP (edges = out-edges
+ * of reached vertices); kind 1: PPR push in float, kind 2: in double (edges = edges
+ * pushed).  With seed_off, query q applies its seeds: the sssp-purn first hop
+ * (src/sssp/purn/Main.cu:72-90) or the ppr-purn one (src/ppr/purn/Main.cu:78-101) with
+ * the push's base values (pr0 = alpha, r0 = 1) unused.  Returns the total edge count. */
 int64_t orc_batch(int kind, int32_t V, const int32_t* row, const int32_t* col, const int32_t* w,
-                  const float* f, int32_t nq, const int32_t* sources, double alpha, double rmax,
-                  int32_t max_iter, int32_t nthreads, int32_t* dist_out, float* pr_out) {
+                  const float* f, int32_t nq, const int32_t* sources, const int32_t* seed_off,
+                  const int32_t* seed_v, const void* seed_w, double alpha, double rmax, int32_t max_iter,
+                  int32_t nthreads, int32_t* dist_out, float* pr_out, double* pr64_out, double* res64_out) {
     if (nthreads < 1) nthreads = 1;
     pthread_t* th = (pthread_t*)malloc(sizeof(pthread_t) * (size_t)nthreads);
     orc_worker* wk = (orc_worker*)calloc((size_t)nthreads, sizeof(orc_worker));
@@ -351,8 +382,8 @@ int64_t orc_batch(int kind, int32_t V, const int32_t* row, const int32_t* col, c
     pthread_mutex_init(&mu, NULL);
     int32_t next = 0;
     for (int t = 0; t < nthreads; ++t) {
-        orc_worker x = {kind, V, row, col, w, f, sources, nq, &next, &mu, alpha, rmax, max_iter, 0,
-                        dist_out, pr_out};
+        orc_worker x = {kind, V, row, col, w, f, sources, seed_off, seed_v, seed_w, nq, &next, &mu, alpha, rmax,
+                        max_iter, 0, dist_out, pr_out, pr64_out, res64_out};
         wk[t] = x;
         pthread_create(&th[t], NULL, orc_worker_main, &wk[t]);
     }

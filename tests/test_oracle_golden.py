@@ -224,3 +224,90 @@ def test_prune_ppr_alpha(tmp_path):
         assert ratio.min() >= 1.0 - 1e-6 and ratio.max() <= (0.85 / 0.8) ** 8 + 1e-6
     with pytest.raises(c2g.C2GError):
         c2g.prune_ppr(d, alpha=1.5)
+
+
+def test_oracle_ingest_reproduces_fixtures(built, gold, tmp_path):
+    """The oracle's own R-MAT writer and pruner restatements (oracle/ingest.c), which
+    build the inputs of the reference arm without the product library, write the
+    fixtures' bytes: the R-MAT inputs and the reference purn-sssp / purn-ppr outputs."""
+    import oracle
+
+    name, g = gold
+    d = str(tmp_path / name)
+    params = {"rmat_s10_ef8_seed3": (10, 8, 3, 100), "rmat_s12_ef8_seed5": (12, 8, 5, 1000)}
+    if name in params:
+        scale, ef, seed, wmax = params[name]
+        oracle.rmat_write(d, scale, ef, seed, 1, wmax)
+        for n in ("vlist", "elist", "wlist", "flist"):
+            assert open(os.path.join(d, "origin", n + ".bin"), "rb").read() == g["origin_" + n].tobytes(), (name, n)
+    else:
+        for sub in ("origin", "sssp", "ppr"):
+            os.makedirs(os.path.join(d, sub))
+        for n in ("vlist", "elist", "wlist", "flist"):
+            g["origin_" + n].tofile(os.path.join(d, "origin", n + ".bin"))
+    oracle.prune_sssp(d)
+    oracle.prune_ppr(d)
+    for sub in ("sssp", "ppr"):
+        for n in ("vlist", "elist", "wlist", "hvlist", "helist", "hwlist"):
+            mine = open(os.path.join(d, sub, n + ".bin"), "rb").read()
+            assert mine == g["%s_%s" % (sub, n)].tobytes(), (name, sub, n)
+    assert np.array_equal(np.fromfile(os.path.join(d, "sssp", "hvmap.bin"), dtype=np.int32), g["hvmap"])
+
+
+def test_oracle_ingest_equals_library(built, tmp_path):
+    """At a larger scale (R-MAT 15, edge factor 16, weights 1..1000) the oracle's writer
+    and pruners (PPR pruned for alpha 0.15) write the same bytes as the library's."""
+    import c2g
+    import oracle
+
+    a, b = str(tmp_path / "oracle"), str(tmp_path / "lib")
+    oracle.rmat_write(a, 15, 16, 2, 1, 1000)
+    oracle.prune_sssp(a)
+    oracle.prune_ppr(a, alpha=0.15)
+    c2g.rmat_write(b, 15, 16, 2, 1, 1000)
+    c2g.prune_sssp(b)
+    c2g.prune_ppr(b, alpha=0.15)
+    files = {"origin": ("vlist", "elist", "wlist", "flist"),
+             "sssp": ("vlist", "elist", "wlist", "hvlist", "helist", "hwlist", "hvmap"),
+             "ppr": ("vlist", "elist", "wlist", "hvlist", "helist", "hwlist")}
+    for sub, names in files.items():
+        for n in names:
+            x = open(os.path.join(a, sub, n + ".bin"), "rb").read()
+            assert x == open(os.path.join(b, sub, n + ".bin"), "rb").read(), (sub, n)
+            assert len(x) > 0 or n in ("helist", "hwlist")
+
+
+def test_oracle_seeded_batch_matches_single_queries(built, tmp_path):
+    """The threaded batch runner with first-hop seeds (the reference arm's work) equals
+    the single-query restatements: EXACT-seeded SSSP on sssp/, seeded PPR on ppr/ in
+    float and double."""
+    import oracle
+
+    d = str(tmp_path)
+    oracle.rmat_write(d, 12, 8, 5, 1, 1000)
+    oracle.prune_sssp(d)
+    oracle.prune_ppr(d, alpha=0.15)
+    s_ds, p_ds = oracle.load_dataset(d, "sssp"), oracle.load_dataset(d, "ppr")
+    deg = np.diff(s_ds["vlist"])
+    src = np.concatenate([s_ds["hvmap"][:3], np.flatnonzero(deg > 0)[:3]]).astype(np.int32)
+    seeds = oracle.query_seeds(s_ds, src, "sssp")
+    _, dist = oracle.batch("sssp", s_ds["vlist"], s_ds["elist"], s_ds["wlist"], None, src, threads=3, keep=True,
+                           seeds=seeds)
+    for i, s in enumerate(src):
+        sv, sw = seeds[1][seeds[0][i]:seeds[0][i + 1]], seeds[2][seeds[0][i]:seeds[0][i + 1]]
+        ref, _ = oracle.sssp_seeded(s_ds["vlist"], s_ds["elist"], s_ds["wlist"], int(s), sv, sw)
+        assert np.array_equal(dist[i], ref)
+        assert (i >= 3) or len(sv) > 0  # the first three own a record
+    pseeds = oracle.query_seeds(p_ds, src, "ppr")
+    _, pr32 = oracle.batch("ppr", p_ds["vlist"], p_ds["elist"], None, p_ds["wlist"], src, alpha=0.15, rmax=1e-7,
+                           threads=2, keep=True, seeds=pseeds)
+    _, (pr64, res64) = oracle.batch("ppr", p_ds["vlist"], p_ds["elist"], None, p_ds["wlist"], src, alpha=0.15,
+                                    rmax=1e-7, threads=2, keep=True, seeds=pseeds, f64=True)
+    for i, s in enumerate(src):
+        sv, sw = pseeds[1][pseeds[0][i]:pseeds[0][i + 1]], pseeds[2][pseeds[0][i]:pseeds[0][i + 1]]
+        rp, rr, _, _ = oracle.ppr_push(p_ds["vlist"], p_ds["elist"], p_ds["wlist"], int(s), 0.15, 1e-7, seeded=True,
+                                       seed_v=sv, seed_w=sw)
+        assert np.array_equal(pr64[i], rp) and np.array_equal(res64[i], rr)
+        fp, _, _, _ = oracle.ppr_push(p_ds["vlist"], p_ds["elist"], p_ds["wlist"], int(s), 0.15, 1e-7, seeded=True,
+                                      seed_v=sv, seed_w=sw, dtype=np.float32)
+        assert np.array_equal(pr32[i], fp)

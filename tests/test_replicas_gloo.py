@@ -68,3 +68,18 @@ def test_two_rank_replicas_over_gloo():
     assert all(d[v] > 0 for v in s0 + s1)
     # without a process group the helpers are the single-GPU identities
     assert replicas.max_over_ranks(7.5) == 7.5
+
+
+def test_bench_selection_equals_library_rule():
+    """bench.py restates the batched configuration's source selection so that its
+    reference arm needs nothing from the library; both give the same sources."""
+    import bench
+    from c2g import replicas
+
+    rng = np.random.default_rng(0)
+    for V in (50, 1000, 4096):
+        deg = rng.integers(0, 30, size=V)
+        deg[rng.choice(V, V // 5, replace=False)] = 0
+        vlist = np.concatenate([[0], np.cumsum(deg)]).astype(np.int32)
+        for n, seed in ((256, 2024), (64, 2025), (7, 3)):
+            assert np.array_equal(bench.workload_sources(vlist, n, seed), replicas.pick_sources(vlist, n, seed))

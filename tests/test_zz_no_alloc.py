@@ -3,9 +3,10 @@
 It is meant for callers that cannot let the library allocate, such as a host whose
 device memory belongs to another allocator, or a serving loop that must not call
 cudaMalloc/cudaFree (they can synchronise the device) once it is running.  It runs on
-caller-owned device arrays with scratch in a static device array.  Its results must
-equal the regular entry point's (c2g_sssp, bit-exact int32), call after call, because
-the shared scratch keeps the previous call's contents.
+caller-owned device arrays with scratch in a static device array.  Its distances must
+be the exact shortest distances (the oracle's Dijkstra, bit-exact int32) and equal the
+regular entry point's (c2g_sssp), call after call, because the shared scratch keeps the
+previous call's contents.
 
 This file is named to be collected last, and it passes alone in a fresh process as
 well as after the other tests.
@@ -18,48 +19,112 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-@pytest.fixture(scope="module")
-def graph16(tmp_path_factory, built):
+def _dataset(tmp_path_factory, name, scale, seed):
     import c2g
 
-    d = str(tmp_path_factory.mktemp("noalloc16"))
-    c2g.rmat_write(d, 16, 16, 3, 1, 1000)
+    d = str(tmp_path_factory.mktemp(name))
+    c2g.rmat_write(d, scale, 16, seed, 1, 1000)
     vl = c2g.read_array(d + "/origin/vlist.bin")
     el = c2g.read_array(d + "/origin/elist.bin")
     wl = c2g.read_array(d + "/origin/wlist.bin")
     return d, vl, el, wl
 
 
-def test_noalloc_matches_regular_entry_point(gpu_available, graph16):
-    import torch
+@pytest.fixture(scope="module")
+def graph16(tmp_path_factory, built):
+    return _dataset(tmp_path_factory, "noalloc16", 16, 3)
 
+
+class _OnDevice:
+    """The caller's device arrays: row, (target, weight) pairs, distances."""
+
+    def __init__(self, vl, el, wl):
+        import torch
+
+        self.dev = torch.device("cuda", 0)
+        torch.cuda.set_device(self.dev)
+        self.V, self.E = len(vl) - 1, len(el)
+        self.row = torch.from_numpy(vl).to(self.dev)
+        self.adj = torch.from_numpy(np.stack([el, wl], axis=1).astype(np.int32)).contiguous().to(self.dev)
+        self.dist = torch.empty(self.V, dtype=torch.int32, device=self.dev)
+        self.stream = torch.cuda.current_stream(self.dev)
+
+    def call(self, source, E=None):
+        import c2g
+
+        st = c2g.Stats()
+        rc = c2g.lib().c2g_sssp_noalloc(ctypes.c_void_p(self.row.data_ptr()), ctypes.c_void_p(self.adj.data_ptr()),
+                                        self.V, self.E if E is None else E, source,
+                                        ctypes.c_void_p(self.dist.data_ptr()),
+                                        ctypes.c_void_p(self.stream.cuda_stream), ctypes.byref(st))
+        return rc, st
+
+
+def test_noalloc_exact_and_matches_regular_entry_point(gpu_available, graph16):
     import c2g
+    import oracle
 
     d, vl, el, wl = graph16
-    V, E = len(vl) - 1, len(el)
-    assert V <= 262144 and E <= 4194304
-    dev = torch.device("cuda", 0)
-    torch.cuda.set_device(dev)
-    row = torch.from_numpy(vl).to(dev)
-    adj = torch.from_numpy(np.stack([el, wl], axis=1).astype(np.int32)).contiguous().to(dev)
-    dist = torch.empty(V, dtype=torch.int32, device=dev)
-    stream = torch.cuda.current_stream(dev)
+    a = _OnDevice(vl, el, wl)
+    assert a.V <= c2g.NOALLOC_MAX_V and a.E <= c2g.NOALLOC_MAX_E
     deg = np.diff(vl)
     sources = [int(np.argmax(deg)), int(np.flatnonzero(deg > 0)[7])]
-    L = c2g.lib()
     with c2g.Graph.load(d, "origin") as g:
         for s in sources:  # two calls in a row on the shared scratch
-            st = c2g.Stats()
-            rc = L.c2g_sssp_noalloc(ctypes.c_void_p(row.data_ptr()), ctypes.c_void_p(adj.data_ptr()), V, E, s,
-                                    ctypes.c_void_p(dist.data_ptr()), ctypes.c_void_p(stream.cuda_stream),
-                                    ctypes.byref(st))
-            assert rc == 0, L.c2g_last_error()
+            rc, st = a.call(s)
+            assert rc == 0, c2g.lib().c2g_last_error()
+            got = a.dist.cpu().numpy()
+            assert np.array_equal(got, oracle.dijkstra(vl, el, wl, [s], [0])), s
             ref, rst = g.sssp(s)
-            assert np.array_equal(dist.cpu().numpy(), ref), s
+            assert np.array_equal(got, ref), s
             # round counts are not compared: they depend on the schedule (an improvement
             # seen early in a round can save a round), and the two entry points run
             # different kernels
             assert st.status_flags == 0 and rst.status_flags == 0 and st.iterations > 0
+
+
+def _chain(n):
+    """A path 0 -> 1 -> ... -> n-1 with weights 1..n-1: the traversal from 0 claims exactly
+    vertex k in round k, so its round tags are the same on every run."""
+    vl = np.concatenate([np.arange(n, dtype=np.int32), [n - 1]]).astype(np.int32)
+    el = np.arange(1, n, dtype=np.int32)
+    wl = np.arange(1, n, dtype=np.int32)
+    ref = np.concatenate([[0], np.cumsum(wl)]).astype(np.int32)
+    return vl, el, wl, ref
+
+
+def test_noalloc_tag_restart_across_graph_sizes(gpu_available):
+    """Calls on graphs of different sizes share the scratch.  A failed call makes the next
+    call restart the round tags; the restart must clear the tags of the whole array, not
+    only of the restarting call's (smaller) graph.  Otherwise a later call on the larger
+    graph whose tags repeat an earlier run's reads that run's leftover tags as current and
+    drops vertices from its frontier.  On path graphs the tags repeat exactly: the small
+    path restarts from the same base both times, so the large path runs twice with the
+    same tags.  The failure is driven from the host: a call that declares no edges fails
+    the kernel's own index check before any edge is read (every array is full-size)."""
+    import c2g
+
+    vs, es, ws, rs = _chain(300)
+    vb, eb, wb, rb = _chain(900)
+    small, big = _OnDevice(vs, es, ws), _OnDevice(vb, eb, wb)
+
+    def fail_small():
+        rc, st = small.call(0, E=0)
+        assert rc == c2g.ERR_OVERFLOW and st.status_flags & c2g.FLAG_BOUNDS
+
+    def ok(g, ref):
+        rc, st = g.call(0)
+        assert rc == 0, c2g.lib().c2g_last_error()
+        assert np.array_equal(g.dist.cpu().numpy(), ref)
+        return st.iterations
+
+    fail_small()
+    ok(small, rs)  # restarts the tags
+    ok(big, rb)
+    fail_small()
+    ok(small, rs)  # restarts them again, from the same base
+    ok(big, rb)    # the same tags as the first run on the large path
+    ok(big, rb)
 
 
 def test_noalloc_rejects_sizes_beyond_scratch(gpu_available):
