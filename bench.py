@@ -256,7 +256,9 @@ def run_ours(args, rank, world, local_rank):
     # Round shape of the batched push from the project's autotuner, on this step's batch
     # (outside the timed region).
     pull_ratio = gp.ppr_batch_autotune(psrc, prm, reps=1)
-    sssp_tile = "per round: 512 edge-word steps with >= 16 per warp, else 128"
+    big, mn = gs.sssp_batch_autotune(ssrc, seeds=True, mode=c2g.SEEDS_EXACT, reps=1)
+    sssp_tile = {"big_steps": big, "min_tiles_per_warp": mn,
+                 "rule": "rounds with >= min_tiles_per_warp big tiles per warp walk big tiles, else 128 steps"}
     dist_d = torch.empty((nS, V), dtype=torch.int32, device=dev)
     pr_d = torch.empty((nP, V), dtype=torch.float32, device=dev)
     dist_h = torch.empty((nS, V), dtype=torch.int32).pin_memory().numpy()

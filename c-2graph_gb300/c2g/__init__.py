@@ -104,6 +104,10 @@ SIGNATURES = {
                                          _I32P, _I32P]),
     "c2g_sssp_batch": (ctypes.c_int, [_P, ctypes.c_int32, _P, ctypes.c_int, ctypes.c_int, _P, ctypes.c_int,
                                       ctypes.c_int, ctypes.POINTER(Stats)]),
+    "c2g_sssp_batch_set_tile": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int32]),
+    "c2g_sssp_batch_get_tile": (ctypes.c_int, [_P, _I32P, _I32P]),
+    "c2g_sssp_batch_autotune": (ctypes.c_int, [_P, ctypes.c_int32, _P, ctypes.c_int, ctypes.c_int, ctypes.c_int32,
+                                               ctypes.c_char_p, _I32P, _I32P]),
     "c2g_ppr": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.POINTER(PprParams), _P, _P, ctypes.c_int,
                                ctypes.POINTER(Stats)]),
     "c2g_ppr_set_config": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int32]),
@@ -266,6 +270,20 @@ class Graph:
                                        os.fsencode(json_path) if json_path else None, ctypes.byref(bd),
                                        ctypes.byref(bt)))
         return bd.value, bt.value
+
+    def sssp_batch_tile(self, big_steps=512, min_tiles_per_warp=16):
+        """Expansion tiles of the batched SSSP (see c2g_sssp_batch_set_tile)."""
+        _check(lib().c2g_sssp_batch_set_tile(self._h, big_steps, min_tiles_per_warp))
+
+    def sssp_batch_autotune(self, sources, seeds=False, mode=SEEDS_COMPAT, reps=1, json_path=None):
+        """Time the batched SSSP's tile candidates on this batch, apply the fastest valid
+        one and return it as (big_steps, min_tiles_per_warp)."""
+        src = np.ascontiguousarray(sources, dtype=np.int32)
+        bb, bm = ctypes.c_int32(), ctypes.c_int32()
+        _check(lib().c2g_sssp_batch_autotune(self._h, len(src), _ptr(src), int(seeds), mode, int(reps),
+                                             os.fsencode(json_path) if json_path else None, ctypes.byref(bb),
+                                             ctypes.byref(bm)))
+        return bb.value, bm.value
 
     def resolve_source(self, source, pruned=False, mode=SEEDS_COMPAT):
         out = ctypes.c_int32()

@@ -9,11 +9,19 @@
 //   purn-sssp <dir>            src/purn-sssp.cpp:61-352
 //   purn-ppr  <dir>            src/purn-ppr.cpp:63-344
 //
-// Output lines kept from the reference: the dataset path, graph sizes, the iteration
-// count, ten "i<TAB>value" result lines, "gpu runtime: <s> seconds" (all 10 launches),
-// and the adjusted source.  A missing input prints "file:<f> not exist." to stderr and
-// exits 0 (core/io.hpp:27-30); other errors print the message and exit 255, as
-// CUDA_ERROR's exit(-1) does (core/Util.cuh:17-24).
+// Standard output follows the reference programs line for line: the dataset path
+// (sssp-*, ppr-purn), the Graph constructor's three lines, the device line (sssp-*),
+// "test for study how to use cuda", the start banner, the per-launch "csr_v" line
+// (ppr-purn), "source = <s>end ------------10" (PPR programs), "gpu runtime: <s> seconds"
+// over the 10 launches, the "flag ... iteration_num：<n>" line, ten (SSSP) or eleven (PPR)
+// result lines, "源顶点source = <s>" (SSSP), the end banner and the Graph destructor's
+// line (src/sssp/purn/Main.cu:24-56,108-123, src/sssp/base/Main.cu:22-100,
+// src/ppr/purn/Main.cu:33-136,448, src/ppr/base/Main.cu:38-110,408,
+// src/adsorption/w-base/Main.cu:39-113, src/sssp/purn/Graph.h:44-46,61).  Numbers print
+// as an ostream prints them (%g for times and floats).  adsorption-base leaves out the
+// reference's per-round "act_num" trace.  A missing input prints "file:<f> not exist." to
+// stderr and exits 0 (core/io.hpp:27-30); other errors print the message and exit 255,
+// as CUDA_ERROR's exit(-1) does (core/Util.cuh:17-24).
 //
 // Environment: C2G_SEEDS=exact makes sssp-purn use the record->vertex sidecar instead
 // of the reference's vertex-indexed hvlist read.
@@ -26,6 +34,13 @@
 
 #include "../../include/c2graph.h"
 
+// The reference's labelled lines (UTF-8, as its sources spell them).
+static const char kFlagLine[] = "flag \u5df2\u8bbe\u7f6e\u6210 -1  \u7ec8\u6b62\u6761\u4ef6\u4ee5\u6ee1\u8db3"
+                                "\t\titeration_num\uff1a%d\n";
+static const char kSourceLine[] = "\u6e90\u9876\u70b9source = %d\n";
+static const char kPprBanner[] = "==================== PPR with FORWARD PUSH %s ====================";
+static const char kSsspBanner[] = "==================== SSSP with FORWARD PUSH %s ============";
+
 static int die(int rc) {
     const char* msg = c2g_last_error();
     if (rc == C2G_ERR_IO) {
@@ -36,49 +51,78 @@ static int die(int rc) {
     exit(255);
 }
 
-static void print_graph(c2g_graph* g) {
+static c2g_graph* load(const char* dir, int variant) {
+    c2g_graph* g = nullptr;
+    int rc = c2g_graph_load(dir, variant, 0, &g);
+    if (rc) die(rc);
     int32_t V = 0, R = 0;
     int64_t E = 0;
     c2g_graph_info(g, &V, &E, &R);
     printf("INIT--class Graph is constructed\n");
     printf("The vertex num is:%d\n", V);
     printf("The edge num is:%lld\n", (long long)E);
+    return g;
+}
+
+static void graph_done(c2g_graph* g) {
+    c2g_graph_free(g);
+    printf("CLEAR--class Graph is destroyed\n");
+}
+
+// Two consecutive int32 values of <dir>/<sub>/<name>.bin at index i (row bounds).
+static int read_pair(const char* dir, const char* sub, const char* name, int32_t i, int32_t* a, int32_t* b) {
+    std::string path = std::string(dir) + "/" + sub + "/" + name + ".bin";
+    FILE* f = fopen(path.c_str(), "rb");
+    if (!f) return -1;
+    int32_t v[2] = {0, 0};
+    const bool ok = fseek(f, (long)i * 4, SEEK_SET) == 0 && fread(v, 4, 2, f) == 2;
+    fclose(f);
+    *a = v[0];
+    *b = v[1];
+    return ok ? 0 : -1;
 }
 
 static int run_sssp(const char* dir, int32_t source, bool pruned) {
     printf("%s\n", dir);
-    c2g_graph* g = nullptr;
-    int rc = c2g_graph_load(dir, pruned ? C2G_GRAPH_SSSP : C2G_GRAPH_ORIGIN, 0, &g);
-    if (rc) die(rc);
-    print_graph(g);
+    c2g_graph* g = load(dir, pruned ? C2G_GRAPH_SSSP : C2G_GRAPH_ORIGIN);
+    int ndev = 0;
+    c2g_device_count(&ndev);
+    printf(ndev > 0 ? "Using GPU device 0\n" : "No GPU available, falling back to CPU\n");
+    printf("test for study how to use cuda\n");
     const char* env = getenv("C2G_SEEDS");
     const int mode = (env && strcmp(env, "exact") == 0) ? C2G_SEEDS_EXACT : C2G_SEEDS_COMPAT;
     int32_t s = source;
+    int rc;
     if ((rc = c2g_sssp_resolve_source(g, source, pruned ? 1 : 0, mode, &s))) die(rc);
     int32_t V = 0;
     c2g_graph_info(g, &V, nullptr, nullptr);
     std::vector<int32_t> dist((size_t)V);
-    printf("\n==================== SSSP with FORWARD PUSH starts ============\n");
+    printf("\n");
+    printf(kSsspBanner, "starts");
+    printf("\n");
     c2g_stats st;
     double total_ms = 0.0;
     for (int i = 0; i < 10; ++i) {  // the reference times 10 launches on one source
         if ((rc = c2g_sssp(g, s, pruned ? 1 : 0, mode, dist.data(), 0, &st))) die(rc);
         total_ms += st.device_ms;
     }
-    printf("iteration_num:%d\n", st.iterations);
+    if (!pruned) {
+        printf("\n");
+        printf(kSsspBanner, "ends");
+        printf("\n");
+    }
+    printf(kFlagLine, st.iterations);
     for (int i = 0; i < 10 && i < V; ++i) printf("%d\t%d\n", i, dist[i]);
     printf("gpu runtime: %g seconds\n", total_ms / 1000.0);
-    printf("source = %d\n", s);
-    c2g_graph_free(g);
+    printf(kSourceLine, s);
+    graph_done(g);
     return 0;
 }
 
 static int run_ppr(const char* dir, int32_t source, bool pruned, bool adsorption) {
-    printf("%s\n", dir);
-    c2g_graph* g = nullptr;
-    int rc = c2g_graph_load(dir, pruned ? C2G_GRAPH_PPR : C2G_GRAPH_ORIGIN, 0, &g);
-    if (rc) die(rc);
-    print_graph(g);
+    if (pruned) printf("%s\n", dir);
+    c2g_graph* g = load(dir, pruned ? C2G_GRAPH_PPR : C2G_GRAPH_ORIGIN);
+    printf("test for study how to use cuda\n");
     int32_t V = 0;
     c2g_graph_info(g, &V, nullptr, nullptr);
     if (source < 0 || source >= V) {
@@ -88,19 +132,28 @@ static int run_ppr(const char* dir, int32_t source, bool pruned, bool adsorption
     c2g_ppr_params p;
     c2g_ppr_default_params(g, adsorption ? 1 : 0, &p);
     std::vector<float> pr((size_t)V), res((size_t)V);
-    printf("\n==================== PPR with FORWARD PUSH starts ====================\n");
+    printf("\n");
+    printf(kPprBanner, "starts");
+    printf("\n");
+    int32_t h0 = 0, h1 = 0, v0 = 0, v1 = 0;
+    if (pruned && (read_pair(dir, "ppr", "hvlist", source, &h0, &h1) || read_pair(dir, "ppr", "vlist", source, &v0, &v1)))
+        die(C2G_ERR_IO);
     c2g_stats st;
     double total_ms = 0.0;
     for (int i = 0; i < 10; ++i) {
-        if ((rc = c2g_ppr(g, source, &p, pr.data(), res.data(), 0, &st))) die(rc);
+        if (pruned) printf("csr_v %d--%d\n", h1 - h0, v1 - v0);
+        int rc = c2g_ppr(g, source, &p, pr.data(), res.data(), 0, &st);
+        if (rc) die(rc);
         total_ms += st.device_ms;
     }
-    printf("source = %d end ------------10\n", source);
+    printf("source = %dend ------------10\n", source);
     printf("gpu runtime: %g seconds\n", total_ms / 1000.0);
-    printf("iteration_num:%d\n", st.iterations);
-    printf("==================== PPR with FORWARD PUSH ends ====================\n\n");
-    for (int i = 0; i <= 10 && i < V; ++i) printf("%d.\tpagerank\t %g\tresidual\t%g\n", i, pr[i], res[i]);
-    c2g_graph_free(g);
+    printf(kFlagLine, st.iterations);
+    printf(kPprBanner, "ends");
+    printf("\n\n");
+    for (int i = 0; i <= 10 && i < V; ++i)
+        printf("%d.\tpagerank\t %g\tresidual\t%g\n", i, (double)pr[i], (double)res[i]);
+    graph_done(g);
     return 0;
 }
 

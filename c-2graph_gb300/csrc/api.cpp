@@ -427,6 +427,30 @@ int c2g_ppr_batch_set_pull(c2g_graph* g, float ratio) {
     return C2G_OK;
 }
 
+static int log2_exact(int32_t x) {
+    int l = 0;
+    while (l < 31 && (1 << l) < x) ++l;
+    return (1 << l) == x ? l : -1;
+}
+
+int c2g_sssp_batch_set_tile(c2g_graph* g, int32_t big_steps, int32_t min_tiles_per_warp) {
+    if (!g) return fail(C2G_ERR_ARG, "graph is NULL");
+    const int lb = log2_exact(big_steps), lm = log2_exact(min_tiles_per_warp);
+    if (lb < 7 || lb > 12) return fail(C2G_ERR_ARG, "big_steps must be a power of two in [128, 4096]");
+    if (lm < 0 || lm > 10) return fail(C2G_ERR_ARG, "min_tiles_per_warp must be a power of two in [1, 1024]");
+    std::lock_guard<std::mutex> lk(g->mu);
+    g->sssp_cfg.batch_tile_big_log = lb;
+    g->sssp_cfg.batch_tile_min_log = lm;
+    return C2G_OK;
+}
+
+int c2g_sssp_batch_get_tile(const c2g_graph* g, int32_t* big_steps, int32_t* min_tiles_per_warp) {
+    if (!g) return fail(C2G_ERR_ARG, "graph is NULL");
+    if (big_steps) *big_steps = 1 << g->sssp_cfg.batch_tile_big_log;
+    if (min_tiles_per_warp) *min_tiles_per_warp = 1 << g->sssp_cfg.batch_tile_min_log;
+    return C2G_OK;
+}
+
 int c2g_sssp_resolve_source(const c2g_graph* g, int32_t source, int pruned, int mode, int32_t* adjusted) {
     if (!g || !adjusted) return fail(C2G_ERR_ARG, "NULL argument");
     for (int32_t s = source;; ++s) {

@@ -52,20 +52,28 @@ struct BatchParams {
     int max_iter;
     unsigned long long barrier_ns;
     long long* counters;  // [2]: relaxations (query, edge), edge-word steps
+    int tile_big_log;     // log2 of the big tile's edge-word steps (>= kBatchTileLog)
+    int tile_min_log;     // a round walks big tiles when it has >= 2^tile_min_log of them per warp
 };
 
 // Warp tiles of the expansion: markers are laid every 2^kBatchTileLog edge-word steps; a
-// round with enough work (at least 16 big tiles per warp) walks tiles of 2^kBatchTileBig
-// steps (every 4th marker), a smaller one tiles of 2^kBatchTileLog.  256 sources at
-// scale 22: 132 ms per SSSP batch with 128-step tiles, 121 ms with 512; 32 sources at
-// scale 20: 4.6 ms with 128, 5.4 ms with 512 (too few tiles per warp).
+// round with enough work (at least 2^tile_min_log big tiles per warp) walks tiles of
+// 2^tile_big_log steps (every 2^(big - kBatchTileLog)-th marker), a smaller one tiles of
+// 2^kBatchTileLog.  The handle's defaults are big 512, at least 16 per warp (256 sources
+// at scale 22: 132 ms per SSSP batch with 128-step tiles, 121 ms with 512; 32 sources at
+// scale 20: 4.6 ms with 128, 5.4 ms with 512, too few tiles per warp);
+// c2g_sssp_batch_autotune picks them per batch.
 constexpr int kBatchTileLog = 7;
-constexpr int kBatchTileBig = 9;
 
-__device__ __forceinline__ int batch_tile_log(unsigned T, unsigned nwarps) {
-    return (unsigned long long)T >= ((unsigned long long)nwarps << (kBatchTileBig + 4)) ? kBatchTileBig
-                                                                                         : kBatchTileLog;
+__device__ __forceinline__ int batch_tile_log(unsigned T, unsigned nwarps, int big, int min_log) {
+    return big > kBatchTileLog && (unsigned long long)T >= ((unsigned long long)nwarps << (big + min_log))
+               ? big
+               : kBatchTileLog;
 }
+
+// The batched push walks big tiles of 512 steps in rounds with at least 16 per warp.
+constexpr int kPushTileBig = 9;
+constexpr int kPushTileMin = 4;
 
 __device__ __forceinline__ FrontierOut batch_out(const BatchParams& p, int buf, int slot) {
     FrontierOut o;
@@ -220,7 +228,7 @@ __global__ void __launch_bounds__(kSsspBatchThreads, 3) sssp_batch_persistent(co
         const int2* q = p.q[buf];
         const unsigned* qm = p.qmask[buf];
         const int* mark = p.mark[buf];
-        const int tl = batch_tile_log(T, nwarps);
+        const int tl = batch_tile_log(T, nwarps, p.tile_big_log, p.tile_min_log);
         const unsigned tile = 1u << tl;
         const unsigned ntiles = (T + tile - 1) >> tl;
         unsigned* tctr = &ctl->tilectr[slot];
@@ -500,6 +508,8 @@ int sssp_batch_launch(c2g_graph* g, int32_t nq, const int32_t* sources, const st
     p.max_iter = g->sssp_cfg.max_iter;
     p.barrier_ns = g->barrier_ns ? g->barrier_ns : 4000000000ull;
     p.counters = w->counters;
+    p.tile_big_log = g->sssp_cfg.batch_tile_big_log;
+    p.tile_min_log = g->sssp_cfg.batch_tile_min_log;
     C2G_CUDA(cudaMemsetAsync(w->ctl, 0, sizeof(TraversalCtl), g->stream));
     C2G_CUDA(cudaMemsetAsync(w->counters, 0, sizeof(long long) * 2, g->stream));
     void* args[] = {&p};
@@ -1037,7 +1047,7 @@ __global__ void __launch_bounds__(kPprBatchThreads, 3) ppr_batch_persistent(cons
             const unsigned* qm = p.qmask[buf];
             const int* mark = p.mark[buf];
             const double* rqb = p.rq[buf];
-            const int tl = batch_tile_log(T, nwarps);
+            const int tl = batch_tile_log(T, nwarps, kPushTileBig, kPushTileMin);
             const unsigned tile = 1u << tl;
             const unsigned ntiles = (T + tile - 1) >> tl;
             unsigned* tctr = &ctl->tilectr[cur % 3];

@@ -89,6 +89,8 @@ struct SsspConfig {
     int delta = 0;       // <= 0: no near/far split
     int log_tile = 8;    // 256 edges per warp tile
     int max_iter = 1 << 20;
+    int batch_tile_big_log = 9;  // batched expansion: 512 edge-word steps per big tile
+    int batch_tile_min_log = 4;  // ... in rounds with at least 16 big tiles per warp
 };
 
 struct PprConfig {

@@ -196,6 +196,24 @@ int c2g_sssp_noalloc(const int32_t* row, const void* adj, int32_t V, int64_t E, 
 int c2g_sssp_batch(c2g_graph* g, int32_t n, const int32_t* sources, int use_seeds, int seed_mode,
                    int32_t* dist, int dist_on_device, int layout, c2g_stats* stats);
 
+/* Expansion tiles of the batched SSSP (c2g_sssp_batch; no counterpart in the reference,
+ * whose launch geometry is fixed at compile time, core/Util.cuh:31-34).  Warps take tiles
+ * of edge-word steps; a round with at least min_tiles_per_warp tiles of big_steps per
+ * warp walks those, a smaller round tiles of 128 steps.  big_steps: power of two in
+ * [128, 4096] (128: always small tiles); min_tiles_per_warp: power of two in [1, 1024].
+ * Defaults 512 and 16.  Distances do not depend on the setting. */
+int c2g_sssp_batch_set_tile(c2g_graph* g, int32_t big_steps, int32_t min_tiles_per_warp);
+int c2g_sssp_batch_get_tile(const c2g_graph* g, int32_t* big_steps, int32_t* min_tiles_per_warp);
+
+/* Autotuner of those tiles (no counterpart in the reference): times 128-step tiles and
+ * big_steps {256, 512, 1024, 2048} x min_tiles_per_warp {4, 16, 64} on this batch (one
+ * warm-up launch, then `reps` timed), rejects any candidate whose distances differ from
+ * the first's on the first 8 queries, applies the fastest, returns it, and writes every
+ * timing as JSON to json_path (may be NULL). */
+int c2g_sssp_batch_autotune(c2g_graph* g, int32_t n, const int32_t* sources, int use_seeds, int seed_mode,
+                            int32_t reps, const char* json_path, int32_t* best_big_steps,
+                            int32_t* best_min_tiles);
+
 /* Autotuner: time every (delta, tile) candidate of the SSSP kernel on the sample
  * sources (distances must agree across candidates), apply the fastest to the handle,
  * return it, and write every timing as JSON to json_path (may be NULL).  The reference's

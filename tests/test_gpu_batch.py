@@ -50,6 +50,50 @@ def test_batch_vs_dijkstra(gpu_available, g17w, n):
             assert np.array_equal(dist[i], ref), (n, i, s)
 
 
+def test_batch_tiles_and_autotune(gpu_available, g17w, tmp_path):
+    """Every tile shape gives the same distances (Dijkstra); the autotuner times its 13
+    candidates, keeps a valid one and applies it."""
+    import json
+
+    import c2g
+    import oracle
+
+    o = oracle.load_dataset(g17w, "origin")
+    src = _sources(o["vlist"], 96, 5)
+    refs = [oracle.dijkstra(o["vlist"], o["elist"], o["wlist"], [int(s)], [0]) for s in src[:6]]
+    with c2g.Graph.load(g17w, "origin") as gr:
+        for big, mn in ((128, 1), (256, 1), (1024, 4), (4096, 1024)):
+            gr.sssp_batch_tile(big, mn)
+            dist, st = gr.sssp_batch(src)
+            assert st.status_flags == 0
+            for i in range(6):
+                assert np.array_equal(dist[i], refs[i]), (big, mn, i)
+        with pytest.raises(c2g.C2GError):
+            gr.sssp_batch_tile(100, 4)
+        with pytest.raises(c2g.C2GError):
+            gr.sssp_batch_tile(512, 3)
+        path = str(tmp_path / "tile.json")
+        big, mn = gr.sssp_batch_autotune(src, reps=1, json_path=path)
+        rec = json.load(open(path))
+        assert len(rec["candidates"]) == 13 and all(c["valid"] for c in rec["candidates"])
+        assert (rec["best"]["big_steps"], rec["best"]["min_tiles_per_warp"]) == (big, mn)
+        b = ctypes_tile(gr)
+        assert b == (big, mn)
+        dist, _ = gr.sssp_batch(src)
+        for i in range(6):
+            assert np.array_equal(dist[i], refs[i])
+
+
+def ctypes_tile(gr):
+    import ctypes
+
+    import c2g
+
+    b, m = ctypes.c_int32(), ctypes.c_int32()
+    assert c2g.lib().c2g_sssp_batch_get_tile(gr._h, ctypes.byref(b), ctypes.byref(m)) == 0
+    return b.value, m.value
+
+
 def test_batch_matches_single_query_with_seeds(gpu_available, g16):
     import c2g
 
