@@ -13,6 +13,7 @@
 namespace c2g {
 
 int build_adj(c2g_graph* g, const int32_t* col, const int32_t* w, int2** out);
+int stream_graph(c2g_graph* g, const std::string& elist_path, const std::string* w_path, const std::string* f_path);
 void adjoint_free(c2g_graph* g);
 
 static const int kNoSidecar = -2;
@@ -75,16 +76,21 @@ static int graph_new(int device, c2g_graph** out) {
     return C2G_OK;
 }
 
-static int graph_fill(c2g_graph* g, const std::vector<int32_t>& vlist, const int32_t* elist, int64_t E,
-                      const int32_t* wlist, const float* flist) {
+static int graph_fill_rows(c2g_graph* g, const std::vector<int32_t>& vlist) {
     g->V = (int32_t)vlist.size() - 1;
-    g->E = E;
     g->h_row = vlist;
     C2G_CUDA(cudaMalloc(&g->row, sizeof(int32_t) * vlist.size()));
     C2G_CUDA(cudaMemcpyAsync(g->row, vlist.data(), sizeof(int32_t) * vlist.size(), cudaMemcpyHostToDevice,
                              g->stream));
     C2G_CUDA(cudaStreamSynchronize(g->stream));
+    return C2G_OK;
+}
+
+static int graph_fill(c2g_graph* g, const std::vector<int32_t>& vlist, const int32_t* elist, int64_t E,
+                      const int32_t* wlist, const float* flist) {
     int rc;
+    if ((rc = graph_fill_rows(g, vlist))) return rc;
+    g->E = E;
     if (wlist && (rc = build_adj(g, elist, wlist, &g->adj_w))) return rc;
     if (flist && (rc = build_adj(g, elist, reinterpret_cast<const int32_t*>(flist), &g->adj_f))) return rc;
     return C2G_OK;
@@ -290,37 +296,35 @@ int c2g_graph_load(const char* dir, int variant, int device, c2g_graph** out) {
         default: return fail(C2G_ERR_ARG, "bad graph variant %d", variant);
     }
     const std::string d = base + sub;
-    std::vector<int32_t> vlist, elist, wlist, hv, he, hwi, hvmap;
-    std::vector<float> flist, hwf;
+    std::vector<int32_t> vlist, hv, he, hwi, hvmap;
+    std::vector<float> hwf;
     int rc;
     if ((rc = read_array4(d + "vlist.bin", vlist))) return rc;
-    if ((rc = read_array4(d + "elist.bin", elist))) return rc;
-    const int32_t* wp = nullptr;
-    const float* fp = nullptr;
+    // Edge arrays are streamed from their files (stream_load.cpp); which weight kinds:
+    std::string wpath, fpath;
     if (variant == C2G_GRAPH_ORIGIN) {
-        const bool hw = file_exists(d + "wlist.bin"), hf = file_exists(d + "flist.bin");
-        if (!hw && !hf) return fail(C2G_ERR_IO, "file:%swlist.bin not exist.", d.c_str());
-        if (hw && (rc = read_array4(d + "wlist.bin", wlist))) return rc;
-        if (hf && (rc = read_array4(d + "flist.bin", flist))) return rc;
-        if (hw) wp = wlist.data();
-        if (hf) fp = flist.data();
+        if (file_exists(d + "wlist.bin")) wpath = d + "wlist.bin";
+        if (file_exists(d + "flist.bin")) fpath = d + "flist.bin";
+        if (wpath.empty() && fpath.empty()) return fail(C2G_ERR_IO, "file:%swlist.bin not exist.", d.c_str());
     } else if (variant == C2G_GRAPH_SSSP) {
-        if ((rc = read_array4(d + "wlist.bin", wlist))) return rc;
-        wp = wlist.data();
+        wpath = d + "wlist.bin";
+    } else {
+        fpath = d + "wlist.bin";  // ppr/wlist.bin holds float weights
+    }
+    if (!file_exists(d + "elist.bin")) return fail(C2G_ERR_IO, "file:%selist.bin not exist.", d.c_str());
+    for (const std::string* path : {&wpath, &fpath})
+        if (!path->empty() && !file_exists(*path)) return fail(C2G_ERR_IO, "file:%s not exist.", path->c_str());
+    if (variant == C2G_GRAPH_SSSP) {
         if ((rc = read_array4(d + "hvlist.bin", hv))) return rc;
         if ((rc = read_array4(d + "helist.bin", he))) return rc;
         if ((rc = read_array4(d + "hwlist.bin", hwi))) return rc;
         if (file_exists(d + "hvmap.bin") && (rc = read_array4(d + "hvmap.bin", hvmap))) return rc;
-    } else {
-        if ((rc = read_array4(d + "wlist.bin", flist))) return rc;
-        fp = flist.data();
+    } else if (variant == C2G_GRAPH_PPR) {
         if ((rc = read_array4(d + "hvlist.bin", hv))) return rc;
         if ((rc = read_array4(d + "helist.bin", he))) return rc;
         if ((rc = read_array4(d + "hwlist.bin", hwf))) return rc;
     }
-    if ((rc = check_csr(vlist, elist))) return rc;
-    if ((wp && wlist.size() < elist.size()) || (fp && flist.size() < elist.size()))
-        return fail(C2G_ERR_FORMAT, "weight file shorter than elist in %s", d.c_str());
+    if ((rc = check_rows(vlist))) return rc;
     if (variant != C2G_GRAPH_ORIGIN) {
         if (hv.empty()) return fail(C2G_ERR_FORMAT, "%shvlist.bin is empty", d.c_str());
         const int64_t H = hv.back();
@@ -333,7 +337,8 @@ int c2g_graph_load(const char* dir, int variant, int device, c2g_graph** out) {
     c2g_graph* g = nullptr;
     if ((rc = graph_new(device, &g))) return rc;
     DeviceScope ds(device);
-    if ((rc = graph_fill(g, vlist, elist.data(), (int64_t)elist.size(), wp, fp))) {
+    if ((rc = graph_fill_rows(g, vlist)) ||
+        (rc = stream_graph(g, d + "elist.bin", wpath.empty() ? nullptr : &wpath, fpath.empty() ? nullptr : &fpath))) {
         graph_release(g);
         return rc;
     }

@@ -43,6 +43,30 @@ int build_adj(c2g_graph* g, const int32_t* col, const int32_t* w, int2** out) {
     return C2G_OK;
 }
 
+// One chunk of the streaming ingest (c2g_graph_load): n edges starting at edge `base`,
+// read from page-locked host memory mapped into the device's address space.  Writes the
+// (target, weight) records of every weight kind present and checks each target against
+// V (the flag records the first bad edge; the target is still stored, never used as an
+// index here).
+__global__ void interleave_chunk_kernel(const int* __restrict__ col, const int* __restrict__ w,
+                                        const int* __restrict__ f, int2* __restrict__ adj_w, int2* __restrict__ adj_f,
+                                        long long base, long long n, int V, long long* bad) {
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const int c = col[i];
+        if ((unsigned)c >= (unsigned)V) atomicMin(reinterpret_cast<unsigned long long*>(bad), (unsigned long long)(base + i));
+        if (adj_w) adj_w[base + i] = make_int2(c, w[i]);
+        if (adj_f) adj_f[base + i] = make_int2(c, f[i]);
+    }
+}
+
+int launch_interleave_chunk(c2g_graph* g, const int* col, const int* w, const int* f, int2* adj_w, int2* adj_f,
+                            long long base, long long n, long long* bad) {
+    interleave_chunk_kernel<<<g->num_sms * 4, 256, 0, g->stream>>>(col, w, f, adj_w, adj_f, base, n, g->V, bad);
+    C2G_CUDA(cudaGetLastError());
+    return C2G_OK;
+}
+
 __global__ void set_weight_bits_kernel(int2* __restrict__ adj, const int* __restrict__ w, long long E) {
     const long long stride = (long long)gridDim.x * blockDim.x;
     for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < E; e += stride) adj[e].y = w[e];

@@ -68,6 +68,15 @@ int make_dir(const std::string& path) {
     return C2G_OK;
 }
 
+int check_rows(const std::vector<int32_t>& vlist) {
+    if (vlist.empty()) return fail(C2G_ERR_FORMAT, "vlist is empty (needs V+1 entries)");
+    const int64_t V = (int64_t)vlist.size() - 1;
+    if (vlist[0] != 0) return fail(C2G_ERR_FORMAT, "vlist[0] = %d, expected 0", vlist[0]);
+    for (int64_t i = 0; i < V; ++i)
+        if (vlist[i + 1] < vlist[i]) return fail(C2G_ERR_FORMAT, "vlist not monotone at %lld", (long long)i);
+    return C2G_OK;
+}
+
 int check_csr(const std::vector<int32_t>& vlist, const std::vector<int32_t>& elist) {
     if (vlist.empty()) return fail(C2G_ERR_FORMAT, "vlist is empty (needs V+1 entries)");
     const int64_t V = (int64_t)vlist.size() - 1;

@@ -25,6 +25,8 @@ int read_array4(const std::string& path, std::vector<float>& out);
 int write_array4(const std::string& path, const void* data, size_t n);
 int make_dir(const std::string& path);
 
+// Check that vlist[V+1] is a row pointer: starts at 0, never decreases.
+int check_rows(const std::vector<int32_t>& vlist);
 // Check that vlist[V+1] is a CSR row pointer over E edges and elist ids are < V.
 int check_csr(const std::vector<int32_t>& vlist, const std::vector<int32_t>& elist);
 
