@@ -442,7 +442,8 @@ def run_serve(args):
         rng.shuffle(kinds)
         gaps = rng.exponential(1.0 / args.serve_rate, size=n)
         with c2g.Server(g, max_batch=256, alpha=ALPHA, rmax=RMAX, ads_iterations=30, p_inj=pp[:, 0],
-                        p_cont=pp[:, 1], p_abnd=pp[:, 2]) as srv:
+                        p_cont=pp[:, 1], p_abnd=pp[:, 2], epoch_rounds=args.serve_epoch_rounds,
+                        preempt_rounds=args.serve_preempt_rounds) as srv:
             # warm-up: one request of each kind (workspaces, graph capture)
             for k in (c2g.REQ_SSSP, c2g.REQ_PPR, c2g.REQ_ADSORPTION):
                 t = srv.submit(k, source=int(cand[0]), seeds=rng.choice(V, 16, replace=False) if k == 2 else None)
@@ -475,8 +476,11 @@ def run_serve(args):
             "config": {"workload": "rmat-s%d-ef%d unpruned, %d requests (%d SSSP / %d PPR / %d adsorption)" % (
                 args.serve_scale, args.edge_factor, n, kinds.count(0), kinds.count(1), kinds.count(2)),
                 "offered_rate_qps": args.serve_rate, "alpha": ALPHA, "rmax": RMAX, "ads_iterations": 30,
-                "ads_labels": 16},
-            "detail": {"batches": list(stats.batches), "max_batch": stats.max_batch, "admit_cap": list(stats.admit_cap),
+                "ads_labels": 16, "epoch_rounds": args.serve_epoch_rounds,
+                "preempt_rounds": args.serve_preempt_rounds,
+                "admission": "SSSP / PPR requests take free slots of the running batch at every epoch boundary"},
+            "detail": {"epochs_or_batches": list(stats.batches), "max_running": stats.max_batch,
+                       "admit_cap": list(stats.admit_cap), "evictions": stats.evictions,
                        "completed_after_warmup": stats.completed - base, "gen_s": gen_s, "wall_s": wall}}
     print(json.dumps(line), flush=True)
 
@@ -574,6 +578,8 @@ def main():
     ap.add_argument("--serve-scale", type=int, default=24)
     ap.add_argument("--serve-requests", type=int, default=200)
     ap.add_argument("--serve-rate", type=float, default=5000.0)
+    ap.add_argument("--serve-epoch-rounds", type=int, default=4)
+    ap.add_argument("--serve-preempt-rounds", type=int, default=0)
     ap.add_argument("--adjoint-scale", type=int, default=20)
     args = ap.parse_args()
     rank, world, local_rank = env_rank()

@@ -54,7 +54,8 @@ class Stats(ctypes.Structure):
 
 class ServerConfig(ctypes.Structure):
     _fields_ = [("max_batch", ctypes.c_int32), ("ads_iterations", ctypes.c_int32), ("alpha", ctypes.c_float),
-                ("rmax", ctypes.c_float), ("hbm_budget_bytes", ctypes.c_int64)]
+                ("rmax", ctypes.c_float), ("hbm_budget_bytes", ctypes.c_int64), ("epoch_rounds", ctypes.c_int32),
+                ("preempt_rounds", ctypes.c_int32)]
 
 
 class Request(ctypes.Structure):
@@ -65,7 +66,7 @@ class Request(ctypes.Structure):
 class ServerStats(ctypes.Structure):
     _fields_ = [("completed", ctypes.c_int64), ("batches", ctypes.c_int64 * 3), ("pending", ctypes.c_int64 * 3),
                 ("admit_cap", ctypes.c_int64 * 3), ("max_batch", ctypes.c_int64), ("p50_ms", ctypes.c_double),
-                ("p99_ms", ctypes.c_double), ("queries_per_s", ctypes.c_double)]
+                ("p99_ms", ctypes.c_double), ("queries_per_s", ctypes.c_double), ("evictions", ctypes.c_int64)]
 
 
 REQ_SSSP, REQ_PPR, REQ_ADSORPTION = 0, 1, 2
@@ -116,6 +117,7 @@ SIGNATURES = {
                                               ctypes.c_char_p, _P]),
     "c2g_graph_set_watchdog": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int32]),
     "c2g_graph_last_phases": (ctypes.c_int, [_P, _P]),
+    "c2g_graph_last_rounds": (ctypes.c_int, [_P, ctypes.c_int32, _P, _P, _P, _I32P]),
     "c2g_ppr_default_params": (ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(PprParams)]),
     "c2g_ppr_batch": (ctypes.c_int, [_P, ctypes.c_int32, _P, ctypes.POINTER(PprParams), _P, _P, ctypes.c_int,
                                      ctypes.c_int, ctypes.POINTER(Stats)]),
@@ -131,6 +133,16 @@ SIGNATURES = {
                                        ctypes.POINTER(ctypes.c_double)]),
     "c2g_server_get_stats": (ctypes.c_int, [_P, ctypes.POINTER(ServerStats)]),
     "c2g_server_destroy": (ctypes.c_int, [_P]),
+    "c2g_session_create": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int32, ctypes.POINTER(PprParams),
+                                          ctypes.POINTER(_P)]),
+    "c2g_session_admit": (ctypes.c_int, [_P, ctypes.c_int32, _I32P]),
+    "c2g_session_step": (ctypes.c_int, [_P, ctypes.c_int32, _P, ctypes.c_int32, _I32P, ctypes.POINTER(Stats)]),
+    "c2g_session_read": (ctypes.c_int, [_P, ctypes.c_int32, _P, _P, ctypes.c_int, ctypes.POINTER(Stats)]),
+    "c2g_session_evict": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.POINTER(_P)]),
+    "c2g_session_resume": (ctypes.c_int, [_P, _P, _I32P]),
+    "c2g_snapshot_free": (None, [_P]),
+    "c2g_session_slot": (ctypes.c_int, [_P, ctypes.c_int32, _I32P, _I32P, _I32P]),
+    "c2g_session_free": (None, [_P]),
     "c2g_rmat_write": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, ctypes.c_uint64,
                                       ctypes.c_int32, ctypes.c_int32, ctypes.c_double, ctypes.c_double,
                                       ctypes.c_double]),
@@ -322,6 +334,15 @@ class Graph:
         _check(lib().c2g_graph_last_phases(self._h, _ptr(out)))
         return tuple(float(x) for x in out)
 
+    def last_rounds(self):
+        """Per-round (ms, work units, pull) of the last batched launch on this handle."""
+        ms = np.zeros(1024, dtype=np.float64)
+        work = np.zeros(1024, dtype=np.int64)
+        shape = np.zeros(1024, dtype=np.int32)
+        n = ctypes.c_int32()
+        _check(lib().c2g_graph_last_rounds(self._h, 1024, _ptr(ms), _ptr(work), _ptr(shape), ctypes.byref(n)))
+        return ms[:n.value], work[:n.value], shape[:n.value]
+
     def watchdog(self, barrier_timeout_ms=0, stall_next_sssp=False):
         _check(lib().c2g_graph_set_watchdog(self._h, barrier_timeout_ms, int(bool(stall_next_sssp))))
 
@@ -421,13 +442,77 @@ class Graph:
         return Y, st
 
 
+class Session:
+    """Resident batch of one query kind (c2g_session_*): admit sources into slots, run
+    epochs, read finished results, evict running queries into snapshots and resume them."""
+
+    def __init__(self, graph, kind, slots, params=None):
+        self.graph = graph
+        self.kind = kind
+        self._h = _P()
+        _check(lib().c2g_session_create(graph._h, kind, slots, ctypes.byref(params) if params is not None else None,
+                                        ctypes.byref(self._h)))
+
+    def admit(self, source):
+        slot = ctypes.c_int32()
+        _check(lib().c2g_session_admit(self._h, int(source), ctypes.byref(slot)))
+        return slot.value
+
+    def step(self, rounds=4):
+        """One epoch; returns (finished slots, stats)."""
+        fin = np.zeros(1024, dtype=np.int32)
+        n = ctypes.c_int32()
+        st = Stats()
+        _check(lib().c2g_session_step(self._h, int(rounds), _ptr(fin), len(fin), ctypes.byref(n), ctypes.byref(st)))
+        return fin[:n.value].tolist(), st
+
+    def read(self, slot, want_res=False):
+        """Result of a finished slot (SSSP int32 distances; PPR (pr, res)); frees it."""
+        V = self.graph.V
+        st = Stats()
+        if self.kind == REQ_SSSP:
+            out = np.empty(V, dtype=np.int32)
+            _check(lib().c2g_session_read(self._h, slot, _ptr(out), None, 0, ctypes.byref(st)))
+            return out, st
+        pr = np.empty(V, dtype=np.float32)
+        res = np.empty(V, dtype=np.float32) if want_res else None
+        _check(lib().c2g_session_read(self._h, slot, _ptr(pr), _ptr(res), 0, ctypes.byref(st)))
+        return (pr, res), st
+
+    def evict(self, slot):
+        snap = _P()
+        _check(lib().c2g_session_evict(self._h, slot, ctypes.byref(snap)))
+        return snap
+
+    def resume(self, snap):
+        slot = ctypes.c_int32()
+        _check(lib().c2g_session_resume(self._h, snap, ctypes.byref(slot)))
+        return slot.value
+
+    def slot(self, slot):
+        st, src, rounds = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+        _check(lib().c2g_session_slot(self._h, slot, ctypes.byref(st), ctypes.byref(src), ctypes.byref(rounds)))
+        return st.value, src.value, rounds.value
+
+    def close(self):
+        if self._h:
+            lib().c2g_session_free(self._h)
+            self._h = _P()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+
 class Server:
     """Continuous-batching request loop over a device-resident graph."""
 
     def __init__(self, graph, max_batch=256, alpha=0.15, rmax=1e-7, ads_iterations=30, hbm_budget_bytes=0,
-                 p_inj=None, p_cont=None, p_abnd=None):
+                 p_inj=None, p_cont=None, p_abnd=None, epoch_rounds=4, preempt_rounds=0):
         self.graph = graph
-        cfg = ServerConfig(max_batch, ads_iterations, alpha, rmax, hbm_budget_bytes)
+        cfg = ServerConfig(max_batch, ads_iterations, alpha, rmax, hbm_budget_bytes, epoch_rounds, preempt_rounds)
         self._p = [None if a is None else np.ascontiguousarray(a, dtype=np.float32) for a in (p_inj, p_cont, p_abnd)]
         h = ctypes.c_void_p()
         _check(lib().c2g_server_create(graph._h, *[_ptr(a) for a in self._p], ctypes.byref(cfg), ctypes.byref(h)))

@@ -406,6 +406,32 @@ int c2g_graph_last_phases(const c2g_graph* g, double ms[4]) {
     return C2G_OK;
 }
 
+int c2g_graph_last_rounds(c2g_graph* g, int32_t cap, double* ms, int64_t* work, int32_t* shape, int32_t* n) {
+    if (!g || !n) return fail(C2G_ERR_ARG, "NULL argument");
+    *n = 0;
+    std::lock_guard<std::mutex> lk(g->mu);
+    if (!g->last_trace) return C2G_OK;
+    DeviceScope ds(g->device);
+    std::vector<RoundTrace> t((size_t)kMaxTraceRounds + 1);
+    C2G_CUDA(cudaMemcpyAsync(t.data(), g->last_trace, sizeof(RoundTrace) * t.size(), cudaMemcpyDeviceToHost,
+                             g->stream));
+    C2G_CUDA(cudaStreamSynchronize(g->stream));
+    int rounds = -1;
+    for (int i = 0; i <= kMaxTraceRounds; ++i)
+        if (t[(size_t)i].shape == -1) {
+            rounds = i;
+            break;
+        }
+    if (rounds < 0) return C2G_OK;  // the launch did not finish cleanly: no trace
+    for (int i = 0; i < rounds && i < cap; ++i) {
+        if (ms) ms[i] = (double)(t[(size_t)i + 1].t_ns - t[(size_t)i].t_ns) * 1e-6;
+        if (work) work[i] = t[(size_t)i].work;
+        if (shape) shape[i] = t[(size_t)i].shape;
+    }
+    *n = rounds;
+    return C2G_OK;
+}
+
 int c2g_graph_set_watchdog(c2g_graph* g, int32_t barrier_timeout_ms, int32_t stall_next_sssp) {
     if (!g) return fail(C2G_ERR_ARG, "graph is NULL");
     if (barrier_timeout_ms < 0) return fail(C2G_ERR_ARG, "barrier_timeout_ms must be >= 0");

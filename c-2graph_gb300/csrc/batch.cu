@@ -54,6 +54,8 @@ struct BatchParams {
     long long* counters;  // [2]: relaxations (query, edge), edge-word steps
     int tile_big_log;     // log2 of the big tile's edge-word steps (>= kBatchTileLog)
     int tile_min_log;     // a round walks big tiles when it has >= 2^tile_min_log of them per warp
+    int epoch_rounds;     // > 0: an epoch of a resident batch (no initialisation; at most this many rounds)
+    RoundTrace* trace;    // [kMaxTraceRounds + 1] per-round trace
 };
 
 // Warp tiles of the expansion: markers are laid every 2^kBatchTileLog edge-word steps; a
@@ -74,6 +76,10 @@ __device__ __forceinline__ int batch_tile_log(unsigned T, unsigned nwarps, int b
 // The batched push walks big tiles of 512 steps in rounds with at least 16 per warp.
 constexpr int kPushTileBig = 9;
 constexpr int kPushTileMin = 4;
+
+__device__ __forceinline__ void trace_round(RoundTrace* tr, int i, long long work, int shape) {
+    if (i <= kMaxTraceRounds) tr[i] = RoundTrace{globaltimer_ns(), work, shape, 0};
+}
 
 __device__ __forceinline__ FrontierOut batch_out(const BatchParams& p, int buf, int slot) {
     FrontierOut o;
@@ -166,6 +172,10 @@ __global__ void __launch_bounds__(kSsspBatchThreads, 3) sssp_batch_persistent(co
     WarpStage fst{sm.v0[wib], sm.d0[wib], sm.x0[wib], 0};
     int* qtab = sm.v1[wib];  // slot -> query position table of the owner being expanded
 
+    // An epoch of a resident batch starts from the state the previous epoch left: the
+    // distances and the improvement masks (queries that joined since have their column
+    // set and their source marked).
+    if (p.epoch_rounds == 0) {
     // Init: dist = INF (vector stores), masks = 0.
     {
         const size_t n4 = ((size_t)p.V * (size_t)p.Q) >> 2;
@@ -190,6 +200,7 @@ __global__ void __launch_bounds__(kSsspBatchThreads, 3) sssp_batch_persistent(co
             }
     }
     if (!grid_sync(bar, flags, p.barrier_ns)) return;
+    }
     phase_mark(ctl->phase_ns, tph, 0);
 
     long long relax = 0, steps = 0;
@@ -206,6 +217,7 @@ __global__ void __launch_bounds__(kSsspBatchThreads, 3) sssp_batch_persistent(co
         phase_mark(ctl->phase_ns, tph, 1);
         const unsigned long long c = ldcg(&ctl->qctr[slot]);
         const unsigned F = (unsigned)(c >> 32), T = (unsigned)c;
+        if (gtid == 0) trace_round(p.trace, iters, (long long)T, 0);
         if (F == 0) break;
         if (++iters > p.max_iter) {
             if (gtid == 0) atomicOr(flags, C2G_FLAG_ITER_CAP);
@@ -318,13 +330,18 @@ __global__ void __launch_bounds__(kSsspBatchThreads, 3) sssp_batch_persistent(co
         if (!grid_sync(bar, flags, p.barrier_ns)) return;
         phase_mark(ctl->phase_ns, tph, 2);
         ++cur;
+        // end of an epoch: the next round's improvements wait in the masks
+        if (p.epoch_rounds > 0 && iters >= p.epoch_rounds) break;
     }
     // relax is counted by lane 0 of each warp
     if (lane == 0) {
         atomicAdd((unsigned long long*)&p.counters[0], (unsigned long long)relax);
         atomicAdd((unsigned long long*)&p.counters[1], (unsigned long long)steps);
     }
-    if (gtid == 0) ctl->iterations = iters;
+    if (gtid == 0) {
+        ctl->iterations = iters;
+        trace_round(p.trace, iters, 0, -1);
+    }
 }
 
 // Copy dist[V][Q] (first nq queries) into the caller's layout.
@@ -405,6 +422,7 @@ struct BatchWork {
     int* seed_v = nullptr;
     int* seed_w = nullptr;
     int* stage = nullptr;  // caller-layout copy for host output
+    RoundTrace* trace = nullptr;
     size_t seed_cap = 0;
     int Q = 0;
     int V = 0;
@@ -413,14 +431,16 @@ struct BatchWork {
 static void batch_free_work(BatchWork* w) {
     if (!w) return;
     void* ptrs[] = {w->dist, w->mask, w->q[0], w->q[1], w->qmask[0], w->qmask[1], w->mark[0], w->mark[1],
-                    w->ctl, w->counters, w->src, w->seed_off, w->seed_v, w->seed_w, w->stage};
+                    w->ctl, w->counters, w->src, w->seed_off, w->seed_v, w->seed_w, w->stage, w->trace};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     delete w;
 }
 
 void batch_free(c2g_graph* g) {
-    batch_free_work(reinterpret_cast<BatchWork*>(g->batch));
+    BatchWork* w = reinterpret_cast<BatchWork*>(g->batch);
+    if (w && g->last_trace == w->trace) g->last_trace = nullptr;
+    batch_free_work(w);
     g->batch = nullptr;
 }
 
@@ -448,8 +468,67 @@ static int batch_alloc(c2g_graph* g, int Q, size_t n_seeds) {
     w->seed_cap = n_seeds > 0 ? n_seeds : 1;
     C2G_CUDA(cudaMalloc(&w->seed_v, sizeof(int) * w->seed_cap));
     C2G_CUDA(cudaMalloc(&w->seed_w, sizeof(int) * w->seed_cap));
+    C2G_CUDA(cudaMalloc(&w->trace, sizeof(RoundTrace) * (kMaxTraceRounds + 1)));
     w->Q = Q;
     w->V = g->V;
+    return C2G_OK;
+}
+
+static void sssp_batch_params(c2g_graph* g, BatchWork* w, int Q, int logW, BatchParams& p) {
+    p.row = g->row;
+    p.adj = g->adj_w;
+    p.E = (unsigned)g->E;
+    p.V = g->V;
+    p.logW = logW;
+    p.Q = Q;
+    p.nq = Q;
+    p.dist = w->dist;
+    p.mask = w->mask;
+    for (int b = 0; b < 2; ++b) {
+        p.q[b] = w->q[b];
+        p.qmask[b] = w->qmask[b];
+        p.mark[b] = w->mark[b];
+    }
+    p.ctl = w->ctl;
+    p.sources = w->src;
+    p.seed_off = nullptr;
+    p.seed_v = w->seed_v;
+    p.seed_w = w->seed_w;
+    p.qcap = (unsigned)((size_t)g->V * (size_t)(Q / 32));
+    p.mark_cap = (unsigned)((((size_t)g->E * (size_t)(Q / 32)) >> kBatchTileLog) + 2);
+    p.max_iter = g->sssp_cfg.max_iter;
+    p.barrier_ns = g->barrier_ns ? g->barrier_ns : 4000000000ull;
+    p.counters = w->counters;
+    p.tile_big_log = g->sssp_cfg.batch_tile_big_log;
+    p.tile_min_log = g->sssp_cfg.batch_tile_min_log;
+    p.epoch_rounds = 0;
+    p.trace = w->trace;
+    g->last_trace = w->trace;
+}
+
+static int sssp_batch_results(c2g_graph* g, BatchWork* w, int Q, int32_t nq, int32_t* out, int out_on_device,
+                              int query_major, float* ms, long long* counters, TraversalCtl* ctl_out) {
+    // Results in the caller's layout (pinned host memory is written directly).
+    int* dst = out;
+    int* direct = out_on_device ? nullptr : static_cast<int*>(mapped_host(out));
+    if (direct) {
+        dst = direct;
+    } else if (!out_on_device) {
+        if (!w->stage) C2G_CUDA(cudaMalloc(&w->stage, sizeof(int) * (size_t)g->V * (size_t)Q));
+        dst = w->stage;
+    }
+    if (query_major)
+        launch_transpose_qmajor<int, int>(w->dist, g->V, Q, nq, dst, g->stream);
+    else
+        batch_transpose<<<g->num_sms * 8, 256, 0, g->stream>>>(w->dist, g->V, Q, nq, dst, query_major);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess && !out_on_device && !direct)
+        e = cudaMemcpyAsync(out, dst, sizeof(int) * (size_t)g->V * (size_t)nq, cudaMemcpyDeviceToHost, g->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(ctl_out, w->ctl, sizeof(TraversalCtl), cudaMemcpyDeviceToHost, g->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(counters, w->counters, sizeof(long long) * 2, cudaMemcpyDeviceToHost, g->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+    C2G_CUDA(e);
+    C2G_CUDA(cudaEventElapsedTime(ms, g->ev0, g->ev1));
     return C2G_OK;
 }
 
@@ -484,32 +563,9 @@ int sssp_batch_launch(c2g_graph* g, int32_t nq, const int32_t* sources, const st
         }
     }
     BatchParams p;
-    p.row = g->row;
-    p.adj = g->adj_w;
-    p.E = (unsigned)g->E;
-    p.V = g->V;
-    p.logW = logW;
-    p.Q = Q;
+    sssp_batch_params(g, w, Q, logW, p);
     p.nq = nq;
-    p.dist = w->dist;
-    p.mask = w->mask;
-    for (int b = 0; b < 2; ++b) {
-        p.q[b] = w->q[b];
-        p.qmask[b] = w->qmask[b];
-        p.mark[b] = w->mark[b];
-    }
-    p.ctl = w->ctl;
-    p.sources = w->src;
     p.seed_off = seed_off ? w->seed_off : nullptr;
-    p.seed_v = w->seed_v;
-    p.seed_w = w->seed_w;
-    p.qcap = (unsigned)((size_t)g->V * (size_t)(Q / 32));
-    p.mark_cap = (unsigned)((((size_t)g->E * (size_t)(Q / 32)) >> kBatchTileLog) + 2);
-    p.max_iter = g->sssp_cfg.max_iter;
-    p.barrier_ns = g->barrier_ns ? g->barrier_ns : 4000000000ull;
-    p.counters = w->counters;
-    p.tile_big_log = g->sssp_cfg.batch_tile_big_log;
-    p.tile_min_log = g->sssp_cfg.batch_tile_min_log;
     C2G_CUDA(cudaMemsetAsync(w->ctl, 0, sizeof(TraversalCtl), g->stream));
     C2G_CUDA(cudaMemsetAsync(w->counters, 0, sizeof(long long) * 2, g->stream));
     void* args[] = {&p};
@@ -518,26 +574,46 @@ int sssp_batch_launch(c2g_graph* g, int32_t nq, const int32_t* sources, const st
     C2G_CUDA(cudaLaunchCooperativeKernel((const void*)sssp_batch_persistent, dim3(blocks), dim3(kSsspBatchThreads),
                                          args, 0, g->stream));
     C2G_CUDA(cudaEventRecord(g->ev1, g->stream));
-    // Results in the caller's layout (pinned host memory is written directly).
-    int* dst = out;
-    int* direct = out_on_device ? nullptr : static_cast<int*>(mapped_host(out));
-    if (direct) {
-        dst = direct;
-    } else if (!out_on_device) {
-        if (!w->stage) C2G_CUDA(cudaMalloc(&w->stage, sizeof(int) * (size_t)g->V * (size_t)Q));
-        dst = w->stage;
-    }
-    if (query_major)
-        launch_transpose_qmajor<int, int>(w->dist, g->V, Q, nq, dst, g->stream);
-    else
-        batch_transpose<<<g->num_sms * 8, 256, 0, g->stream>>>(w->dist, g->V, Q, nq, dst, query_major);
-    cudaError_t e = cudaGetLastError();
-    if (e == cudaSuccess && !out_on_device && !direct)
-        e = cudaMemcpyAsync(out, dst, sizeof(int) * (size_t)g->V * (size_t)nq, cudaMemcpyDeviceToHost, g->stream);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(ctl_out, w->ctl, sizeof(TraversalCtl), cudaMemcpyDeviceToHost, g->stream);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(counters, w->counters, sizeof(long long) * 2, cudaMemcpyDeviceToHost, g->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
-    C2G_CUDA(e);
+    return sssp_batch_results(g, w, Q, nq, out, out_on_device, query_major, ms, counters, ctl_out);
+}
+
+// Resident batch (c2g_session): the workspace of Q query slots with every mask clear, and
+// one epoch of at most `rounds` rounds from the state the previous epoch left.
+int sssp_batch_reserve(c2g_graph* g, int Q, int** dist, unsigned** mask) {
+    if (!g->adj_w) return fail(C2G_ERR_UNSUPPORTED, "graph has no int32 weights (wlist)");
+    if ((size_t)g->V * (size_t)(Q / 32) >= (size_t(1) << 31) || (size_t)g->E * (size_t)(Q / 32) >= (size_t(1) << 32))
+        return fail(C2G_ERR_RANGE, "%d slots too many for this graph", Q);
+    int rc;
+    if ((rc = batch_alloc(g, Q, 0))) return rc;
+    BatchWork* w = reinterpret_cast<BatchWork*>(g->batch);
+    C2G_CUDA(cudaMemsetAsync(w->mask, 0, sizeof(unsigned) * (size_t)g->V * (size_t)(Q / 32), g->stream));
+    C2G_CUDA(cudaStreamSynchronize(g->stream));
+    *dist = w->dist;
+    *mask = w->mask;
+    return C2G_OK;
+}
+
+int sssp_batch_epoch(c2g_graph* g, int Q, int rounds, float* ms, long long* counters, TraversalCtl* ctl_out) {
+    BatchWork* w = reinterpret_cast<BatchWork*>(g->batch);
+    if (!w || w->Q < Q) return fail(C2G_ERR_ARG, "resident SSSP batch has no workspace");
+    int logW = 0;
+    while ((32 << logW) < Q) ++logW;
+    int per_sm = 0;
+    C2G_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sssp_batch_persistent, kSsspBatchThreads, 0));
+    if (per_sm < 1) return fail(C2G_ERR_CUDA, "batch kernel cannot be resident");
+    BatchParams p;
+    sssp_batch_params(g, w, Q, logW, p);
+    p.epoch_rounds = rounds < 1 ? 1 : rounds;
+    C2G_CUDA(cudaMemsetAsync(w->ctl, 0, sizeof(TraversalCtl), g->stream));
+    C2G_CUDA(cudaMemsetAsync(w->counters, 0, sizeof(long long) * 2, g->stream));
+    void* args[] = {&p};
+    C2G_CUDA(cudaEventRecord(g->ev0, g->stream));
+    C2G_CUDA(cudaLaunchCooperativeKernel((const void*)sssp_batch_persistent, dim3(grid_blocks(g, per_sm)),
+                                         dim3(kSsspBatchThreads), args, 0, g->stream));
+    C2G_CUDA(cudaEventRecord(g->ev1, g->stream));
+    C2G_CUDA(cudaMemcpyAsync(ctl_out, w->ctl, sizeof(TraversalCtl), cudaMemcpyDeviceToHost, g->stream));
+    C2G_CUDA(cudaMemcpyAsync(counters, w->counters, sizeof(long long) * 2, cudaMemcpyDeviceToHost, g->stream));
+    C2G_CUDA(cudaStreamSynchronize(g->stream));
     C2G_CUDA(cudaEventElapsedTime(ms, g->ev0, g->ev1));
     return C2G_OK;
 }
@@ -570,6 +646,7 @@ struct PprBatchParams {
     float2* rqf[2];   // the same as a float pair hi + lo (pull rounds)
     unsigned* amask[2];  // [V][W] lanes activated with out-edges, by frontier buffer (pull lookup)
     unsigned* tmask;  // [V][W] touched lanes this round, zero between rounds
+    unsigned* dmask;  // [V][W] lanes activated without out-edges (popped next round), zero between launches
     int2* q[2];       // frontier entries (v*W + w, edge base)
     unsigned* qmask[2];
     int* mark[2];
@@ -592,6 +669,9 @@ struct PprBatchParams {
     const int* mark_r;
     unsigned ntiles_r;
     unsigned long long pull_min;
+    int epoch_rounds;  // > 0: an epoch of a resident batch (state at rest in the arrays; at most this many rounds)
+    int cur0;          // round index the epoch starts at (its parity picks the frontier buffers)
+    RoundTrace* trace;  // [kMaxTraceRounds + 1] per-round trace
 };
 
 __device__ __forceinline__ FrontierOut pbatch_out(const PprBatchParams& p, int buf, int slot) {
@@ -658,6 +738,7 @@ __device__ __forceinline__ void pbatch_apply_word(const PprBatchParams& p, bool 
                 p.dangle[slot] = make_int2(vw, (int)bits);
             else
                 atomicOr(&p.ctl->flags, C2G_FLAG_QUEUE_OVERFLOW);
+            p.dmask[vw] = bits;  // the same lanes at rest, for an epoch boundary
         } else {
             p.amask[ob][vw] = bits;
             psum += (unsigned long long)__popc(bits) * (unsigned long long)dg;
@@ -911,6 +992,43 @@ __device__ __forceinline__ unsigned pbatch_pull(const PprBatchParams& p, int buf
     return cnt;
 }
 
+// Start of an epoch of a resident batch: round `slot`'s frontier from the state at rest,
+// the activity masks of buffer b (lanes activated with out-edges, their pushed residuals
+// in rq[b] / rqf[b]) and dmask (lanes activated without out-edges), as the apply sweep
+// of the previous round would have built it: entries (vertex, word) with their lanes,
+// the dangling list, and the round's push count.
+__device__ __noinline__ void pbatch_rebuild(const PprBatchParams& p, int b, int slot, WarpStage& fst,
+                                               unsigned gwarp, unsigned nwarps, int lane) {
+    const unsigned nm = (unsigned)p.V << p.logW;
+    const FrontierOut out = pbatch_out(p, b, slot);
+    unsigned long long ps = 0;
+    for (unsigned base = gwarp * 32u; base < nm; base += nwarps * 32u) {
+        const unsigned i = base + (unsigned)lane;
+        unsigned a = 0u, d = 0u;
+        int deg = 0;
+        if (i < nm) {
+            a = ldcg(p.amask[b] + i);
+            d = ldcg(p.dmask + i);
+            if (a) {
+                const int v = (int)(i >> p.logW);
+                deg = __ldg(p.row + v + 1) - __ldg(p.row + v);
+            }
+        }
+        if (a && deg > 0) ps += (unsigned long long)__popc(a) * (unsigned long long)deg;
+        stage_push(fst, out, a != 0u && deg > 0, (int)i, deg, __int_as_float((int)a));
+        if (d) {
+            const unsigned k = atomicAdd(&p.ctl->dctr[slot], 1u);
+            if (k < p.qcap)
+                p.dangle[k] = make_int2((int)i, (int)d);
+            else
+                atomicOr(&p.ctl->flags, C2G_FLAG_QUEUE_OVERFLOW);
+        }
+    }
+    stage_flush(fst, out);
+    for (int o = 16; o >= 1; o >>= 1) ps += __shfl_xor_sync(kFull, ps, o);
+    if (lane == 0 && ps) atomicAdd(&p.ctl->pcount[slot], ps);
+}
+
 __global__ void __launch_bounds__(kPprBatchThreads, 3) ppr_batch_persistent(const PprBatchParams p) {
     TraversalCtl* ctl = p.ctl;
     GridBarrier* bar = reinterpret_cast<GridBarrier*>(&ctl->bar_count);
@@ -929,7 +1047,8 @@ __global__ void __launch_bounds__(kPprBatchThreads, 3) ppr_batch_persistent(cons
     unsigned long long tph = globaltimer_ns();
     unsigned long long psum = 0;  // next round's pushes counted by this warp (lane 0)
 
-    // Init: pr = res = 0 (msg, tmask and amask are zero between launches).
+    if (p.epoch_rounds == 0) {
+    // Init: pr = res = 0 (msg, tmask, amask and dmask are zero between launches).
     {
         const size_t n4 = ((size_t)p.V * (size_t)p.Q) >> 2;
         float4* a4 = reinterpret_cast<float4*>(p.pr);
@@ -980,11 +1099,16 @@ __global__ void __launch_bounds__(kPprBatchThreads, 3) ppr_batch_persistent(cons
     if (lane == 0 && psum) atomicAdd(&ctl->pcount[1], psum);
     psum = 0;
     if (!grid_sync(bar, flags, p.barrier_ns)) return;
+    } else {
+        // An epoch of a resident batch: the state is at rest in the arrays.
+        pbatch_rebuild(p, p.cur0 & 1, p.cur0 % 3, fst, gwarp, nwarps, lane);
+        if (!grid_sync(bar, flags, p.barrier_ns)) return;
+    }
     phase_mark(ctl->phase_ns, tph, 0);
 
     long long pushes = 0, steps = 0;
     unsigned long long touched = 0;
-    int cur = 1, iters = 0;
+    int cur = p.epoch_rounds > 0 ? p.cur0 : 1, iters = 0;
     bool bad = false;
     for (;;) {
         const unsigned long long c = ldcg(&ctl->qctr[cur % 3]);
@@ -992,7 +1116,10 @@ __global__ void __launch_bounds__(kPprBatchThreads, 3) ppr_batch_persistent(cons
         const unsigned D = min(ldcg(&ctl->dctr[cur % 3]), p.qcap);
         const unsigned long long P = ldcg(&ctl->pcount[cur % 3]);  // this round's (query, edge) pushes
         const int buf = cur & 1, ob = (cur + 1) & 1;
+        if (gtid == 0) trace_round(p.trace, iters, (long long)P, P > p.pull_min ? 1 : 0);
         if (F == 0 && D == 0) break;
+        // end of an epoch: the state rests in the arrays for the next one
+        if (p.epoch_rounds > 0 && iters >= p.epoch_rounds) break;
         if (++iters > p.max_iter) {
             // Round cap: activated lanes keep their residual (never popped); their
             // activity masks are cleared for the next launch.
@@ -1004,6 +1131,8 @@ __global__ void __launch_bounds__(kPprBatchThreads, 3) ppr_batch_persistent(cons
                 if ((lanes >> lane) & 1u) p.res[off] = ldcg(p.rq[buf] + off) / one_m_a;
                 if (lane == 0) p.amask[buf][vw] = 0u;
             }
+            for (unsigned j = gwarp; j < D; j += nwarps)
+                if (lane == 0) p.dmask[ldcg(p.dangle + j).x] = 0u;
             break;
         }
         // Pop the activated lanes without out-edges.
@@ -1011,6 +1140,7 @@ __global__ void __launch_bounds__(kPprBatchThreads, 3) ppr_batch_persistent(cons
             const int2 dv = ldcg(p.dangle + j);
             const size_t off = (size_t)(dv.x >> p.logW) * p.Q + ((dv.x & (W - 1)) << 5) + lane;
             if (((unsigned)dv.y >> lane) & 1u) p.res[off] = 0.0;
+            if (lane == 0) p.dmask[dv.x] = 0u;
         }
         if (F == 0) break;
         const bool pull = P > p.pull_min;  // grid-uniform
@@ -1176,7 +1306,10 @@ __global__ void __launch_bounds__(kPprBatchThreads, 3) ppr_batch_persistent(cons
         atomicAdd((unsigned long long*)&p.counters[1], (unsigned long long)steps);
         atomicAdd((unsigned long long*)&ctl->touched, tl);
     }
-    if (gtid == 0) ctl->iterations = iters;
+    if (gtid == 0) {
+        ctl->iterations = iters;
+        trace_round(p.trace, iters, 0, -1);
+    }
 }
 
 // [V][Q] float -> caller layout (first nq queries).
@@ -1220,6 +1353,7 @@ struct PprBatchWork {
     float2* rqf[2] = {nullptr, nullptr};
     unsigned* amask[2] = {nullptr, nullptr};
     unsigned* tmask = nullptr;
+    unsigned* dmask = nullptr;
     int2* q[2] = {nullptr, nullptr};
     unsigned* qmask[2] = {nullptr, nullptr};
     int* mark[2] = {nullptr, nullptr};
@@ -1231,6 +1365,7 @@ struct PprBatchWork {
     int* seed_v = nullptr;
     float* seed_w = nullptr;
     float* stage = nullptr;
+    RoundTrace* trace = nullptr;
     size_t seed_cap = 0;
     int Q = 0;
     bool clean = false;  // msg, tmask and amask are zero
@@ -1239,10 +1374,12 @@ struct PprBatchWork {
 void ppr_batch_free(c2g_graph* g) {
     PprBatchWork* w = reinterpret_cast<PprBatchWork*>(g->ppr_batch);
     if (!w) return;
-    void* ptrs[] = {w->pr, w->res, w->msg, w->rq, w->rq2, w->rqf[0], w->rqf[1], w->amask[0], w->amask[1], w->tmask, w->q[0], w->q[1],
+    if (g->last_trace == w->trace) g->last_trace = nullptr;
+    void* ptrs[] = {w->pr, w->res, w->msg, w->rq, w->rq2, w->rqf[0], w->rqf[1], w->amask[0], w->amask[1], w->tmask, w->dmask,
+                    w->q[0], w->q[1],
                     w->qmask[0], w->qmask[1],
                     w->mark[0], w->mark[1], w->dangle, w->ctl, w->counters, w->src, w->seed_off,
-                    w->seed_v, w->seed_w, w->stage};
+                    w->seed_v, w->seed_w, w->stage, w->trace};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     delete w;
@@ -1267,6 +1404,7 @@ static int ppr_batch_alloc(c2g_graph* g, int Q, size_t n_seeds) {
     C2G_CUDA(cudaMalloc(&w->rqf[0], sizeof(float2) * VQ));
     C2G_CUDA(cudaMalloc(&w->rqf[1], sizeof(float2) * VQ));
     C2G_CUDA(cudaMalloc(&w->tmask, sizeof(unsigned) * qcap));
+    C2G_CUDA(cudaMalloc(&w->dmask, sizeof(unsigned) * qcap));
     C2G_CUDA(cudaMalloc(&w->amask[0], sizeof(unsigned) * qcap));
     C2G_CUDA(cudaMalloc(&w->amask[1], sizeof(unsigned) * qcap));
     for (int b = 0; b < 2; ++b) {
@@ -1282,6 +1420,7 @@ static int ppr_batch_alloc(c2g_graph* g, int Q, size_t n_seeds) {
     w->seed_cap = n_seeds > 0 ? n_seeds : 1;
     C2G_CUDA(cudaMalloc(&w->seed_v, sizeof(int) * w->seed_cap));
     C2G_CUDA(cudaMalloc(&w->seed_w, sizeof(float) * w->seed_cap));
+    C2G_CUDA(cudaMalloc(&w->trace, sizeof(RoundTrace) * (kMaxTraceRounds + 1)));
     w->Q = Q;
     w->clean = false;
     return C2G_OK;
@@ -1320,55 +1459,38 @@ int ppr_pull_prepare(c2g_graph* g) {
     return C2G_OK;
 }
 
-int ppr_batch_launch(c2g_graph* g, int32_t nq, const int32_t* sources, const c2g_ppr_params& prm,
-                     const std::vector<int32_t>* seed_off, const std::vector<int32_t>* seed_v,
-                     const std::vector<float>* seed_w, float* pr_out, float* res_out, int on_device, int query_major,
-                     float* ms, long long* counters, TraversalCtl* ctl_out) {
-    if (!g->adj_f) return fail(C2G_ERR_UNSUPPORTED, "graph has no float weights (flist / ppr wlist)");
-    int Q = 32, logW = 0;
-    while (Q < nq) {
-        Q <<= 1;
-        ++logW;
-    }
-    if ((size_t)g->V * (size_t)(Q / 32) >= (size_t(1) << 31) || (size_t)g->E * (size_t)(Q / 32) >= (size_t(1) << 32))
-        return fail(C2G_ERR_RANGE, "batch of %d queries too large for this graph", nq);
-    int rc;
-    const size_t ns = seed_v ? seed_v->size() : 0;
-    // Pull rounds need the reverse CSR (a view uses its base's, never builds it) and finite
-    // weights; with rmax below 1e-30 pushed residuals may leave the FP32 range of the pull's
-    // float pairs, so such launches push only.
-    unsigned long long pull_min = ~0ull;
+// Push count above which a round pulls (c2g_ppr_batch_set_pull): pull rounds need the
+// reverse CSR (a view uses its base's, never builds it) and finite weights; with rmax
+// below 1e-30 pushed residuals may leave the FP32 range of the pull's float pairs, so such
+// launches push only.
+static int ppr_pull_threshold(c2g_graph* g, const c2g_ppr_params& prm, unsigned long long* pull_min) {
+    *pull_min = ~0ull;
     const float ratio = g->ppr_cfg.batch_pull_ratio;
     if (ratio >= 0.f && g->E > 0 && prm.rmax >= 1e-30f && (g->wstat_valid || !g->borrowed)) {
+        int rc;
         if (!g->borrowed && (rc = ppr_pull_prepare(g))) return rc;
         float wmax;
         std::memcpy(&wmax, &g->wstat_wmax_bits, sizeof(float));
-        if (std::isfinite(wmax)) pull_min = (unsigned long long)((double)ratio * (double)g->E);
+        if (std::isfinite(wmax)) *pull_min = (unsigned long long)((double)ratio * (double)g->E);
     }
-    if ((rc = ppr_batch_alloc(g, Q, ns))) return rc;
-    PprBatchWork* w = reinterpret_cast<PprBatchWork*>(g->ppr_batch);
-    int coop = 0, per_sm = 0;
-    C2G_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, g->device));
-    if (!coop) return fail(C2G_ERR_UNSUPPORTED, "device lacks cooperative launch");
-    C2G_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ppr_batch_persistent, kPprBatchThreads, 0));
-    if (per_sm < 1) return fail(C2G_ERR_CUDA, "batch kernel cannot be resident");
+    return C2G_OK;
+}
+
+// msg, tmask, dmask and both activity masks are zero between launches.
+static int ppr_batch_clean(c2g_graph* g, PprBatchWork* w) {
+    if (w->clean) return C2G_OK;
     const size_t VQ = (size_t)g->V * (size_t)w->Q;
-    if (!w->clean) {
-        C2G_CUDA(cudaMemsetAsync(w->msg, 0, sizeof(double) * VQ, g->stream));
-        for (unsigned* m : {w->tmask, w->amask[0], w->amask[1]})
-            C2G_CUDA(cudaMemsetAsync(m, 0, sizeof(unsigned) * (size_t)g->V * (size_t)(w->Q / 32), g->stream));
-        w->clean = true;
-    }
-    C2G_CUDA(cudaMemcpyAsync(w->src, sources, sizeof(int) * (size_t)nq, cudaMemcpyHostToDevice, g->stream));
-    if (seed_off) {
-        C2G_CUDA(cudaMemcpyAsync(w->seed_off, seed_off->data(), sizeof(int) * seed_off->size(), cudaMemcpyHostToDevice,
-                                 g->stream));
-        if (ns) {
-            C2G_CUDA(cudaMemcpyAsync(w->seed_v, seed_v->data(), sizeof(int) * ns, cudaMemcpyHostToDevice, g->stream));
-            C2G_CUDA(cudaMemcpyAsync(w->seed_w, seed_w->data(), sizeof(float) * ns, cudaMemcpyHostToDevice, g->stream));
-        }
-    }
-    PprBatchParams p;
+    C2G_CUDA(cudaMemsetAsync(w->msg, 0, sizeof(double) * VQ, g->stream));
+    for (unsigned* m : {w->tmask, w->dmask, w->amask[0], w->amask[1]})
+        C2G_CUDA(cudaMemsetAsync(m, 0, sizeof(unsigned) * (size_t)g->V * (size_t)(w->Q / 32), g->stream));
+    w->clean = true;
+    return C2G_OK;
+}
+
+static void ppr_batch_params(c2g_graph* g, PprBatchWork* w, int Q, int logW, const c2g_ppr_params& prm,
+                             unsigned long long pull_min, PprBatchParams& p) {
+    const int nq = Q;
+    const std::vector<int32_t>* seed_off = nullptr;
     p.row = g->row;
     p.adj = g->adj_f;
     p.E = (unsigned)g->E;
@@ -1386,6 +1508,9 @@ int ppr_batch_launch(c2g_graph* g, int32_t nq, const int32_t* sources, const c2g
     p.rqf[0] = w->rqf[0];
     p.rqf[1] = w->rqf[1];
     p.tmask = w->tmask;
+    p.dmask = w->dmask;
+    p.epoch_rounds = 0;
+    p.cur0 = 1;
     for (int b = 0; b < 2; ++b) {
         p.q[b] = w->q[b];
         p.qmask[b] = w->qmask[b];
@@ -1412,6 +1537,48 @@ int ppr_batch_launch(c2g_graph* g, int32_t nq, const int32_t* sources, const c2g
     p.mark_r = g->mark_r;
     p.ntiles_r = (unsigned)(((size_t)g->E + (1u << kPullTileLog) - 1) >> kPullTileLog);
     p.pull_min = pull_min;
+    p.trace = w->trace;
+    g->last_trace = w->trace;
+}
+
+int ppr_batch_launch(c2g_graph* g, int32_t nq, const int32_t* sources, const c2g_ppr_params& prm,
+                     const std::vector<int32_t>* seed_off, const std::vector<int32_t>* seed_v,
+                     const std::vector<float>* seed_w, float* pr_out, float* res_out, int on_device, int query_major,
+                     float* ms, long long* counters, TraversalCtl* ctl_out) {
+    if (!g->adj_f) return fail(C2G_ERR_UNSUPPORTED, "graph has no float weights (flist / ppr wlist)");
+    int Q = 32, logW = 0;
+    while (Q < nq) {
+        Q <<= 1;
+        ++logW;
+    }
+    if ((size_t)g->V * (size_t)(Q / 32) >= (size_t(1) << 31) || (size_t)g->E * (size_t)(Q / 32) >= (size_t(1) << 32))
+        return fail(C2G_ERR_RANGE, "batch of %d queries too large for this graph", nq);
+    int rc;
+    const size_t ns = seed_v ? seed_v->size() : 0;
+    unsigned long long pull_min = ~0ull;
+    if ((rc = ppr_pull_threshold(g, prm, &pull_min))) return rc;
+    if ((rc = ppr_batch_alloc(g, Q, ns))) return rc;
+    PprBatchWork* w = reinterpret_cast<PprBatchWork*>(g->ppr_batch);
+    int coop = 0, per_sm = 0;
+    C2G_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, g->device));
+    if (!coop) return fail(C2G_ERR_UNSUPPORTED, "device lacks cooperative launch");
+    C2G_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ppr_batch_persistent, kPprBatchThreads, 0));
+    if (per_sm < 1) return fail(C2G_ERR_CUDA, "batch kernel cannot be resident");
+    const size_t VQ = (size_t)g->V * (size_t)w->Q;
+    if ((rc = ppr_batch_clean(g, w))) return rc;
+    C2G_CUDA(cudaMemcpyAsync(w->src, sources, sizeof(int) * (size_t)nq, cudaMemcpyHostToDevice, g->stream));
+    if (seed_off) {
+        C2G_CUDA(cudaMemcpyAsync(w->seed_off, seed_off->data(), sizeof(int) * seed_off->size(), cudaMemcpyHostToDevice,
+                                 g->stream));
+        if (ns) {
+            C2G_CUDA(cudaMemcpyAsync(w->seed_v, seed_v->data(), sizeof(int) * ns, cudaMemcpyHostToDevice, g->stream));
+            C2G_CUDA(cudaMemcpyAsync(w->seed_w, seed_w->data(), sizeof(float) * ns, cudaMemcpyHostToDevice, g->stream));
+        }
+    }
+    PprBatchParams p;
+    ppr_batch_params(g, w, Q, logW, prm, pull_min, p);
+    p.nq = nq;
+    p.seed_off = seed_off ? w->seed_off : nullptr;
     C2G_CUDA(cudaMemsetAsync(w->ctl, 0, sizeof(TraversalCtl), g->stream));
     C2G_CUDA(cudaMemsetAsync(w->counters, 0, sizeof(long long) * 2, g->stream));
     void* args[] = {&p};
@@ -1453,6 +1620,65 @@ int ppr_batch_launch(c2g_graph* g, int32_t nq, const int32_t* sources, const c2g
     if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
     C2G_CUDA(e);
     if (ctl_out->flags & (C2G_FLAG_BARRIER_TIMEOUT | C2G_FLAG_QUEUE_OVERFLOW | C2G_FLAG_BOUNDS)) w->clean = false;
+    C2G_CUDA(cudaEventElapsedTime(ms, g->ev0, g->ev1));
+    return C2G_OK;
+}
+
+// Resident batch (c2g_session): the workspace of Q query slots with every array at rest
+// (pr, res, msg and the masks zero), its arrays, and one epoch of at most `rounds` rounds
+// starting at round cur0 from the state the previous epoch (and the joins since) left.
+int ppr_batch_reserve(c2g_graph* g, int Q, PprBatchArrays* a) {
+    if (!g->adj_f) return fail(C2G_ERR_UNSUPPORTED, "graph has no float weights (flist / ppr wlist)");
+    if ((size_t)g->V * (size_t)(Q / 32) >= (size_t(1) << 31) || (size_t)g->E * (size_t)(Q / 32) >= (size_t(1) << 32))
+        return fail(C2G_ERR_RANGE, "%d slots too many for this graph", Q);
+    int rc;
+    if ((rc = ppr_batch_alloc(g, Q, 0))) return rc;
+    PprBatchWork* w = reinterpret_cast<PprBatchWork*>(g->ppr_batch);
+    w->clean = false;
+    if ((rc = ppr_batch_clean(g, w))) return rc;
+    const size_t VQ = (size_t)g->V * (size_t)w->Q;
+    C2G_CUDA(cudaMemsetAsync(w->pr, 0, sizeof(float) * VQ, g->stream));
+    C2G_CUDA(cudaMemsetAsync(w->res, 0, sizeof(double) * VQ, g->stream));
+    C2G_CUDA(cudaStreamSynchronize(g->stream));
+    a->pr = w->pr;
+    a->res = w->res;
+    a->rq[0] = w->rq;
+    a->rq[1] = w->rq2;
+    a->rqf[0] = w->rqf[0];
+    a->rqf[1] = w->rqf[1];
+    a->amask[0] = w->amask[0];
+    a->amask[1] = w->amask[1];
+    a->dmask = w->dmask;
+    return C2G_OK;
+}
+
+int ppr_batch_epoch(c2g_graph* g, int Q, const c2g_ppr_params& prm, int cur0, int rounds, float* ms,
+                    long long* counters, TraversalCtl* ctl_out) {
+    PprBatchWork* w = reinterpret_cast<PprBatchWork*>(g->ppr_batch);
+    if (!w || w->Q < Q) return fail(C2G_ERR_ARG, "resident PPR batch has no workspace");
+    int logW = 0;
+    while ((32 << logW) < Q) ++logW;
+    int rc;
+    unsigned long long pull_min = ~0ull;
+    if ((rc = ppr_pull_threshold(g, prm, &pull_min))) return rc;
+    int per_sm = 0;
+    C2G_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ppr_batch_persistent, kPprBatchThreads, 0));
+    if (per_sm < 1) return fail(C2G_ERR_CUDA, "batch kernel cannot be resident");
+    PprBatchParams p;
+    ppr_batch_params(g, w, Q, logW, prm, pull_min, p);
+    p.epoch_rounds = rounds < 1 ? 1 : rounds;
+    p.cur0 = cur0;
+    p.max_iter = 1 << 30;  // the per-query caps are the session's
+    C2G_CUDA(cudaMemsetAsync(w->ctl, 0, sizeof(TraversalCtl), g->stream));
+    C2G_CUDA(cudaMemsetAsync(w->counters, 0, sizeof(long long) * 2, g->stream));
+    void* args[] = {&p};
+    C2G_CUDA(cudaEventRecord(g->ev0, g->stream));
+    C2G_CUDA(cudaLaunchCooperativeKernel((const void*)ppr_batch_persistent, dim3(grid_blocks(g, per_sm)),
+                                         dim3(kPprBatchThreads), args, 0, g->stream));
+    C2G_CUDA(cudaEventRecord(g->ev1, g->stream));
+    C2G_CUDA(cudaMemcpyAsync(ctl_out, w->ctl, sizeof(TraversalCtl), cudaMemcpyDeviceToHost, g->stream));
+    C2G_CUDA(cudaMemcpyAsync(counters, w->counters, sizeof(long long) * 2, cudaMemcpyDeviceToHost, g->stream));
+    C2G_CUDA(cudaStreamSynchronize(g->stream));
     C2G_CUDA(cudaEventElapsedTime(ms, g->ev0, g->ev1));
     return C2G_OK;
 }

@@ -46,6 +46,18 @@ struct TraversalCtl {
     unsigned long long pcount[3];    // batched PPR: (query, edge) pushes of the frontier per round slot
 };
 
+// Per-round trace of a batched launch (c2g_graph_last_rounds): the device time at the
+// start of each round (block 0, right after the grid barrier that ends the previous
+// round), the round's work units and its shape; the entry after the last round holds the
+// end time.
+constexpr int kMaxTraceRounds = 1024;
+struct RoundTrace {
+    unsigned long long t_ns;
+    long long work;  // PPR: (query, edge) pushes of the round; SSSP: edge-word steps
+    int shape;       // PPR: 1 pull round, 0 push round; SSSP: 0
+    int pad;
+};
+
 // Stamps survive across launches; the kernel advances the bases itself.
 struct StampState {
     int stamp_base;
@@ -155,6 +167,7 @@ struct c2g_graph {
     bool wstat_valid = false;
     uint32_t wstat_wmax_bits = 0;
     int stall_next_sssp = 0;            // failure-detection test: next SSSP barrier cannot complete
+    c2g::RoundTrace* last_trace = nullptr;  // device trace of the last batched launch (in its workspace)
     bool borrowed = false;    // a view: graph arrays belong to another handle
 };
 
@@ -184,6 +197,22 @@ int ppr_batch_launch(c2g_graph* g, int32_t nq, const int32_t* sources, const c2g
                      const std::vector<int32_t>* seed_off, const std::vector<int32_t>* seed_v,
                      const std::vector<float>* seed_w, float* pr_out, float* res_out, int on_device, int query_major,
                      float* ms, long long* counters, TraversalCtl* ctl_out);
+// Resident batches (session.cu): workspaces of Q slots that keep their state between
+// launches, and one epoch (at most `rounds` rounds) of the batched kernels over them.
+struct PprBatchArrays {
+    float* pr;
+    double* res;
+    double* rq[2];
+    float2* rqf[2];
+    unsigned* amask[2];
+    unsigned* dmask;
+};
+void session_set_grid_share(c2g_session* s, float share);
+int sssp_batch_reserve(c2g_graph* g, int Q, int** dist, unsigned** mask);
+int sssp_batch_epoch(c2g_graph* g, int Q, int rounds, float* ms, long long* counters, TraversalCtl* ctl_out);
+int ppr_batch_reserve(c2g_graph* g, int Q, PprBatchArrays* a);
+int ppr_batch_epoch(c2g_graph* g, int Q, const c2g_ppr_params& prm, int cur0, int rounds, float* ms,
+                    long long* counters, TraversalCtl* ctl_out);
 int sssp_batch_launch(c2g_graph* g, int32_t nq, const int32_t* sources, const std::vector<int32_t>* seed_off,
                       const std::vector<int32_t>* seed_v, const std::vector<int32_t>* seed_w, int32_t* out,
                       int out_on_device, int query_major, float* ms, long long* counters, TraversalCtl* ctl_out);

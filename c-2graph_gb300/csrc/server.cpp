@@ -1,19 +1,25 @@
 // Serving loop with continuous batching, state resident on the device.
 //
 // Replaces the reference's C^2graph-PM scheduler (src/sssp/purn-perk/Main.cu:87-246):
-// there a host loop alternates single-query launches on two streams and ships state to
-// a CPU thread.  Here:
-//   * one worker thread per query kind (SSSP, PPR, adsorption), each with its own CUDA
-//     stream and workspace (a view handle sharing the graph's device arrays);
-//   * requests wait in a per-kind queue; whenever a kind's previous batch finishes, its
-//     worker admits every waiting request the HBM budget allows, so requests that
-//     arrive while others run join the next batch of their kind, and the three kinds'
-//     batches run on the device at the same time (each batched launch uses a share of
-//     the SMs, so the persistent kernels are co-resident);
-//   * admission by HBM footprint: each kind gets a third of the budget and a batch
-//     holds at most budget / (state bytes of one query) queries;
+// there a host loop alternates single-query launches on two streams and ships a running
+// query's state to a CPU thread through a pinned ring of snapshots.  Here:
+//   * one worker thread per query kind (SSSP, PPR, adsorption), each on its own CUDA
+//     stream; the three kinds run on the device at the same time, each batched launch on
+//     a third of the SMs so the persistent kernels are co-resident;
+//   * SSSP and PPR requests run in a resident batch (c2g_session): the worker runs epochs
+//     of a few rounds, and between epochs it admits waiting requests into free slots, so a
+//     request that arrives while others run starts at the next epoch, not after the
+//     whole batch; a request completes as soon as its own query finishes;
+//   * admission by HBM footprint: each kind gets a third of the budget, and its session
+//     has at most budget / (state bytes of one query) slots;
+//   * preemption (preempt_rounds > 0): when requests wait and every slot is taken, the
+//     running query with the most rounds (at least preempt_rounds) is evicted into a
+//     device-resident snapshot and the waiting request takes its slot; evicted queries
+//     resume, before new requests, as slots free up (the analogue of the reference's
+//     migration of long-running queries off the GPU, without leaving the device);
+//   * adsorption label propagation runs request by request (fixed iteration count);
 //   * latency = completion time - submit time per request; p50/p99 over all completed.
-// Results are those of c2g_sssp_batch / c2g_ppr_batch / c2g_adsorption for the same
+// Results are those of c2g_sssp / c2g_ppr (base mode) / c2g_adsorption for the same
 // inputs: a request's result does not depend on what it is batched with.
 #include <algorithm>
 #include <chrono>
@@ -34,6 +40,7 @@
 namespace c2g {
 int build_reverse_graph(c2g_graph* g);
 void graph_free_view(c2g_graph* g);
+void session_set_grid_share(c2g_session* s, float share);
 }  // namespace c2g
 
 using namespace c2g;
@@ -59,6 +66,7 @@ struct Done {
 struct c2g_server {
     c2g_graph* base = nullptr;
     c2g_graph* views[3] = {nullptr, nullptr, nullptr};
+    c2g_session* sessions[2] = {nullptr, nullptr};  // SSSP, PPR
     c2g_server_config cfg{};
     std::vector<float> p_inj, p_cont, p_abnd;
     int64_t bytes_per_query[3] = {0, 0, 0};
@@ -70,6 +78,7 @@ struct c2g_server {
     std::vector<double> latencies;
     int64_t next_ticket = 1;
     int64_t batches[3] = {0, 0, 0};
+    int64_t evictions = 0;
     int64_t completed = 0;
     int64_t max_batch_seen = 0;
     bool stop = false;
@@ -80,82 +89,149 @@ struct c2g_server {
 
 namespace {
 
-void run_batch(c2g_server* s, int kind, std::vector<Pending>& batch) {
-    c2g_graph* g = s->views[kind];
-    const int n = (int)batch.size();
-    const size_t V = (size_t)g->V;
-    std::vector<int> status(n, C2G_OK);
-    std::vector<Clock::time_point> t_done(n);  // when each request's result was complete
-    if (kind == C2G_REQ_SSSP) {
-        std::vector<int32_t> src(n);
-        for (int i = 0; i < n; ++i) src[i] = batch[i].req.source;
-        std::vector<int32_t> outv((size_t)n * V);
-        int32_t* out = outv.data();
-        c2g_stats st;
-        const int rc = c2g_sssp_batch(g, n, src.data(), 0, C2G_SEEDS_COMPAT, out, 0, C2G_LAYOUT_QUERY_MAJOR, &st);
-        for (int i = 0; i < n; ++i) {
-            status[i] = rc;
-            if (!rc && batch[i].req.out) std::memcpy(batch[i].req.out, out + (size_t)i * V, sizeof(int32_t) * V);
-        }
-        std::fill(t_done.begin(), t_done.end(), Clock::now());
-    } else if (kind == C2G_REQ_PPR) {
-        std::vector<int32_t> src(n);
-        for (int i = 0; i < n; ++i) src[i] = batch[i].req.source;
-        std::vector<float> prv((size_t)n * V);
-        float* pr = prv.data();
-        c2g_ppr_params p;
-        c2g_ppr_default_params(g, 0, &p);
-        p.alpha = s->cfg.alpha;
-        p.rmax = s->cfg.rmax;
-        p.r0 = 1.0f;
-        p.pr0 = s->cfg.alpha;
-        p.seeded = 0;
-        c2g_stats st;
-        const int rc = c2g_ppr_batch(g, n, src.data(), &p, pr, nullptr, 0, C2G_LAYOUT_QUERY_MAJOR, &st);
-        for (int i = 0; i < n; ++i) {
-            status[i] = rc;
-            if (!rc && batch[i].req.out) std::memcpy(batch[i].req.out, pr + (size_t)i * V, sizeof(float) * V);
-        }
-        std::fill(t_done.begin(), t_done.end(), Clock::now());
-    } else {
-        // Label propagation runs request by request: each result is published as soon as
-        // it is complete, so a waiter does not wait for the rest of the batch.
-        std::vector<float> Y(V * 16);
-        for (int i = 0; i < n; ++i) {
-            c2g_stats st;
-            const int rc = c2g_adsorption(g, 16, batch[i].seeds.data(), s->p_inj.data(), s->p_cont.data(),
-                                          s->p_abnd.data(), s->cfg.ads_iterations,
-                                          batch[i].req.out ? static_cast<float*>(batch[i].req.out) : Y.data(), 0, &st);
-            const auto ti = Clock::now();
-            std::lock_guard<std::mutex> lk(s->mu);
-            const double ms = std::chrono::duration<double, std::milli>(ti - batch[i].t_submit).count();
-            s->done[batch[i].ticket] = Done{rc, ms};
-            s->latencies.push_back(ms);
-            s->completed += 1;
-            s->t_last_done = ti;
-            s->cv_done.notify_all();
-        }
-        std::lock_guard<std::mutex> lk(s->mu);
-        s->batches[kind] += 1;
-        s->max_batch_seen = std::max<int64_t>(s->max_batch_seen, n);
-        return;
-    }
+void publish(c2g_server* s, const Pending& p, int status) {
     const auto t = Clock::now();
     std::lock_guard<std::mutex> lk(s->mu);
-    for (int i = 0; i < n; ++i) {
-        const double ms = std::chrono::duration<double, std::milli>(t_done[i] - batch[i].t_submit).count();
-        s->done[batch[i].ticket] = Done{status[i], ms};
-        s->latencies.push_back(ms);
-    }
-    s->completed += n;
-    s->batches[kind] += 1;
-    s->max_batch_seen = std::max<int64_t>(s->max_batch_seen, n);
+    const double ms = std::chrono::duration<double, std::milli>(t - p.t_submit).count();
+    s->done[p.ticket] = Done{status, ms};
+    s->latencies.push_back(ms);
+    s->completed += 1;
     s->t_last_done = t;
     s->cv_done.notify_all();
 }
 
+// Adsorption: request by request, each result published as soon as it is complete.
+void run_adsorption(c2g_server* s, std::vector<Pending>& batch) {
+    c2g_graph* g = s->views[C2G_REQ_ADSORPTION];
+    std::vector<float> Y((size_t)g->V * 16);
+    for (auto& p : batch) {
+        c2g_stats st;
+        const int rc = c2g_adsorption(g, 16, p.seeds.data(), s->p_inj.data(), s->p_cont.data(), s->p_abnd.data(),
+                                      s->cfg.ads_iterations, p.req.out ? static_cast<float*>(p.req.out) : Y.data(), 0,
+                                      &st);
+        publish(s, p, rc);
+    }
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->batches[C2G_REQ_ADSORPTION] += 1;
+    s->max_batch_seen = std::max<int64_t>(s->max_batch_seen, (int64_t)batch.size());
+}
+
+// An evicted query waiting to resume.
+struct Parked {
+    Pending p;
+    c2g_snapshot* snap;
+};
+
+// SSSP / PPR: a resident batch run in epochs; waiting requests (evicted ones first) take
+// free slots between epochs.
+void session_worker(c2g_server* s, int kind) {
+    c2g_session* ss = s->sessions[kind];
+    int32_t cap = 1;
+    {
+        const int64_t cap_mem = s->bytes_per_query[kind] > 0 ? s->budget_per_kind / s->bytes_per_query[kind] : 1;
+        cap = (int32_t)std::max<int64_t>(1, std::min<int64_t>(s->cfg.max_batch, cap_mem));
+    }
+    std::vector<Pending> slot_req((size_t)cap);
+    std::vector<bool> used((size_t)cap, false);
+    std::deque<Parked> parked;
+    std::vector<int32_t> finished((size_t)cap);
+    std::vector<float> scratch((size_t)s->base->V);
+    const int rounds = s->cfg.epoch_rounds > 0 ? s->cfg.epoch_rounds : 4;
+    int running = 0;
+    for (;;) {
+        std::vector<Pending> admit;
+        {
+            std::unique_lock<std::mutex> lk(s->mu);
+            s->cv_work.wait(lk, [&] { return s->stop || !s->queue[kind].empty() || running > 0 || !parked.empty(); });
+            if (s->stop && s->queue[kind].empty() && running == 0 && parked.empty()) return;
+            int room = cap - running - (int)parked.size();
+            // Preemption: requests wait, no slot is free, and a query has run long enough.
+            if (room <= 0 && parked.empty() && !s->queue[kind].empty() && s->cfg.preempt_rounds > 0) {
+                int victim = -1, most = s->cfg.preempt_rounds - 1;
+                for (int i = 0; i < cap; ++i) {
+                    int32_t st = 0, r = 0;
+                    if (!used[i] || c2g_session_slot(ss, i, &st, nullptr, &r) || st != 1) continue;
+                    if (r > most) {
+                        most = r;
+                        victim = i;
+                    }
+                }
+                c2g_snapshot* snap = nullptr;
+                if (victim >= 0 && c2g_session_evict(ss, victim, &snap) == C2G_OK) {
+                    parked.push_back(Parked{std::move(slot_req[victim]), snap});
+                    used[victim] = false;
+                    --running;
+                    ++s->evictions;
+                    room = 1;
+                }
+            }
+            for (; room > 0 && !s->queue[kind].empty(); --room) {
+                admit.push_back(std::move(s->queue[kind].front()));
+                s->queue[kind].pop_front();
+            }
+        }
+        // evicted queries resume first, into slots not taken by this round's admissions
+        while (!parked.empty() && running + (int)admit.size() < cap) {
+            int32_t slot = -1;
+            if (c2g_session_resume(ss, parked.front().snap, &slot) != C2G_OK) break;
+            slot_req[slot] = std::move(parked.front().p);
+            used[slot] = true;
+            ++running;
+            parked.pop_front();
+        }
+        for (size_t a = 0; a < admit.size(); ++a) {
+            Pending& p = admit[a];
+            int32_t slot = -1;
+            const int rc = c2g_session_admit(ss, p.req.source, &slot);
+            if (rc == C2G_ERR_OVERFLOW) {  // no slot after all: back to the head of the queue
+                std::lock_guard<std::mutex> lk(s->mu);
+                for (size_t b = admit.size(); b > a; --b) s->queue[kind].push_front(std::move(admit[b - 1]));
+                break;
+            }
+            if (rc) {
+                publish(s, p, rc);
+                continue;
+            }
+            slot_req[slot] = std::move(p);
+            used[slot] = true;
+            ++running;
+        }
+        if (running == 0) continue;
+        int32_t nf = 0;
+        c2g_stats st;
+        int rc = c2g_session_step(ss, rounds, finished.data(), cap, &nf, &st);
+        {
+            std::lock_guard<std::mutex> lk(s->mu);
+            s->batches[kind] += 1;
+            s->max_batch_seen = std::max<int64_t>(s->max_batch_seen, running);
+        }
+        if (rc) {  // the epoch failed: every running request fails with its code
+            for (int i = 0; i < cap; ++i)
+                if (used[i]) {
+                    publish(s, slot_req[i], rc);
+                    used[i] = false;
+                }
+            running = 0;
+            continue;
+        }
+        for (int k = 0; k < nf; ++k) {
+            const int slot = finished[k];
+            Pending& p = slot_req[slot];
+            void* out = p.req.out ? p.req.out : scratch.data();
+            const int rr = c2g_session_read(ss, slot, out, nullptr, 0, nullptr);
+            publish(s, p, rr);
+            used[slot] = false;
+            --running;
+        }
+    }
+}
+
 void worker(c2g_server* s, int kind) {
     cudaSetDevice(s->base->device);
+    if (kind != C2G_REQ_ADSORPTION) {
+        session_worker(s, kind);
+        return;
+    }
     const int64_t cap_mem = s->bytes_per_query[kind] > 0 ? s->budget_per_kind / s->bytes_per_query[kind] : 1;
     const int64_t cap = std::max<int64_t>(1, std::min<int64_t>(s->cfg.max_batch, cap_mem));
     for (;;) {
@@ -169,7 +245,7 @@ void worker(c2g_server* s, int kind) {
                 s->queue[kind].pop_front();
             }
         }
-        run_batch(s, kind, batch);
+        run_adsorption(s, batch);
     }
 }
 
@@ -205,19 +281,39 @@ int c2g_server_create(c2g_graph* g, const float* p_inj, const float* p_cont, con
         rc = graph_view(g, &s->views[k]);
         if (!rc) s->views[k]->grid_scale = 1.0f / 3.0f;
     }
-    // Per-query device state (bytes) and the admission budget.
-    const int64_t W = 1;  // words per query amortise to 1/32 per query; counted per query
-    s->bytes_per_query[C2G_REQ_SSSP] = (int64_t)V * (4 + 4) + (int64_t)V * 20 * W / 32;  // dist + staging + masks/queues
-    s->bytes_per_query[C2G_REQ_PPR] = (int64_t)V * (4 + 8 * 6 + 4) + (int64_t)V * 12 / 32;  // pr,res,msg,rq x2,rq pairs x2,staging,masks
-    s->bytes_per_query[C2G_REQ_ADSORPTION] = (int64_t)V * 16 * 4 * 3;                     // Y, acc, host-copy stage
+    // Per-query device state (bytes) and the admission budget.  Per (vertex, query): SSSP
+    // distance 4 B plus 20 B per 32 queries (mask, two frontier entries and masks); PPR
+    // pr 4, res 8, msg 8, two pushed residuals 16 and their float pairs 16, plus 32 B per
+    // 32 queries of masks and frontier entries; adsorption 16 labels x (Y, accumulator,
+    // host stage).
+    s->bytes_per_query[C2G_REQ_SSSP] = (int64_t)V * 4 + (int64_t)V * 20 / 32;
+    s->bytes_per_query[C2G_REQ_PPR] = (int64_t)V * 52 + (int64_t)V * 32 / 32;
+    s->bytes_per_query[C2G_REQ_ADSORPTION] = (int64_t)V * 16 * 4 * 3;
     size_t free_b = 0, total_b = 0;
     if (!rc && cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) rc = fail(C2G_ERR_CUDA, "cudaMemGetInfo failed");
     const int64_t budget = cfg->hbm_budget_bytes > 0 ? cfg->hbm_budget_bytes : (int64_t)(0.8 * (double)free_b);
     s->budget_per_kind = budget / 3;
+    // Resident batches of SSSP and PPR with as many slots as the budget admits.
+    for (int k = 0; k < 2 && !rc; ++k) {
+        if ((k == C2G_REQ_SSSP && !g->adj_w) || (k == C2G_REQ_PPR && !g->adj_f)) continue;
+        const int64_t cap = std::max<int64_t>(1, std::min<int64_t>(cfg->max_batch, s->budget_per_kind /
+                                                                                      s->bytes_per_query[k]));
+        c2g_ppr_params prm;
+        c2g_ppr_default_params(g, 0, &prm);
+        prm.alpha = cfg->alpha;
+        prm.rmax = cfg->rmax;
+        prm.r0 = 1.0f;
+        prm.pr0 = cfg->alpha;
+        prm.seeded = 0;
+        rc = c2g_session_create(g, k, (int32_t)cap, k == C2G_REQ_PPR ? &prm : nullptr, &s->sessions[k]);
+        if (!rc) session_set_grid_share(s->sessions[k], 1.0f / 3.0f);
+    }
     if (prev >= 0) cudaSetDevice(prev);
     if (rc) {
         for (auto* v : s->views)
             if (v) graph_free_view(v);
+        for (auto* ss : s->sessions)
+            if (ss) c2g_session_free(ss);
         delete s;
         return rc;
     }
@@ -281,6 +377,7 @@ int c2g_server_get_stats(c2g_server* s, c2g_server_stats* out) {
         out->pending[k] = (int64_t)s->queue[k].size();
     }
     out->max_batch = s->max_batch_seen;
+    out->evictions = s->evictions;
     if (!s->latencies.empty()) {
         std::vector<double> l = s->latencies;
         std::sort(l.begin(), l.end());
@@ -309,6 +406,8 @@ int c2g_server_destroy(c2g_server* s) {
         if (t.joinable()) t.join();
     for (auto* v : s->views)
         if (v) graph_free_view(v);
+    for (auto* ss : s->sessions)
+        if (ss) c2g_session_free(ss);
     delete s;
     return C2G_OK;
 }

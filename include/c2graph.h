@@ -28,7 +28,7 @@
 extern "C" {
 #endif
 
-#define C2G_ABI_VERSION 1
+#define C2G_ABI_VERSION 2
 
 /* ---- status codes --------------------------------------------------------------- */
 #define C2G_OK               0
@@ -138,6 +138,13 @@ int  c2g_graph_set_watchdog(c2g_graph* g, int32_t barrier_timeout_ms, int32_t st
  * filter, ms[2] expansion / push, ms[3] reserved (0).  The phases add up to the
  * launch's device time. */
 int  c2g_graph_last_phases(const c2g_graph* g, double ms[4]);
+/* Tracing (no counterpart in the reference): per-round trace of the last batched launch
+ * (c2g_sssp_batch / c2g_ppr_batch, or a session epoch) on this handle, up to 1024 rounds:
+ * ms[i] the device time of round i (from one grid barrier to the next, as block 0 sees
+ * it), work[i] its work units (PPR: (query, edge) pushes; SSSP: edge-word steps),
+ * shape[i] 1 for a pull round, 0 otherwise.  Arrays hold `cap` entries (any may be NULL);
+ * *n gets the number of rounds (0 when no batched launch finished cleanly). */
+int  c2g_graph_last_rounds(c2g_graph* g, int32_t cap, double* ms, int64_t* work, int32_t* shape, int32_t* n);
 
 /* ---- SSSP -------------------------------------------------------------------------- */
 /* Source-skip rule of the drop-in programs: sssp-base skips sources without
@@ -298,9 +305,13 @@ int c2g_adsorption(c2g_graph* g, int32_t n_labels, const int32_t* seed_vertices,
 /* Continuous-batching request loop with the graph and per-query state resident on the
  * device (replaces the reference's C^2graph-PM CPU/GPU migration loop,
  * src/sssp/purn-perk/Main.cu:87-246).  One worker per request kind, each on its own
- * stream; requests that arrive while a batch runs join the next batch of their kind,
- * within an HBM budget split between the kinds (state bytes per query).  The three
- * kinds' batches run on the device concurrently.  A request's result equals the
+ * stream; the three kinds run on the device concurrently.  SSSP and PPR requests run in a
+ * resident batch (c2g_session) in epochs of epoch_rounds rounds: a request that arrives
+ * while others run takes a free slot at the next epoch and completes as soon as its own
+ * query finishes.  Slots are bounded by an HBM budget split between the kinds (state
+ * bytes per query).  With preempt_rounds > 0, a waiting request may take the slot of the
+ * running query with the most rounds (at least preempt_rounds), which is evicted into a
+ * device snapshot and resumed first when a slot frees.  A request's result equals the
  * corresponding single call (c2g_sssp / c2g_ppr base mode / c2g_adsorption). */
 #define C2G_REQ_SSSP       0
 #define C2G_REQ_PPR        1
@@ -313,6 +324,9 @@ typedef struct c2g_server_config {
     int32_t ads_iterations;   /* adsorption iterations                                 */
     float   alpha, rmax;      /* PPR parameters (base mode)                            */
     int64_t hbm_budget_bytes; /* admission budget for per-query state, 0 = 80% of free */
+    int32_t epoch_rounds;     /* rounds per epoch of the SSSP / PPR batches (0: 4)     */
+    int32_t preempt_rounds;   /* evict queries past this many rounds when requests wait
+                                 and no slot is free (0: never)                         */
 } c2g_server_config;
 
 typedef struct c2g_request {
@@ -328,9 +342,10 @@ typedef struct c2g_server_stats {
     int64_t batches[3];
     int64_t pending[3];
     int64_t admit_cap[3];     /* queries per batch allowed by the HBM budget            */
-    int64_t max_batch;        /* largest batch run so far                               */
+    int64_t max_batch;        /* most queries of one kind running at once so far       */
     double  p50_ms, p99_ms;   /* latency percentiles of completed requests              */
     double  queries_per_s;    /* completed / (last completion - first submit)           */
+    int64_t evictions;        /* queries moved to a snapshot to free a slot             */
 } c2g_server_stats;
 
 /* g must carry int32 weights (SSSP) and float weights (PPR, adsorption); p_* (V
@@ -344,6 +359,51 @@ int c2g_server_wait(c2g_server* s, int64_t ticket, double timeout_s, int* status
 int c2g_server_get_stats(c2g_server* s, c2g_server_stats* out);
 /* Finish queued requests, stop the workers and release the server. */
 int c2g_server_destroy(c2g_server* s);
+
+/* ---- resident batches: slot-level continuous batching, snapshot / evict --------------- */
+/* A session keeps `slots` queries of one kind (C2G_REQ_SSSP: plain SSSP on the graph's
+ * int32 weights; C2G_REQ_PPR: base-mode push with `params`, seeded = 0) resident on the
+ * device and runs them in epochs of a bounded number of rounds of the batched kernels.
+ * Between epochs each query's state (SSSP: distances and next-round lanes; PPR: pr, res,
+ * pushed residuals, frontier and dangling lanes) rests in the batch arrays, so a query
+ * admitted while others run joins at the next epoch, and a running query can be evicted
+ * into a device-resident snapshot and resumed later, in this or another session on the
+ * same graph, continuing the same rounds.  Results equal c2g_sssp / c2g_ppr (base mode)
+ * for the same source: SSSP bit-exact, PPR within summation order.  PPR round caps
+ * (params->max_iter) are per query.  Replaces the reference's C^2graph-PM split of a query
+ * between GPU iterations and a CPU thread over a pinned ring of per-query snapshots
+ * (src/sssp/purn-perk/SSSP.h:13-29, src/sssp/purn-perk/Main.cu:87-246,
+ * src/ppr/w-purn-perk/Main.cu:91-275): here the query stays on the device and only
+ * yields its slot.  A session has its own stream and workspace; calls on one session are
+ * serialised. */
+typedef struct c2g_session c2g_session;
+typedef struct c2g_snapshot c2g_snapshot;
+
+int c2g_session_create(c2g_graph* g, int kind, int32_t slots, const c2g_ppr_params* params, c2g_session** out);
+/* Take a free slot for `source`; the query starts at the next step.  C2G_ERR_OVERFLOW when
+ * every slot is taken. */
+int c2g_session_admit(c2g_session* s, int32_t source, int32_t* slot);
+/* Apply admissions and resumptions, run one epoch of at most `rounds` rounds (fewer when a
+ * PPR query would pass its cap, or when every query finishes), and report the slots whose
+ * query finished: their ids go to finished[0 .. min(n, cap)), n to *n_finished.  A finished
+ * slot keeps its result until c2g_session_read.  stats (may be NULL): the epoch's rounds,
+ * pushes / relaxations and device time. */
+int c2g_session_step(c2g_session* s, int32_t rounds, int32_t* finished, int32_t cap, int32_t* n_finished,
+                     c2g_stats* stats);
+/* Result of a finished slot (SSSP: int32 distances; PPR: float pr and, if res_out is not
+ * NULL, float res; V entries each, host or device memory), then free the slot.  stats (may
+ * be NULL): source, rounds run, status flags (C2G_FLAG_ITER_CAP if the cap stopped it). */
+int c2g_session_read(c2g_session* s, int32_t slot, void* out, float* res_out, int on_device, c2g_stats* stats);
+/* Move a running query out of its slot into a snapshot in device memory (the caller owns
+ * it); the slot is free at once. */
+int c2g_session_evict(c2g_session* s, int32_t slot, c2g_snapshot** out);
+/* Continue a snapshot in a free slot from the next step; on success the session owns the
+ * snapshot. */
+int c2g_session_resume(c2g_session* s, c2g_snapshot* snap, int32_t* slot);
+void c2g_snapshot_free(c2g_snapshot* snap);
+/* Slot state (0 free, 1 running, 2 finished), its source and the rounds it has run. */
+int c2g_session_slot(c2g_session* s, int32_t slot, int32_t* state, int32_t* source, int32_t* rounds);
+void c2g_session_free(c2g_session* s);
 
 /* ---- offline tools (host) ---------------------------------------------------------- */
 /* Seeded R-MAT graph written as <dir>/origin/{vlist,elist,wlist,flist}.bin with

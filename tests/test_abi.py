@@ -34,7 +34,7 @@ def test_header_symbols_exported(built):
 def test_abi_version(built):
     import c2g
 
-    assert c2g.lib().c2g_abi_version() == 1
+    assert c2g.lib().c2g_abi_version() == 2
 
 
 def test_missing_dataset_is_io_error(built, tmp_path):

@@ -354,3 +354,30 @@ def test_ppr_batch_pull_word_counts_vs_fp64(gpu_available, g14p, n):
             rp, rr, _, _ = oracle.ppr_push(o["vlist"], o["elist"], o["flist"], int(src[i]), 0.15, 1e-7)
             assert _l1(pr[i], rp) <= 1e-6, (n, i, _l1(pr[i], rp))
             assert _l1(res[i], rr) <= 1e-6, (n, i)
+
+
+def test_batch_round_trace(gpu_available, g17w, g14p):
+    """The per-round trace of a batched launch: one entry per round, the work units add
+    up to the launch's counters, and the rounds' times add up to (nearly all of) the
+    launch's device time."""
+    import c2g
+
+    with c2g.Graph.load(g17w, "origin") as gr:
+        src = _sources(np.fromfile(g17w + "/origin/vlist.bin", dtype=np.int32), 64, 4)
+        _, st = gr.sssp_batch(src)
+        ms, work, shape = gr.last_rounds()
+        assert len(ms) == st.iterations and len(ms) > 3
+        assert int(work.sum()) == st.touched  # edge-word steps
+        assert np.all(shape == 0) and np.all(ms > 0)
+        assert 0.5 * st.device_ms <= ms.sum() <= st.device_ms * 1.01
+    with c2g.Graph.load(g14p, "origin") as gr:
+        vl = np.fromfile(g14p + "/origin/vlist.bin", dtype=np.int32)
+        src = _sources(vl, 64, 6)
+        prm = gr.ppr_params(alpha=0.15, rmax=1e-7, seeded=0, pr0=0.15, r0=1.0)
+        gr.ppr_batch_pull(1.0)
+        _, _, st = gr.ppr_batch(src, prm, want_res=False)
+        ms, work, shape = gr.last_rounds()
+        assert len(ms) == st.iterations
+        assert int(work.sum()) == st.edges_relaxed  # (query, edge) pushes
+        assert shape.max() == 1 and shape.min() == 0  # some rounds pulled, some pushed
+        assert 0.5 * st.device_ms <= ms.sum() <= st.device_ms * 1.01

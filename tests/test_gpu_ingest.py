@@ -22,7 +22,7 @@ def test_rmat_gpu_matches_host(gpu_available, built, tmp_path, scale, ef, seed, 
 
 def test_streamed_load_equals_host_arrays(gpu_available, built, tmp_path):
     """c2g_graph_load streams the edge files (memory-mapped, page-locked double buffer,
-    interleaved on the device in chunks of 4M edges).  At scale 19 (8.4M edges, three
+    interleaved on the device in chunks of 4M edges).  At scale 19 (8.0M edges, two
     chunks, the last one partial) a loaded graph gives the same SSSP distances and PPR
     vectors as one built from the host arrays, for every variant."""
     import numpy as np
@@ -35,7 +35,7 @@ def test_streamed_load_equals_host_arrays(gpu_available, built, tmp_path):
     c2g.prune_sssp(d)
     c2g.prune_ppr(d, alpha=0.15)
     o = oracle.load_dataset(d, "origin")
-    assert len(o["elist"]) > 2 * (1 << 22)
+    assert (1 << 22) < len(o["elist"]) < 2 * (1 << 22)
     deg = np.diff(o["vlist"])
     srcs = [int(np.argmax(deg)), int(np.flatnonzero(deg > 0)[11])]
     with c2g.Graph.load(d, "origin") as gl, \
