@@ -117,7 +117,7 @@ SIGNATURES = {
                                               ctypes.c_char_p, _P]),
     "c2g_graph_set_watchdog": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int32]),
     "c2g_graph_last_phases": (ctypes.c_int, [_P, _P]),
-    "c2g_graph_last_rounds": (ctypes.c_int, [_P, ctypes.c_int32, _P, _P, _P, _I32P]),
+    "c2g_graph_last_rounds": (ctypes.c_int, [_P, ctypes.c_int32, _P, _P, _P, _P, _I32P]),
     "c2g_ppr_default_params": (ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(PprParams)]),
     "c2g_ppr_batch": (ctypes.c_int, [_P, ctypes.c_int32, _P, ctypes.POINTER(PprParams), _P, _P, ctypes.c_int,
                                      ctypes.c_int, ctypes.POINTER(Stats)]),
@@ -334,14 +334,18 @@ class Graph:
         _check(lib().c2g_graph_last_phases(self._h, _ptr(out)))
         return tuple(float(x) for x in out)
 
-    def last_rounds(self):
-        """Per-round (ms, work units, pull) of the last batched launch on this handle."""
+    def last_rounds(self, first_phase=False):
+        """Per-round (ms, work units, pull) of the last batched launch on this handle;
+        with first_phase, (ms, first-phase ms, work units, pull)."""
         ms = np.zeros(1024, dtype=np.float64)
+        first = np.zeros(1024, dtype=np.float64)
         work = np.zeros(1024, dtype=np.int64)
         shape = np.zeros(1024, dtype=np.int32)
         n = ctypes.c_int32()
-        _check(lib().c2g_graph_last_rounds(self._h, 1024, _ptr(ms), _ptr(work), _ptr(shape), ctypes.byref(n)))
-        return ms[:n.value], work[:n.value], shape[:n.value]
+        _check(lib().c2g_graph_last_rounds(self._h, 1024, _ptr(ms), _ptr(first), _ptr(work), _ptr(shape),
+                                           ctypes.byref(n)))
+        k = n.value
+        return (ms[:k], first[:k], work[:k], shape[:k]) if first_phase else (ms[:k], work[:k], shape[:k])
 
     def watchdog(self, barrier_timeout_ms=0, stall_next_sssp=False):
         _check(lib().c2g_graph_set_watchdog(self._h, barrier_timeout_ms, int(bool(stall_next_sssp))))

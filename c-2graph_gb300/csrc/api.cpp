@@ -406,7 +406,8 @@ int c2g_graph_last_phases(const c2g_graph* g, double ms[4]) {
     return C2G_OK;
 }
 
-int c2g_graph_last_rounds(c2g_graph* g, int32_t cap, double* ms, int64_t* work, int32_t* shape, int32_t* n) {
+int c2g_graph_last_rounds(c2g_graph* g, int32_t cap, double* ms, double* first_ms, int64_t* work, int32_t* shape,
+                          int32_t* n) {
     if (!g || !n) return fail(C2G_ERR_ARG, "NULL argument");
     *n = 0;
     std::lock_guard<std::mutex> lk(g->mu);
@@ -425,6 +426,7 @@ int c2g_graph_last_rounds(c2g_graph* g, int32_t cap, double* ms, int64_t* work, 
     if (rounds < 0) return C2G_OK;  // the launch did not finish cleanly: no trace
     for (int i = 0; i < rounds && i < cap; ++i) {
         if (ms) ms[i] = (double)(t[(size_t)i + 1].t_ns - t[(size_t)i].t_ns) * 1e-6;
+        if (first_ms) first_ms[i] = (double)t[(size_t)i].mid_ns * 1e-6;
         if (work) work[i] = t[(size_t)i].work;
         if (shape) shape[i] = t[(size_t)i].shape;
     }

@@ -78,7 +78,12 @@ constexpr int kPushTileBig = 9;
 constexpr int kPushTileMin = 4;
 
 __device__ __forceinline__ void trace_round(RoundTrace* tr, int i, long long work, int shape) {
-    if (i <= kMaxTraceRounds) tr[i] = RoundTrace{globaltimer_ns(), work, shape, 0};
+    if (i <= kMaxTraceRounds) tr[i] = RoundTrace{globaltimer_ns(), work, shape, 0u};
+}
+
+// The end of round i's first phase (right after its grid barrier).
+__device__ __forceinline__ void trace_mid(RoundTrace* tr, int i) {
+    if (i >= 0 && i <= kMaxTraceRounds) tr[i].mid_ns = (unsigned)(globaltimer_ns() - tr[i].t_ns);
 }
 
 __device__ __forceinline__ FrontierOut batch_out(const BatchParams& p, int buf, int slot) {
@@ -329,6 +334,7 @@ __global__ void __launch_bounds__(kSsspBatchThreads, 3) sssp_batch_persistent(co
         }
         if (!grid_sync(bar, flags, p.barrier_ns)) return;
         phase_mark(ctl->phase_ns, tph, 2);
+        if (gtid == 0) trace_mid(p.trace, iters - 1);
         ++cur;
         // end of an epoch: the next round's improvements wait in the masks
         if (p.epoch_rounds > 0 && iters >= p.epoch_rounds) break;
@@ -1286,6 +1292,7 @@ __global__ void __launch_bounds__(kPprBatchThreads, 3) ppr_batch_persistent(cons
         }
         if (!grid_sync(bar, flags, p.barrier_ns)) return;
         phase_mark(ctl->phase_ns, tph, 2);
+        if (gtid == 0) trace_mid(p.trace, iters - 1);
         // The frontier just consumed leaves the pull lookup.
         for (unsigned j = gtid; j < F; j += nthreads) p.amask[buf][ldcg(p.q[buf] + j).x] = 0u;
         // Phase B: apply the messages of the touched pairs and activate.

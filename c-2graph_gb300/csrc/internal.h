@@ -55,7 +55,7 @@ struct RoundTrace {
     unsigned long long t_ns;
     long long work;  // PPR: (query, edge) pushes of the round; SSSP: edge-word steps
     int shape;       // PPR: 1 pull round, 0 push round; SSSP: 0
-    int pad;
+    unsigned mid_ns;  // from the round's start to the end of its first phase (expansion / push or pull)
 };
 
 // Stamps survive across launches; the kernel advances the bases itself.

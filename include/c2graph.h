@@ -140,11 +140,14 @@ int  c2g_graph_set_watchdog(c2g_graph* g, int32_t barrier_timeout_ms, int32_t st
 int  c2g_graph_last_phases(const c2g_graph* g, double ms[4]);
 /* Tracing (no counterpart in the reference): per-round trace of the last batched launch
  * (c2g_sssp_batch / c2g_ppr_batch, or a session epoch) on this handle, up to 1024 rounds:
- * ms[i] the device time of round i (from one grid barrier to the next, as block 0 sees
- * it), work[i] its work units (PPR: (query, edge) pushes; SSSP: edge-word steps),
+ * ms[i] the device time of round i (as block 0 sees it from one round's start to the
+ * next), first_ms[i] the part of it up to the end of the round's first phase (PPR: the
+ * push or pull, the apply sweep follows; SSSP: the expansion, the next mask sweep
+ * follows), work[i] its work units (PPR: (query, edge) pushes; SSSP: edge-word steps),
  * shape[i] 1 for a pull round, 0 otherwise.  Arrays hold `cap` entries (any may be NULL);
  * *n gets the number of rounds (0 when no batched launch finished cleanly). */
-int  c2g_graph_last_rounds(c2g_graph* g, int32_t cap, double* ms, int64_t* work, int32_t* shape, int32_t* n);
+int  c2g_graph_last_rounds(c2g_graph* g, int32_t cap, double* ms, double* first_ms, int64_t* work, int32_t* shape,
+                           int32_t* n);
 
 /* ---- SSSP -------------------------------------------------------------------------- */
 /* Source-skip rule of the drop-in programs: sssp-base skips sources without

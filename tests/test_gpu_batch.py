@@ -376,8 +376,9 @@ def test_batch_round_trace(gpu_available, g17w, g14p):
         prm = gr.ppr_params(alpha=0.15, rmax=1e-7, seeded=0, pr0=0.15, r0=1.0)
         gr.ppr_batch_pull(1.0)
         _, _, st = gr.ppr_batch(src, prm, want_res=False)
-        ms, work, shape = gr.last_rounds()
+        ms, first, work, shape = gr.last_rounds(first_phase=True)
         assert len(ms) == st.iterations
+        assert np.all(first > 0) and np.all(first < ms)  # the apply sweep follows the push / pull
         assert int(work.sum()) == st.edges_relaxed  # (query, edge) pushes
         assert shape.max() == 1 and shape.min() == 0  # some rounds pulled, some pushed
         assert 0.5 * st.device_ms <= ms.sum() <= st.device_ms * 1.01
