@@ -173,7 +173,13 @@ void session_worker(c2g_server* s, int kind) {
         // evicted queries resume first, into slots not taken by this round's admissions
         while (!parked.empty() && running + (int)admit.size() < cap) {
             int32_t slot = -1;
-            if (c2g_session_resume(ss, parked.front().snap, &slot) != C2G_OK) break;
+            const int rr = c2g_session_resume(ss, parked.front().snap, &slot);
+            if (rr) {  // cannot continue: the request fails with the code
+                c2g_snapshot_free(parked.front().snap);
+                publish(s, parked.front().p, rr);
+                parked.pop_front();
+                continue;
+            }
             slot_req[slot] = std::move(parked.front().p);
             used[slot] = true;
             ++running;

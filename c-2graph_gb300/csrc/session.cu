@@ -195,6 +195,7 @@ struct c2g_snapshot {
     int32_t V = 0;
     int32_t source = 0;
     int32_t rounds = 0;   // rounds run so far (PPR: counts toward the cap)
+    float alpha = 0.f, rmax = 0.f;  // PPR: the push it belongs to
     void* col4 = nullptr;       // SSSP distances (int32) / PPR pr (float)
     double* res = nullptr;      // PPR residuals
     double* rq = nullptr;       // PPR pushed residuals of the frontier lanes
@@ -538,6 +539,8 @@ int c2g_session_evict(c2g_session* s, int32_t slot, c2g_snapshot** out) {
     sn->source = s->source[slot];
     sn->rounds = s->rounds[slot];
     sn->device = g->device;
+    sn->alpha = s->prm.alpha;
+    sn->rmax = s->prm.rmax;
     cudaError_t e = cudaMalloc(&sn->col4, sizeof(int32_t) * (size_t)V);
     if (e == cudaSuccess) e = cudaMalloc(&sn->bits_a, sizeof(unsigned) * nb);
     if (e == cudaSuccess && s->kind == C2G_REQ_PPR) {
@@ -578,6 +581,8 @@ int c2g_session_resume(c2g_session* s, c2g_snapshot* snap, int32_t* slot) {
     std::lock_guard<std::mutex> lk(s->mu);
     if (snap->kind != s->kind || snap->V != s->g->V || snap->device != s->g->device)
         return fail(C2G_ERR_ARG, "snapshot belongs to another kind of session or graph");
+    if (s->kind == C2G_REQ_PPR && (snap->alpha != s->prm.alpha || snap->rmax != s->prm.rmax))
+        return fail(C2G_ERR_ARG, "snapshot belongs to a push with other parameters (alpha, rmax)");
     if (s->kind == C2G_REQ_PPR && snap->rounds > s->prm.max_iter)
         return fail(C2G_ERR_ARG, "snapshot has run past this session's round cap");
     const int i = free_slot(s);

@@ -196,3 +196,30 @@ def test_session_errors(gpu_available, g15):
             sess.read(a)  # still running
         with pytest.raises(c2g.C2GError):
             sess.admit(g.V)
+
+
+def test_session_snapshot_needs_the_same_push(gpu_available, g15):
+    """A PPR snapshot resumes only in a session of the same push (alpha, rmax) and kind;
+    elsewhere it is refused and stays the caller's."""
+    import c2g
+
+    with c2g.Graph.load(g15, "origin") as g:
+        p1 = g.ppr_params(alpha=0.15, rmax=1e-7, seeded=0, pr0=0.15, r0=1.0)
+        p2 = g.ppr_params(alpha=0.2, rmax=1e-7, seeded=0, pr0=0.2, r0=1.0)
+        s = int(np.argmax(np.diff(np.fromfile(g15 + "/origin/vlist.bin", dtype=np.int32))))
+        with c2g.Session(g, c2g.REQ_PPR, 32, p1) as a, c2g.Session(g, c2g.REQ_PPR, 32, p2) as b, \
+                c2g.Session(g, c2g.REQ_SSSP, 32) as c:
+            sl = a.admit(s)
+            a.step(1)
+            snap = a.evict(sl)
+            for other in (b, c):
+                with pytest.raises(c2g.C2GError) as e:
+                    other.resume(snap)
+                assert e.value.code == c2g.ERR_ARG
+            sl2 = a.resume(snap)  # its own session takes it back
+            fin = []
+            for _ in range(200):
+                fin, _ = a.step(8)
+                if fin:
+                    break
+            assert fin == [sl2]
