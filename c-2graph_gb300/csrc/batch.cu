@@ -24,6 +24,7 @@
 #include <vector>
 
 #include "device_common.cuh"
+#include "f32x2.h"
 #include "fp64_mul.h"
 #include "internal.h"
 
@@ -652,6 +653,8 @@ struct PprBatchParams {
     float2* rqf[2];   // the same as a float pair hi + lo (pull rounds)
     unsigned* amask[2];  // [V][W] lanes activated with out-edges, by frontier buffer (pull lookup)
     unsigned* tmask;  // [V][W] touched lanes this round, zero between rounds
+    unsigned* slist;  // pull rounds: the (vertex, word)s a pull left in tmask (tile-straddling targets)
+    unsigned slist_cap;
     unsigned* dmask;  // [V][W] lanes activated without out-edges (popped next round), zero between launches
     int2* q[2];       // frontier entries (v*W + w, edge base)
     unsigned* qmask[2];
@@ -754,24 +757,29 @@ __device__ __forceinline__ void pbatch_apply_word(const PprBatchParams& p, bool 
 }
 
 // Apply sweep: every (vertex, word) whose touched mask is non-zero applies its messages
-// lane by lane (lane = query) and activates; the mask is cleared.  After a pull round only
-// the targets whose in-edges cross a tile boundary are left to it.  Pushes
-// mark targets with red.or, so the push never waits on an atomic's return; the sweep
-// reads V * W mask words per round.  A warp takes 32 words at a time (their degrees
-// loaded lane-parallel) and applies up to kApplyGroup touched words at once: all their
-// residual, message and pr loads are issued before any of them is used, so the words'
-// memory latencies overlap instead of adding up.
+// lane by lane (lane = query) and activates; the mask is cleared.  Pushes mark targets with
+// red.or, so the push never waits on an atomic's return; the sweep reads V * W mask words
+// per round.  After a pull round only the targets whose in-edges cross a tile boundary
+// are left, and the sweep visits just those, from the list the pull wrote (list != null:
+// nlist word indices; 842 vs 875 ms per 256-query batch at scale 22 against sweeping all
+// V * W words).  A warp takes 32 words at a time (their degrees loaded lane-parallel) and
+// applies up to kApplyGroup touched words at once: all their residual, message and pr
+// loads are issued before any of them is used, so the words' memory latencies overlap
+// instead of adding up.  (Loading 2 or 4 blocks of 32 mask words before applying any
+// measured slower: 852 and 870 ms.)
 constexpr int kApplyGroup = 3;  // 4 spills at 64 registers
 
-__device__ __forceinline__ unsigned pbatch_sweep(const PprBatchParams& p, bool force, int ob,
-                                                 WarpStage& fst, const FrontierOut& out, unsigned* dctr,
-                                                 unsigned long long& psum, unsigned gwarp, unsigned nwarps, int lane) {
-    const unsigned nm = (unsigned)p.V << p.logW;
+__device__ __forceinline__ unsigned pbatch_sweep(const PprBatchParams& p, bool force, int ob, const unsigned* list,
+                                                 unsigned nlist, WarpStage& fst, const FrontierOut& out,
+                                                 unsigned* dctr, unsigned long long& psum, unsigned gwarp,
+                                                 unsigned nwarps, int lane) {
+    const unsigned nm = list ? nlist : (unsigned)p.V << p.logW;
     const unsigned long long rmax_bits = c2g_dbits((double)p.rmax);
     unsigned cnt = 0;
     for (unsigned b = gwarp * 32u; b < nm; b += nwarps * 32u) {
-        const unsigned i = b + (unsigned)lane;
-        const unsigned tm = i < nm ? ldcg(p.tmask + i) : 0u;
+        const unsigned pos = b + (unsigned)lane;
+        const unsigned i = pos < nm ? (list ? ldcg(list + pos) : pos) : 0u;  // this lane's (vertex, word)
+        const unsigned tm = pos < nm ? ldcg(p.tmask + i) : 0u;
         int dg = 0;
         if (tm) {
             p.tmask[i] = 0u;
@@ -794,7 +802,8 @@ __device__ __forceinline__ unsigned pbatch_sweep(const PprBatchParams& p, bool f
             for (int u = 0; u < kApplyGroup; ++u) {
                 const int k = ks[u] < 0 ? 0 : ks[u];
                 const unsigned ln = ks[u] < 0 ? 0u : (unsigned)__shfl_sync(kFull, (int)tm, k);
-                const size_t off = ((size_t)(b + (unsigned)k) << 5) + lane;
+                const unsigned vw = (unsigned)__shfl_sync(kFull, (int)i, k);
+                const size_t off = ((size_t)vw << 5) + lane;
                 const bool mine = (ln >> lane) & 1u;
                 r[u] = mine ? ldcg(p.res + off) : 0.0;
                 m[u] = (mine && !force) ? ldcg(p.msg + off) : 0.0;
@@ -805,7 +814,7 @@ __device__ __forceinline__ unsigned pbatch_sweep(const PprBatchParams& p, bool f
                 if (ks[u] < 0) break;  // warp-uniform
                 const unsigned ln = (unsigned)__shfl_sync(kFull, (int)tm, ks[u]);
                 const int dgu = __shfl_sync(kFull, dg, ks[u]);
-                const int vw = (int)(b + (unsigned)ks[u]);
+                const int vw = __shfl_sync(kFull, (int)i, ks[u]);
                 const size_t off = ((size_t)(unsigned)vw << 5) + lane;
                 const bool mine = (ln >> lane) & 1u;
                 if (mine && !force) p.msg[off] = 0.0;
@@ -840,11 +849,14 @@ constexpr int kPullEdges = 2;  // in-edges whose rq rows are gathered before the
 // whose in-edges lie in this tile has them all: it is applied here, by the pulling warp
 // (the pullers read the other round parity's rq pairs and activity masks, so this apply
 // does not disturb them).  An owner whose in-edges cross a tile boundary adds its part to
-// msg in FP64 (atomics) and marks tmask; the apply sweep after the barrier finishes it.
+// msg in FP64 (atomics) and marks tmask; the apply after the barrier finishes it.  The
+// first part to mark a (vertex, word) appends it to slist (counter sctr), so that apply
+// visits only the listed words instead of sweeping all V * W (at most one owner straddles
+// each tile boundary, so the list holds at most ntiles_r * W words).
 __device__ __forceinline__ unsigned pbatch_pull_owner(const PprBatchParams& p, int v, unsigned w0, bool whole,
                                                       const float (&sh)[kPullWords], const float (&sl)[kPullWords],
                                                       int ob, unsigned long long rmax_bits, WarpStage& fst,
-                                                      const FrontierOut& out, unsigned* dctr,
+                                                      const FrontierOut& out, unsigned* dctr, unsigned* sctr,
                                                       unsigned long long& psum, int lane) {
     const unsigned W = 1u << p.logW;
     unsigned cnt = 0;
@@ -859,7 +871,10 @@ __device__ __forceinline__ unsigned pbatch_pull_owner(const PprBatchParams& p, i
                 if (nz)
                     atomicAdd(p.msg + (vw << 5) + lane, c2g_float_bits_to_double(__float_as_uint(sh[j])) +
                                                             c2g_float_bits_to_double(__float_as_uint(sl[j])));
-                if (lane == 0) atomicOr(p.tmask + vw, bits);
+                if (lane == 0 && atomicOr(p.tmask + vw, bits) == 0u) {
+                    const unsigned k = atomicAdd(sctr, 1u);
+                    if (k < p.slist_cap) p.slist[k] = (unsigned)vw;
+                }
             }
         }
         return 0;
@@ -889,13 +904,23 @@ __device__ __forceinline__ unsigned pbatch_pull_owner(const PprBatchParams& p, i
     return cnt;
 }
 
+// A warp's chunk of 32 in-edges, staged in shared memory: source, weight bits and the
+// source's active lanes in the item's 4 query words.  Each lane loads one in-edge; the
+// warp then reads them one by one as broadcasts (two shared loads per in-edge instead of
+// six shuffles, and the chunk's values leave the registers of the gather loop).
+struct PullChunk {
+    int2 ed[32];
+    uint4 mk[32];
+};
+
 // Phase A of a pull round.  A warp takes (tile, word group) items from the round's queue
 // and walks the tile's owners one by one: for each owner, its in-edges in the tile in
-// chunks of 32 (source, weight and the source's active lanes loaded lane-parallel), the
-// pushed residuals of kPullEdges in-edges gathered before they are summed.
+// chunks of 32 (loaded lane-parallel and staged in pc), the pushed residuals of
+// kPullEdges in-edges gathered before they are summed, two query words per packed
+// instruction (f32x2.h).
 __device__ __forceinline__ unsigned pbatch_pull(const PprBatchParams& p, int buf, int ob, unsigned* qctr,
-                                                WarpStage& fst, const FrontierOut& out, unsigned* dctr,
-                                                unsigned long long& psum, int lane, bool& bad) {
+                                                PullChunk& pc, WarpStage& fst, const FrontierOut& out, unsigned* dctr,
+                                                unsigned* sctr, unsigned long long& psum, int lane, bool& bad) {
     const unsigned W = 1u << p.logW;
     const int lg = p.logW >= 2 ? p.logW - 2 : 0;  // word groups per tile = 2^lg (kPullWords = 4)
     const unsigned nitems = p.ntiles_r << lg;
@@ -907,8 +932,11 @@ __device__ __forceinline__ unsigned pbatch_pull(const PprBatchParams& p, int buf
     unsigned itn = next_tile(qctr, lane);
     for (unsigned it = itn; it < nitems; it = itn) {
         itn = next_tile(qctr, lane);  // the next item, fetched while this one runs
-        const unsigned t = it >> lg;
-        const unsigned w0 = (it & ((1u << lg) - 1u)) * (unsigned)kPullWords;
+        // word group major: all tiles of one word group, then the next, so the residual
+        // rows that L2 holds for the busiest sources are one word group's (1 KB per source,
+        // not 2 at 256 queries): 818 vs 843 ms per 256-query batch at scale 22
+        const unsigned t = it % p.ntiles_r;
+        const unsigned w0 = (it / p.ntiles_r) * (unsigned)kPullWords;
         const unsigned e0 = t << kPullTileLog;
         const unsigned e1 = min(e0 + tw, p.E);
         int v = __ldg(p.mark_r + t);  // owner of in-edge e0
@@ -917,9 +945,10 @@ __device__ __forceinline__ unsigned pbatch_pull(const PprBatchParams& p, int buf
             const unsigned ve = (unsigned)__ldg(p.row_r + v + 1);
             const unsigned ea = max(vs, e0), ez = min(ve, e1);
             if (ea < ez) {  // warp-uniform: v has in-edges in this tile
-                float sh[kPullWords], sl[kPullWords];
+                // message sums hi + lo of words (0, 1) and (2, 3), packed
+                f32x2 sh2[kPullWords / 2], sl2[kPullWords / 2];
 #pragma unroll
-                for (int j = 0; j < kPullWords; ++j) sh[j] = sl[j] = 0.f;
+                for (int j = 0; j < kPullWords / 2; ++j) sh2[j] = sl2[j] = 0ull;
                 for (unsigned b = ea; b < ez; b += 32u) {
                     const unsigned e = b + (unsigned)lane;
                     int src = 0;
@@ -949,6 +978,10 @@ __device__ __forceinline__ unsigned pbatch_pull(const PprBatchParams& p, int buf
                         }
                     }
                     const unsigned n = min(32u, ez - b);
+                    __syncwarp();  // the previous chunk's reads are done
+                    pc.ed[lane] = make_int2(src, __float_as_int(wt));
+                    pc.mk[lane] = make_uint4(mk[0], mk[1], mk[2], mk[3]);
+                    __syncwarp();
                     for (unsigned k0 = 0; k0 < n; k0 += kPullEdges) {
                         // gather the pushed residuals of kPullEdges in-edges, then add them
                         float2 qb[kPullEdges][kPullWords];
@@ -956,11 +989,13 @@ __device__ __forceinline__ unsigned pbatch_pull(const PprBatchParams& p, int buf
 #pragma unroll
                         for (int h = 0; h < kPullEdges; ++h) {
                             const unsigned k = k0 + h < n ? k0 + h : n - 1u;
-                            wk[h] = __shfl_sync(kFull, wt, (int)k);
-                            const int u = __shfl_sync(kFull, src, (int)k);
+                            const int2 ek = pc.ed[k];
+                            const uint4 mq = pc.mk[k];
+                            wk[h] = __int_as_float(ek.y);
+                            const int u = ek.x;
 #pragma unroll
                             for (int j = 0; j < kPullWords; ++j) {
-                                const unsigned mj = (unsigned)__shfl_sync(kFull, (int)mk[j], (int)k);
+                                const unsigned mj = j == 0 ? mq.x : j == 1 ? mq.y : j == 2 ? mq.z : mq.w;
                                 const bool on = k0 + h < n && ((mj >> lane) & 1u);
                                 qb[h][j] = on ? ldcg(rqb + ((size_t)(unsigned)u << (p.logW + 5)) + ((w0 + j) << 5) +
                                                      lane)
@@ -969,25 +1004,39 @@ __device__ __forceinline__ unsigned pbatch_pull(const PprBatchParams& p, int buf
                         }
 #pragma unroll
                         for (int h = 0; h < kPullEdges; ++h) {
+                            const f32x2 w2 = f2_pack(wk[h], wk[h]);
+                            const f32x2 nw2 = f2_pack(-wk[h], -wk[h]);
 #pragma unroll
-                            for (int j = 0; j < kPullWords; ++j) {
-                                // message (hi + lo) * w = pm + pe; two-sum of sh + pm
-                                // (explicit roundings: nothing may be contracted into an FMA)
-                                const float pm = __fmul_rn(qb[h][j].x, wk[h]);
-                                const float pe =
-                                    __fmaf_rn(qb[h][j].y, wk[h], __fmaf_rn(qb[h][j].x, wk[h], -pm));
-                                const float s = __fadd_rn(sh[j], pm);
-                                const float bv = __fadd_rn(s, -sh[j]);
-                                const float av = __fadd_rn(s, -bv);
-                                const float te = __fadd_rn(__fadd_rn(sh[j], -av), __fadd_rn(pm, -bv));
-                                sl[j] = __fadd_rn(sl[j], __fadd_rn(te, pe));
-                                sh[j] = s;
+                            for (int j = 0; j < kPullWords / 2; ++j) {
+                                // message (hi + lo) * w = pm + pe; two-sum of sh + pm, for words
+                                // 2j and 2j+1 at once.  npm = -pm exactly (round-to-nearest is
+                                // symmetric), so every line rounds as the scalar form
+                                //   pm = hi*w, pe = fma(lo, w, fma(hi, w, -pm)), s = sh + pm,
+                                //   bv = s - sh, av = s - bv, te = (sh - av) + (pm - bv),
+                                //   sl += te + pe, sh = s
+                                // does: pm - bv = -(npm + bv).
+                                const f32x2 hi = f2_pack(qb[h][2 * j].x, qb[h][2 * j + 1].x);
+                                const f32x2 lo = f2_pack(qb[h][2 * j].y, qb[h][2 * j + 1].y);
+                                const f32x2 npm = f2_mul(hi, nw2);
+                                const f32x2 pe = f2_fma(lo, w2, f2_fma(hi, w2, npm));
+                                const f32x2 s2 = f2_sub(sh2[j], npm);
+                                const f32x2 bv = f2_sub(s2, sh2[j]);
+                                const f32x2 av = f2_sub(s2, bv);
+                                const f32x2 te = f2_sub(f2_sub(sh2[j], av), f2_add(npm, bv));
+                                sl2[j] = f2_add(sl2[j], f2_add(te, pe));
+                                sh2[j] = s2;
                             }
                         }
                     }
                 }
+                float sh[kPullWords], sl[kPullWords];
+#pragma unroll
+                for (int j = 0; j < kPullWords / 2; ++j) {
+                    f2_unpack(sh2[j], sh[2 * j], sh[2 * j + 1]);
+                    f2_unpack(sl2[j], sl[2 * j], sl[2 * j + 1]);
+                }
                 cnt += pbatch_pull_owner(p, v, w0, vs >= e0 && ve <= e1, sh, sl, ob, rmax_bits, fst, out, dctr,
-                                         psum, lane);
+                                         sctr, psum, lane);
             }
             if (ve >= e1) break;
             ++v;
@@ -1049,6 +1098,7 @@ __global__ void __launch_bounds__(kPprBatchThreads, 3) ppr_batch_persistent(cons
     const int wib = threadIdx.x >> 5;
     WarpStage fst{sm.v0[wib], sm.d0[wib], sm.x0[wib], 0};
     int* qtab = sm.v1[wib];  // slot -> query position table of the owner being expanded
+    __shared__ PullChunk pcs[kPprBatchThreads / 32];  // pull rounds' in-edge chunks
     const double one_m_a = 1.0 - (double)p.alpha;
     unsigned long long tph = globaltimer_ns();
     unsigned long long psum = 0;  // next round's pushes counted by this warp (lane 0)
@@ -1101,7 +1151,7 @@ __global__ void __launch_bounds__(kPprBatchThreads, 3) ppr_batch_persistent(cons
     }
     if (!grid_sync(bar, flags, p.barrier_ns)) return;
     // Round-1 frontier: every touched (vertex, word) activates its touched lanes.
-    pbatch_sweep(p, true, 1, fst, pbatch_out(p, 1, 1), &ctl->dctr[1], psum, gwarp, nwarps, lane);
+    pbatch_sweep(p, true, 1, nullptr, 0u, fst, pbatch_out(p, 1, 1), &ctl->dctr[1], psum, gwarp, nwarps, lane);
     if (lane == 0 && psum) atomicAdd(&ctl->pcount[1], psum);
     psum = 0;
     if (!grid_sync(bar, flags, p.barrier_ns)) return;
@@ -1162,6 +1212,7 @@ __global__ void __launch_bounds__(kPprBatchThreads, 3) ppr_batch_persistent(cons
             ctl->qctr[fslot] = 0ull;
             ctl->dctr[fslot] = 0u;
             ctl->tilectr[fslot] = 0u;
+            ctl->listctr[fslot] = 0u;
             ctl->pcount[fslot] = 0ull;
             ctl->popped += F;
             ctl->relaxed += T;
@@ -1173,8 +1224,8 @@ __global__ void __launch_bounds__(kPprBatchThreads, 3) ppr_batch_persistent(cons
                 pushes += (long long)P;
                 steps += T;
             }
-            touched += pbatch_pull(p, buf, ob, &ctl->tilectr[cur % 3], fst, pbatch_out(p, ob, nslot),
-                                   &ctl->dctr[nslot], psum, lane, bad);
+            touched += pbatch_pull(p, buf, ob, &ctl->tilectr[cur % 3], pcs[wib], fst, pbatch_out(p, ob, nslot),
+                                   &ctl->dctr[nslot], &ctl->listctr[cur % 3], psum, lane, bad);
         } else {
             // Push round, phase A: push along the frontier's edges (owner runs, as in the
             // SSSP batch): red.add of the FP64 message per active lane, red.or of the
@@ -1295,9 +1346,12 @@ __global__ void __launch_bounds__(kPprBatchThreads, 3) ppr_batch_persistent(cons
         if (gtid == 0) trace_mid(p.trace, iters - 1);
         // The frontier just consumed leaves the pull lookup.
         for (unsigned j = gtid; j < F; j += nthreads) p.amask[buf][ldcg(p.q[buf] + j).x] = 0u;
-        // Phase B: apply the messages of the touched pairs and activate.
-        touched += pbatch_sweep(p, false, ob, fst, pbatch_out(p, ob, nslot), &ctl->dctr[nslot], psum, gwarp, nwarps,
-                                lane);
+        // Phase B: apply the messages of the touched pairs and activate: after a pull, the
+        // listed straddlers (unless the list overflowed); after a push, every touched word.
+        const unsigned nl = pull ? ldcg(&ctl->listctr[cur % 3]) : 0u;
+        const bool listed = pull && nl <= p.slist_cap;  // grid-uniform
+        touched += pbatch_sweep(p, false, ob, listed ? p.slist : nullptr, nl, fst, pbatch_out(p, ob, nslot),
+                                &ctl->dctr[nslot], psum, gwarp, nwarps, lane);
         if (lane == 0 && psum) atomicAdd(&ctl->pcount[nslot], psum);
         psum = 0;
         if (!grid_sync(bar, flags, p.barrier_ns)) return;
@@ -1360,6 +1414,8 @@ struct PprBatchWork {
     float2* rqf[2] = {nullptr, nullptr};
     unsigned* amask[2] = {nullptr, nullptr};
     unsigned* tmask = nullptr;
+    unsigned* slist = nullptr;
+    unsigned slist_cap = 0;
     unsigned* dmask = nullptr;
     int2* q[2] = {nullptr, nullptr};
     unsigned* qmask[2] = {nullptr, nullptr};
@@ -1382,7 +1438,8 @@ void ppr_batch_free(c2g_graph* g) {
     PprBatchWork* w = reinterpret_cast<PprBatchWork*>(g->ppr_batch);
     if (!w) return;
     if (g->last_trace == w->trace) g->last_trace = nullptr;
-    void* ptrs[] = {w->pr, w->res, w->msg, w->rq, w->rq2, w->rqf[0], w->rqf[1], w->amask[0], w->amask[1], w->tmask, w->dmask,
+    void* ptrs[] = {w->pr, w->res, w->msg, w->rq, w->rq2, w->rqf[0], w->rqf[1], w->amask[0], w->amask[1], w->tmask,
+                    w->slist, w->dmask,
                     w->q[0], w->q[1],
                     w->qmask[0], w->qmask[1],
                     w->mark[0], w->mark[1], w->dangle, w->ctl, w->counters, w->src, w->seed_off,
@@ -1411,6 +1468,10 @@ static int ppr_batch_alloc(c2g_graph* g, int Q, size_t n_seeds) {
     C2G_CUDA(cudaMalloc(&w->rqf[0], sizeof(float2) * VQ));
     C2G_CUDA(cudaMalloc(&w->rqf[1], sizeof(float2) * VQ));
     C2G_CUDA(cudaMalloc(&w->tmask, sizeof(unsigned) * qcap));
+    // pull rounds' straddlers: at most one owner per in-edge tile boundary, W words each
+    const size_t ntiles_r = (((size_t)g->E + (1u << kPullTileLog) - 1) >> kPullTileLog) + 1;
+    w->slist_cap = (unsigned)std::min(qcap, ntiles_r * W);
+    C2G_CUDA(cudaMalloc(&w->slist, sizeof(unsigned) * w->slist_cap));
     C2G_CUDA(cudaMalloc(&w->dmask, sizeof(unsigned) * qcap));
     C2G_CUDA(cudaMalloc(&w->amask[0], sizeof(unsigned) * qcap));
     C2G_CUDA(cudaMalloc(&w->amask[1], sizeof(unsigned) * qcap));
@@ -1515,6 +1576,8 @@ static void ppr_batch_params(c2g_graph* g, PprBatchWork* w, int Q, int logW, con
     p.rqf[0] = w->rqf[0];
     p.rqf[1] = w->rqf[1];
     p.tmask = w->tmask;
+    p.slist = w->slist;
+    p.slist_cap = w->slist_cap;
     p.dmask = w->dmask;
     p.epoch_rounds = 0;
     p.cur0 = 1;
