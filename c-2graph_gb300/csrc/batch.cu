@@ -193,14 +193,17 @@ __global__ void __launch_bounds__(kSsspBatchThreads, 3) sssp_batch_persistent(co
     }
     if (!grid_sync(bar, flags, p.barrier_ns)) return;
 
-    // Sources and their seeds: dist[s][q] = 0, dist[seed][q] = min(w); mark them.
-    for (unsigned qi = gtid; qi < (unsigned)p.nq; qi += nthreads) {
+    // Sources and their seeds: dist[s][q] = 0, dist[seed][q] = min(w); mark them.  A warp
+    // per query, its lanes over the seed records.
+    for (unsigned qi = gwarp; qi < (unsigned)p.nq; qi += nwarps) {
         const int s = p.sources[qi];
         const unsigned bit = 1u << (qi & 31), w = qi >> 5;
-        atomicMin(p.dist + (size_t)s * p.Q + qi, 0);
-        atomicOr(p.mask + ((size_t)s << p.logW) + w, bit);
+        if (lane == 0) {
+            atomicMin(p.dist + (size_t)s * p.Q + qi, 0);
+            atomicOr(p.mask + ((size_t)s << p.logW) + w, bit);
+        }
         if (p.seed_off)
-            for (int k = p.seed_off[qi]; k < p.seed_off[qi + 1]; ++k) {
+            for (int k = p.seed_off[qi] + lane; k < p.seed_off[qi + 1]; k += 32) {
                 atomicMin(p.dist + (size_t)p.seed_v[k] * p.Q + qi, p.seed_w[k]);
                 atomicOr(p.mask + ((size_t)p.seed_v[k] << p.logW) + w, bit);
             }
@@ -904,10 +907,11 @@ __device__ __forceinline__ unsigned pbatch_pull_owner(const PprBatchParams& p, i
     return cnt;
 }
 
-// A warp's chunk of 32 in-edges, staged in shared memory: source, weight bits and the
-// source's active lanes in the item's 4 query words.  Each lane loads one in-edge; the
-// warp then reads them one by one as broadcasts (two shared loads per in-edge instead of
-// six shuffles, and the chunk's values leave the registers of the gather loop).
+// A warp's chunk of up to 32 in-edges, staged in shared memory: source, weight bits and
+// the source's active lanes in the item's 4 query words.  Each lane loads one in-edge and
+// the live ones (a source with an active lane) are compacted into the chunk; the warp
+// then reads them one by one as broadcasts (two shared loads per in-edge instead of six
+// shuffles, and the chunk's values leave the registers of the gather loop).
 struct PullChunk {
     int2 ed[32];
     uint4 mk[32];
@@ -977,10 +981,17 @@ __device__ __forceinline__ unsigned pbatch_pull(const PprBatchParams& p, int buf
                             }
                         }
                     }
-                    const unsigned n = min(32u, ez - b);
+                    // only in-edges whose source has an active lane in the item's words are
+                    // staged (in order): the others would add exact zeros
+                    const bool live = (mk[0] | mk[1] | mk[2] | mk[3]) != 0u;
+                    const unsigned lm = __ballot_sync(kFull, live);
+                    const unsigned n = (unsigned)__popc(lm);
                     __syncwarp();  // the previous chunk's reads are done
-                    pc.ed[lane] = make_int2(src, __float_as_int(wt));
-                    pc.mk[lane] = make_uint4(mk[0], mk[1], mk[2], mk[3]);
+                    if (live) {
+                        const unsigned at = (unsigned)__popc(lm & ((1u << lane) - 1u));
+                        pc.ed[at] = make_int2(src, __float_as_int(wt));
+                        pc.mk[at] = make_uint4(mk[0], mk[1], mk[2], mk[3]);
+                    }
                     __syncwarp();
                     for (unsigned k0 = 0; k0 < n; k0 += kPullEdges) {
                         // gather the pushed residuals of kPullEdges in-edges, then add them
@@ -1119,20 +1130,24 @@ __global__ void __launch_bounds__(kPprBatchThreads, 3) ppr_batch_persistent(cons
     }
     if (!grid_sync(bar, flags, p.barrier_ns)) return;
     // Sources: base mode puts r0 on the source; seeded mode applies the host-side first
-    // hop (records + kept out-edges) to pr/res.  Either way the touched lanes are marked.
-    for (unsigned qi = gtid; qi < (unsigned)p.nq; qi += nthreads) {
+    // hop (records + kept out-edges) to pr/res, a warp per query with its lanes over the
+    // records and edges (a hub source has thousands).  Either way the touched lanes are
+    // marked.
+    for (unsigned qi = gwarp; qi < (unsigned)p.nq; qi += nwarps) {
         const int s = p.sources[qi];
         const int w = (int)(qi >> 5);
         const unsigned bit = 1u << (qi & 31);
         if (!p.seeded) {
-            atomicAdd(p.pr + (size_t)s * p.Q + qi, p.pr0);
-            atomicAdd(p.res + (size_t)s * p.Q + qi, (double)p.r0);
-            atomicOr(p.tmask + ((size_t)s << p.logW) + w, bit);
+            if (lane == 0) {
+                atomicAdd(p.pr + (size_t)s * p.Q + qi, p.pr0);
+                atomicAdd(p.res + (size_t)s * p.Q + qi, (double)p.r0);
+                atomicOr(p.tmask + ((size_t)s << p.logW) + w, bit);
+            }
         } else {
-            atomicAdd(p.pr + (size_t)s * p.Q + qi, p.alpha);
+            if (lane == 0) atomicAdd(p.pr + (size_t)s * p.Q + qi, p.alpha);
             const int rs = __ldg(p.row + s), re = __ldg(p.row + s + 1);
             const int n_rec = p.seed_off[qi + 1] - p.seed_off[qi];
-            for (int k = 0; k < n_rec + (re - rs); ++k) {
+            for (int k = lane; k < n_rec + (re - rs); k += 32) {
                 int v;
                 float wt;
                 if (k < n_rec) {
