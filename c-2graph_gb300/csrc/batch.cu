@@ -699,10 +699,12 @@ __device__ __forceinline__ FrontierOut pbatch_out(const PprBatchParams& p, int b
     return o;
 }
 
-// Launch shape of the batched PPR: 3 blocks of 384 threads per SM, as for the SSSP batch
-// (1.96 s vs 2.08 s for 2 x 512 at 256 sources, scale 22, despite a few spilled
-// registers at the 56-register cap).
-constexpr int kPprBatchThreads = 384;
+// Launch shape of the batched PPR: 2 blocks of 512 threads per SM (64 registers).  With the
+// pull rounds staged through shared memory it beats 3 x 384 (56 registers) by about 1% at
+// 256 sources, scale 22 (766 vs 775 ms: faster pulls, slower pushes) and 4 x 256 (778 ms);
+// before the staging 3 x 384 had been the faster one (962 vs 1,030 ms).
+constexpr int kPprBatchThreads = 512;
+constexpr int kPprBatchBlocksPerSm = 2;
 constexpr int kPprBatchUnroll = 3;  // push items in flight per lane
 
 // Apply of one (vertex, word) to the lanes that received messages: res += m; a lane whose
@@ -1095,7 +1097,8 @@ __device__ __noinline__ void pbatch_rebuild(const PprBatchParams& p, int b, int 
     if (lane == 0 && ps) atomicAdd(&p.ctl->pcount[slot], ps);
 }
 
-__global__ void __launch_bounds__(kPprBatchThreads, 3) ppr_batch_persistent(const PprBatchParams p) {
+__global__ void __launch_bounds__(kPprBatchThreads, kPprBatchBlocksPerSm)
+    ppr_batch_persistent(const PprBatchParams p) {
     TraversalCtl* ctl = p.ctl;
     GridBarrier* bar = reinterpret_cast<GridBarrier*>(&ctl->bar_count);
     int* flags = &ctl->flags;

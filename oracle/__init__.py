@@ -49,6 +49,8 @@ def lib():
         L.orc_prune_sssp.argtypes = [ctypes.c_char_p]
         L.orc_prune_ppr.restype = ctypes.c_int
         L.orc_prune_ppr.argtypes = [ctypes.c_char_p, ctypes.c_double]
+        L.orc_prune_depth.restype = ctypes.c_int
+        L.orc_prune_depth.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_double, _P]
         _lib = L
     return _lib
 
@@ -221,6 +223,23 @@ def prune_ppr(dir, alpha=None):
     rc = lib().orc_prune_ppr(os.fsencode(dir), 0.8 if alpha is None else 1.0 - alpha)
     if rc:
         raise RuntimeError("orc_prune_ppr failed: %d" % rc)
+
+
+def prune_depth(dir, kind, alpha=None):
+    """Run a pruner (kind "sssp" or "ppr") with the dependency analysis of its visiting
+    order (oracle/ingest.c orc_prune_depth); writes the same outputs as prune_sssp /
+    prune_ppr.  Returns the visits, the visits that moved edges, the visiting decisions,
+    the depth (the longest chain of dependent operations, decisions included, and of
+    pruning visits alone), the widest level, and the visits in levels of >= 32 and
+    >= 1024 visits."""
+    st = np.zeros(8, np.int64)
+    keep = 0.8 if alpha is None else 1.0 - alpha
+    rc = lib().orc_prune_depth(os.fsencode(dir), 1 if kind == "ppr" else 0, keep, st.ctypes.data)
+    if rc:
+        raise RuntimeError("orc_prune_depth failed: %d" % rc)
+    keys = ("visits", "removing", "decisions", "depth", "visit_depth", "widest", "in_levels_ge32",
+            "in_levels_ge1024")
+    return {k: int(x) for k, x in zip(keys, st)}
 
 
 def adsorption_labels(row, col, f, seeds, p_inj, p_cont, iterations):

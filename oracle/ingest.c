@@ -28,6 +28,10 @@
  *                      (w * keep) * w' in double and rounded to float (:244-259), keep =
  *                      0.8 in the reference.
  *
+ *   orc_prune_depth    either pruner with a dependency analysis of its visiting order
+ *                      (not a restatement: an analysis of the sequential algorithm, for
+ *                      the question whether a parallel pruner could reproduce its bytes).
+ *
  * The pruners keep the reference's per-vertex state: the out-rows as sorted
  * (target, weight) lists built from each row's distinct pairs without self-loops
  * (core/util.hpp:80-96), the in-rows as sorted (source, alive) lists
@@ -340,9 +344,52 @@ typedef struct {
     ilist hv, he, hw, owner;
 } records;
 
+/* Dependency depth of a pruning order.  Every visit is an operation with read and write
+ * sets over the rows it touches: the out-rows, and the in-rows with their live in-degree.
+ * An operation's level is one more than the latest level that wrote a row it touches or
+ * read a row it writes (read-after-write, write-after-read and write-after-write all
+ * order two operations).  A visit includes its decision; the decision of a vertex that
+ * is not pruned at its turn (its live in-degree out of bounds, or no out-edges) is an
+ * operation of its own that reads the vertex's in-row and out-row.  The largest level is the length of the longest chain of
+ * dependent operations: the fewest steps in which any parallel pruner that reproduces
+ * the sequential bytes can run. */
+typedef struct {
+    int32_t *wo, *ro; /* out-row x: latest level that wrote / read it */
+    int32_t *wi, *ri; /* in-row x (with the live in-degree) */
+    int32_t depth;    /* largest level of any operation */
+    int32_t pdepth;   /* largest level of a pruning visit */
+    int64_t visits, removing, decisions;
+    int64_t* width; /* pruning visits per level */
+    int64_t width_cap;
+} depth_track;
+
+static int32_t imax(int32_t a, int32_t b) { return a > b ? a : b; }
+
+static void depth_width(depth_track* d, int32_t lv) {
+    if (lv >= d->width_cap) {
+        int64_t cap = d->width_cap ? d->width_cap : 1024;
+        while (cap <= lv) cap *= 2;
+        d->width = (int64_t*)realloc(d->width, sizeof(int64_t) * (size_t)cap);
+        memset(d->width + d->width_cap, 0, sizeof(int64_t) * (size_t)(cap - d->width_cap));
+        d->width_cap = cap;
+    }
+    d->width[lv]++;
+}
+
+/* the visiting decision of vertex i: reads its in-row and out-row */
+static void depth_decide(depth_track* d, int32_t i) {
+    if (!d) return;
+    const int32_t lv = 1 + imax(d->wi[i], d->wo[i]);
+    d->ri[i] = imax(d->ri[i], lv);
+    d->ro[i] = imax(d->ro[i], lv);
+    d->depth = imax(d->depth, lv);
+    d->decisions++;
+}
+
 /* Prune vertex i (src/purn-sssp.cpp:151-286, src/purn-ppr.cpp:154-284).  Returns 0, or
  * -3 when the in/out rows disagree (the reference prints "something error2"). */
-static int prune_one(const prune_rule* rule, int32_t i, orow* out, irow* in, int32_t* indeg, records* rec) {
+static int prune_one(const prune_rule* rule, int32_t i, orow* out, irow* in, int32_t* indeg, records* rec,
+                     depth_track* dt) {
     const int32_t j = indeg[i];
     int32_t* root = (int32_t*)malloc(sizeof(int32_t) * (size_t)(j ? j : 1));
     uint32_t* dis = (uint32_t*)malloc(sizeof(uint32_t) * (size_t)(j ? j : 1));
@@ -421,6 +468,29 @@ static int prune_one(const prune_rule* rule, int32_t i, orow* out, irow* in, int
             kt[nk] = v, kw[nk] = d3, ++nk;
         }
     }
+    if (dt) { /* reads: in-row i, out-rows of i and its roots; writes when edges move */
+        int32_t lv = imax(dt->wi[i], dt->wo[i]);
+        for (int32_t k = 0; k < j; ++k) lv = imax(lv, dt->wo[root[k]]);
+        if (nrm > 0) {
+            lv = imax(lv, imax(dt->ro[i], dt->ri[i]));
+            for (int32_t k = 0; k < j; ++k) lv = imax(lv, dt->ro[root[k]]);
+            for (int32_t k = 0; k < nrm; ++k) lv = imax(lv, imax(dt->wi[rt[k]], dt->ri[rt[k]]));
+        }
+        ++lv;
+        dt->ri[i] = imax(dt->ri[i], lv);
+        dt->ro[i] = imax(dt->ro[i], lv);
+        for (int32_t k = 0; k < j; ++k) dt->ro[root[k]] = imax(dt->ro[root[k]], lv);
+        if (nrm > 0) {
+            dt->wo[i] = lv;
+            for (int32_t k = 0; k < j; ++k) dt->wo[root[k]] = lv;
+            for (int32_t k = 0; k < nrm; ++k) dt->wi[rt[k]] = lv;
+            dt->removing++;
+        }
+        dt->depth = imax(dt->depth, lv);
+        dt->pdepth = imax(dt->pdepth, lv);
+        dt->visits++;
+        depth_width(dt, lv);
+    }
     /* fold the removed edges into every root's row (a sorted merge) */
     for (int32_t k = 0; k < j && nrm > 0; ++k) {
         orow* o = &out[root[k]];
@@ -455,7 +525,7 @@ static int prune_one(const prune_rule* rule, int32_t i, orow* out, irow* in, int
     return 0;
 }
 
-static int prune_dir(const char* dir, int ppr, double keep) {
+static int prune_dir(const char* dir, int ppr, double keep, depth_track* dt) {
     size_t nv = 0, ne = 0, nw = 0;
     int32_t* vl = orc_read4(dir, "origin", "vlist", &nv);
     int32_t* el = orc_read4(dir, "origin", "elist", &ne);
@@ -469,6 +539,12 @@ static int prune_dir(const char* dir, int ppr, double keep) {
     irow* in = (irow*)calloc((size_t)(V ? V : 1), sizeof(irow));
     int32_t* indeg = (int32_t*)malloc(sizeof(int32_t) * (size_t)(V ? V : 1));
     prune_rows(V, vl, el, wl, ppr, out, in, indeg);
+    if (dt) {
+        dt->wo = (int32_t*)calloc((size_t)(V ? V : 1), sizeof(int32_t));
+        dt->ro = (int32_t*)calloc((size_t)(V ? V : 1), sizeof(int32_t));
+        dt->wi = (int32_t*)calloc((size_t)(V ? V : 1), sizeof(int32_t));
+        dt->ri = (int32_t*)calloc((size_t)(V ? V : 1), sizeof(int32_t));
+    }
     free(el);
     free(wl);
     prune_rule rule = {ppr, keep};
@@ -481,17 +557,25 @@ static int prune_dir(const char* dir, int ppr, double keep) {
         unsigned char* seen = (unsigned char*)calloc((size_t)(V ? V : 1), 1);
         for (int32_t k = 0; k <= dmax && !rc; ++k)
             for (int32_t i = 0; i < V && !rc; ++i) {
-                if (indeg[i] > k || seen[i] || indeg[i] == 0) continue;
+                if (seen[i]) continue;
+                if (indeg[i] > k || indeg[i] == 0) {
+                    depth_decide(dt, i);
+                    continue;
+                }
                 seen[i] = 1;
-                if (out[i].n > 0 && indeg[i] > 0 && indeg[i] <= dmax) rc = prune_one(&rule, i, out, in, indeg, &rec);
+                if (out[i].n > 0 && indeg[i] > 0 && indeg[i] <= dmax)
+                    rc = prune_one(&rule, i, out, in, indeg, &rec, dt);
+                else
+                    depth_decide(dt, i);
             }
         free(seen);
     } else {
         const int32_t dmax = 5;
         for (int32_t i = 0; i < V && !rc; ++i) {
             if (out[i].n > 0 && indeg[i] > 0 && indeg[i] <= dmax) {
-                rc = prune_one(&rule, i, out, in, indeg, &rec);
+                rc = prune_one(&rule, i, out, in, indeg, &rec, dt);
             } else {
+                depth_decide(dt, i);
                 il_push(&rec.hv, (uint32_t)rec.he.n);
                 il_push(&rec.owner, (uint32_t)i);
             }
@@ -529,11 +613,35 @@ static int prune_dir(const char* dir, int ppr, double keep) {
         free(in[v].s), free(in[v].alive);
     }
     free(out), free(in), free(indeg), free(vl);
+    if (dt) free(dt->wo), free(dt->ro), free(dt->wi), free(dt->ri);
     free(rec.hv.a), free(rec.he.a), free(rec.hw.a), free(rec.owner.a);
     return rc;
 }
 
-int orc_prune_sssp(const char* dir) { return dir ? prune_dir(dir, 0, 0.0) : -1; }
+int orc_prune_sssp(const char* dir) { return dir ? prune_dir(dir, 0, 0.0, NULL) : -1; }
 
 /* keep = 1 - alpha of the push the pruned graph serves; 0.8 is the reference's */
-int orc_prune_ppr(const char* dir, double keep) { return dir ? prune_dir(dir, 1, keep) : -1; }
+int orc_prune_ppr(const char* dir, double keep) { return dir ? prune_dir(dir, 1, keep, NULL) : -1; }
+
+/* The pruner of kind ppr (0: purn-sssp, 1: purn-ppr with keep) with the dependency
+ * analysis above; its outputs are written as by orc_prune_sssp / orc_prune_ppr.  st[8]:
+ * pruning visits, visits that moved edges, visiting decisions, depth over all operations,
+ * depth over the pruning visits, the widest level's visits, and the visits that sit in
+ * levels of at least 32 and of at least 1024 visits. */
+int orc_prune_depth(const char* dir, int ppr, double keep, int64_t* st) {
+    if (!dir || !st) return -1;
+    depth_track d;
+    memset(&d, 0, sizeof(d));
+    const int rc = prune_dir(dir, ppr ? 1 : 0, keep, &d);
+    int64_t wmax = 0, w32 = 0, w1k = 0;
+    for (int64_t l = 0; l < d.width_cap; ++l) {
+        const int64_t w = d.width[l];
+        if (w > wmax) wmax = w;
+        if (w >= 32) w32 += w;
+        if (w >= 1024) w1k += w;
+    }
+    st[0] = d.visits, st[1] = d.removing, st[2] = d.decisions, st[3] = d.depth, st[4] = d.pdepth;
+    st[5] = wmax, st[6] = w32, st[7] = w1k;
+    free(d.width);
+    return rc;
+}

@@ -1,0 +1,63 @@
+"""Dependency depth of the pruners' visiting order (oracle/ingest.c orc_prune_depth).
+
+The pruners visit vertices in a fixed sequential order, and a visit reads and writes
+rows (out-rows of the vertex and its roots, in-rows of the targets it moves) that later
+visits read.  The analysis gives every visit the level one past the latest visit it
+depends on (read-after-write, write-after-read, write-after-write); the largest level is
+the fewest steps in which a parallel pruner that reproduces the sequential bytes could
+run.  These tests check that the analysis leaves the outputs unchanged and that its
+counts are consistent; the figures at scale 22 are quoted with the command that makes
+them in the design notes.
+"""
+import filecmp
+import os
+
+import pytest
+
+
+@pytest.mark.parametrize("kind", ["sssp", "ppr"])
+def test_prune_depth_outputs_and_counts(tmp_path, kind):
+    import oracle
+
+    a, b = str(tmp_path / "a"), str(tmp_path / "b")
+    for d in (a, b):
+        oracle.rmat_write(d, 14, 16, 5, 1, 1000)
+    st = oracle.prune_depth(a, kind, 0.15 if kind == "ppr" else None)
+    if kind == "ppr":
+        oracle.prune_ppr(b, 0.15)
+    else:
+        oracle.prune_sssp(b)
+    names = sorted(os.listdir(os.path.join(b, kind)))
+    assert names == sorted(os.listdir(os.path.join(a, kind)))
+    for f in names:  # the analysis does not change what the pruner writes
+        assert filecmp.cmp(os.path.join(a, kind, f), os.path.join(b, kind, f), shallow=False), f
+    assert 0 < st["removing"] <= st["visits"]
+    assert st["visit_depth"] <= st["depth"]
+    # a chain cannot be longer than the operations in it (visits plus decisions) ...
+    assert st["depth"] <= st["visits"] + st["decisions"]
+    # ... and the levels hold every visit once
+    assert st["widest"] <= st["visits"] and st["in_levels_ge1024"] <= st["in_levels_ge32"] <= st["visits"]
+    # the order is far from a single chain even at this scale
+    assert st["visits"] >= 8 * st["visit_depth"]
+
+
+def test_prune_depth_of_a_chain_is_sequential(tmp_path):
+    """A path 0 -> 1 -> ... -> n-1 pruned by purn-sssp.  Vertex 1's visit moves its edge
+    1 -> 2 into vertex 0's row, so vertex 2's only live root becomes 0, and so on: every
+    visit reads and rewrites row 0 after the one before it.  The visits form one chain,
+    which starts after vertex 0's own decision (it is not pruned) has read row 0."""
+    import numpy as np
+
+    import oracle
+
+    d = str(tmp_path / "chain")
+    n = 40
+    vl = np.concatenate([np.arange(n, dtype=np.int32), [n - 1]]).astype(np.int32)
+    el = np.arange(1, n, dtype=np.int32)
+    wl = np.arange(1, n, dtype=np.int32)
+    os.makedirs(os.path.join(d, "origin"))
+    for name, arr in (("vlist", vl), ("elist", el), ("wlist", wl)):
+        arr.tofile(os.path.join(d, "origin", name + ".bin"))
+    st = oracle.prune_depth(d, "sssp")
+    assert st["visits"] == n - 2  # vertices 1 .. n-2 have one root and an out-edge
+    assert st["removing"] == st["visits"] and st["visit_depth"] == st["visits"] + 1
