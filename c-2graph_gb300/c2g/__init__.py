@@ -113,6 +113,7 @@ SIGNATURES = {
                                ctypes.POINTER(Stats)]),
     "c2g_ppr_set_config": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int32]),
     "c2g_ppr_batch_set_pull": (ctypes.c_int, [_P, ctypes.c_float]),
+    "c2g_sssp_batch_set_pull": (ctypes.c_int, [_P, ctypes.c_float]),
     "c2g_ppr_batch_autotune": (ctypes.c_int, [_P, ctypes.c_int32, _P, ctypes.POINTER(PprParams), ctypes.c_int32,
                                               ctypes.c_char_p, _P]),
     "c2g_graph_set_watchdog": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int32]),
@@ -286,6 +287,11 @@ class Graph:
     def sssp_batch_tile(self, big_steps=512, min_tiles_per_warp=16):
         """Expansion tiles of the batched SSSP (see c2g_sssp_batch_set_tile)."""
         _check(lib().c2g_sssp_batch_set_tile(self._h, big_steps, min_tiles_per_warp))
+
+    def sssp_batch_pull(self, frac=0.5):
+        """Batched SSSP rounds with more than frac * E * words edge-word steps pull over the
+        reverse CSR (frac < 0: expand only; 0: every round)."""
+        _check(lib().c2g_sssp_batch_set_pull(self._h, float(frac)))
 
     def sssp_batch_autotune(self, sources, seeds=False, mode=SEEDS_COMPAT, reps=1, json_path=None):
         """Time the batched SSSP's tile candidates on this batch, apply the fastest valid

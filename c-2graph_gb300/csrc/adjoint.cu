@@ -102,6 +102,8 @@ __global__ void adjoint_grad_kernel(const int* __restrict__ row, const int2* __r
 // Reverse CSR of the float-weighted graph (in-edges carrying w(u,v)), built once.
 int build_reverse_graph(c2g_graph* g) {
     if (g->adj_r) return C2G_OK;
+    const int2* fwd = g->adj_f ? g->adj_f : g->adj_w;  // float weights when the graph has them
+    if (!fwd) return fail(C2G_ERR_UNSUPPORTED, "graph has no edge weights");
     const size_t V = (size_t)g->V, E = (size_t)g->E;
     int* indeg = nullptr;
     C2G_CUDA(cudaMalloc(&g->row_r, sizeof(int) * (V + 1)));
@@ -109,7 +111,7 @@ int build_reverse_graph(c2g_graph* g) {
     C2G_CUDA(cudaMalloc(&indeg, sizeof(int) * (V ? V : 1)));
     cudaError_t e = cudaMemsetAsync(indeg, 0, sizeof(int) * V, g->stream);
     if (e == cudaSuccess && E) {
-        count_in_kernel<<<g->num_sms * 4, 256, 0, g->stream>>>(g->adj_f, (long long)E, indeg);
+        count_in_kernel<<<g->num_sms * 4, 256, 0, g->stream>>>(fwd, (long long)E, indeg);
         e = cudaGetLastError();
     }
     std::vector<int> h(V + 1, 0);
@@ -120,7 +122,7 @@ int build_reverse_graph(c2g_graph* g) {
         e = cudaMemcpyAsync(g->row_r, h.data(), sizeof(int) * (V + 1), cudaMemcpyHostToDevice, g->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(indeg, h.data(), sizeof(int) * V, cudaMemcpyHostToDevice, g->stream);
     if (e == cudaSuccess && E) {
-        scatter_in_kernel<<<g->num_sms * 4, 256, 0, g->stream>>>(g->row, g->adj_f, g->V, indeg, g->adj_r);
+        scatter_in_kernel<<<g->num_sms * 4, 256, 0, g->stream>>>(g->row, fwd, g->V, indeg, g->adj_r);
         e = cudaGetLastError();
     }
     if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
@@ -131,7 +133,36 @@ int build_reverse_graph(c2g_graph* g) {
     return rc;
 }
 
+// The in-edges with int32 weights for the batched SSSP's pull rounds, in row_r's rows: adj_r
+// itself when the graph has no float weights, else a second scatter of adj_w (the order
+// within a row may differ from adj_r's; a minimum does not depend on it).
+int build_reverse_int(c2g_graph* g) {
+    if (g->adj_rw) return C2G_OK;
+    if (!g->adj_w) return fail(C2G_ERR_UNSUPPORTED, "graph has no int32 weights (wlist)");
+    int rc = build_reverse_graph(g);
+    if (rc) return rc;
+    if (!g->adj_f) {
+        g->adj_rw = g->adj_r;
+        return C2G_OK;
+    }
+    const size_t V = (size_t)g->V, E = (size_t)g->E;
+    int* cursor = nullptr;
+    C2G_CUDA(cudaMalloc(&g->adj_rw, sizeof(int2) * (E ? E : 1)));
+    C2G_CUDA(cudaMalloc(&cursor, sizeof(int) * (V ? V : 1)));
+    cudaError_t e = cudaMemcpyAsync(cursor, g->row_r, sizeof(int) * V, cudaMemcpyDeviceToDevice, g->stream);
+    if (e == cudaSuccess && E) {
+        scatter_in_kernel<<<g->num_sms * 4, 256, 0, g->stream>>>(g->row, g->adj_w, g->V, cursor, g->adj_rw);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+    cudaFree(cursor);
+    C2G_CUDA(e);
+    return C2G_OK;
+}
+
 void adjoint_free(c2g_graph* g) {
+    if (g->adj_rw && g->adj_rw != g->adj_r) cudaFree(g->adj_rw);
+    g->adj_rw = nullptr;
     void* ptrs[] = {g->row_r, g->adj_r, g->mark_r, g->mark_f};
     for (void* p : ptrs)
         if (p) cudaFree(p);

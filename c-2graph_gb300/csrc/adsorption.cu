@@ -236,6 +236,7 @@ extern "C" int c2g_adsorption(c2g_graph* g, int32_t n_labels, const int32_t* see
     if (!g || !seed_vertices || !p_inj || !p_cont || !Y_out) return fail(C2G_ERR_ARG, "NULL argument");
     if (n_labels != kAdsL) return fail(C2G_ERR_UNSUPPORTED, "adsorption supports %d labels per query", kAdsL);
     if (iterations < 0) return fail(C2G_ERR_ARG, "iterations must be >= 0");
+    if (!g->adj_f) return fail(C2G_ERR_UNSUPPORTED, "graph has no float weights (flist)");
     (void)p_abnd;  // the abandonment share goes to the unstored dummy label
     for (int32_t l = 0; l < n_labels; ++l)
         if (seed_vertices[l] < 0 || seed_vertices[l] >= g->V)

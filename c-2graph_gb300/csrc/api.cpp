@@ -217,6 +217,7 @@ int graph_view(c2g_graph* base, c2g_graph** out) {
     g->adj_f = base->adj_f;
     g->row_r = base->row_r;
     g->adj_r = base->adj_r;
+    g->adj_rw = base->adj_rw;
     g->mark_r = base->mark_r;
     g->mark_f = base->mark_f;
     g->R = base->R;
@@ -457,6 +458,14 @@ int c2g_ppr_batch_set_pull(c2g_graph* g, float ratio) {
     if (ratio != ratio) return fail(C2G_ERR_ARG, "ratio is NaN");
     std::lock_guard<std::mutex> lk(g->mu);
     g->ppr_cfg.batch_pull_ratio = ratio;
+    return C2G_OK;
+}
+
+int c2g_sssp_batch_set_pull(c2g_graph* g, float frac) {
+    if (!g) return fail(C2G_ERR_ARG, "graph is NULL");
+    if (frac != frac) return fail(C2G_ERR_ARG, "frac is NaN");
+    std::lock_guard<std::mutex> lk(g->mu);
+    g->sssp_cfg.batch_pull_frac = frac;
     return C2G_OK;
 }
 

@@ -57,6 +57,25 @@ struct BatchParams {
     int tile_min_log;     // a round walks big tiles when it has >= 2^tile_min_log of them per warp
     int epoch_rounds;     // > 0: an epoch of a resident batch (no initialisation; at most this many rounds)
     RoundTrace* trace;    // [kMaxTraceRounds + 1] per-round trace
+    // pull rounds: reverse CSR with int32 weights and its tile owners; a round pulls when its
+    // edge-word steps exceed pull_min (~0: never); amask[b] holds the frontier's lanes per
+    // (vertex, word) of the rounds of parity b (zero elsewhere)
+    const int* row_r;
+    const int2* adj_rw;
+    const int* mark_r;
+    unsigned ntiles_r;
+    unsigned long long pull_min;
+    unsigned* amask[2];
+};
+
+// A warp's chunk of up to 32 in-edges of a pull round (batched SSSP and PPR), staged in shared memory: source, weight bits and
+// the source's active lanes in the item's 4 query words.  Each lane loads one in-edge and
+// the live ones (a source with an active lane) are compacted into the chunk; the warp
+// then reads them one by one as broadcasts (two shared loads per in-edge instead of six
+// shuffles, and the chunk's values leave the registers of the gather loop).
+struct PullChunk {
+    int2 ed[32];
+    uint4 mk[32];
 };
 
 // Warp tiles of the expansion: markers are laid every 2^kBatchTileLog edge-word steps; a
@@ -105,8 +124,8 @@ __device__ __forceinline__ FrontierOut batch_out(const BatchParams& p, int buf, 
 // entry (v * W + w, edge base) carrying the mask.  Entries come out in sweep order per
 // warp.  Relaxations set masks with fire-and-forget red.or, so no relaxation waits on an
 // atomic's return; the sweep reads V * W words per round.
-__device__ __forceinline__ void batch_sweep(const BatchParams& p, const FrontierOut& out, WarpStage& fst,
-                                            unsigned gwarp, unsigned nwarps, int lane) {
+__device__ __forceinline__ void batch_sweep(const BatchParams& p, const FrontierOut& out, unsigned* am,
+                                            WarpStage& fst, unsigned gwarp, unsigned nwarps, int lane) {
     const unsigned nm = (unsigned)p.V << p.logW;
     for (unsigned b = gwarp * 32u; b < nm; b += nwarps * 32u) {
         const unsigned i = b + (unsigned)lane;
@@ -120,6 +139,7 @@ __device__ __forceinline__ void batch_sweep(const BatchParams& p, const Frontier
                 deg = __ldg(p.row + v + 1) - __ldg(p.row + v);
             }
         }
+        if (am && m != 0u && deg > 0) am[i] = m;  // the pull rounds' lookup of the frontier's lanes
         stage_push(fst, out, m != 0u && deg > 0, (int)i, deg, __int_as_float((int)m));
     }
     stage_flush(fst, out);
@@ -162,6 +182,129 @@ __device__ __forceinline__ void owner_items(unsigned cnt, unsigned len, int lane
     }
 }
 
+// Pull round of the batched SSSP.  In a dense round (most (vertex, word) pairs improved in
+// the previous round) the expansion reads a 128-byte distance line per edge-word step and
+// issues red.min for every improvement.  A pull round walks the reverse CSR instead: for
+// each target v and query word it takes the minimum of dist[u] + w over the in-edges
+// u -> v whose source improved in the previous round (amask), lane by lane (lane = query),
+// then compares it with dist[v]: a target whose in-edges lie in one tile gets plain
+// stores of its improved lanes and of its next-round mask word; a target whose in-edges
+// cross a tile boundary gets atomicMin / atomicOr.  Items are (tile of 2^kPullTileLog
+// in-edges, group of 4 query words), in word-group-major order; a warp stages each chunk's
+// live in-edges (a source with an active lane in the item's words) in shared memory, as
+// the PPR pull does, and gathers the source lines of two in-edges before it uses them.
+// Any order of relaxations reaches the same fixed point, so the distances are those of
+// the push rounds; pull and push rounds mix freely.
+__device__ __forceinline__ void sbatch_pull(const BatchParams& p, int buf, unsigned* qctr, PullChunk& pc,
+                                            unsigned long long& prelax, int lane, bool& bad) {
+    const unsigned W = 1u << p.logW;
+    const int lg = p.logW >= 2 ? p.logW - 2 : 0;  // word groups per tile
+    const unsigned nitems = p.ntiles_r << lg;
+    const unsigned* am = p.amask[buf];
+    const unsigned tw = 1u << kPullTileLog;
+    const unsigned Qu = (unsigned)p.Q;
+    unsigned itn = next_tile(qctr, lane);
+    for (unsigned it = itn; it < nitems; it = itn) {
+        itn = next_tile(qctr, lane);  // the next item, fetched while this one runs
+        const unsigned t = it % p.ntiles_r;
+        const unsigned w0 = (it / p.ntiles_r) * 4u;
+        const unsigned e0 = t << kPullTileLog;
+        const unsigned e1 = min(e0 + tw, p.E);
+        int v = __ldg(p.mark_r + t);  // owner of in-edge e0
+        unsigned vs = (unsigned)__ldg(p.row_r + v);
+        for (;;) {
+            const unsigned ve = (unsigned)__ldg(p.row_r + v + 1);
+            const unsigned ea = max(vs, e0), ez = min(ve, e1);
+            if (ea < ez) {  // warp-uniform: v has in-edges in this tile
+                int mn[4] = {INT_MAX, INT_MAX, INT_MAX, INT_MAX};  // this lane's query in each word
+                for (unsigned b = ea; b < ez; b += 32u) {
+                    const unsigned e = b + (unsigned)lane;
+                    int src = 0, wt = 0;
+                    unsigned mk[4] = {0u, 0u, 0u, 0u};
+                    if (e < ez) {
+                        const int2 ed = __ldg(p.adj_rw + e);
+                        if ((unsigned)ed.x >= (unsigned)p.V) {
+                            bad = true;
+                        } else {
+                            src = ed.x;
+                            wt = ed.y;
+                            const unsigned* ms = am + ((size_t)(unsigned)src << p.logW) + w0;
+                            if (W >= 4u) {  // four words, 16-byte aligned
+                                const uint4 m4 = ldcg(reinterpret_cast<const uint4*>(ms));
+                                mk[0] = m4.x;
+                                mk[1] = m4.y;
+                                mk[2] = m4.z;
+                                mk[3] = m4.w;
+                            } else {
+#pragma unroll
+                                for (int j = 0; j < 4; ++j)
+                                    if ((unsigned)j < W) mk[j] = ldcg(ms + j);
+                            }
+                        }
+                    }
+                    prelax += (unsigned long long)(__popc(mk[0]) + __popc(mk[1]) + __popc(mk[2]) + __popc(mk[3]));
+                    const bool live = (mk[0] | mk[1] | mk[2] | mk[3]) != 0u;
+                    const unsigned lm = __ballot_sync(kFull, live);
+                    const unsigned n = (unsigned)__popc(lm);
+                    __syncwarp();  // the previous chunk's reads are done
+                    if (live) {
+                        const unsigned at = (unsigned)__popc(lm & ((1u << lane) - 1u));
+                        pc.ed[at] = make_int2(src, wt);
+                        pc.mk[at] = make_uint4(mk[0], mk[1], mk[2], mk[3]);
+                    }
+                    __syncwarp();
+                    for (unsigned k0 = 0; k0 < n; k0 += 2u) {
+                        // the source lines of two in-edges, then their candidates
+                        int dv[2][4];
+                        int wk[2];
+#pragma unroll
+                        for (int h = 0; h < 2; ++h) {
+                            const unsigned k = k0 + h < n ? k0 + h : n - 1u;
+                            const int2 ek = pc.ed[k];
+                            const uint4 mq = pc.mk[k];
+                            wk[h] = ek.y;
+#pragma unroll
+                            for (int j = 0; j < 4; ++j) {
+                                const unsigned mj = j == 0 ? mq.x : j == 1 ? mq.y : j == 2 ? mq.z : mq.w;
+                                const bool on = k0 + h < n && ((mj >> lane) & 1u);
+                                // L2-coherent: other warps lower distances during the round
+                                dv[h][j] = on ? ldcg(p.dist + (size_t)(unsigned)ek.x * Qu + ((w0 + j) << 5) + lane)
+                                              : INT_MAX;
+                            }
+                        }
+#pragma unroll
+                        for (int h = 0; h < 2; ++h)
+#pragma unroll
+                            for (int j = 0; j < 4; ++j)
+                                if (dv[h][j] != INT_MAX) mn[j] = min(mn[j], dv[h][j] + wk[h]);
+                    }
+                }
+                const bool whole = vs >= e0 && ve <= e1;
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    if (w0 + j >= W) break;  // warp-uniform
+                    const size_t off = (size_t)(unsigned)v * Qu + ((w0 + j) << 5) + lane;
+                    const unsigned vw = ((unsigned)v << p.logW) + w0 + (unsigned)j;
+                    const bool imp = mn[j] != INT_MAX && mn[j] < ldcg(p.dist + off);
+                    const unsigned bits = __ballot_sync(kFull, imp);
+                    if (bits) {
+                        if (whole) {  // this warp holds all of v's in-edges: no other writer
+                            if (imp) p.dist[off] = mn[j];
+                            if (lane == 0) p.mask[vw] = bits;
+                        } else {
+                            if (imp) atomicMin(p.dist + off, mn[j]);
+                            if (lane == 0) atomicOr(p.mask + vw, bits);
+                        }
+                    }
+                }
+            }
+            if (ve >= e1) break;
+            ++v;
+            vs = ve;
+        }
+    }
+}
+
 __global__ void __launch_bounds__(kSsspBatchThreads, 3) sssp_batch_persistent(const BatchParams p) {
     TraversalCtl* ctl = p.ctl;
     GridBarrier* bar = reinterpret_cast<GridBarrier*>(&ctl->bar_count);
@@ -177,6 +320,10 @@ __global__ void __launch_bounds__(kSsspBatchThreads, 3) sssp_batch_persistent(co
     unsigned long long tph = globaltimer_ns();
     WarpStage fst{sm.v0[wib], sm.d0[wib], sm.x0[wib], 0};
     int* qtab = sm.v1[wib];  // slot -> query position table of the owner being expanded
+    __shared__ PullChunk pcs[kSsspBatchThreads / 32];  // pull rounds' in-edge chunks
+    const bool pulls = p.pull_min != ~0ull;
+    unsigned long long prelax = 0;  // relaxations of the pull rounds, counted by every lane
+    bool bad_in = false;
 
     // An epoch of a resident batch starts from the state the previous epoch left: the
     // distances and the improvement masks (queries that joined since have their column
@@ -221,12 +368,13 @@ __global__ void __launch_bounds__(kSsspBatchThreads, 3) sssp_batch_persistent(co
             ctl->qctr[(cur + 1) % 3] = 0ull;
             ctl->tilectr[(cur + 1) % 3] = 0u;
         }
-        batch_sweep(p, batch_out(p, buf, slot), fst, gwarp, nwarps, lane);
+        batch_sweep(p, batch_out(p, buf, slot), pulls ? p.amask[buf] : nullptr, fst, gwarp, nwarps, lane);
         if (!grid_sync(bar, flags, p.barrier_ns)) return;
         phase_mark(ctl->phase_ns, tph, 1);
         const unsigned long long c = ldcg(&ctl->qctr[slot]);
         const unsigned F = (unsigned)(c >> 32), T = (unsigned)c;
-        if (gtid == 0) trace_round(p.trace, iters, (long long)T, 0);
+        const bool pull = (unsigned long long)T > p.pull_min;  // grid-uniform
+        if (gtid == 0) trace_round(p.trace, iters, (long long)T, pull ? 1 : 0);
         if (F == 0) break;
         if (++iters > p.max_iter) {
             if (gtid == 0) atomicOr(flags, C2G_FLAG_ITER_CAP);
@@ -241,6 +389,16 @@ __global__ void __launch_bounds__(kSsspBatchThreads, 3) sssp_batch_persistent(co
             ctl->relaxed += T;
         }
 
+        if (pulls) {
+            // The previous round's frontier leaves the pull lookup (the lookup of this round,
+            // amask[buf], is the one a pull reads; the next round writes amask[buf ^ 1]).
+            const unsigned Fp = min((unsigned)(ldcg(&ctl->qctr[(cur + 2) % 3]) >> 32), p.qcap);
+            for (unsigned j = gtid; j < Fp; j += nthreads) p.amask[buf ^ 1][ldcg(p.q[buf ^ 1] + j).x] = 0u;
+        }
+        if (pull) {
+            if (gtid == 0) steps += T;
+            sbatch_pull(p, buf, &ctl->tilectr[slot], pcs[wib], prelax, lane, bad_in);
+        } else {
         // Phase 2: expand.  Warps take tiles of edge-word steps and walk owner runs: the
         // owner's row of distances is read once; its edges are read 32 at a time (one per
         // lane, coalesced) and broadcast by shuffles; each edge costs one 128-byte read of
@@ -336,6 +494,7 @@ __global__ void __launch_bounds__(kSsspBatchThreads, 3) sssp_batch_persistent(co
                 o += 32;
             }
         }
+        }
         if (!grid_sync(bar, flags, p.barrier_ns)) return;
         phase_mark(ctl->phase_ns, tph, 2);
         if (gtid == 0) trace_mid(p.trace, iters - 1);
@@ -343,9 +502,11 @@ __global__ void __launch_bounds__(kSsspBatchThreads, 3) sssp_batch_persistent(co
         // end of an epoch: the next round's improvements wait in the masks
         if (p.epoch_rounds > 0 && iters >= p.epoch_rounds) break;
     }
-    // relax is counted by lane 0 of each warp
+    if (bad_in) atomicOr(flags, C2G_FLAG_BOUNDS);
+    // relax is counted by lane 0 of each warp, prelax by every lane
+    for (int o = 16; o >= 1; o >>= 1) prelax += __shfl_xor_sync(kFull, prelax, o);
     if (lane == 0) {
-        atomicAdd((unsigned long long*)&p.counters[0], (unsigned long long)relax);
+        atomicAdd((unsigned long long*)&p.counters[0], (unsigned long long)relax + prelax);
         atomicAdd((unsigned long long*)&p.counters[1], (unsigned long long)steps);
     }
     if (gtid == 0) {
@@ -433,6 +594,7 @@ struct BatchWork {
     int* seed_w = nullptr;
     int* stage = nullptr;  // caller-layout copy for host output
     RoundTrace* trace = nullptr;
+    unsigned* amask[2] = {nullptr, nullptr};  // pull rounds' lookups of the frontier's lanes
     size_t seed_cap = 0;
     int Q = 0;
     int V = 0;
@@ -441,7 +603,8 @@ struct BatchWork {
 static void batch_free_work(BatchWork* w) {
     if (!w) return;
     void* ptrs[] = {w->dist, w->mask, w->q[0], w->q[1], w->qmask[0], w->qmask[1], w->mark[0], w->mark[1],
-                    w->ctl, w->counters, w->src, w->seed_off, w->seed_v, w->seed_w, w->stage, w->trace};
+                    w->ctl, w->counters, w->src, w->seed_off, w->seed_v, w->seed_w, w->stage, w->trace,
+                    w->amask[0], w->amask[1]};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     delete w;
@@ -479,8 +642,32 @@ static int batch_alloc(c2g_graph* g, int Q, size_t n_seeds) {
     C2G_CUDA(cudaMalloc(&w->seed_v, sizeof(int) * w->seed_cap));
     C2G_CUDA(cudaMalloc(&w->seed_w, sizeof(int) * w->seed_cap));
     C2G_CUDA(cudaMalloc(&w->trace, sizeof(RoundTrace) * (kMaxTraceRounds + 1)));
+    for (int b = 0; b < 2; ++b) C2G_CUDA(cudaMalloc(&w->amask[b], sizeof(unsigned) * qcap));
     w->Q = Q;
     w->V = g->V;
+    return C2G_OK;
+}
+
+// The pull rounds of a batched SSSP launch (p.pull_min: edge-word steps above which a
+// round pulls, ~0: never): they need the reverse CSR with int32 weights (a view uses its
+// base's, never builds it), whose arrays are set into p here, after they exist.  The pull
+// lookups start clear; a launch leaves the entries of its last rounds behind.
+static int sssp_pull_setup(c2g_graph* g, BatchWork* w, int Q, BatchParams& p) {
+    p.pull_min = ~0ull;
+    const float frac = g->sssp_cfg.batch_pull_frac;
+    if (!(frac >= 0.f) || g->E == 0) return C2G_OK;
+    if (!g->adj_rw) {
+        if (g->borrowed) return C2G_OK;
+        int rc = build_reverse_int(g);
+        if (rc) return rc;
+    }
+    if (!g->row_r || !g->adj_rw || !g->mark_r) return C2G_OK;
+    p.row_r = g->row_r;
+    p.adj_rw = g->adj_rw;
+    p.mark_r = g->mark_r;
+    for (int b = 0; b < 2; ++b)
+        C2G_CUDA(cudaMemsetAsync(w->amask[b], 0, sizeof(unsigned) * (size_t)g->V * (size_t)(Q / 32), g->stream));
+    p.pull_min = (unsigned long long)((double)frac * (double)g->E * (double)(Q / 32));
     return C2G_OK;
 }
 
@@ -514,6 +701,13 @@ static void sssp_batch_params(c2g_graph* g, BatchWork* w, int Q, int logW, Batch
     p.epoch_rounds = 0;
     p.trace = w->trace;
     g->last_trace = w->trace;
+    p.row_r = nullptr;  // set by sssp_pull_setup when the launch may pull
+    p.adj_rw = nullptr;
+    p.mark_r = nullptr;
+    p.ntiles_r = (unsigned)(((size_t)g->E + (1u << kPullTileLog) - 1) >> kPullTileLog);
+    p.pull_min = ~0ull;
+    p.amask[0] = w->amask[0];
+    p.amask[1] = w->amask[1];
 }
 
 static int sssp_batch_results(c2g_graph* g, BatchWork* w, int Q, int32_t nq, int32_t* out, int out_on_device,
@@ -574,6 +768,7 @@ int sssp_batch_launch(c2g_graph* g, int32_t nq, const int32_t* sources, const st
     }
     BatchParams p;
     sssp_batch_params(g, w, Q, logW, p);
+    if ((rc = sssp_pull_setup(g, w, Q, p))) return rc;
     p.nq = nq;
     p.seed_off = seed_off ? w->seed_off : nullptr;
     C2G_CUDA(cudaMemsetAsync(w->ctl, 0, sizeof(TraversalCtl), g->stream));
@@ -613,6 +808,8 @@ int sssp_batch_epoch(c2g_graph* g, int Q, int rounds, float* ms, long long* coun
     if (per_sm < 1) return fail(C2G_ERR_CUDA, "batch kernel cannot be resident");
     BatchParams p;
     sssp_batch_params(g, w, Q, logW, p);
+    int rc;
+    if ((rc = sssp_pull_setup(g, w, Q, p))) return rc;
     p.epoch_rounds = rounds < 1 ? 1 : rounds;
     C2G_CUDA(cudaMemsetAsync(w->ctl, 0, sizeof(TraversalCtl), g->stream));
     C2G_CUDA(cudaMemsetAsync(w->counters, 0, sizeof(long long) * 2, g->stream));
@@ -908,16 +1105,6 @@ __device__ __forceinline__ unsigned pbatch_pull_owner(const PprBatchParams& p, i
     }
     return cnt;
 }
-
-// A warp's chunk of up to 32 in-edges, staged in shared memory: source, weight bits and
-// the source's active lanes in the item's 4 query words.  Each lane loads one in-edge and
-// the live ones (a source with an active lane) are compacted into the chunk; the warp
-// then reads them one by one as broadcasts (two shared loads per in-edge instead of six
-// shuffles, and the chunk's values leave the registers of the gather loop).
-struct PullChunk {
-    int2 ed[32];
-    uint4 mk[32];
-};
 
 // Phase A of a pull round.  A warp takes (tile, word group) items from the round's queue
 // and walks the tile's owners one by one: for each owner, its in-edges in the tile in

@@ -103,6 +103,8 @@ struct SsspConfig {
     int max_iter = 1 << 20;
     int batch_tile_big_log = 9;  // batched expansion: 512 edge-word steps per big tile
     int batch_tile_min_log = 4;  // ... in rounds with at least 16 big tiles per warp
+    float batch_pull_frac = 0.5f;  // batched rounds with more edge-word steps than this * E * words
+                                   // pull over the reverse CSR (< 0: never)
 };
 
 struct PprConfig {
@@ -131,6 +133,8 @@ struct c2g_graph {
     int2* adj_f = nullptr;
     int32_t* row_r = nullptr;  // reverse CSR with float weights (pull rounds, adjoint), on demand
     int2* adj_r = nullptr;
+    int2* adj_rw = nullptr;     // the same in-edges with int32 weights (batched SSSP pull rounds), on
+                                // demand; adj_r itself when the graph has no float weights
     int32_t* mark_r = nullptr;  // pull-tile owner markers over row_r
     int32_t* mark_f = nullptr;  // pull-tile owner markers over row (pulls on the reverse graph)
     // pruned records
@@ -191,6 +195,8 @@ void batch_free(c2g_graph* g);
 void ppr_batch_free(c2g_graph* g);
 void ads_free(c2g_graph* g);
 int build_reverse_graph(c2g_graph* g);
+// The reverse CSR's in-edges with int32 weights (batched SSSP pull rounds).
+int build_reverse_int(c2g_graph* g);
 // Reverse CSR and the weight statistics of the batched pull rounds (once per weights).
 int ppr_pull_prepare(c2g_graph* g);
 int ppr_batch_launch(c2g_graph* g, int32_t nq, const int32_t* sources, const c2g_ppr_params& prm,

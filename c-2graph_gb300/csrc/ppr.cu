@@ -604,6 +604,7 @@ int ppr_launch(c2g_graph* g, int32_t source, const c2g_ppr_params& pp, const int
     const int32_t* row_r = nullptr;
     const int2* adj_r = nullptr;
     const int32_t* mark_r = nullptr;
+    if (!g->adj_f) return fail(C2G_ERR_UNSUPPORTED, "graph has no float weights (flist)");
     if (g->ppr_cfg.pull_div > 0) {
         int rc = build_reverse_graph(g);
         if (rc) return rc;

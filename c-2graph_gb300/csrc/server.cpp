@@ -282,17 +282,20 @@ int c2g_server_create(c2g_graph* g, const float* p_inj, const float* p_cont, con
     {
         std::lock_guard<std::mutex> lk(g->mu);
         if (g->adj_f) rc = ppr_pull_prepare(g);
+        // the batched SSSP's pull rounds: the views share the base's reverse CSR
+        if (!rc && g->adj_w && g->sssp_cfg.batch_pull_frac >= 0.f) rc = build_reverse_int(g);
     }
     for (int k = 0; k < 3 && !rc; ++k) {
         rc = graph_view(g, &s->views[k]);
         if (!rc) s->views[k]->grid_scale = 1.0f / 3.0f;
     }
     // Per-query device state (bytes) and the admission budget.  Per (vertex, query): SSSP
-    // distance 4 B plus 20 B per 32 queries (mask, two frontier entries and masks); PPR
+    // distance 4 B plus 28 B per 32 queries (mask, two frontier entries and masks, two pull
+    // lookups); PPR
     // pr 4, res 8, msg 8, two pushed residuals 16 and their float pairs 16, plus 32 B per
     // 32 queries of masks and frontier entries; adsorption 16 labels x (Y, accumulator,
     // host stage).
-    s->bytes_per_query[C2G_REQ_SSSP] = (int64_t)V * 4 + (int64_t)V * 20 / 32;
+    s->bytes_per_query[C2G_REQ_SSSP] = (int64_t)V * 4 + (int64_t)V * 28 / 32;
     s->bytes_per_query[C2G_REQ_PPR] = (int64_t)V * 52 + (int64_t)V * 32 / 32;
     s->bytes_per_query[C2G_REQ_ADSORPTION] = (int64_t)V * 16 * 4 * 3;
     size_t free_b = 0, total_b = 0;

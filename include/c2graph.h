@@ -215,6 +215,14 @@ int c2g_sssp_batch(c2g_graph* g, int32_t n, const int32_t* sources, int use_seed
 int c2g_sssp_batch_set_tile(c2g_graph* g, int32_t big_steps, int32_t min_tiles_per_warp);
 int c2g_sssp_batch_get_tile(const c2g_graph* g, int32_t* big_steps, int32_t* min_tiles_per_warp);
 
+/* Round shape of the batched SSSP (c2g_sssp_batch and resident SSSP batches; no
+ * counterpart in the reference): a round whose frontier has more than frac * E * words
+ * edge-word steps (words = query slots / 32) pulls over the reverse CSR with int32
+ * weights (built on first use): each target takes the minimum over its in-edges from
+ * sources that improved in the previous round.  frac < 0: expand (push) only; 0: pull
+ * every round; default 0.5.  Distances do not depend on the setting. */
+int c2g_sssp_batch_set_pull(c2g_graph* g, float frac);
+
 /* Autotuner of those tiles (no counterpart in the reference): times 128-step tiles and
  * big_steps {256, 512, 1024, 2048} x min_tiles_per_warp {4, 16, 64} on this batch (one
  * warm-up launch, then `reps` timed), rejects any candidate whose distances differ from

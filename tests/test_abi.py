@@ -59,6 +59,7 @@ def test_bad_variant_and_args(built, tmp_path):
     assert c2g.lib().c2g_rmat_write(b"/tmp/x", 0, 8, 1, 1, 10, 0.57, 0.19, 0.19) == c2g.ERR_ARG
     # batched-query tuning entry points: a NULL handle or batch is a status, never a crash
     assert c2g.lib().c2g_ppr_batch_set_pull(None, 8.0) == c2g.ERR_ARG
+    assert c2g.lib().c2g_sssp_batch_set_pull(None, 0.5) == c2g.ERR_ARG
     src = np.zeros(4, dtype=np.int32)
     prm = c2g.PprParams()
     assert c2g.lib().c2g_ppr_batch_autotune(None, 4, c2g._ptr(src), ctypes.byref(prm), 1, None, None) == c2g.ERR_ARG

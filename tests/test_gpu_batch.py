@@ -50,6 +50,36 @@ def test_batch_vs_dijkstra(gpu_available, g17w, n):
             assert np.array_equal(dist[i], ref), (n, i, s)
 
 
+@pytest.mark.parametrize("frac", [-1.0, 0.0, 0.5])
+def test_sssp_batch_pull_shapes_vs_dijkstra(gpu_available, g17w, g16, frac):
+    """Expand-only rounds, pull rounds in every round and the default mix give the exact
+    distances: 1, 2, 4 and 8 query words on origin/ (float and int weights, so the pull's
+    int32 in-edges are a second scatter), and EXACT-seeded queries on the pruned sssp/
+    (int weights only: the pull uses the one reverse CSR) against the single query."""
+    import c2g
+    import oracle
+
+    o = oracle.load_dataset(g17w, "origin")
+    with c2g.Graph.load(g17w, "origin") as gr:
+        gr.sssp_batch_pull(frac)
+        for n in (20, 50, 100, 256):
+            src = _sources(o["vlist"], n, 40 + n)
+            dist, st = gr.sssp_batch(src)
+            assert st.status_flags == 0
+            for i in range(0, n, max(1, n // 16)):  # a sample of the queries
+                ref = oracle.dijkstra(o["vlist"], o["elist"], o["wlist"], [int(src[i])], [0])
+                assert np.array_equal(dist[i], ref), (frac, n, i)
+    with c2g.Graph.load(g16, "sssp") as gr:
+        gr.sssp_batch_pull(frac)
+        vl = np.fromfile(g16 + "/sssp/vlist.bin", dtype=np.int32)
+        src = _sources(vl, 96, 7)
+        dist, st = gr.sssp_batch(src, seeds=True, mode=c2g.SEEDS_EXACT)
+        assert st.status_flags == 0
+        for i in range(0, 96, 6):
+            ref, _ = gr.sssp(int(src[i]), seeds=True, mode=c2g.SEEDS_EXACT)
+            assert np.array_equal(dist[i], ref), (frac, i)
+
+
 def test_batch_tiles_and_autotune(gpu_available, g17w, tmp_path):
     """Every tile shape gives the same distances (Dijkstra); the autotuner times its 13
     candidates, keeps a valid one and applies it."""
@@ -364,12 +394,16 @@ def test_batch_round_trace(gpu_available, g17w, g14p):
 
     with c2g.Graph.load(g17w, "origin") as gr:
         src = _sources(np.fromfile(g17w + "/origin/vlist.bin", dtype=np.int32), 64, 4)
-        _, st = gr.sssp_batch(src)
-        ms, work, shape = gr.last_rounds()
-        assert len(ms) == st.iterations and len(ms) > 3
-        assert int(work.sum()) == st.touched  # edge-word steps
-        assert np.all(shape == 0) and np.all(ms > 0)
-        assert 0.5 * st.device_ms <= ms.sum() <= st.device_ms * 1.01
+        for frac, want in ((-1.0, 0), (0.0, 1), (0.5, None)):
+            gr.sssp_batch_pull(frac)
+            _, st = gr.sssp_batch(src)
+            ms, work, shape = gr.last_rounds()
+            assert len(ms) == st.iterations and len(ms) > 3
+            assert int(work.sum()) == st.touched  # edge-word steps
+            if want is not None:  # expand only / pull every round
+                assert np.all(shape == want), frac
+            assert np.all(ms > 0)
+            assert 0.5 * st.device_ms <= ms.sum() <= st.device_ms * 1.01
     with c2g.Graph.load(g14p, "origin") as gr:
         vl = np.fromfile(g14p + "/origin/vlist.bin", dtype=np.int32)
         src = _sources(vl, 64, 6)
