@@ -258,7 +258,10 @@ def run_ours(args, rank, world, local_rank):
     pull_ratio = gp.ppr_batch_autotune(psrc, prm, reps=1)
     big, mn = gs.sssp_batch_autotune(ssrc, seeds=True, mode=c2g.SEEDS_EXACT, reps=1)
     sssp_tile = {"big_steps": big, "min_tiles_per_warp": mn,
-                 "rule": "rounds with >= min_tiles_per_warp big tiles per warp walk big tiles, else 128 steps"}
+                 "rule": "rounds with >= min_tiles_per_warp big tiles per warp walk big tiles, else 128 steps",
+                 "pull_frac": gs.sssp_batch_pull_frac(),
+                 "pull_rule": "rounds with more than pull_frac * E * Q (query, edge) relaxations pull over the "
+                              "reverse CSR"}
     dist_d = torch.empty((nS, V), dtype=torch.int32, device=dev)
     pr_d = torch.empty((nP, V), dtype=torch.float32, device=dev)
     dist_h = torch.empty((nS, V), dtype=torch.int32).pin_memory().numpy()

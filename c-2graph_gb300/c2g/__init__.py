@@ -114,6 +114,7 @@ SIGNATURES = {
     "c2g_ppr_set_config": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int32]),
     "c2g_ppr_batch_set_pull": (ctypes.c_int, [_P, ctypes.c_float]),
     "c2g_sssp_batch_set_pull": (ctypes.c_int, [_P, ctypes.c_float]),
+    "c2g_sssp_batch_get_pull": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_float)]),
     "c2g_ppr_batch_autotune": (ctypes.c_int, [_P, ctypes.c_int32, _P, ctypes.POINTER(PprParams), ctypes.c_int32,
                                               ctypes.c_char_p, _P]),
     "c2g_graph_set_watchdog": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int32]),
@@ -289,9 +290,15 @@ class Graph:
         _check(lib().c2g_sssp_batch_set_tile(self._h, big_steps, min_tiles_per_warp))
 
     def sssp_batch_pull(self, frac=0.5):
-        """Batched SSSP rounds with more than frac * E * words edge-word steps pull over the
-        reverse CSR (frac < 0: expand only; 0: every round)."""
+        """Batched SSSP rounds with more than frac * E * Q (query, edge) relaxations pull over
+        the reverse CSR (Q: query slots; frac < 0: expand only; 0: every round)."""
         _check(lib().c2g_sssp_batch_set_pull(self._h, float(frac)))
+
+    def sssp_batch_pull_frac(self):
+        """The batched SSSP's current pull fraction (c2g_sssp_batch_get_pull)."""
+        f = ctypes.c_float()
+        _check(lib().c2g_sssp_batch_get_pull(self._h, ctypes.byref(f)))
+        return f.value
 
     def sssp_batch_autotune(self, sources, seeds=False, mode=SEEDS_COMPAT, reps=1, json_path=None):
         """Time the batched SSSP's tile candidates on this batch, apply the fastest valid

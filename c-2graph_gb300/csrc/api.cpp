@@ -469,6 +469,12 @@ int c2g_sssp_batch_set_pull(c2g_graph* g, float frac) {
     return C2G_OK;
 }
 
+int c2g_sssp_batch_get_pull(const c2g_graph* g, float* frac) {
+    if (!g || !frac) return fail(C2G_ERR_ARG, "NULL argument");
+    *frac = g->sssp_cfg.batch_pull_frac;
+    return C2G_OK;
+}
+
 static int log2_exact(int32_t x) {
     int l = 0;
     while (l < 31 && (1 << l) < x) ++l;

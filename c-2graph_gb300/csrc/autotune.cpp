@@ -76,15 +76,18 @@ extern "C" int c2g_sssp_autotune(c2g_graph* g, int32_t n, const int32_t* sources
     return C2G_OK;
 }
 
-// Autotuner of the batched SSSP's expansion tiles (c2g_sssp_batch_set_tile): the size of
-// the big tiles and the per-warp tile count above which a round walks them.  Big tiles cut
-// the tile-queue traffic and the owner lookups of long rounds; small ones balance the
-// short rounds.  Which split is best depends on the batch (queries, graph, weights), so
-// c2g_sssp_batch_autotune times each candidate on the caller's batch (one warm-up launch,
-// then `reps` timed ones; the batch kernel's device time).  A candidate whose distances
-// differ from the first candidate's on any of the first 8 queries is rejected (every
-// candidate must reach the same fixed point).  The winner is applied to the handle and,
-// when a path is given, written as a JSON record of every timing.
+// Autotuner of the batched SSSP's expansion tiles (c2g_sssp_batch_set_tile) and round
+// shape (c2g_sssp_batch_set_pull): the size of the big tiles and the per-warp tile count
+// above which a round walks them, then, at the chosen tiles, the relaxation share above
+// which a round pulls over the reverse CSR.  Big tiles cut the tile-queue traffic and the
+// owner lookups of long rounds; small ones balance the short rounds; pull rounds pay in
+// the rounds where most queries of most active words are active.  Which settings are best
+// depends on the batch (queries, graph, weights), so c2g_sssp_batch_autotune times each
+// candidate on the caller's batch (one warm-up launch, then `reps` timed ones; the batch
+// kernel's device time).  A candidate whose distances differ from the first candidate's
+// on any of the first 8 queries is rejected (every candidate must reach the same fixed
+// point).  The winners are applied to the handle and, when a path is given, written as a
+// JSON record of every timing.
 extern "C" int c2g_sssp_batch_autotune(c2g_graph* g, int32_t n, const int32_t* sources, int use_seeds,
                                        int seed_mode, int32_t reps, const char* json_path, int32_t* best_big_steps,
                                        int32_t* best_min_tiles) {
@@ -93,10 +96,15 @@ extern "C" int c2g_sssp_batch_autotune(c2g_graph* g, int32_t n, const int32_t* s
     if (reps < 1) reps = 1;
     struct Cand {
         int big, min;
+        float frac;
     };
-    std::vector<Cand> cands = {{128, 1}};
+    int32_t saved_big = 512, saved_min = 16;
+    c2g_sssp_batch_get_tile(g, &saved_big, &saved_min);
+    float saved_frac = 0.3f;
+    c2g_sssp_batch_get_pull(g, &saved_frac);
+    std::vector<Cand> tiles = {{128, 1, saved_frac}};
     for (int big : {256, 512, 1024, 2048})
-        for (int mn : {4, 16, 64}) cands.push_back({big, mn});
+        for (int mn : {4, 16, 64}) tiles.push_back({big, mn, saved_frac});
     const size_t V = (size_t)g->V, rows = (size_t)(n < 8 ? n : 8);
     int32_t* dd = nullptr;
     {
@@ -108,50 +116,66 @@ extern "C" int c2g_sssp_batch_autotune(c2g_graph* g, int32_t n, const int32_t* s
         if (e != cudaSuccess) return fail(C2G_ERR_CUDA, "autotune: %s", cudaGetErrorString(e));
     }
     std::vector<int32_t> ref(rows * V), got(rows * V);
-    int32_t saved_big = 512, saved_min = 16;
-    c2g_sssp_batch_get_tile(g, &saved_big, &saved_min);
     double best_ms = 1e300;
-    Cand best{saved_big, saved_min};
+    Cand best{saved_big, saved_min, saved_frac};
     std::string json = "{\"candidates\": [";
     int rc = C2G_OK;
     bool first = true;
-    for (const Cand& c : cands) {
-        if ((rc = c2g_sssp_batch_set_tile(g, c.big, c.min))) break;
+    // one candidate: applied, timed and checked; the fastest valid one becomes `best`
+    auto run = [&](const Cand& c) {
+        if ((rc = c2g_sssp_batch_set_tile(g, c.big, c.min)) || (rc = c2g_sssp_batch_set_pull(g, c.frac))) return;
         c2g_stats st;
         double ms = 0.0;
         for (int k = 0; k <= reps && !rc; ++k) {
             rc = c2g_sssp_batch(g, n, sources, use_seeds, seed_mode, dd, 1, C2G_LAYOUT_QUERY_MAJOR, &st);
             if (k > 0) ms += st.device_ms;
         }
-        if (rc) break;
+        if (rc) return;
         ms /= reps;
         int32_t* dst = first ? ref.data() : got.data();
         if (cudaMemcpy(dst, dd, sizeof(int32_t) * rows * V, cudaMemcpyDeviceToHost) != cudaSuccess) {
             rc = fail(C2G_ERR_CUDA, "autotune: copying results failed");
-            break;
+            return;
         }
         const bool same = first || std::memcmp(got.data(), ref.data(), sizeof(int32_t) * rows * V) == 0;
         const bool valid = same && st.status_flags == 0;
-        char buf[192];
-        snprintf(buf, sizeof(buf), "%s{\"big_steps\": %d, \"min_tiles_per_warp\": %d, \"ms_per_batch\": %.3f, "
-                 "\"valid\": %s}", first ? "" : ", ", c.big, c.min, ms, valid ? "true" : "false");
+        char buf[224];
+        snprintf(buf, sizeof(buf),
+                 "%s{\"big_steps\": %d, \"min_tiles_per_warp\": %d, \"pull_frac\": %g, \"ms_per_batch\": %.3f, "
+                 "\"valid\": %s}",
+                 first ? "" : ", ", c.big, c.min, (double)c.frac, ms, valid ? "true" : "false");
         json += buf;
         if (valid && ms < best_ms) {
             best_ms = ms;
             best = c;
         }
         first = false;
+    };
+    for (const Cand& c : tiles) {
+        run(c);
+        if (rc) break;
+    }
+    if (!rc) {  // the round shape at the chosen tiles
+        const Cand tiled = best;
+        for (float f : {-1.f, 0.15f, 0.3f, 0.5f, 0.75f}) {
+            if (f == tiled.frac) continue;  // timed with the tiles
+            run({tiled.big, tiled.min, f});
+            if (rc) break;
+        }
     }
     cudaFree(dd);
     if (rc) {
         c2g_sssp_batch_set_tile(g, saved_big, saved_min);
+        c2g_sssp_batch_set_pull(g, saved_frac);
         return rc;
     }
-    char tail[160];
-    snprintf(tail, sizeof(tail), "], \"best\": {\"big_steps\": %d, \"min_tiles_per_warp\": %d, \"ms_per_batch\": %.3f}}\n",
-             best.big, best.min, best_ms);
+    char tail[192];
+    snprintf(tail, sizeof(tail),
+             "], \"best\": {\"big_steps\": %d, \"min_tiles_per_warp\": %d, \"pull_frac\": %g, \"ms_per_batch\": %.3f}}\n",
+             best.big, best.min, (double)best.frac, best_ms);
     json += tail;
-    if ((rc = c2g_sssp_batch_set_tile(g, best.big, best.min))) return rc;
+    if ((rc = c2g_sssp_batch_set_tile(g, best.big, best.min)) || (rc = c2g_sssp_batch_set_pull(g, best.frac)))
+        return rc;
     if (json_path) {
         FILE* f = fopen(json_path, "w");
         if (!f) return fail(C2G_ERR_IO, "cannot write %s", json_path);

@@ -58,7 +58,7 @@ struct BatchParams {
     int epoch_rounds;     // > 0: an epoch of a resident batch (no initialisation; at most this many rounds)
     RoundTrace* trace;    // [kMaxTraceRounds + 1] per-round trace
     // pull rounds: reverse CSR with int32 weights and its tile owners; a round pulls when its
-    // edge-word steps exceed pull_min (~0: never); amask[b] holds the frontier's lanes per
+    // (query, edge) relaxations exceed pull_min (~0: never); amask[b] holds the frontier's lanes per
     // (vertex, word) of the rounds of parity b (zero elsewhere)
     const int* row_r;
     const int2* adj_rw;
@@ -125,8 +125,10 @@ __device__ __forceinline__ FrontierOut batch_out(const BatchParams& p, int buf, 
 // warp.  Relaxations set masks with fire-and-forget red.or, so no relaxation waits on an
 // atomic's return; the sweep reads V * W words per round.
 __device__ __forceinline__ void batch_sweep(const BatchParams& p, const FrontierOut& out, unsigned* am,
-                                            WarpStage& fst, unsigned gwarp, unsigned nwarps, int lane) {
+                                            unsigned long long* pcount, WarpStage& fst, unsigned gwarp,
+                                            unsigned nwarps, int lane) {
     const unsigned nm = (unsigned)p.V << p.logW;
+    unsigned long long rel = 0;  // (query, edge) relaxations of the frontier
     for (unsigned b = gwarp * 32u; b < nm; b += nwarps * 32u) {
         const unsigned i = b + (unsigned)lane;
         unsigned m = 0u;
@@ -139,10 +141,17 @@ __device__ __forceinline__ void batch_sweep(const BatchParams& p, const Frontier
                 deg = __ldg(p.row + v + 1) - __ldg(p.row + v);
             }
         }
-        if (am && m != 0u && deg > 0) am[i] = m;  // the pull rounds' lookup of the frontier's lanes
+        if (am && m != 0u && deg > 0) {
+            am[i] = m;  // the pull rounds' lookup of the frontier's lanes
+            rel += (unsigned long long)__popc(m) * (unsigned long long)deg;
+        }
         stage_push(fst, out, m != 0u && deg > 0, (int)i, deg, __int_as_float((int)m));
     }
     stage_flush(fst, out);
+    if (am) {
+        for (int o = 16; o >= 1; o >>= 1) rel += __shfl_xor_sync(kFull, rel, o);
+        if (lane == 0 && rel) atomicAdd(pcount, rel);
+    }
 }
 
 constexpr int kBatchUnroll = 4;  // relaxation items in flight per lane
@@ -192,11 +201,11 @@ __device__ __forceinline__ void owner_items(unsigned cnt, unsigned len, int lane
 // cross a tile boundary gets atomicMin / atomicOr.  Items are (tile of 2^kPullTileLog
 // in-edges, group of 4 query words), in word-group-major order; a warp stages each chunk's
 // live in-edges (a source with an active lane in the item's words) in shared memory, as
-// the PPR pull does, and gathers the source lines of two in-edges before it uses them.
+// the PPR pull does, and reads each live in-edge's source lines for the item's words.
 // Any order of relaxations reaches the same fixed point, so the distances are those of
 // the push rounds; pull and push rounds mix freely.
 __device__ __forceinline__ void sbatch_pull(const BatchParams& p, int buf, unsigned* qctr, PullChunk& pc,
-                                            unsigned long long& prelax, int lane, bool& bad) {
+                                            long long& relax, int lane) {
     const unsigned W = 1u << p.logW;
     const int lg = p.logW >= 2 ? p.logW - 2 : 0;  // word groups per tile
     const unsigned nitems = p.ntiles_r << lg;
@@ -224,7 +233,7 @@ __device__ __forceinline__ void sbatch_pull(const BatchParams& p, int buf, unsig
                     if (e < ez) {
                         const int2 ed = __ldg(p.adj_rw + e);
                         if ((unsigned)ed.x >= (unsigned)p.V) {
-                            bad = true;
+                            atomicOr(&p.ctl->flags, C2G_FLAG_BOUNDS);
                         } else {
                             src = ed.x;
                             wt = ed.y;
@@ -242,7 +251,10 @@ __device__ __forceinline__ void sbatch_pull(const BatchParams& p, int buf, unsig
                             }
                         }
                     }
-                    prelax += (unsigned long long)(__popc(mk[0]) + __popc(mk[1]) + __popc(mk[2]) + __popc(mk[3]));
+                    // (query, edge) relaxations of the chunk, counted by lane 0
+                    const unsigned nrel = __reduce_add_sync(
+                        kFull, (unsigned)(__popc(mk[0]) + __popc(mk[1]) + __popc(mk[2]) + __popc(mk[3])));
+                    if (lane == 0) relax += (long long)nrel;
                     const bool live = (mk[0] | mk[1] | mk[2] | mk[3]) != 0u;
                     const unsigned lm = __ballot_sync(kFull, live);
                     const unsigned n = (unsigned)__popc(lm);
@@ -253,30 +265,23 @@ __device__ __forceinline__ void sbatch_pull(const BatchParams& p, int buf, unsig
                         pc.mk[at] = make_uint4(mk[0], mk[1], mk[2], mk[3]);
                     }
                     __syncwarp();
-                    for (unsigned k0 = 0; k0 < n; k0 += 2u) {
-                        // the source lines of two in-edges, then their candidates
-                        int dv[2][4];
-                        int wk[2];
+                    for (unsigned k = 0; k < n; ++k) {
+                        // one in-edge's source lines, then its candidates (two in-edges in
+                        // flight measured slower: 93.8 vs 90.2 ms per 256-query batch)
+                        const int2 ek = pc.ed[k];
+                        const uint4 mq = pc.mk[k];
+                        int dv[4];
 #pragma unroll
-                        for (int h = 0; h < 2; ++h) {
-                            const unsigned k = k0 + h < n ? k0 + h : n - 1u;
-                            const int2 ek = pc.ed[k];
-                            const uint4 mq = pc.mk[k];
-                            wk[h] = ek.y;
-#pragma unroll
-                            for (int j = 0; j < 4; ++j) {
-                                const unsigned mj = j == 0 ? mq.x : j == 1 ? mq.y : j == 2 ? mq.z : mq.w;
-                                const bool on = k0 + h < n && ((mj >> lane) & 1u);
-                                // L2-coherent: other warps lower distances during the round
-                                dv[h][j] = on ? ldcg(p.dist + (size_t)(unsigned)ek.x * Qu + ((w0 + j) << 5) + lane)
-                                              : INT_MAX;
-                            }
+                        for (int j = 0; j < 4; ++j) {
+                            const unsigned mj = j == 0 ? mq.x : j == 1 ? mq.y : j == 2 ? mq.z : mq.w;
+                            // L2-coherent: other warps lower distances during the round
+                            dv[j] = ((mj >> lane) & 1u)
+                                        ? ldcg(p.dist + (size_t)(unsigned)ek.x * Qu + ((w0 + j) << 5) + lane)
+                                        : INT_MAX;
                         }
 #pragma unroll
-                        for (int h = 0; h < 2; ++h)
-#pragma unroll
-                            for (int j = 0; j < 4; ++j)
-                                if (dv[h][j] != INT_MAX) mn[j] = min(mn[j], dv[h][j] + wk[h]);
+                        for (int j = 0; j < 4; ++j)
+                            if (dv[j] != INT_MAX) mn[j] = min(mn[j], dv[j] + ek.y);
                     }
                 }
                 const bool whole = vs >= e0 && ve <= e1;
@@ -321,9 +326,6 @@ __global__ void __launch_bounds__(kSsspBatchThreads, 3) sssp_batch_persistent(co
     WarpStage fst{sm.v0[wib], sm.d0[wib], sm.x0[wib], 0};
     int* qtab = sm.v1[wib];  // slot -> query position table of the owner being expanded
     __shared__ PullChunk pcs[kSsspBatchThreads / 32];  // pull rounds' in-edge chunks
-    const bool pulls = p.pull_min != ~0ull;
-    unsigned long long prelax = 0;  // relaxations of the pull rounds, counted by every lane
-    bool bad_in = false;
 
     // An epoch of a resident batch starts from the state the previous epoch left: the
     // distances and the improvement masks (queries that joined since have their column
@@ -367,13 +369,18 @@ __global__ void __launch_bounds__(kSsspBatchThreads, 3) sssp_batch_persistent(co
         if (gtid == 0) {
             ctl->qctr[(cur + 1) % 3] = 0ull;
             ctl->tilectr[(cur + 1) % 3] = 0u;
+            ctl->pcount[(cur + 1) % 3] = 0ull;
         }
-        batch_sweep(p, batch_out(p, buf, slot), pulls ? p.amask[buf] : nullptr, fst, gwarp, nwarps, lane);
+        batch_sweep(p, batch_out(p, buf, slot), p.pull_min != ~0ull ? p.amask[buf] : nullptr, &ctl->pcount[slot], fst,
+                    gwarp, nwarps, lane);
         if (!grid_sync(bar, flags, p.barrier_ns)) return;
         phase_mark(ctl->phase_ns, tph, 1);
         const unsigned long long c = ldcg(&ctl->qctr[slot]);
         const unsigned F = (unsigned)(c >> 32), T = (unsigned)c;
-        const bool pull = (unsigned long long)T > p.pull_min;  // grid-uniform
+        // pull when the frontier's (query, edge) relaxations exceed pull_min: the dense rounds
+        // in which most active words have most of their queries active (the push pays a
+        // red.min per improvement there), not every round with many edge-word steps
+        const bool pull = ldcg(&ctl->pcount[slot]) > p.pull_min;  // grid-uniform
         if (gtid == 0) trace_round(p.trace, iters, (long long)T, pull ? 1 : 0);
         if (F == 0) break;
         if (++iters > p.max_iter) {
@@ -389,7 +396,7 @@ __global__ void __launch_bounds__(kSsspBatchThreads, 3) sssp_batch_persistent(co
             ctl->relaxed += T;
         }
 
-        if (pulls) {
+        if (p.pull_min != ~0ull) {
             // The previous round's frontier leaves the pull lookup (the lookup of this round,
             // amask[buf], is the one a pull reads; the next round writes amask[buf ^ 1]).
             const unsigned Fp = min((unsigned)(ldcg(&ctl->qctr[(cur + 2) % 3]) >> 32), p.qcap);
@@ -397,7 +404,7 @@ __global__ void __launch_bounds__(kSsspBatchThreads, 3) sssp_batch_persistent(co
         }
         if (pull) {
             if (gtid == 0) steps += T;
-            sbatch_pull(p, buf, &ctl->tilectr[slot], pcs[wib], prelax, lane, bad_in);
+            sbatch_pull(p, buf, &ctl->tilectr[slot], pcs[wib], relax, lane);
         } else {
         // Phase 2: expand.  Warps take tiles of edge-word steps and walk owner runs: the
         // owner's row of distances is read once; its edges are read 32 at a time (one per
@@ -502,11 +509,9 @@ __global__ void __launch_bounds__(kSsspBatchThreads, 3) sssp_batch_persistent(co
         // end of an epoch: the next round's improvements wait in the masks
         if (p.epoch_rounds > 0 && iters >= p.epoch_rounds) break;
     }
-    if (bad_in) atomicOr(flags, C2G_FLAG_BOUNDS);
-    // relax is counted by lane 0 of each warp, prelax by every lane
-    for (int o = 16; o >= 1; o >>= 1) prelax += __shfl_xor_sync(kFull, prelax, o);
+    // relax is counted by lane 0 of each warp
     if (lane == 0) {
-        atomicAdd((unsigned long long*)&p.counters[0], (unsigned long long)relax + prelax);
+        atomicAdd((unsigned long long*)&p.counters[0], (unsigned long long)relax);
         atomicAdd((unsigned long long*)&p.counters[1], (unsigned long long)steps);
     }
     if (gtid == 0) {
@@ -648,8 +653,8 @@ static int batch_alloc(c2g_graph* g, int Q, size_t n_seeds) {
     return C2G_OK;
 }
 
-// The pull rounds of a batched SSSP launch (p.pull_min: edge-word steps above which a
-// round pulls, ~0: never): they need the reverse CSR with int32 weights (a view uses its
+// The pull rounds of a batched SSSP launch (p.pull_min: (query, edge) relaxations of the
+// frontier above which a round pulls, ~0: never): they need the reverse CSR with int32 weights (a view uses its
 // base's, never builds it), whose arrays are set into p here, after they exist.  The pull
 // lookups start clear; a launch leaves the entries of its last rounds behind.
 static int sssp_pull_setup(c2g_graph* g, BatchWork* w, int Q, BatchParams& p) {
@@ -667,7 +672,7 @@ static int sssp_pull_setup(c2g_graph* g, BatchWork* w, int Q, BatchParams& p) {
     p.mark_r = g->mark_r;
     for (int b = 0; b < 2; ++b)
         C2G_CUDA(cudaMemsetAsync(w->amask[b], 0, sizeof(unsigned) * (size_t)g->V * (size_t)(Q / 32), g->stream));
-    p.pull_min = (unsigned long long)((double)frac * (double)g->E * (double)(Q / 32));
+    p.pull_min = (unsigned long long)((double)frac * (double)g->E * (double)Q);
     return C2G_OK;
 }
 

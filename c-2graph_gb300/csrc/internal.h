@@ -54,7 +54,7 @@ constexpr int kMaxTraceRounds = 1024;
 struct RoundTrace {
     unsigned long long t_ns;
     long long work;  // PPR: (query, edge) pushes of the round; SSSP: edge-word steps
-    int shape;       // PPR: 1 pull round, 0 push round; SSSP: 0
+    int shape;       // 1 pull round, 0 push (PPR) or expansion (SSSP) round
     unsigned mid_ns;  // from the round's start to the end of its first phase (expansion / push or pull)
 };
 
@@ -103,7 +103,7 @@ struct SsspConfig {
     int max_iter = 1 << 20;
     int batch_tile_big_log = 9;  // batched expansion: 512 edge-word steps per big tile
     int batch_tile_min_log = 4;  // ... in rounds with at least 16 big tiles per warp
-    float batch_pull_frac = 0.5f;  // batched rounds with more edge-word steps than this * E * words
+    float batch_pull_frac = 0.3f;  // batched rounds with more (query, edge) relaxations than this * E * Q
                                    // pull over the reverse CSR (< 0: never)
 };
 

@@ -142,7 +142,7 @@ int  c2g_graph_last_phases(const c2g_graph* g, double ms[4]);
  * (c2g_sssp_batch / c2g_ppr_batch, or a session epoch) on this handle, up to 1024 rounds:
  * ms[i] the device time of round i (as block 0 sees it from one round's start to the
  * next), first_ms[i] the part of it up to the end of the round's first phase (PPR: the
- * push or pull, the apply sweep follows; SSSP: the expansion, the next mask sweep
+ * push or pull, the apply sweep follows; SSSP: the expansion or pull, the next mask sweep
  * follows), work[i] its work units (PPR: (query, edge) pushes; SSSP: edge-word steps),
  * shape[i] 1 for a pull round, 0 otherwise.  Arrays hold `cap` entries (any may be NULL);
  * *n gets the number of rounds (0 when no batched launch finished cleanly). */
@@ -216,18 +216,21 @@ int c2g_sssp_batch_set_tile(c2g_graph* g, int32_t big_steps, int32_t min_tiles_p
 int c2g_sssp_batch_get_tile(const c2g_graph* g, int32_t* big_steps, int32_t* min_tiles_per_warp);
 
 /* Round shape of the batched SSSP (c2g_sssp_batch and resident SSSP batches; no
- * counterpart in the reference): a round whose frontier has more than frac * E * words
- * edge-word steps (words = query slots / 32) pulls over the reverse CSR with int32
- * weights (built on first use): each target takes the minimum over its in-edges from
- * sources that improved in the previous round.  frac < 0: expand (push) only; 0: pull
- * every round; default 0.5.  Distances do not depend on the setting. */
+ * counterpart in the reference): a round whose frontier makes more than frac * E * Q
+ * (query, edge) relaxations (Q = query slots, a multiple of 32) pulls over the reverse
+ * CSR with int32 weights (built on first use): each target takes the minimum over its
+ * in-edges from sources that improved in the previous round.  frac < 0: expand (push)
+ * only; 0: pull every round; default 0.3.  Distances do not depend on the setting. */
 int c2g_sssp_batch_set_pull(c2g_graph* g, float frac);
+int c2g_sssp_batch_get_pull(const c2g_graph* g, float* frac);
 
-/* Autotuner of those tiles (no counterpart in the reference): times 128-step tiles and
- * big_steps {256, 512, 1024, 2048} x min_tiles_per_warp {4, 16, 64} on this batch (one
- * warm-up launch, then `reps` timed), rejects any candidate whose distances differ from
- * the first's on the first 8 queries, applies the fastest, returns it, and writes every
- * timing as JSON to json_path (may be NULL). */
+/* Autotuner of those tiles and of the round shape (no counterpart in the reference):
+ * times 128-step tiles and big_steps {256, 512, 1024, 2048} x min_tiles_per_warp
+ * {4, 16, 64} on this batch (one warm-up launch, then `reps` timed), then, at the fastest
+ * tiles, pull fractions {expand only, 0.15, 0.3, 0.5, 0.75}; rejects any candidate whose
+ * distances differ from the first's on the first 8 queries, applies the fastest tiles
+ * and fraction, returns the tiles, and writes every timing as JSON to json_path (may be
+ * NULL). */
 int c2g_sssp_batch_autotune(c2g_graph* g, int32_t n, const int32_t* sources, int use_seeds, int seed_mode,
                             int32_t reps, const char* json_path, int32_t* best_big_steps,
                             int32_t* best_min_tiles);

@@ -81,8 +81,9 @@ def test_sssp_batch_pull_shapes_vs_dijkstra(gpu_available, g17w, g16, frac):
 
 
 def test_batch_tiles_and_autotune(gpu_available, g17w, tmp_path):
-    """Every tile shape gives the same distances (Dijkstra); the autotuner times its 13
-    candidates, keeps a valid one and applies it."""
+    """Every tile shape gives the same distances (Dijkstra); the autotuner times its 13 tile
+    candidates, then 4 more pull fractions at the fastest tiles, keeps valid ones and
+    applies them."""
     import json
 
     import c2g
@@ -105,10 +106,12 @@ def test_batch_tiles_and_autotune(gpu_available, g17w, tmp_path):
         path = str(tmp_path / "tile.json")
         big, mn = gr.sssp_batch_autotune(src, reps=1, json_path=path)
         rec = json.load(open(path))
-        assert len(rec["candidates"]) == 13 and all(c["valid"] for c in rec["candidates"])
+        assert len(rec["candidates"]) == 17 and all(c["valid"] for c in rec["candidates"])
         assert (rec["best"]["big_steps"], rec["best"]["min_tiles_per_warp"]) == (big, mn)
+        assert {c["pull_frac"] for c in rec["candidates"][13:]} | {0.3} == {-1, 0.15, 0.3, 0.5, 0.75}
         b = ctypes_tile(gr)
         assert b == (big, mn)
+        assert abs(gr.sssp_batch_pull_frac() - rec["best"]["pull_frac"]) < 1e-6
         dist, _ = gr.sssp_batch(src)
         for i in range(6):
             assert np.array_equal(dist[i], refs[i])
