@@ -342,9 +342,9 @@ def run_ours(args, rank, world, local_rank):
     kernel_name = "sssp_batch_persistent" if dominant == "s" else "ppr_batch_persistent"
     # DRAM bytes (read + write) per unit processed (push or relaxation), from an ncu
     # capture of the kernel, scaled to this run's average launch.
-    # Full-size step, ratio 1 (the autotuner's pick): 2,422 GB per 371.46 G pushes for the
-    # PPR launch, 327 GB per 61.37 G relaxations for the SSSP launch.
-    traffic_per_unit = {"p": 2.422e12 / 371.46e9, "s": 327.0e9 / 61.37e9}[dominant]
+    # Full-size step (the autotuners' picks): 2,422 GB per 371.46 G pushes for the PPR
+    # launch, 290.4 GB per 61.37 G relaxations for the SSSP launch.
+    traffic_per_unit = {"p": 2.422e12 / 371.46e9, "s": 290.4e9 / 61.37e9}[dominant]
     units = tot["p_push"] if dominant == "p" else tot["s_rel"]
     traffic = traffic_per_unit * units / args.steps
 
