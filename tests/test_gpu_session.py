@@ -74,6 +74,31 @@ def test_session_sssp_staggered_admission_and_slot_reuse(gpu_available, g15):
     assert sorted(seen) == sorted(srcs)  # 80 queries through 48 slots: slots were reused
 
 
+@pytest.mark.parametrize("frac", [0.0, -1.0])
+def test_session_sssp_pull_rounds(gpu_available, g15, frac):
+    """Resident SSSP batches whose rounds all pull over the reverse CSR (frac 0: every
+    round with a frontier pulls) or all expand (frac -1): queries joining at epoch
+    boundaries still get the exact distances, so the pull lookups rebuilt by each epoch's
+    sweeps hold no stale state."""
+    import c2g
+    import oracle
+
+    o = oracle.load_dataset(g15, "origin")
+    srcs = _srcs(o["vlist"], 40, 11)
+    plan = {0: srcs[:12], 1: srcs[12:24], 4: srcs[24:]}
+    seen = []
+    with c2g.Graph.load(g15, "origin") as g:
+        g.sssp_batch_pull(frac)
+        with c2g.Session(g, c2g.REQ_SSSP, 32) as sess:
+            def done(s, sl):
+                dist, st = sess.read(sl)
+                assert np.array_equal(dist, oracle.dijkstra(o["vlist"], o["elist"], o["wlist"], [s], [0])), (frac, s)
+                seen.append(s)
+
+            _run(sess, plan, 2, done)
+    assert sorted(seen) == sorted(srcs)
+
+
 def test_session_ppr_staggered_admission_vs_fp64(gpu_available, g15):
     import c2g
     import oracle
