@@ -51,6 +51,8 @@ def lib():
         L.orc_prune_ppr.argtypes = [ctypes.c_char_p, ctypes.c_double]
         L.orc_prune_depth.restype = ctypes.c_int
         L.orc_prune_depth.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_double, _P]
+        L.orc_prune_ppr_speculative.restype = ctypes.c_int
+        L.orc_prune_ppr_speculative.argtypes = [ctypes.c_char_p, ctypes.c_double, ctypes.c_int32, ctypes.c_char_p, _P]
         _lib = L
     return _lib
 
@@ -240,6 +242,18 @@ def prune_depth(dir, kind, alpha=None):
     keys = ("visits", "removing", "decisions", "depth", "visit_depth", "widest", "in_levels_ge32",
             "in_levels_ge1024")
     return {k: int(x) for k, x in zip(keys, st)}
+
+
+def prune_ppr_speculative(dir, alpha=None, window=1024, sub="ppr_spec"):
+    """purn-ppr's visits run in rounds of a speculative, reservation-based schedule
+    (oracle/ingest.c orc_prune_ppr_speculative); outputs in dir/<sub>/ in the ppr/
+    layout.  Returns the rounds, the committed visits and the largest round."""
+    st = np.zeros(3, np.int64)
+    keep = 0.8 if alpha is None else 1.0 - alpha
+    rc = lib().orc_prune_ppr_speculative(os.fsencode(dir), keep, int(window), sub.encode(), st.ctypes.data)
+    if rc:
+        raise RuntimeError("orc_prune_ppr_speculative failed: %d" % rc)
+    return {"rounds": int(st[0]), "visits": int(st[1]), "widest": int(st[2])}
 
 
 def adsorption_labels(row, col, f, seeds, p_inj, p_cont, iterations):

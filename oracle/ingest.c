@@ -645,3 +645,207 @@ int orc_prune_depth(const char* dir, int ppr, double keep, int64_t* st) {
     free(d.width);
     return rc;
 }
+
+/* ---- a parallel schedule of purn-ppr, checked on the CPU ------------------------------
+ * purn-ppr visits every vertex once in id order.  orc_prune_ppr_speculative runs the same
+ * visits (prune_one, unchanged) in rounds over a window of the next `window` unvisited
+ * vertices, the schedule a parallel pruner would use (deterministic reservations): each
+ * candidate computes, on the current state, the rows it reads (its in-row, its out-row,
+ * its live roots' out-rows) and the rows it would write (its out-row and its roots'
+ * out-rows when it moves edges, the in-rows of the targets it moves); it reserves them
+ * under its id; it commits when no earlier candidate of the window writes a row it reads
+ * and none touches a row it writes, unless an earlier candidate that failed had a row it
+ * reads written in this round (its plan, and so the rows it will touch, may change):
+ * candidates past the first such one wait.  Records are gathered per vertex and written
+ * in id order.  The outputs go to dir/<sub>/ in the ppr/ layout, so a test compares them
+ * byte by byte with orc_prune_ppr's.  st[3]: rounds, committed visits, the largest round. */
+typedef struct {
+    int32_t* a;
+    int32_t n, cap;
+} rowset;
+
+static void rs_push(rowset* v, int32_t x) {
+    if (v->n == v->cap) {
+        v->cap = v->cap ? 2 * v->cap : 16;
+        v->a = (int32_t*)realloc(v->a, sizeof(int32_t) * (size_t)v->cap);
+    }
+    v->a[v->n++] = x;
+}
+
+/* rows of visit i on the current state: out-row x is x, in-row x is V + x */
+static void ppr_visit_rows(int32_t i, int32_t V, const orow* out, const irow* in, const int32_t* indeg, rowset* R,
+                           rowset* W) {
+    const int32_t dmax = 5;
+    R->n = W->n = 0;
+    rs_push(R, V + i);
+    rs_push(R, i);
+    if (!(out[i].n > 0 && indeg[i] > 0 && indeg[i] <= dmax)) return;
+    int32_t root[8], nr = 0, cur[8] = {0};
+    for (int32_t k = 0; k < in[i].n; ++k)
+        if (in[i].alive[k] && nr < 8) root[nr++] = in[i].s[k];
+    const int32_t j = indeg[i] < nr ? indeg[i] : nr;
+    for (int32_t k = 0; k < nr; ++k) rs_push(R, root[k]);
+    int moves = 0;
+    const orow* oi = &out[i];
+    for (int32_t e = 0; e < oi->n; ++e) { /* the decisions of prune_one, without its writes */
+        const int32_t v = oi->t[e];
+        int is_root = 0;
+        for (int32_t k = 0; k < j; ++k)
+            if (root[k] == v) is_root = 1;
+        if (is_root) continue;
+        int32_t cnt = 0;
+        for (int32_t k = 0; k < j; ++k) {
+            const orow* o = &out[root[k]];
+            if (cur[k] + 1 < o->n && o->t[cur[k]] < v) cur[k] = lower_i32(o->t, cur[k], o->n - 1, v);
+            if (o->t[cur[k]] == v) ++cnt;
+        }
+        if (cnt + 2 > j) {
+            rs_push(W, V + v);
+            moves = 1;
+        }
+    }
+    if (moves) {
+        rs_push(W, i);
+        for (int32_t k = 0; k < nr; ++k) rs_push(W, root[k]);
+    }
+}
+
+int orc_prune_ppr_speculative(const char* dir, double keep, int32_t window, const char* sub, int64_t* st) {
+    if (!dir || !sub || !st || window < 1) return -1;
+    size_t nv = 0, ne = 0, nw = 0;
+    int32_t* vl = orc_read4(dir, "origin", "vlist", &nv);
+    int32_t* el = orc_read4(dir, "origin", "elist", &ne);
+    uint32_t* wl = (uint32_t*)orc_read4(dir, "origin", "flist", &nw);
+    if (!vl || !el || !wl || nv < 1 || nw < ne || (size_t)vl[nv - 1] != ne) {
+        free(vl), free(el), free(wl);
+        return -2;
+    }
+    const int32_t V = (int32_t)nv - 1;
+    orow* out = (orow*)calloc((size_t)(V ? V : 1), sizeof(orow));
+    irow* in = (irow*)calloc((size_t)(V ? V : 1), sizeof(irow));
+    int32_t* indeg = (int32_t*)malloc(sizeof(int32_t) * (size_t)(V ? V : 1));
+    prune_rows(V, vl, el, wl, 1, out, in, indeg);
+    free(el);
+    free(wl);
+    const prune_rule rule = {1, keep};
+    unsigned char* done = (unsigned char*)calloc((size_t)(V ? V : 1), 1);
+    int64_t* resA = (int64_t*)calloc(2 * (size_t)(V ? V : 1), sizeof(int64_t)); /* (round << 32) | ~id: max wins */
+    int64_t* resW = (int64_t*)calloc(2 * (size_t)(V ? V : 1), sizeof(int64_t));
+    int32_t* wmark = (int32_t*)calloc(2 * (size_t)(V ? V : 1), sizeof(int32_t));
+    rowset* R = (rowset*)calloc((size_t)window, sizeof(rowset));
+    rowset* W = (rowset*)calloc((size_t)window, sizeof(rowset));
+    int32_t* cand = (int32_t*)malloc(sizeof(int32_t) * (size_t)window);
+    unsigned char* pass = (unsigned char*)malloc((size_t)window);
+    int64_t* rec_off = (int64_t*)calloc((size_t)V + 1, sizeof(int64_t)); /* per-vertex records, in commit order */
+    int32_t* rec_n = (int32_t*)calloc((size_t)(V ? V : 1), sizeof(int32_t));
+    ilist pool_t, pool_w;
+    memset(&pool_t, 0, sizeof(pool_t));
+    memset(&pool_w, 0, sizeof(pool_w));
+    records one;
+    memset(&one, 0, sizeof(one));
+    int32_t pos = 0, rounds = 0, widest = 0;
+    int64_t commits = 0;
+    int rc = 0;
+    while (pos < V && !rc) {
+        ++rounds;
+        int32_t n = 0;
+        for (int32_t v = pos; v < V && n < window; ++v)
+            if (!done[v]) cand[n++] = v;
+        const int64_t tag = (int64_t)rounds << 32;
+        for (int32_t c = 0; c < n; ++c) { /* plan and reserve */
+            ppr_visit_rows(cand[c], V, out, in, indeg, &R[c], &W[c]);
+            const int64_t key = tag | (int64_t)(uint32_t)~(uint32_t)cand[c];
+            for (int32_t k = 0; k < R[c].n; ++k)
+                if (resA[R[c].a[k]] < key) resA[R[c].a[k]] = key;
+            for (int32_t k = 0; k < W[c].n; ++k) {
+                if (resA[W[c].a[k]] < key) resA[W[c].a[k]] = key;
+                if (resW[W[c].a[k]] < key) resW[W[c].a[k]] = key;
+            }
+        }
+        for (int32_t c = 0; c < n; ++c) { /* check; the passers mark the rows they write */
+            const int64_t key = tag | (int64_t)(uint32_t)~(uint32_t)cand[c];
+            int ok = 1;
+            for (int32_t k = 0; k < W[c].n && ok; ++k)
+                if (resA[W[c].a[k]] != key) ok = 0;
+            for (int32_t k = 0; k < R[c].n && ok; ++k)
+                if (resW[R[c].a[k]] > key) ok = 0; /* an earlier writer this round */
+            pass[c] = (unsigned char)ok;
+            if (ok)
+                for (int32_t k = 0; k < W[c].n; ++k) wmark[W[c].a[k]] = rounds;
+        }
+        int32_t dmin = V; /* the first failed candidate whose reads a passer writes */
+        for (int32_t c = 0; c < n && dmin == V; ++c) {
+            if (pass[c]) continue;
+            for (int32_t k = 0; k < R[c].n; ++k)
+                if (wmark[R[c].a[k]] == rounds) {
+                    dmin = cand[c];
+                    break;
+                }
+        }
+        int32_t nc = 0;
+        for (int32_t c = 0; c < n && !rc; ++c) { /* commit */
+            const int32_t i = cand[c];
+            if (!pass[c] || i > dmin) continue;
+            if (out[i].n > 0 && indeg[i] > 0 && indeg[i] <= 5) {
+                one.he.n = one.hw.n = one.hv.n = one.owner.n = 0;
+                il_push(&one.hv, 0);
+                if (prune_one(&rule, i, out, in, indeg, &one, NULL)) rc = -3;
+                rec_off[i] = pool_t.n;
+                rec_n[i] = (int32_t)one.he.n;
+                for (int64_t k = 0; k < one.he.n; ++k) {
+                    il_push(&pool_t, one.he.a[k]);
+                    il_push(&pool_w, one.hw.a[k]);
+                }
+            }
+            done[i] = 1;
+            ++nc;
+        }
+        commits += nc;
+        if (nc > widest) widest = nc;
+        while (pos < V && done[pos]) ++pos;
+    }
+    if (!rc) {
+        records rec;
+        memset(&rec, 0, sizeof(rec));
+        il_push(&rec.hv, 0);
+        for (int32_t v = 0; v < V; ++v) {
+            for (int32_t k = 0; k < rec_n[v]; ++k) {
+                il_push(&rec.he, pool_t.a[rec_off[v] + k]);
+                il_push(&rec.hw, pool_w.a[rec_off[v] + k]);
+            }
+            il_push(&rec.hv, (uint32_t)rec.he.n);
+        }
+        int64_t E = 0;
+        for (int32_t v = 0; v < V; ++v) E += out[v].n;
+        int32_t* pe = (int32_t*)malloc(sizeof(int32_t) * (size_t)(E ? E : 1));
+        uint32_t* pw = (uint32_t*)malloc(sizeof(uint32_t) * (size_t)(E ? E : 1));
+        int64_t e = 0;
+        vl[0] = 0;
+        for (int32_t v = 0; v < V; ++v) {
+            memcpy(pe + e, out[v].t, sizeof(int32_t) * (size_t)out[v].n);
+            memcpy(pw + e, out[v].w, sizeof(uint32_t) * (size_t)out[v].n);
+            e += out[v].n;
+            vl[v + 1] = (int32_t)e;
+        }
+        char p[4096];
+        snprintf(p, sizeof(p), "%s/%s", dir, sub);
+        rc = orc_mkdir(p);
+        if (!rc) rc = orc_write4(dir, sub, "hvlist", rec.hv.a, (size_t)rec.hv.n);
+        if (!rc) rc = orc_write4(dir, sub, "helist", rec.he.a, (size_t)rec.he.n);
+        if (!rc) rc = orc_write4(dir, sub, "hwlist", rec.hw.a, (size_t)rec.hw.n);
+        if (!rc) rc = orc_write4(dir, sub, "vlist", vl, (size_t)V + 1);
+        if (!rc) rc = orc_write4(dir, sub, "elist", pe, (size_t)E);
+        if (!rc) rc = orc_write4(dir, sub, "wlist", pw, (size_t)E);
+        free(pe), free(pw), free(rec.hv.a), free(rec.he.a), free(rec.hw.a);
+    }
+    st[0] = rounds, st[1] = commits, st[2] = widest;
+    for (int32_t v = 0; v < V; ++v) {
+        free(out[v].t), free(out[v].w);
+        free(in[v].s), free(in[v].alive);
+    }
+    for (int32_t c = 0; c < window; ++c) free(R[c].a), free(W[c].a);
+    free(out), free(in), free(indeg), free(vl), free(done), free(resA), free(resW), free(wmark), free(R), free(W);
+    free(cand), free(pass), free(rec_off), free(rec_n), free(pool_t.a), free(pool_w.a);
+    free(one.hv.a), free(one.he.a), free(one.hw.a), free(one.owner.a);
+    return rc;
+}

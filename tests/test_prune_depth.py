@@ -61,3 +61,22 @@ def test_prune_depth_of_a_chain_is_sequential(tmp_path):
     st = oracle.prune_depth(d, "sssp")
     assert st["visits"] == n - 2  # vertices 1 .. n-2 have one root and an out-edge
     assert st["removing"] == st["visits"] and st["visit_depth"] == st["visits"] + 1
+
+
+@pytest.mark.parametrize("alpha,window", [(None, 64), (0.15, 1024)])
+def test_prune_ppr_speculative_schedule_reproduces_the_bytes(tmp_path, alpha, window):
+    """purn-ppr's visits in rounds of the reservation-based schedule a parallel pruner
+    would run (every vertex visited once, committed out of id order) write the same bytes
+    as the sequential pass, in far fewer rounds than visits."""
+    import oracle
+
+    d = str(tmp_path / "g")
+    oracle.rmat_write(d, 14, 16, 6, 1, 1000)
+    oracle.prune_ppr(d, alpha)
+    st = oracle.prune_ppr_speculative(d, alpha, window)
+    for f in ("vlist", "elist", "wlist", "hvlist", "helist", "hwlist"):
+        assert filecmp.cmp(os.path.join(d, "ppr", f + ".bin"), os.path.join(d, "ppr_spec", f + ".bin"),
+                           shallow=False), f
+    V = 1 << 14
+    assert st["visits"] == V
+    assert st["rounds"] * 8 < V and st["widest"] > 32
