@@ -31,6 +31,10 @@
  *   orc_prune_depth    either pruner with a dependency analysis of its visiting order
  *                      (not a restatement: an analysis of the sequential algorithm, for
  *                      the question whether a parallel pruner could reproduce its bytes).
+ *   orc_prune_ppr_speculative
+ *                      purn-ppr's visits in rounds of a reservation-based parallel
+ *                      schedule, run on the CPU, to check that schedule against the
+ *                      sequential pass's bytes.
  *
  * The pruners keep the reference's per-vertex state: the out-rows as sorted
  * (target, weight) lists built from each row's distinct pairs without self-loops
