@@ -154,6 +154,8 @@ SIGNATURES = {
     "c2g_prune_sssp": (ctypes.c_int, [ctypes.c_char_p]),
     "c2g_prune_ppr": (ctypes.c_int, [ctypes.c_char_p]),
     "c2g_prune_ppr_alpha": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_double]),
+    "c2g_prune_ppr_device": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_double, ctypes.c_int,
+                                            ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_int32)]),
 }
 
 
@@ -208,6 +210,15 @@ def prune_ppr(dir, alpha=None):
         _check(lib().c2g_prune_ppr(os.fsencode(dir)))
     else:
         _check(lib().c2g_prune_ppr_alpha(os.fsencode(dir), float(alpha)))
+
+
+def prune_ppr_device(dir, alpha=0.2, device=0):
+    """purn-ppr on the GPU (same files as prune_ppr(dir, alpha)).  Returns (kernel ms, rounds)."""
+    ms = ctypes.c_float(0.0)
+    rounds = ctypes.c_int32(0)
+    _check(lib().c2g_prune_ppr_device(os.fsencode(dir), float(alpha), int(device), ctypes.byref(ms),
+                                      ctypes.byref(rounds)))
+    return float(ms.value), int(rounds.value)
 
 
 def read_array(path, dtype=np.int32):

@@ -13,6 +13,7 @@
 // appends records in pruning order (rounds k = 0..29 over all vertices), while the
 // traversal indexes hvlist by vertex id (src/sssp/purn/Main.cu:68-79).
 #include <algorithm>
+#include <cstring>
 #include <cstdint>
 #include <string>
 #include <utility>
@@ -232,6 +233,46 @@ void flatten(const Adj<W>& out, int32_t V, std::vector<int32_t>& vlist, std::vec
 }
 
 }  // namespace
+
+// The rows purn-ppr starts from, flat, for the device pruner (prune_gpu.cu): out-rows of
+// distinct (target, weight bits) pairs without self-loops, sorted; in-rows of the distinct
+// sources, sorted.  orow / irow are row pointers over V + 1 entries.
+int prune_ppr_initial_rows(const std::string& dir, int32_t& V, std::vector<int32_t>& orow, std::vector<int32_t>& ot,
+                           std::vector<uint32_t>& ow, std::vector<int32_t>& irow, std::vector<int32_t>& is) {
+    std::vector<int32_t> vlist, elist;
+    std::vector<float> flist;
+    int rc;
+    if ((rc = read_array4(dir + "/origin/vlist.bin", vlist))) return rc;
+    if ((rc = read_array4(dir + "/origin/elist.bin", elist))) return rc;
+    if ((rc = read_array4(dir + "/origin/flist.bin", flist))) return rc;
+    if ((rc = check_csr(vlist, elist))) return rc;
+    if (flist.size() < elist.size()) return fail(C2G_ERR_FORMAT, "flist shorter than elist");
+    V = (int32_t)vlist.size() - 1;
+    Adj<float> out;
+    InAdj in;
+    build_out(vlist, elist, flist, V, out);
+    build_in(vlist, elist, V, in);
+    orow.assign((size_t)V + 1, 0);
+    irow.assign((size_t)V + 1, 0);
+    for (int32_t v = 0; v < V; ++v) {
+        orow[v + 1] = orow[v] + (int32_t)out[v].size();
+        irow[v + 1] = irow[v] + (int32_t)in[v].size();
+    }
+    ot.resize((size_t)orow[V]);
+    ow.resize((size_t)orow[V]);
+    is.resize((size_t)irow[V]);
+    for (int32_t v = 0; v < V; ++v) {
+        size_t k = (size_t)orow[v];
+        for (const auto& e : out[v]) {
+            ot[k] = e.first;
+            std::memcpy(&ow[k], &e.second, 4);
+            ++k;
+        }
+        k = (size_t)irow[v];
+        for (const auto& e : in[v]) is[k++] = e.first;
+    }
+    return C2G_OK;
+}
 
 int prune_sssp_dir(const std::string& dir) {
     std::vector<int32_t> vlist, elist, wlist;

@@ -443,6 +443,14 @@ int c2g_prune_ppr(const char* dir);
  * on the pruned graph follows the unpruned push.  alpha = 0.2 writes exactly what
  * c2g_prune_ppr writes (1 - 0.2 and 0.8 are the same double). */
 int c2g_prune_ppr_alpha(const char* dir, double alpha);
+/* purn-ppr on a GPU: the same visits as c2g_prune_ppr_alpha in rounds of a speculative
+ * schedule (every unvisited vertex of a window plans its visit and reserves the rows it
+ * reads and writes; the visits that no earlier planned visit conflicts with run in
+ * parallel, one warp each), writing the same six files byte for byte.  Replaces the
+ * sequential pass of purn-ppr (src/purn-ppr.cpp:146-283) on `device`.  *ms (may be NULL)
+ * gets the kernel time, *rounds (may be NULL) the number of rounds.  Returns
+ * C2G_ERR_OVERFLOW when a device row pool runs out (nothing is written). */
+int c2g_prune_ppr_device(const char* dir, double alpha, int device, float* ms, int32_t* rounds);
 
 #ifdef __cplusplus
 }
