@@ -8,19 +8,25 @@
 // its out-row, its roots' out-rows and the in-rows of the targets it moves, so the order
 // matters only between visits that share rows.  The device pruner runs the same visits in
 // rounds of a speculative schedule (deterministic reservations): every unvisited vertex of
-// a window plans its visit on the current state (the rows it reads and would write) and
-// reserves those rows under its id; it commits when no earlier candidate of the window
-// writes a row it reads or touches a row it writes, unless an earlier candidate that
-// failed had a row it reads written in this round (its plan may change), past which
-// nothing commits.  The first unvisited vertex always commits, so every round makes
-// progress.  Committed visits touch disjoint rows and run in parallel, one warp each, with
-// the reference's steps: roots in in-row order, membership of each out-edge's target in
-// every root's sorted row, the in-row updates of the moved targets in out-row order (lane
-// 0: a moved pair can repeat a target), and a sorted merge of the moved pairs into each
-// root's row with the weight (w * keep) * w' in double, rounded to float.  Rows live in
-// device pools; a merge or a grown in-row takes a new block from the pool (bump
-// allocation), so no row is ever shared.  The schedule is the one orc_prune_ppr_speculative
-// checks on the CPU.
+// a window plans its visit on the current state (the rows it reads and would write, and
+// which out-edges move) and reserves those rows under its id; it commits when no earlier
+// candidate of the window writes a row it reads or touches a row it writes, unless an
+// earlier candidate that failed had a row it reads written in this round (its plan may
+// change), past which nothing commits.  The first unvisited vertex always commits, so every
+// round makes progress.  The schedule is the one orc_prune_ppr_speculative checks on the
+// CPU.
+//
+// Committed visits touch disjoint rows and run in parallel, one warp each, with the
+// reference's steps: roots in in-row order; the out-row split into kept pairs (compacted
+// in place) and moved pairs (the record); each moved target's in-row gains the roots that
+// lack the target (a revived entry, or an inserted one) and loses i; the moved pairs merge
+// into each root's sorted row, a pair with a target the row has adding (w * keep) * w' to
+// the weight (double, rounded to float), a new target inserted with that weight.  Updates
+// of existing entries are made in place.  A row that gains entries moves to a new block of
+// its pool (bump allocation): the visit writes the new entries there and queues the old
+// row's segments between them as copy tasks of at most kPgTask elements, which the whole
+// grid runs after the commit phase.  So the copying of long rows (hubs are the roots of
+// many pruned vertices) is spread over every SM instead of one warp.
 #include <algorithm>
 #include <cstring>
 #include <string>
@@ -39,6 +45,8 @@ int prune_ppr_initial_rows(const std::string& dir, int32_t& V, std::vector<int32
 constexpr int kPgThreads = 256;
 constexpr int kPgMaxRoots = 5;  // the in-degree bound of purn-ppr (src/purn-ppr.cpp:146-152)
 constexpr int kPgMaxR = 2 + kPgMaxRoots;  // rows a visit reads: its in-row, its out-row, its roots' out-rows
+constexpr int kPgTask = 1024;             // elements per copy task
+constexpr int kPgMoved = 0x100;           // plan code of an out-edge that moves (| the roots lacking it)
 
 struct PgCtl {
     unsigned bar_count, bar_gen;  // GridBarrier
@@ -49,6 +57,12 @@ struct PgCtl {
     int finished;
     int pad;
     unsigned long long out_top, in_top, rec_top, wscr_top;  // pool bump pointers
+    unsigned long long task_top[2];                         // copy tasks, by round parity
+};
+
+struct PgTask {
+    long long src, dst;
+    int len, kind;  // kind 0: out-row pairs (ot, ow); 1: in-row entries (is, ia)
 };
 
 struct PgParams {
@@ -62,7 +76,6 @@ struct PgParams {
     unsigned long long out_cap;
     long long* in_off;
     int* in_n;
-    int* in_cap;
     int* is;
     unsigned char* ia;  // alive flags of the in-row entries
     unsigned long long in_pool_cap;
@@ -79,11 +92,13 @@ struct PgParams {
     int* wmark;                // [2V] round in which a committer writes the row
     int* slot_r;               // [span][kPgMaxR] rows read (out-row x is x, in-row x is V + x)
     int* slot_rn;              // rows read, -1: no candidate
-    long long* slot_woff;      // rows written, in wscr
+    long long* slot_woff;      // plan block in wscr: rows written, then one code per out-edge
     int* slot_wn;
     unsigned char* slot_pass;
     int* wscr;
     unsigned long long wscr_cap;
+    PgTask* task;
+    unsigned long long task_cap;
     PgCtl* ctl;
     unsigned long long barrier_ns;
     int max_rounds;
@@ -101,12 +116,13 @@ __device__ __forceinline__ unsigned long long pg_key(int round, int i) {
     return ((unsigned long long)(unsigned)round << 32) | (unsigned long long)(~(unsigned)i);
 }
 
-// first index of row [off, off + n) of `t` with t >= key, or n
-__device__ __forceinline__ int pg_lower(const int* t, long long off, int n, int key) {
-    int lo = 0, hi = n;
+// first index of [lo, n) of row `off` of `t` with t > key (upper) or t >= key (lower), or n
+__device__ __forceinline__ int pg_search(const int* t, long long off, int lo, int n, int key, bool upper) {
+    int hi = n;
     while (lo < hi) {
         const int mid = (lo + hi) >> 1;
-        if (ldcg(t + off + mid) < key)
+        const int x = ldcg(t + off + mid);
+        if (x < key || (upper && x == key))
             lo = mid + 1;
         else
             hi = mid;
@@ -114,11 +130,32 @@ __device__ __forceinline__ int pg_lower(const int* t, long long off, int n, int 
     return lo;
 }
 
-// The live roots of i in in-row order (every lane gets them).  Returns their count.
-__device__ int pg_roots(const PgParams& p, int i, int* rt, int lane) {
+// A vertex's live roots in in-row order and their out-rows (registers; indexed only in
+// unrolled loops).
+struct PgRoots {
+    int j;
+    int r[kPgMaxRoots];
+    long long off[kPgMaxRoots];
+    int n[kPgMaxRoots];
+};
+
+template <typename T>
+__device__ __forceinline__ T pg_pick(const T (&a)[kPgMaxRoots], int k) {
+    T x = a[0];
+#pragma unroll
+    for (int q = 1; q < kPgMaxRoots; ++q)
+        if (q == k) x = a[q];
+    return x;
+}
+
+// The live roots of i (every lane gets them).  Returns their count (kPgMaxRoots + 1 means
+// more than kPgMaxRoots; R.j keeps the first kPgMaxRoots).
+__device__ __forceinline__ int pg_roots(const PgParams& p, int i, PgRoots& R, int lane) {
     const long long off = ldl(p.in_off + i);
     const int n = ldcg(p.in_n + i);
     int nr = 0;
+#pragma unroll
+    for (int q = 0; q < kPgMaxRoots; ++q) R.r[q] = 0;
     for (int b = 0; b < n && nr <= kPgMaxRoots; b += 32) {
         const int k = b + lane;
         const bool a = k < n && ldb(p.ia + off + k) != 0;
@@ -126,34 +163,73 @@ __device__ int pg_roots(const PgParams& p, int i, int* rt, int lane) {
         unsigned m = __ballot_sync(kFull, a);
         while (m && nr <= kPgMaxRoots) {
             const int src = __shfl_sync(kFull, s, __ffs(m) - 1);
-            if (nr < kPgMaxRoots) rt[nr] = src;
+#pragma unroll
+            for (int q = 0; q < kPgMaxRoots; ++q)
+                if (q == nr) R.r[q] = src;
             ++nr;
             m &= m - 1u;
+        }
+    }
+    R.j = min(nr, kPgMaxRoots);
+#pragma unroll
+    for (int q = 0; q < kPgMaxRoots; ++q) {
+        R.off[q] = 0;
+        R.n[q] = 0;
+        if (q < R.j) {
+            R.off[q] = ldl(p.out_off + R.r[q]);
+            R.n[q] = ldcg(p.out_n + R.r[q]);
         }
     }
     return nr;
 }
 
-__device__ __forceinline__ bool pg_member(const PgParams& p, int r, int v) {
-    const long long off = ldl(p.out_off + r);
-    const int n = ldcg(p.out_n + r);
-    const int k = pg_lower(p.ot, off, n, v);
-    return k < n && ldcg(p.ot + off + k) == v;
-}
-
 // Does the edge i -> v move (every root but at most one has v)?  miss: roots without v.
-__device__ __forceinline__ bool pg_moves(const PgParams& p, const int* rt, int j, int v, unsigned& miss) {
+// Membership in a root's sorted row is the reference's monotone cursor test
+// (src/purn-ppr.cpp:170-186) as a lower bound; the roots' searches run in lockstep.
+__device__ __forceinline__ bool pg_moves(const PgParams& p, const PgRoots& R, int v, unsigned& miss) {
     miss = 0u;
-    for (int k = 0; k < j; ++k)
-        if (rt[k] == v) return false;  // a root keeps its edge
+    bool root = false;
+#pragma unroll
+    for (int k = 0; k < kPgMaxRoots; ++k) root |= k < R.j && R.r[k] == v;
+    if (root) return false;  // a root keeps its edge
+    int lo[kPgMaxRoots], hi[kPgMaxRoots];
+#pragma unroll
+    for (int k = 0; k < kPgMaxRoots; ++k) {
+        lo[k] = 0;
+        hi[k] = k < R.j ? R.n[k] : 0;
+    }
+    for (;;) {
+        int t[kPgMaxRoots];
+        bool any = false;
+#pragma unroll
+        for (int k = 0; k < kPgMaxRoots; ++k) {
+            t[k] = 0;
+            if (lo[k] < hi[k]) {
+                t[k] = ldcg(p.ot + R.off[k] + ((lo[k] + hi[k]) >> 1));
+                any = true;
+            }
+        }
+        if (!any) break;
+#pragma unroll
+        for (int k = 0; k < kPgMaxRoots; ++k)
+            if (lo[k] < hi[k]) {
+                const int mid = (lo[k] + hi[k]) >> 1;
+                if (t[k] < v)
+                    lo[k] = mid + 1;
+                else
+                    hi[k] = mid;
+            }
+    }
     int cnt = 0;
-    for (int k = 0; k < j; ++k) {
-        if (pg_member(p, rt[k], v))
+#pragma unroll
+    for (int k = 0; k < kPgMaxRoots; ++k) {
+        if (k >= R.j) continue;
+        if (lo[k] < R.n[k] && ldcg(p.ot + R.off[k] + lo[k]) == v)
             ++cnt;
         else
             miss |= 1u << k;
     }
-    return cnt + 2 > j;
+    return cnt + 2 > R.j;
 }
 
 __device__ __forceinline__ bool pg_prunes(const PgParams& p, int i) {
@@ -161,46 +237,73 @@ __device__ __forceinline__ bool pg_prunes(const PgParams& p, int i) {
     return ldcg(p.out_n + i) > 0 && d > 0 && d <= kPgMaxRoots;
 }
 
-// Plan of candidate i (slot c): the rows it reads and the rows it would write; reserve them.
-__device__ void pg_plan(const PgParams& p, int i, int c, int round, int lane) {
+// Queue the copy of `len` entries from src to dst (pool indices) as tasks.
+__device__ __forceinline__ void pg_emit(const PgParams& p, int par, int kind, long long src, long long dst,
+                                        long long len) {
+    for (long long x = 0; x < len; x += kPgTask) {
+        const unsigned long long t = atomicAdd(&p.ctl->task_top[par], 1ull);
+        if (t >= p.task_cap) {
+            atomicOr(&p.ctl->flags, kPgErrPool);
+            return;
+        }
+        PgTask* tk = p.task + t;
+        tk->src = src + x;
+        tk->dst = dst + x;
+        tk->len = (int)min((long long)kPgTask, len - x);
+        tk->kind = kind;
+    }
+}
+
+// Plan of candidate i (slot c): the rows it reads, the rows it would write, and per
+// out-edge whether it moves; reserve the rows.  The plan block in wscr holds the written
+// rows (at most on + 6) in [0, on + 8) and the out-edge codes in [on + 8, 2 on + 8).
+__device__ __forceinline__ void pg_plan(const PgParams& p, int i, int c, int round, int lane) {
     const int V = p.V;
-    int* R = p.slot_r + (size_t)c * kPgMaxR;
+    int* Rw = p.slot_r + (size_t)c * kPgMaxR;
     int rn = 2;
     if (lane == 0) {
-        R[0] = V + i;
-        R[1] = i;
+        Rw[0] = V + i;
+        Rw[1] = i;
     }
     long long woff = 0;
     int wn = 0;
     if (pg_prunes(p, i)) {
-        int rt[kPgMaxRoots];
-        const int nr = pg_roots(p, i, rt, lane);
-        const int j = min(nr, kPgMaxRoots);
-        if (lane == 0)
-            for (int k = 0; k < j; ++k) R[2 + k] = rt[k];
+        PgRoots R;
+        pg_roots(p, i, R, lane);
+        const int j = R.j;
+        if (lane == 0) {
+#pragma unroll
+            for (int k = 0; k < kPgMaxRoots; ++k)
+                if (k < j) Rw[2 + k] = R.r[k];
+        }
         rn = 2 + j;
         const long long off = ldl(p.out_off + i);
         const int on = ldcg(p.out_n + i);
+        const unsigned long long need = 2ull * (unsigned long long)on + 8ull;
         unsigned long long wb = 0;
-        if (lane == 0) wb = atomicAdd(&p.ctl->wscr_top, (unsigned long long)on + 8ull);
+        if (lane == 0) wb = atomicAdd(&p.ctl->wscr_top, need);
         wb = __shfl_sync(kFull, wb, 0);
-        if (wb + (unsigned long long)on + 8ull > p.wscr_cap) {
+        if (wb + need > p.wscr_cap) {
             if (lane == 0) atomicOr(&p.ctl->flags, kPgErrPool);
-            wn = 0;
         } else {
             woff = (long long)wb;
+            int* code = p.wscr + woff + on + 8;
             for (int b = 0; b < on; b += 32) {
                 const int e = b + lane;
-                unsigned miss;
-                const bool mv = e < on && pg_moves(p, rt, j, ldcg(p.ot + off + e), miss);
+                unsigned miss = 0u;
+                const int v = e < on ? ldcg(p.ot + off + e) : 0;
+                const bool mv = e < on && pg_moves(p, R, v, miss);
+                if (e < on) code[e] = mv ? (int)(kPgMoved | miss) : 0;
                 const unsigned m = __ballot_sync(kFull, mv);
-                if (mv) p.wscr[woff + wn + __popc(m & ((1u << lane) - 1u))] = V + ldcg(p.ot + off + e);
+                if (mv) p.wscr[woff + wn + __popc(m & ((1u << lane) - 1u))] = V + v;
                 wn += __popc(m);
             }
             if (wn > 0) {  // it moves edges: its out-row and its roots' out-rows change
                 if (lane == 0) {
                     p.wscr[woff + wn] = i;
-                    for (int k = 0; k < j; ++k) p.wscr[woff + wn + 1 + k] = rt[k];
+#pragma unroll
+                    for (int k = 0; k < kPgMaxRoots; ++k)
+                        if (k < j) p.wscr[woff + wn + 1 + k] = R.r[k];
                 }
                 wn += 1 + j;
             }
@@ -213,7 +316,7 @@ __device__ void pg_plan(const PgParams& p, int i, int c, int round, int lane) {
     }
     __syncwarp();
     const unsigned long long key = pg_key(round, i);
-    if (lane < rn) atomicMax(p.resA + R[lane], key);
+    if (lane < rn) atomicMax(p.resA + Rw[lane], key);
     for (int k = lane; k < wn; k += 32) {
         const int r = p.wscr[woff + k];
         atomicMax(p.resA + r, key);
@@ -221,169 +324,266 @@ __device__ void pg_plan(const PgParams& p, int i, int c, int round, int lane) {
     }
 }
 
-// A committed visit of vertex i (the reference's steps; the plan's rows are unchanged).
-__device__ void pg_visit(const PgParams& p, int i, int lane) {
-    int rt[kPgMaxRoots];
-    const int nr = pg_roots(p, i, rt, lane);
-    const int j = ldcg(p.indeg + i);
-    if (nr != j || j > kPgMaxRoots) {  // the reference stops on this (something error2)
+// v's in-row after the `cnt` moved pairs i -> v of a visit (one lane): every root in `miss`
+// gets a live entry (revived, or inserted in source order) and counts in v's in-degree, and
+// i's entry dies once per pair (src/purn-ppr.cpp:196-236).
+__device__ __forceinline__ void pg_in_update(const PgParams& p, const PgRoots& R, int i, int v, unsigned miss,
+                                             int cnt, int par) {
+    const long long off = ldl(p.in_off + v);
+    const int n = ldcg(p.in_n + v);
+    // lockstep lower bounds: the missing roots (0 .. kPgMaxRoots - 1) and i (kPgMaxRoots)
+    int lo[kPgMaxRoots + 1], hi[kPgMaxRoots + 1];
+#pragma unroll
+    for (int k = 0; k <= kPgMaxRoots; ++k) {
+        const bool use = k == kPgMaxRoots || (k < R.j && ((miss >> k) & 1u));
+        lo[k] = 0;
+        hi[k] = use ? n : 0;
+    }
+    for (;;) {
+        int t[kPgMaxRoots + 1];
+        bool any = false;
+#pragma unroll
+        for (int k = 0; k <= kPgMaxRoots; ++k) {
+            t[k] = 0;
+            if (lo[k] < hi[k]) {
+                t[k] = ldcg(p.is + off + ((lo[k] + hi[k]) >> 1));
+                any = true;
+            }
+        }
+        if (!any) break;
+#pragma unroll
+        for (int k = 0; k <= kPgMaxRoots; ++k)
+            if (lo[k] < hi[k]) {
+                const int mid = (lo[k] + hi[k]) >> 1;
+                const int key = k < kPgMaxRoots ? R.r[k] : i;
+                if (t[k] < key)
+                    lo[k] = mid + 1;
+                else
+                    hi[k] = mid;
+            }
+    }
+    const int qi = lo[kPgMaxRoots];
+    if (qi >= n || ldcg(p.is + off + qi) != i) {
+        atomicOr(&p.ctl->flags, kPgErrRows);
+        return;
+    }
+    int inc = 0;
+    unsigned ins = 0u;
+#pragma unroll
+    for (int k = 0; k < kPgMaxRoots; ++k) {
+        if (!(k < R.j && ((miss >> k) & 1u))) continue;
+        const int q = lo[k];
+        if (q < n && ldcg(p.is + off + q) == R.r[k]) {
+            if (!ldb(p.ia + off + q)) {
+                p.ia[off + q] = 1;
+                ++inc;
+            }
+        } else {
+            ins |= 1u << k;
+            ++inc;
+        }
+    }
+    p.ia[off + qi] = 0;
+    p.indeg[v] = ldcg(p.indeg + v) + inc - cnt;
+    if (ins) {
+        const int nins = __popc(ins);
+        const unsigned long long nb = atomicAdd(&p.ctl->in_top, (unsigned long long)(n + nins));
+        if (nb + (unsigned long long)(n + nins) > p.in_pool_cap) {
+            atomicOr(&p.ctl->flags, kPgErrPool);
+            return;
+        }
+        const long long nbo = (long long)nb;
+        int s = 0, prev = 0;
+#pragma unroll
+        for (int k = 0; k < kPgMaxRoots; ++k) {
+            if (!((ins >> k) & 1u)) continue;
+            const int at = lo[k];  // roots ascend, so the insertion points do too
+            pg_emit(p, par, 1, off + prev, nbo + prev + s, at - prev);
+            p.is[nbo + at + s] = R.r[k];
+            p.ia[nbo + at + s] = 1;
+            prev = at;
+            ++s;
+        }
+        pg_emit(p, par, 1, off + prev, nbo + prev + s, n - prev);
+        p.in_off[v] = nbo;
+        p.in_n[v] = n + nins;
+    }
+}
+
+// A committed visit of vertex i (slot c; the plan's rows are unchanged since the plan).
+__device__ __forceinline__ void pg_visit(const PgParams& p, int i, int c, int par, int lane) {
+    PgRoots R;
+    const int nr = pg_roots(p, i, R, lane);
+    const int j = R.j;
+    if (nr != ldcg(p.indeg + i) || nr > kPgMaxRoots) {  // the reference stops on this (something error2)
         if (lane == 0) atomicOr(&p.ctl->flags, kPgErrRows);
         return;
     }
-    // dis[k]: weight of root k -> i, its first pair with target i
-    unsigned dis[kPgMaxRoots];
-    for (int k = 0; k < j; ++k) {
-        unsigned d = 0u;
-        if (lane == 0) {
-            const long long off = ldl(p.out_off + rt[k]);
-            const int n = ldcg(p.out_n + rt[k]);
-            const int q = pg_lower(p.ot, off, n, i);
-            if (q < n && ldcg(p.ot + off + q) == i)
-                d = ldcg(p.ow + off + q);
-            else
-                atomicOr(&p.ctl->flags, kPgErrRows);
-        }
-        dis[k] = (unsigned)__shfl_sync(kFull, (int)d, 0);
+    // lane k < j: the weight of root k -> i, its first pair with target i
+    unsigned dis = 0u;
+    if (lane < j) {
+        const long long off = pg_pick(R.off, lane);
+        const int n = pg_pick(R.n, lane);
+        const int q = pg_search(p.ot, off, 0, n, i, false);
+        if (q < n && ldcg(p.ot + off + q) == i)
+            dis = ldcg(p.ow + off + q);
+        else
+            atomicOr(&p.ctl->flags, kPgErrRows);
     }
     const long long ooff = ldl(p.out_off + i);
     const int on = ldcg(p.out_n + i);
+    const long long woff = ldl(p.slot_woff + c);
+    const int wn = ldcg(p.slot_wn + c);
+    const int nrm = wn > 0 ? wn - 1 - j : 0;
+    int* code = p.wscr + woff + on + 8;
     unsigned long long rb = 0;
-    if (lane == 0) rb = atomicAdd(&p.ctl->rec_top, (unsigned long long)on);
-    rb = __shfl_sync(kFull, rb, 0);
-    if (rb + (unsigned long long)on > p.rec_cap) {
-        if (lane == 0) atomicOr(&p.ctl->flags, kPgErrPool);
-        return;
+    if (nrm > 0) {
+        if (lane == 0) rb = atomicAdd(&p.ctl->rec_top, (unsigned long long)nrm);
+        rb = __shfl_sync(kFull, rb, 0);
+        if (rb + (unsigned long long)nrm > p.rec_cap) {
+            if (lane == 0) atomicOr(&p.ctl->flags, kPgErrPool);
+            return;
+        }
     }
     // split the out-row: moved pairs to the record (in order), kept ones compacted in place
-    int nrm = 0, kn = 0;
+    int nm = 0, kn = 0;
     for (int b = 0; b < on; b += 32) {
         const int e = b + lane;
         const bool valid = e < on;
         const int v = valid ? ldcg(p.ot + ooff + e) : 0;
-        const unsigned d3 = valid ? ldcg(p.ow + ooff + e) : 0u;
-        unsigned miss = 0u;
-        const bool mv = valid && pg_moves(p, rt, j, v, miss);
+        const unsigned w = valid ? ldcg(p.ow + ooff + e) : 0u;
+        const int cd = valid ? ldcg(code + e) : 0;
+        const bool mv = (cd & kPgMoved) != 0;
         const bool kp = valid && !mv;
         const unsigned mm = __ballot_sync(kFull, mv), mk = __ballot_sync(kFull, kp);
         const unsigned lt = (1u << lane) - 1u;
         if (mv) {
-            const long long at = (long long)rb + nrm + __popc(mm & lt);
-            p.rt[at] = v;
-            p.rw[at] = d3;
-            p.rmiss[at] = (unsigned char)miss;
+            const int x = nm + __popc(mm & lt);
+            if (x < nrm) {
+                p.rt[rb + x] = v;
+                p.rw[rb + x] = w;
+                p.rmiss[rb + x] = (unsigned char)(cd & 0xff);
+            }
         }
         __syncwarp();  // every lane has read its pair before the compaction writes
         if (kp) {
             const long long at = ooff + kn + __popc(mk & lt);
             p.ot[at] = v;
-            p.ow[at] = d3;
+            p.ow[at] = w;
         }
-        nrm += __popc(mm);
+        nm += __popc(mm);
         kn += __popc(mk);
         __syncwarp();
     }
-    // in-rows of the moved targets, in out-row order: every root without the target gains
-    // it (a new entry or a revived one), and i dies in it (src/purn-ppr.cpp:196-236)
-    if (lane == 0) {
-        for (int k = 0; k < nrm; ++k) {
-            const int v = ldcg(p.rt + rb + k);
-            const unsigned miss = ldb(p.rmiss + rb + k);
-            for (int q = 0; q < j; ++q) {
-                if (!((miss >> q) & 1u)) continue;
-                const int r = rt[q];
-                long long off = ldl(p.in_off + v);
-                int n = ldcg(p.in_n + v);
-                const int at = pg_lower(p.is, off, n, r);
-                if (at < n && ldcg(p.is + off + at) == r) {
-                    if (!ldb(p.ia + off + at)) {
-                        p.ia[off + at] = 1;
-                        p.indeg[v] = ldcg(p.indeg + v) + 1;
-                    }
-                    continue;
-                }
-                if (n < ldcg(p.in_cap + v)) {  // room in place: shift the tail
-                    for (int x = n; x > at; --x) {
-                        p.is[off + x] = ldcg(p.is + off + x - 1);
-                        p.ia[off + x] = ldb(p.ia + off + x - 1);
-                    }
-                } else {  // a new block twice the size
-                    const int cap = 2 * n + 4;
-                    const unsigned long long nb = atomicAdd(&p.ctl->in_top, (unsigned long long)cap);
-                    if (nb + (unsigned long long)cap > p.in_pool_cap) {
-                        atomicOr(&p.ctl->flags, kPgErrPool);
-                        return;
-                    }
-                    const long long noff = (long long)nb;
-                    for (int x = 0; x < at; ++x) {
-                        p.is[noff + x] = ldcg(p.is + off + x);
-                        p.ia[noff + x] = ldb(p.ia + off + x);
-                    }
-                    for (int x = at; x < n; ++x) {
-                        p.is[noff + x + 1] = ldcg(p.is + off + x);
-                        p.ia[noff + x + 1] = ldb(p.ia + off + x);
-                    }
-                    off = noff;
-                    p.in_off[v] = noff;
-                    p.in_cap[v] = cap;
-                }
-                p.is[off + at] = r;
-                p.ia[off + at] = 1;
-                p.in_n[v] = n + 1;
-                p.indeg[v] = ldcg(p.indeg + v) + 1;
-            }
-            const long long off = ldl(p.in_off + v);
-            const int n = ldcg(p.in_n + v);
-            const int at = pg_lower(p.is, off, n, i);
-            if (at >= n || ldcg(p.is + off + at) != i) {
-                atomicOr(&p.ctl->flags, kPgErrRows);
-                return;
-            }
-            p.indeg[v] = ldcg(p.indeg + v) - 1;
-            p.ia[off + at] = 0;
-        }
+    if (nm != nrm) {
+        if (lane == 0) atomicOr(&p.ctl->flags, kPgErrRows);
+        return;
     }
-    // the moved pairs merge into every root's sorted row, one lane per root
-    if (nrm > 0 && lane < j) {
-        const int r = rt[lane];
-        const double dk = (double)__uint_as_float(dis[lane]);
-        const long long off = ldl(p.out_off + r);
-        const int n = ldcg(p.out_n + r);
-        const unsigned long long nb = atomicAdd(&p.ctl->out_top, (unsigned long long)(n + nrm));
-        if (nb + (unsigned long long)(n + nrm) > p.out_cap) {
-            atomicOr(&p.ctl->flags, kPgErrPool);
-        } else {
-            const long long noff = (long long)nb;
-            int a = 0, b = 0, m = 0;
-            while (a < n || b < nrm) {
-                const int ta = a < n ? ldcg(p.ot + off + a) : 0;
-                const int tb = b < nrm ? ldcg(p.rt + rb + b) : 0;
-                if (a < n && (b == nrm || ta < tb)) {
-                    p.ot[noff + m] = ta;
-                    p.ow[noff + m] = ldcg(p.ow + off + a);
-                    ++a;
-                } else if (a < n && ta == tb) {  // (double)old + (w * keep) * w', to float
+    // in-rows of the moved targets: one lane per run of equal targets
+    for (int b0 = 0; b0 < nrm; b0 += 32) {
+        const int b = b0 + lane;
+        if (b >= nrm) continue;
+        const int v = ldcg(p.rt + rb + b);
+        if (b > 0 && ldcg(p.rt + rb + b - 1) == v) continue;
+        int cnt = 1;
+        while (b + cnt < nrm && ldcg(p.rt + rb + b + cnt) == v) ++cnt;
+        pg_in_update(p, R, i, v, ldb(p.rmiss + rb + b), cnt, par);
+    }
+    __syncwarp();
+    // the moved pairs merge into every root's sorted row (the codes' space holds, per moved
+    // pair, its insertion point in the root's row, or -1 when it adds to an existing pair)
+    for (int k = 0; k < j && nrm > 0; ++k) {
+        const int r = pg_pick(R.r, k);
+        const long long aoff = pg_pick(R.off, k);
+        const int an = pg_pick(R.n, k);
+        const double dk = (double)__uint_as_float((unsigned)__shfl_sync(kFull, (int)dis, k));
+        int nnew = 0, run = 0;
+        for (int b0 = 0; b0 < nrm; b0 += 32) {
+            const int b = b0 + lane;
+            const bool valid = b < nrm;
+            const int tb = valid ? ldcg(p.rt + rb + b) : 0;
+            const bool st = valid && (b == 0 || ldcg(p.rt + rb + b - 1) != tb);
+            const unsigned sm = __ballot_sync(kFull, st) & ((2u << lane) - 1u);
+            const int rs = sm ? b0 + 31 - __clz(sm) : run;  // where this pair's run of equal targets starts
+            run = __shfl_sync(kFull, rs, 31);
+            int ins = -1;
+            if (valid) {
+                const int lb = pg_search(p.ot, aoff, 0, an, tb, false);
+                const int q = lb + (b - rs);  // the reference pairs a run's k-th pair with the row's k-th
+                if (q < an && ldcg(p.ot + aoff + q) == tb) {  // (double)old + (w * keep) * w', to float
                     const double f = __dmul_rn(__dmul_rn((double)__uint_as_float(ldcg(p.rw + rb + b)), p.keep), dk);
-                    p.ot[noff + m] = ta;
-                    p.ow[noff + m] =
-                        __float_as_uint(__double2float_rn(__dadd_rn((double)__uint_as_float(ldcg(p.ow + off + a)), f)));
-                    ++a;
-                    ++b;
-                } else {  // a new pair: (w * keep) * w', to float
-                    const double f = __dmul_rn(__dmul_rn((double)__uint_as_float(ldcg(p.rw + rb + b)), p.keep), dk);
-                    p.ot[noff + m] = tb;
-                    p.ow[noff + m] = __float_as_uint(__double2float_rn(f));
-                    ++b;
+                    p.ow[aoff + q] = __float_as_uint(
+                        __double2float_rn(__dadd_rn((double)__uint_as_float(ldcg(p.ow + aoff + q)), f)));
+                } else {
+                    ins = pg_search(p.ot, aoff, lb, an, tb, true);
                 }
-                ++m;
+                code[b] = ins;
             }
-            p.out_off[r] = noff;
-            p.out_n[r] = m;
+            nnew += __popc(__ballot_sync(kFull, ins >= 0));
         }
+        if (nnew == 0) continue;  // every pair added to an existing one, in place
+        __syncwarp();
+        unsigned long long nb = 0;
+        if (lane == 0) nb = atomicAdd(&p.ctl->out_top, (unsigned long long)(an + nnew));
+        nb = __shfl_sync(kFull, nb, 0);
+        if (nb + (unsigned long long)(an + nnew) > p.out_cap) {
+            if (lane == 0) atomicOr(&p.ctl->flags, kPgErrPool);
+            return;
+        }
+        const long long nbo = (long long)nb;
+        int s0 = 0, last = 0;
+        for (int b0 = 0; b0 < nrm; b0 += 32) {
+            const int b = b0 + lane;
+            const int ins = b < nrm ? ldcg(code + b) : -1;
+            const unsigned nwm = __ballot_sync(kFull, ins >= 0);
+            const unsigned below = nwm & ((1u << lane) - 1u);
+            const int pl = below ? 31 - __clz(below) : 0;
+            const int pin = __shfl_sync(kFull, ins, pl);
+            if (ins >= 0) {  // a new pair: (w * keep) * w', to float, after the row's segment before it
+                const int s = s0 + __popc(below);
+                const int prev = below ? pin : last;
+                pg_emit(p, par, 0, aoff + prev, nbo + prev + s, ins - prev);
+                const double f = __dmul_rn(__dmul_rn((double)__uint_as_float(ldcg(p.rw + rb + b)), p.keep), dk);
+                p.ot[nbo + ins + s] = ldcg(p.rt + rb + b);
+                p.ow[nbo + ins + s] = __float_as_uint(__double2float_rn(f));
+            }
+            if (nwm) last = __shfl_sync(kFull, ins, 31 - __clz(nwm));
+            s0 += __popc(nwm);
+        }
+        if (lane == 0) {
+            pg_emit(p, par, 0, aoff + last, nbo + last + nnew, an - last);
+            p.out_off[r] = nbo;
+            p.out_n[r] = an + nnew;
+        }
+        __syncwarp();
     }
     if (lane == 0) {
         p.out_n[i] = kn;
         p.rec_off[i] = (long long)rb;
         p.rec_n[i] = nrm;
+    }
+}
+
+// The queued copies of this round, one task per warp at a time.
+__device__ __forceinline__ void pg_copy(const PgParams& p, int par, int gwarp, int nwarps, int lane) {
+    const unsigned long long nt = min(ldcg(&p.ctl->task_top[par]), p.task_cap);
+    for (unsigned long long t = (unsigned long long)gwarp; t < nt; t += (unsigned long long)nwarps) {
+        const PgTask* tk = p.task + t;
+        const long long src = ldl(&tk->src), dst = ldl(&tk->dst);
+        const int len = ldcg(&tk->len), kind = ldcg(&tk->kind);
+        if (kind == 0) {
+#pragma unroll 4
+            for (int x = lane; x < len; x += 32) {
+                p.ot[dst + x] = ldcg(p.ot + src + x);
+                p.ow[dst + x] = ldcg(p.ow + src + x);
+            }
+        } else {
+#pragma unroll 4
+            for (int x = lane; x < len; x += 32) {
+                p.is[dst + x] = ldcg(p.is + src + x);
+                p.ia[dst + x] = ldb(p.ia + src + x);
+            }
+        }
     }
 }
 
@@ -396,6 +596,7 @@ __global__ void __launch_bounds__(kPgThreads) prune_ppr_rounds(const PgParams p)
     const int gwarp = (int)(gtid >> 5), nwarps = (int)((gridDim.x * blockDim.x) >> 5);
     for (int guard = 0; guard < p.max_rounds; ++guard) {
         const int pos = ldcg(&ctl->pos), round = ldcg(&ctl->round);
+        const int par = round & 1;
         // plan and reserve
         for (int c = gwarp; c < p.span; c += nwarps) {
             const int i = pos + c;
@@ -437,15 +638,18 @@ __global__ void __launch_bounds__(kPgThreads) prune_ppr_rounds(const PgParams p)
         if (!grid_sync(bar, flags, p.barrier_ns)) return;
         // commit
         const int dmin = ldcg(&ctl->dmin);
-        for (int c = gwarp; c < p.span; c += nwarps) {
-            const int i = pos + c;
-            if (i >= p.V || i > dmin) break;
-            if (ldcg(p.slot_rn + c) < 0 || !ldb(p.slot_pass + c)) continue;
-            if (pg_prunes(p, i)) pg_visit(p, i, lane);
-            if (lane == 0) p.done[i] = 1;
+        if (!(ldcg(flags) & (kPgErrPool | kPgErrRows))) {
+            for (int c = gwarp; c < p.span; c += nwarps) {
+                const int i = pos + c;
+                if (i >= p.V || i > dmin) break;
+                if (ldcg(p.slot_rn + c) < 0 || !ldb(p.slot_pass + c)) continue;
+                if (pg_prunes(p, i)) pg_visit(p, i, c, par, lane);
+                if (lane == 0) p.done[i] = 1;
+            }
         }
         if (!grid_sync(bar, flags, p.barrier_ns)) return;
-        // next window
+        // the queued copies; the next window
+        pg_copy(p, par, gwarp, nwarps, lane);
         if (gtid < 32) {
             int q = pos;
             for (;;) {
@@ -464,6 +668,7 @@ __global__ void __launch_bounds__(kPgThreads) prune_ppr_rounds(const PgParams p)
                 ctl->dmin = p.V;
                 ctl->round = round + 1;
                 ctl->wscr_top = 0ull;
+                ctl->task_top[par ^ 1] = 0ull;
                 if (q >= p.V) ctl->finished = 1;
             }
         }
@@ -526,14 +731,22 @@ static int prune_ppr_device_dir(const std::string& dir, double keep, int device,
     if (per_sm < 1) return fail(C2G_ERR_CUDA, "pruner kernel cannot be resident");
     const size_t E0 = ot.size(), I0 = is.size();
     const int span = 8192;
-    // pools: the rows a merge or an in-row growth writes anew take fresh blocks
+    // Pools: a row that gains entries takes a fresh block, so a pool holds every version of
+    // its rows.  At R-MAT scale 20 / 22 the blocks taken add up to about 21 / 29 times the
+    // original out-pairs and 22 / 33 times the original in-entries; give each 64 times, within
+    // 60% of the free memory.
     size_t free_b = 0, total_b = 0;
     C2G_CUDA(cudaMemGetInfo(&free_b, &total_b));
-    const size_t want_out = E0 * 48 + (1u << 20);
-    const size_t out_cap = std::min(want_out, (size_t)(0.45 * (double)free_b) / 8);
-    const size_t in_cap_pool = I0 * 8 + (1u << 20);
+    size_t out_cap = E0 * 64 + (1u << 20), in_cap_pool = I0 * 64 + (1u << 20);
+    const double want = 8.0 * (double)out_cap + 5.0 * (double)in_cap_pool, room = 0.6 * (double)free_b;
+    if (want > room) {
+        out_cap = (size_t)((double)out_cap * room / want);
+        in_cap_pool = (size_t)((double)in_cap_pool * room / want);
+    }
+    if (out_cap < E0 || in_cap_pool < I0) return fail(C2G_ERR_OOM, "pruner: not enough device memory for the row pools");
     const size_t rec_cap = E0 * 6 + (1u << 20);
-    const size_t wscr_cap = E0 * 2 + (size_t)span * 16;
+    const size_t wscr_cap = E0 * 4 + (size_t)span * 16;
+    const size_t task_cap = (size_t)1 << 22;
     DevBuf db;
     PgParams p;
     std::memset(&p, 0, sizeof(p));
@@ -547,7 +760,6 @@ static int prune_ppr_device_dir(const std::string& dir, double keep, int device,
     if (e == cudaSuccess) e = db.get(&p.ow, out_cap);
     if (e == cudaSuccess) e = db.get(&p.in_off, (size_t)V);
     if (e == cudaSuccess) e = db.get(&p.in_n, (size_t)V);
-    if (e == cudaSuccess) e = db.get(&p.in_cap, (size_t)V);
     if (e == cudaSuccess) e = db.get(&p.is, in_cap_pool);
     if (e == cudaSuccess) e = db.get(&p.ia, in_cap_pool);
     if (e == cudaSuccess) e = db.get(&p.indeg, (size_t)V);
@@ -566,32 +778,28 @@ static int prune_ppr_device_dir(const std::string& dir, double keep, int device,
     if (e == cudaSuccess) e = db.get(&p.slot_wn, (size_t)span);
     if (e == cudaSuccess) e = db.get(&p.slot_pass, (size_t)span);
     if (e == cudaSuccess) e = db.get(&p.wscr, wscr_cap);
+    if (e == cudaSuccess) e = db.get(&p.task, task_cap);
     if (e == cudaSuccess) e = db.get(&p.ctl, 1);
     C2G_CUDA(e);
     p.out_cap = out_cap;
     p.in_pool_cap = in_cap_pool;
     p.rec_cap = rec_cap;
     p.wscr_cap = wscr_cap;
+    p.task_cap = task_cap;
     p.barrier_ns = 20000000000ull;
     p.max_rounds = V + 16;
-    // the initial rows: in-rows get room for two insertions each before they move
+    // the initial rows
     {
         std::vector<long long> oo((size_t)V), io((size_t)V);
-        std::vector<int> on((size_t)V), in_n((size_t)V), ic((size_t)V), deg((size_t)V);
-        std::vector<int32_t> is2(in_cap_pool < I0 + 2 * (size_t)V ? 0 : I0 + 2 * (size_t)V);
-        if (is2.empty()) return fail(C2G_ERR_RANGE, "pruner: in-row pool too small");
-        long long at = 0;
+        std::vector<int> on((size_t)V), in_n((size_t)V);
         for (int32_t v = 0; v < V; ++v) {
             oo[v] = orow[v];
             on[v] = orow[v + 1] - orow[v];
+            io[v] = irow[v];
             in_n[v] = irow[v + 1] - irow[v];
-            deg[v] = in_n[v];
-            io[v] = at;
-            ic[v] = in_n[v] + 2;
-            std::copy(is.begin() + irow[v], is.begin() + irow[v + 1], is2.begin() + at);
-            at += ic[v];
         }
-        std::vector<unsigned char> alive((size_t)at, 1);
+        const size_t at = I0;
+        std::vector<unsigned char> alive(at, 1);
         PgCtl c;
         std::memset(&c, 0, sizeof(c));
         c.out_top = E0;
@@ -603,15 +811,14 @@ static int prune_ppr_device_dir(const std::string& dir, double keep, int device,
             C2G_CUDA(cudaMemcpy(p.ow, ow.data(), sizeof(uint32_t) * E0, cudaMemcpyHostToDevice));
         }
         if (at) {
-            C2G_CUDA(cudaMemcpy(p.is, is2.data(), sizeof(int32_t) * (size_t)at, cudaMemcpyHostToDevice));
-            C2G_CUDA(cudaMemcpy(p.ia, alive.data(), (size_t)at, cudaMemcpyHostToDevice));
+            C2G_CUDA(cudaMemcpy(p.is, is.data(), sizeof(int32_t) * at, cudaMemcpyHostToDevice));
+            C2G_CUDA(cudaMemcpy(p.ia, alive.data(), at, cudaMemcpyHostToDevice));
         }
         C2G_CUDA(cudaMemcpy(p.out_off, oo.data(), sizeof(long long) * (size_t)V, cudaMemcpyHostToDevice));
         C2G_CUDA(cudaMemcpy(p.out_n, on.data(), sizeof(int) * (size_t)V, cudaMemcpyHostToDevice));
         C2G_CUDA(cudaMemcpy(p.in_off, io.data(), sizeof(long long) * (size_t)V, cudaMemcpyHostToDevice));
         C2G_CUDA(cudaMemcpy(p.in_n, in_n.data(), sizeof(int) * (size_t)V, cudaMemcpyHostToDevice));
-        C2G_CUDA(cudaMemcpy(p.in_cap, ic.data(), sizeof(int) * (size_t)V, cudaMemcpyHostToDevice));
-        C2G_CUDA(cudaMemcpy(p.indeg, deg.data(), sizeof(int) * (size_t)V, cudaMemcpyHostToDevice));
+        C2G_CUDA(cudaMemcpy(p.indeg, in_n.data(), sizeof(int) * (size_t)V, cudaMemcpyHostToDevice));
         C2G_CUDA(cudaMemset(p.rec_n, 0, sizeof(int) * (size_t)V));
         C2G_CUDA(cudaMemset(p.rec_off, 0, sizeof(long long) * (size_t)V));
         C2G_CUDA(cudaMemset(p.done, 0, (size_t)V));
