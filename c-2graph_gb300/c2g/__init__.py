@@ -155,7 +155,8 @@ SIGNATURES = {
     "c2g_prune_ppr": (ctypes.c_int, [ctypes.c_char_p]),
     "c2g_prune_ppr_alpha": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_double]),
     "c2g_prune_ppr_device": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_double, ctypes.c_int,
-                                            ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_int32)]),
+                                            ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_int32),
+                                            ctypes.c_void_p]),
 }
 
 
@@ -212,12 +213,17 @@ def prune_ppr(dir, alpha=None):
         _check(lib().c2g_prune_ppr_alpha(os.fsencode(dir), float(alpha)))
 
 
-def prune_ppr_device(dir, alpha=0.2, device=0):
-    """purn-ppr on the GPU (same files as prune_ppr(dir, alpha)).  Returns (kernel ms, rounds)."""
+def prune_ppr_device(dir, alpha=0.2, device=0, phases=False):
+    """purn-ppr on the GPU (same files as prune_ppr(dir, alpha)).  Returns (kernel ms, rounds),
+    and with phases=True also the kernel ms of the rounds' plan, check, disturb, commit and copy
+    phases."""
     ms = ctypes.c_float(0.0)
     rounds = ctypes.c_int32(0)
+    ph = np.zeros(5, np.int64)
     _check(lib().c2g_prune_ppr_device(os.fsencode(dir), float(alpha), int(device), ctypes.byref(ms),
-                                      ctypes.byref(rounds)))
+                                      ctypes.byref(rounds), ph.ctypes.data))
+    if phases:
+        return float(ms.value), int(rounds.value), [float(x) / 1e6 for x in ph]
     return float(ms.value), int(rounds.value)
 
 

@@ -24,7 +24,8 @@
 // as CUDA_ERROR's exit(-1) does (core/Util.cuh:17-24).
 //
 // Environment: C2G_SEEDS=exact makes sssp-purn use the record->vertex sidecar instead
-// of the reference's vertex-indexed hvlist read.
+// of the reference's vertex-indexed hvlist read.  C2G_PRUNE_GPU=<device> makes purn-ppr
+// run its visits on that GPU (c2g_prune_ppr_device: the same files, byte for byte).
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
@@ -159,7 +160,12 @@ static int run_ppr(const char* dir, int32_t source, bool pruned, bool adsorption
 
 static int run_prune(const char* dir, bool ppr) {
     auto t0 = std::chrono::steady_clock::now();
-    int rc = ppr ? c2g_prune_ppr(dir) : c2g_prune_sssp(dir);
+    const char* gpu = getenv("C2G_PRUNE_GPU");
+    int rc;
+    if (ppr && gpu && *gpu)  // alpha 0.2: the reference's baked factor 0.8 (1 - 0.2 is the same double)
+        rc = c2g_prune_ppr_device(dir, 0.2, atoi(gpu), nullptr, nullptr, nullptr);
+    else
+        rc = ppr ? c2g_prune_ppr(dir) : c2g_prune_sssp(dir);
     if (rc) die(rc);
     const double s = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     fprintf(stderr, "Filter time : %.4f(s)\n", s);

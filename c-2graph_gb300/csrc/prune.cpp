@@ -15,9 +15,12 @@
 #include <algorithm>
 #include <cstring>
 #include <cstdint>
+#include <memory>
 #include <string>
 #include <utility>
 #include <vector>
+
+#include <omp.h>
 
 #include "../../include/c2graph.h"
 #include "host_io.h"
@@ -234,11 +237,16 @@ void flatten(const Adj<W>& out, int32_t V, std::vector<int32_t>& vlist, std::vec
 
 }  // namespace
 
-// The rows purn-ppr starts from, flat, for the device pruner (prune_gpu.cu): out-rows of
-// distinct (target, weight bits) pairs without self-loops, sorted; in-rows of the distinct
-// sources, sorted.  orow / irow are row pointers over V + 1 entries.
+// The rows purn-ppr starts from, flat, for the device pruner (prune_gpu.cu): the rows
+// build_out and build_in make (out-rows: the (target, weight) pairs without self-loops,
+// sorted as pair<int32, float> and without repeated pairs; in-rows: the distinct sources of
+// each vertex, ascending), built without one allocation per row.  Input rows that are
+// already strictly increasing and free of self-loops (the R-MAT writer's) are the out-rows
+// as they are; other rows are sorted in parallel.  The in-rows are a stable counting sort
+// of the out-rows by target, each thread filling its own range of sources.  orow / irow are
+// row pointers over V + 1 entries.
 int prune_ppr_initial_rows(const std::string& dir, int32_t& V, std::vector<int32_t>& orow, std::vector<int32_t>& ot,
-                           std::vector<uint32_t>& ow, std::vector<int32_t>& irow, std::vector<int32_t>& is) {
+                           std::vector<float>& ow, std::vector<int32_t>& irow, std::vector<int32_t>& is) {
     std::vector<int32_t> vlist, elist;
     std::vector<float> flist;
     int rc;
@@ -248,28 +256,78 @@ int prune_ppr_initial_rows(const std::string& dir, int32_t& V, std::vector<int32
     if ((rc = check_csr(vlist, elist))) return rc;
     if (flist.size() < elist.size()) return fail(C2G_ERR_FORMAT, "flist shorter than elist");
     V = (int32_t)vlist.size() - 1;
-    Adj<float> out;
-    InAdj in;
-    build_out(vlist, elist, flist, V, out);
-    build_in(vlist, elist, V, in);
-    orow.assign((size_t)V + 1, 0);
-    irow.assign((size_t)V + 1, 0);
-    for (int32_t v = 0; v < V; ++v) {
-        orow[v + 1] = orow[v] + (int32_t)out[v].size();
-        irow[v + 1] = irow[v] + (int32_t)in[v].size();
-    }
-    ot.resize((size_t)orow[V]);
-    ow.resize((size_t)orow[V]);
-    is.resize((size_t)irow[V]);
-    for (int32_t v = 0; v < V; ++v) {
-        size_t k = (size_t)orow[v];
-        for (const auto& e : out[v]) {
-            ot[k] = e.first;
-            std::memcpy(&ow[k], &e.second, 4);
-            ++k;
+    int plain = 1;
+#pragma omp parallel for schedule(dynamic, 4096) reduction(& : plain)
+    for (int32_t v = 0; v < V; ++v)
+        for (int32_t e = vlist[v]; e < vlist[v + 1]; ++e)
+            if (elist[e] == v || (e > vlist[v] && elist[e] <= elist[e - 1])) plain = 0;
+    if (plain) {
+        orow = vlist;
+        flist.resize(elist.size());
+        ot = std::move(elist);
+        ow = std::move(flist);
+    } else {
+        std::vector<std::pair<int32_t, float>> pr(elist.size());
+        std::vector<int32_t> cnt((size_t)V, 0);
+#pragma omp parallel for schedule(dynamic, 4096)
+        for (int32_t v = 0; v < V; ++v) {
+            auto* row = pr.data() + vlist[v];
+            int32_t k = 0;
+            for (int32_t e = vlist[v]; e < vlist[v + 1]; ++e)
+                if (elist[e] != v) row[k++] = std::make_pair(elist[e], flist[e]);
+            std::sort(row, row + k);
+            cnt[v] = (int32_t)(std::unique(row, row + k) - row);
         }
-        k = (size_t)irow[v];
-        for (const auto& e : in[v]) is[k++] = e.first;
+        orow.assign((size_t)V + 1, 0);
+        for (int32_t v = 0; v < V; ++v) orow[v + 1] = orow[v] + cnt[v];
+        ot.resize((size_t)orow[V]);
+        ow.resize((size_t)orow[V]);
+#pragma omp parallel for schedule(dynamic, 4096)
+        for (int32_t v = 0; v < V; ++v) {
+            const auto* row = pr.data() + vlist[v];
+            for (int32_t x = 0; x < cnt[v]; ++x) {
+                ot[(size_t)orow[v] + x] = row[x].first;
+                ow[(size_t)orow[v] + x] = row[x].second;
+            }
+        }
+    }
+    // in-rows: thread t counts, then fills, the distinct targets of sources [V t / T, V (t+1) / T)
+    const int T = std::max(1, std::min(omp_get_max_threads(), 64));
+    std::unique_ptr<int32_t[]> c(new int32_t[(size_t)T * (size_t)V + 1]);
+    irow.assign((size_t)V + 1, 0);
+    auto distinct = [&](int32_t v, size_t x) { return x == (size_t)orow[v] || ot[x] != ot[x - 1]; };
+#pragma omp parallel num_threads(T)
+    {
+        const int t = omp_get_thread_num();
+        int32_t* ct = c.get() + (size_t)t * V;
+        std::fill(ct, ct + V, 0);
+        const int32_t v0 = (int32_t)((int64_t)V * t / T), v1 = (int32_t)((int64_t)V * (t + 1) / T);
+        for (int32_t v = v0; v < v1; ++v)
+            for (size_t x = (size_t)orow[v]; x < (size_t)orow[v + 1]; ++x)
+                if (distinct(v, x)) ++ct[ot[x]];
+#pragma omp barrier
+#pragma omp for schedule(static)
+        for (int32_t d = 0; d < V; ++d) {
+            int32_t n = 0;
+            for (int u = 0; u < T; ++u) n += c[(size_t)u * V + d];
+            irow[(size_t)d + 1] = n;
+        }
+#pragma omp single
+        for (int32_t d = 0; d < V; ++d) irow[(size_t)d + 1] += irow[d];
+#pragma omp for schedule(static)
+        for (int32_t d = 0; d < V; ++d) {
+            int32_t run = irow[d];
+            for (int u = 0; u < T; ++u) {
+                const int32_t k = c[(size_t)u * V + d];
+                c[(size_t)u * V + d] = run;
+                run += k;
+            }
+        }
+#pragma omp single
+        is.resize((size_t)irow[V]);
+        for (int32_t v = v0; v < v1; ++v)
+            for (size_t x = (size_t)orow[v]; x < (size_t)orow[v + 1]; ++x)
+                if (distinct(v, x)) is[(size_t)ct[ot[x]]++] = v;
     }
     return C2G_OK;
 }

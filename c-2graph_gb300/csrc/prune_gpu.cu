@@ -40,7 +40,7 @@
 namespace c2g {
 
 int prune_ppr_initial_rows(const std::string& dir, int32_t& V, std::vector<int32_t>& orow, std::vector<int32_t>& ot,
-                           std::vector<uint32_t>& ow, std::vector<int32_t>& irow, std::vector<int32_t>& is);
+                           std::vector<float>& ow, std::vector<int32_t>& irow, std::vector<int32_t>& is);
 
 constexpr int kPgThreads = 256;
 constexpr int kPgMaxRoots = 5;  // the in-degree bound of purn-ppr (src/purn-ppr.cpp:146-152)
@@ -58,6 +58,7 @@ struct PgCtl {
     int pad;
     unsigned long long out_top, in_top, rec_top, wscr_top;  // pool bump pointers
     unsigned long long task_top[2];                         // copy tasks, by round parity
+    unsigned long long phase_ns[5];  // block 0's time in plan, check, disturb, commit, copy (waits included)
 };
 
 struct PgTask {
@@ -256,7 +257,8 @@ __device__ __forceinline__ void pg_emit(const PgParams& p, int par, int kind, lo
 
 // Plan of candidate i (slot c): the rows it reads, the rows it would write, and per
 // out-edge whether it moves; reserve the rows.  The plan block in wscr holds the written
-// rows (at most on + 6) in [0, on + 8) and the out-edge codes in [on + 8, 2 on + 8).
+// rows (at most on + 6) in [0, on + 8) and the out-edge codes in [on + 8, 2 on + 8); the
+// commit reuses [on + 8, 7 on + 8) for the merges' scratch.
 __device__ __forceinline__ void pg_plan(const PgParams& p, int i, int c, int round, int lane) {
     const int V = p.V;
     int* Rw = p.slot_r + (size_t)c * kPgMaxR;
@@ -279,7 +281,7 @@ __device__ __forceinline__ void pg_plan(const PgParams& p, int i, int c, int rou
         rn = 2 + j;
         const long long off = ldl(p.out_off + i);
         const int on = ldcg(p.out_n + i);
-        const unsigned long long need = 2ull * (unsigned long long)on + 8ull;
+        const unsigned long long need = 7ull * (unsigned long long)on + 8ull;
         unsigned long long wb = 0;
         if (lane == 0) wb = atomicAdd(&p.ctl->wscr_top, need);
         wb = __shfl_sync(kFull, wb, 0);
@@ -490,43 +492,69 @@ __device__ __forceinline__ void pg_visit(const PgParams& p, int i, int c, int pa
         pg_in_update(p, R, i, v, ldb(p.rmiss + rb + b), cnt, par);
     }
     __syncwarp();
-    // the moved pairs merge into every root's sorted row (the codes' space holds, per moved
-    // pair, its insertion point in the root's row, or -1 when it adds to an existing pair)
-    for (int k = 0; k < j && nrm > 0; ++k) {
+    // The moved pairs merge into every root's sorted row.  Pass 1 takes every (root, pair)
+    // item at once: a pair whose target the row has (the k-th pair of a run of equal targets
+    // goes with the row's k-th pair of that target, as the reference's two-cursor merge pairs
+    // them) adds (w * keep) * w' to that pair in place, in double, rounded to float; a new
+    // one gets its insertion point.  The codes' space holds each pair's rank in its run, then
+    // the items' insertion points (-1: added in place).  Pass 2 moves each root's row that
+    // gains pairs to a new block.
+    int* kbs = code;
+    int* insp = code + nrm;
+    int run = 0;
+    for (int b0 = 0; b0 < nrm; b0 += 32) {
+        const int b = b0 + lane;
+        const bool valid = b < nrm;
+        const int tb = valid ? ldcg(p.rt + rb + b) : 0;
+        const bool st = valid && (b == 0 || ldcg(p.rt + rb + b - 1) != tb);
+        const unsigned sm = __ballot_sync(kFull, st) & ((2u << lane) - 1u);
+        const int rs = sm ? b0 + 31 - __clz(sm) : run;  // where this pair's run starts
+        run = __shfl_sync(kFull, rs, 31);
+        if (valid) kbs[b] = b - rs;
+    }
+    __syncwarp();
+    int nnew[kPgMaxRoots];
+#pragma unroll
+    for (int k = 0; k < kPgMaxRoots; ++k) nnew[k] = 0;
+    const int items = j * nrm;
+    for (int i0 = 0; i0 < items; i0 += 32) {
+        const int it = i0 + lane;
+        const bool valid = it < items;
+        const int k = valid ? it / nrm : 0;
+        const int b = valid ? it - k * nrm : 0;
+        const double dk = (double)__uint_as_float((unsigned)__shfl_sync(kFull, (int)dis, k));
+        int ins = -1;
+        if (valid) {
+            const long long aoff = pg_pick(R.off, k);
+            const int an = pg_pick(R.n, k);
+            const int tb = ldcg(p.rt + rb + b);
+            const int lb = pg_search(p.ot, aoff, 0, an, tb, false);
+            const int q = lb + ldcg(kbs + b);
+            if (q < an && ldcg(p.ot + aoff + q) == tb) {
+                const double f = __dmul_rn(__dmul_rn((double)__uint_as_float(ldcg(p.rw + rb + b)), p.keep), dk);
+                p.ow[aoff + q] = __float_as_uint(
+                    __double2float_rn(__dadd_rn((double)__uint_as_float(ldcg(p.ow + aoff + q)), f)));
+            } else {  // after the row's pairs with this target (fewer than this pair's rank)
+                ins = lb;
+                while (ins < an && ldcg(p.ot + aoff + ins) == tb) ++ins;
+            }
+            insp[it] = ins;
+        }
+#pragma unroll
+        for (int kk = 0; kk < kPgMaxRoots; ++kk) nnew[kk] += __popc(__ballot_sync(kFull, ins >= 0 && k == kk));
+    }
+    __syncwarp();
+    for (int k = 0; k < j; ++k) {
+        const int nk = pg_pick(nnew, k);
+        if (nk == 0) continue;  // every pair added to an existing one, in place
         const int r = pg_pick(R.r, k);
         const long long aoff = pg_pick(R.off, k);
         const int an = pg_pick(R.n, k);
         const double dk = (double)__uint_as_float((unsigned)__shfl_sync(kFull, (int)dis, k));
-        int nnew = 0, run = 0;
-        for (int b0 = 0; b0 < nrm; b0 += 32) {
-            const int b = b0 + lane;
-            const bool valid = b < nrm;
-            const int tb = valid ? ldcg(p.rt + rb + b) : 0;
-            const bool st = valid && (b == 0 || ldcg(p.rt + rb + b - 1) != tb);
-            const unsigned sm = __ballot_sync(kFull, st) & ((2u << lane) - 1u);
-            const int rs = sm ? b0 + 31 - __clz(sm) : run;  // where this pair's run of equal targets starts
-            run = __shfl_sync(kFull, rs, 31);
-            int ins = -1;
-            if (valid) {
-                const int lb = pg_search(p.ot, aoff, 0, an, tb, false);
-                const int q = lb + (b - rs);  // the reference pairs a run's k-th pair with the row's k-th
-                if (q < an && ldcg(p.ot + aoff + q) == tb) {  // (double)old + (w * keep) * w', to float
-                    const double f = __dmul_rn(__dmul_rn((double)__uint_as_float(ldcg(p.rw + rb + b)), p.keep), dk);
-                    p.ow[aoff + q] = __float_as_uint(
-                        __double2float_rn(__dadd_rn((double)__uint_as_float(ldcg(p.ow + aoff + q)), f)));
-                } else {
-                    ins = pg_search(p.ot, aoff, lb, an, tb, true);
-                }
-                code[b] = ins;
-            }
-            nnew += __popc(__ballot_sync(kFull, ins >= 0));
-        }
-        if (nnew == 0) continue;  // every pair added to an existing one, in place
-        __syncwarp();
         unsigned long long nb = 0;
-        if (lane == 0) nb = atomicAdd(&p.ctl->out_top, (unsigned long long)(an + nnew));
+        if (lane == 0) nb = atomicAdd(&p.ctl->out_top, (unsigned long long)(an + nk));
         nb = __shfl_sync(kFull, nb, 0);
-        if (nb + (unsigned long long)(an + nnew) > p.out_cap) {
+        if (nb + (unsigned long long)(an + nk) > p.out_cap) {
             if (lane == 0) atomicOr(&p.ctl->flags, kPgErrPool);
             return;
         }
@@ -534,7 +562,7 @@ __device__ __forceinline__ void pg_visit(const PgParams& p, int i, int c, int pa
         int s0 = 0, last = 0;
         for (int b0 = 0; b0 < nrm; b0 += 32) {
             const int b = b0 + lane;
-            const int ins = b < nrm ? ldcg(code + b) : -1;
+            const int ins = b < nrm ? ldcg(insp + k * nrm + b) : -1;
             const unsigned nwm = __ballot_sync(kFull, ins >= 0);
             const unsigned below = nwm & ((1u << lane) - 1u);
             const int pl = below ? 31 - __clz(below) : 0;
@@ -551,9 +579,9 @@ __device__ __forceinline__ void pg_visit(const PgParams& p, int i, int c, int pa
             s0 += __popc(nwm);
         }
         if (lane == 0) {
-            pg_emit(p, par, 0, aoff + last, nbo + last + nnew, an - last);
+            pg_emit(p, par, 0, aoff + last, nbo + last + nk, an - last);
             p.out_off[r] = nbo;
-            p.out_n[r] = an + nnew;
+            p.out_n[r] = an + nk;
         }
         __syncwarp();
     }
@@ -571,29 +599,57 @@ __device__ __forceinline__ void pg_copy(const PgParams& p, int par, int gwarp, i
         const PgTask* tk = p.task + t;
         const long long src = ldl(&tk->src), dst = ldl(&tk->dst);
         const int len = ldcg(&tk->len), kind = ldcg(&tk->kind);
-        if (kind == 0) {
-#pragma unroll 4
-            for (int x = lane; x < len; x += 32) {
-                p.ot[dst + x] = ldcg(p.ot + src + x);
-                p.ow[dst + x] = ldcg(p.ow + src + x);
-            }
-        } else {
-#pragma unroll 4
-            for (int x = lane; x < len; x += 32) {
-                p.is[dst + x] = ldcg(p.is + src + x);
-                p.ia[dst + x] = ldb(p.ia + src + x);
+        // a task's source and destination never overlap: each lane loads its share of 256
+        // entries before it stores any
+        constexpr int kU = 8;
+        for (int x0 = 0; x0 < len; x0 += 32 * kU) {
+            if (kind == 0) {
+                int tv[kU];
+                unsigned wv[kU];
+#pragma unroll
+                for (int u = 0; u < kU; ++u) {
+                    const int x = x0 + u * 32 + lane;
+                    tv[u] = x < len ? ldcg(p.ot + src + x) : 0;
+                    wv[u] = x < len ? ldcg(p.ow + src + x) : 0u;
+                }
+#pragma unroll
+                for (int u = 0; u < kU; ++u) {
+                    const int x = x0 + u * 32 + lane;
+                    if (x < len) {
+                        p.ot[dst + x] = tv[u];
+                        p.ow[dst + x] = wv[u];
+                    }
+                }
+            } else {
+                int sv[kU];
+                unsigned char av[kU];
+#pragma unroll
+                for (int u = 0; u < kU; ++u) {
+                    const int x = x0 + u * 32 + lane;
+                    sv[u] = x < len ? ldcg(p.is + src + x) : 0;
+                    av[u] = x < len ? ldb(p.ia + src + x) : (unsigned char)0;
+                }
+#pragma unroll
+                for (int u = 0; u < kU; ++u) {
+                    const int x = x0 + u * 32 + lane;
+                    if (x < len) {
+                        p.is[dst + x] = sv[u];
+                        p.ia[dst + x] = av[u];
+                    }
+                }
             }
         }
     }
 }
 
-__global__ void __launch_bounds__(kPgThreads) prune_ppr_rounds(const PgParams p) {
+__global__ void __launch_bounds__(kPgThreads, 3) prune_ppr_rounds(const PgParams p) {
     PgCtl* ctl = p.ctl;
     GridBarrier* bar = reinterpret_cast<GridBarrier*>(&ctl->bar_count);
     int* flags = &ctl->flags;
     const int lane = threadIdx.x & 31;
     const unsigned gtid = blockIdx.x * blockDim.x + threadIdx.x;
     const int gwarp = (int)(gtid >> 5), nwarps = (int)((gridDim.x * blockDim.x) >> 5);
+    unsigned long long tmark = globaltimer_ns();
     for (int guard = 0; guard < p.max_rounds; ++guard) {
         const int pos = ldcg(&ctl->pos), round = ldcg(&ctl->round);
         const int par = round & 1;
@@ -608,6 +664,7 @@ __global__ void __launch_bounds__(kPgThreads) prune_ppr_rounds(const PgParams p)
             pg_plan(p, i, c, round, lane);
         }
         if (!grid_sync(bar, flags, p.barrier_ns)) return;
+        phase_mark(ctl->phase_ns, tmark, 0);
         // check: the passers mark the rows they write
         for (int c = gwarp; c < p.span; c += nwarps) {
             const int i = pos + c;
@@ -626,6 +683,7 @@ __global__ void __launch_bounds__(kPgThreads) prune_ppr_rounds(const PgParams p)
                 for (int k = lane; k < wn; k += 32) p.wmark[ldcg(p.wscr + woff + k)] = round;
         }
         if (!grid_sync(bar, flags, p.barrier_ns)) return;
+        phase_mark(ctl->phase_ns, tmark, 1);
         // a failed candidate whose reads a passer writes holds back the ones after it
         for (int c = gwarp; c < p.span; c += nwarps) {
             const int i = pos + c;
@@ -636,6 +694,7 @@ __global__ void __launch_bounds__(kPgThreads) prune_ppr_rounds(const PgParams p)
             if (__any_sync(kFull, hit) && lane == 0) atomicMin(&ctl->dmin, i);
         }
         if (!grid_sync(bar, flags, p.barrier_ns)) return;
+        phase_mark(ctl->phase_ns, tmark, 2);
         // commit
         const int dmin = ldcg(&ctl->dmin);
         if (!(ldcg(flags) & (kPgErrPool | kPgErrRows))) {
@@ -648,6 +707,7 @@ __global__ void __launch_bounds__(kPgThreads) prune_ppr_rounds(const PgParams p)
             }
         }
         if (!grid_sync(bar, flags, p.barrier_ns)) return;
+        phase_mark(ctl->phase_ns, tmark, 3);
         // the queued copies; the next window
         pg_copy(p, par, gwarp, nwarps, lane);
         if (gtid < 32) {
@@ -673,6 +733,7 @@ __global__ void __launch_bounds__(kPgThreads) prune_ppr_rounds(const PgParams p)
             }
         }
         if (!grid_sync(bar, flags, p.barrier_ns)) return;
+        phase_mark(ctl->phase_ns, tmark, 4);
         if (ldcg(&ctl->finished) || (ldcg(flags) & (kPgErrPool | kPgErrRows))) return;
     }
     if (gtid == 0) atomicOr(flags, C2G_FLAG_ITER_CAP);
@@ -708,10 +769,11 @@ struct DevBuf {
     }
 };
 
-static int prune_ppr_device_dir(const std::string& dir, double keep, int device, float* ms, int* rounds) {
+static int prune_ppr_device_dir(const std::string& dir, double keep, int device, float* ms, int* rounds,
+                                int64_t* phase_ns) {
     int32_t V = 0;
     std::vector<int32_t> orow, ot, irow, is;
-    std::vector<uint32_t> ow;
+    std::vector<float> ow;
     int rc = prune_ppr_initial_rows(dir, V, orow, ot, ow, irow, is);
     if (rc) return rc;
     int prev = -1;
@@ -745,7 +807,7 @@ static int prune_ppr_device_dir(const std::string& dir, double keep, int device,
     }
     if (out_cap < E0 || in_cap_pool < I0) return fail(C2G_ERR_OOM, "pruner: not enough device memory for the row pools");
     const size_t rec_cap = E0 * 6 + (1u << 20);
-    const size_t wscr_cap = E0 * 4 + (size_t)span * 16;
+    const size_t wscr_cap = E0 * 16 + (size_t)span * 64;
     const size_t task_cap = (size_t)1 << 22;
     DevBuf db;
     PgParams p;
@@ -846,6 +908,8 @@ static int prune_ppr_device_dir(const std::string& dir, double keep, int device,
     C2G_CUDA(cudaMemcpy(&c, p.ctl, sizeof(c), cudaMemcpyDeviceToHost));
     if (ms) *ms = t;
     if (rounds) *rounds = c.round - 1;
+    if (phase_ns)
+        for (int k = 0; k < 5; ++k) phase_ns[k] = (int64_t)c.phase_ns[k];
     if (c.flags & kPgErrPool) return fail(C2G_ERR_OVERFLOW, "pruner: a row pool ran out");
     if (c.flags & kPgErrRows) return fail(C2G_ERR_FORMAT, "pruner: in-row and out-rows disagree");
     if (c.flags & (C2G_FLAG_BARRIER_TIMEOUT | C2G_FLAG_ITER_CAP) || (V > 0 && !c.finished))
@@ -863,52 +927,64 @@ static int prune_ppr_device_dir(const std::string& dir, double keep, int device,
         hv[v + 1] = hv[v] + rn[v];
     }
     const size_t E = (size_t)pv[V], H = (size_t)hv[V];
-    std::vector<int32_t> pe(E), he(H);
-    std::vector<uint32_t> pw(E), hw(H);
-    {
-        DevBuf tmp;
-        long long *dob = nullptr, *drb = nullptr;
-        int *dpe = nullptr, *dhe = nullptr;
-        unsigned *dpw = nullptr, *dhw = nullptr;
-        e = tmp.get(&dob, (size_t)V);
-        if (e == cudaSuccess) e = tmp.get(&drb, (size_t)V);
-        if (e == cudaSuccess) e = tmp.get(&dpe, E);
-        if (e == cudaSuccess) e = tmp.get(&dpw, E);
-        if (e == cudaSuccess) e = tmp.get(&dhe, H);
-        if (e == cudaSuccess) e = tmp.get(&dhw, H);
-        C2G_CUDA(e);
-        C2G_CUDA(cudaMemcpy(dob, ob.data(), sizeof(long long) * (size_t)V, cudaMemcpyHostToDevice));
-        C2G_CUDA(cudaMemcpy(drb, rbase.data(), sizeof(long long) * (size_t)V, cudaMemcpyHostToDevice));
-        if (V > 0) {
-            pg_gather_rows<<<sms * 8, 256>>>(p.out_off, p.out_n, dob, V, p.ot, p.ow, dpe, dpw);
-            pg_gather_rows<<<sms * 8, 256>>>(p.rec_off, p.rec_n, drb, V, p.rt, p.rw, dhe, dhw);
-            C2G_CUDA(cudaGetLastError());
-        }
-        C2G_CUDA(cudaDeviceSynchronize());
-        if (E) {
-            C2G_CUDA(cudaMemcpy(pe.data(), dpe, sizeof(int32_t) * E, cudaMemcpyDeviceToHost));
-            C2G_CUDA(cudaMemcpy(pw.data(), dpw, sizeof(uint32_t) * E, cudaMemcpyDeviceToHost));
-        }
-        if (H) {
-            C2G_CUDA(cudaMemcpy(he.data(), dhe, sizeof(int32_t) * H, cudaMemcpyDeviceToHost));
-            C2G_CUDA(cudaMemcpy(hw.data(), dhw, sizeof(uint32_t) * H, cudaMemcpyDeviceToHost));
-        }
+    DevBuf tmp;
+    long long *dob = nullptr, *drb = nullptr;
+    int *dpe = nullptr, *dhe = nullptr;
+    unsigned *dpw = nullptr, *dhw = nullptr;
+    e = tmp.get(&dob, (size_t)V);
+    if (e == cudaSuccess) e = tmp.get(&drb, (size_t)V);
+    if (e == cudaSuccess) e = tmp.get(&dpe, E);
+    if (e == cudaSuccess) e = tmp.get(&dpw, E);
+    if (e == cudaSuccess) e = tmp.get(&dhe, H);
+    if (e == cudaSuccess) e = tmp.get(&dhw, H);
+    C2G_CUDA(e);
+    C2G_CUDA(cudaMemcpy(dob, ob.data(), sizeof(long long) * (size_t)V, cudaMemcpyHostToDevice));
+    C2G_CUDA(cudaMemcpy(drb, rbase.data(), sizeof(long long) * (size_t)V, cudaMemcpyHostToDevice));
+    if (V > 0) {
+        pg_gather_rows<<<sms * 8, 256>>>(p.out_off, p.out_n, dob, V, p.ot, p.ow, dpe, dpw);
+        pg_gather_rows<<<sms * 8, 256>>>(p.rec_off, p.rec_n, drb, V, p.rt, p.rw, dhe, dhw);
+        C2G_CUDA(cudaGetLastError());
     }
+    C2G_CUDA(cudaDeviceSynchronize());
+    // the files, the device arrays streamed through a pinned staging buffer
+    const size_t stage_n = (size_t)1 << 24;
+    void* stage = nullptr;
+    C2G_CUDA(cudaMallocHost(&stage, 4 * stage_n));
+    struct FreeHost {
+        void* q;
+        ~FreeHost() { cudaFreeHost(q); }
+    } free_stage{stage};
+    auto put = [&](const std::string& path, const void* dev, size_t n) -> int {
+        FILE* fp = fopen(path.c_str(), "wb");
+        if (!fp) return fail(C2G_ERR_IO, "cannot create %s", path.c_str());
+        for (size_t x = 0; x < n; x += stage_n) {
+            const size_t k = std::min(stage_n, n - x);
+            const cudaError_t ce = cudaMemcpy(stage, static_cast<const char*>(dev) + 4 * x, 4 * k, cudaMemcpyDeviceToHost);
+            if (ce != cudaSuccess || fwrite(stage, 4, k, fp) != k) {
+                fclose(fp);
+                return ce != cudaSuccess ? fail(C2G_ERR_CUDA, "%s", cudaGetErrorString(ce))
+                                         : fail(C2G_ERR_IO, "short write on %s", path.c_str());
+            }
+        }
+        if (fclose(fp) != 0) return fail(C2G_ERR_IO, "short write on %s", path.c_str());
+        return C2G_OK;
+    };
     const std::string s = dir + "/ppr/";
     if ((rc = make_dir(dir + "/ppr"))) return rc;
     if ((rc = write_array4(s + "hvlist.bin", hv.data(), hv.size()))) return rc;
-    if ((rc = write_array4(s + "helist.bin", he.data(), he.size()))) return rc;
-    if ((rc = write_array4(s + "hwlist.bin", hw.data(), hw.size()))) return rc;
+    if ((rc = put(s + "helist.bin", dhe, H))) return rc;
+    if ((rc = put(s + "hwlist.bin", dhw, H))) return rc;
     if ((rc = write_array4(s + "vlist.bin", pv.data(), pv.size()))) return rc;
-    if ((rc = write_array4(s + "elist.bin", pe.data(), pe.size()))) return rc;
-    if ((rc = write_array4(s + "wlist.bin", pw.data(), pw.size()))) return rc;
+    if ((rc = put(s + "elist.bin", dpe, E))) return rc;
+    if ((rc = put(s + "wlist.bin", dpw, E))) return rc;
     return C2G_OK;
 }
 
 }  // namespace c2g
 
-extern "C" int c2g_prune_ppr_device(const char* dir, double alpha, int device, float* ms, int32_t* rounds) {
+extern "C" int c2g_prune_ppr_device(const char* dir, double alpha, int device, float* ms, int32_t* rounds,
+                                    int64_t* phase_ns) {
     if (!dir) return c2g::fail(C2G_ERR_ARG, "prune: dir is NULL");
     if (!(alpha > 0.0 && alpha < 1.0)) return c2g::fail(C2G_ERR_ARG, "prune: alpha must be in (0, 1)");
-    return c2g::prune_ppr_device_dir(dir, 1.0 - alpha, device, ms, rounds);
+    return c2g::prune_ppr_device_dir(dir, 1.0 - alpha, device, ms, rounds, phase_ns);
 }

@@ -48,7 +48,7 @@ def _write(d, vl, el, fl):
 def test_prune_ppr_device_edge_cases(gpu_available, built, tmp_path):
     """Repeated targets with different weights (kept as separate pairs, merged one by
     one), self-loops (dropped), a chain whose visits each rewrite the row the next one
-    reads, and a graph without edges."""
+    reads, a graph without edges, and unsorted rows with repeated pairs."""
     import c2g
     import oracle
 
@@ -68,6 +68,22 @@ def test_prune_ppr_device_edge_cases(gpu_available, built, tmp_path):
     cases["chain"] = (np.concatenate([np.arange(n), [n - 1]]), np.arange(1, n),
                       np.linspace(0.1, 0.9, n - 1).astype(np.float32))
     cases["empty"] = (np.zeros(9, np.int32), np.zeros(0, np.int32), np.zeros(0, np.float32))
+    # an R-MAT graph with every row shuffled and some pairs repeated: the rows are sorted and
+    # deduplicated before the visits (the R-MAT writer's own rows are taken as they are)
+    g = str(tmp_path / "rmat")
+    oracle.rmat_write(g, 12, 16, 4, 1, 1000)
+    o = oracle.load_dataset(g, "origin")
+    vl, el, fl = o["vlist"], o["elist"].copy(), o["flist"].copy()
+    rows_e, rows_f = [], []
+    for v in range(len(vl) - 1):
+        e, f = el[vl[v]:vl[v + 1]], fl[vl[v]:vl[v + 1]]
+        if len(e) > 2 and v % 3 == 0:
+            e, f = np.concatenate([e, e[:2]]), np.concatenate([f, f[:2]])
+        q = rng.permutation(len(e))
+        rows_e.append(e[q])
+        rows_f.append(f[q])
+    cases["shuffled"] = (np.concatenate([[0], np.cumsum([len(e) for e in rows_e])]), np.concatenate(rows_e),
+                         np.concatenate(rows_f))
     for name, (vl, el, fl) in cases.items():
         ref, dev = str(tmp_path / (name + "_ref")), str(tmp_path / (name + "_dev"))
         _write(ref, vl, el, fl)
@@ -86,3 +102,23 @@ def test_prune_ppr_device_bad_alpha(gpu_available, built, tmp_path):
     with pytest.raises(c2g.C2GError) as e:
         c2g.prune_ppr_device(str(tmp_path), 0.15)  # no origin/ files
     assert e.value.code == c2g.ERR_IO
+
+
+def test_purn_ppr_program_on_the_gpu(gpu_available, built, tmp_path):
+    """The drop-in purn-ppr with C2G_PRUNE_GPU=0 writes the reference factor's files (0.8),
+    the same bytes as the program's host pass."""
+    import subprocess
+
+    import oracle
+    from conftest import PKG
+
+    host, dev = str(tmp_path / "host"), str(tmp_path / "dev")
+    oracle.rmat_write(host, 13, 16, 9, 1, 1000)
+    shutil.copytree(host, dev)
+    prog = os.path.join(PKG, "bin", "purn-ppr")
+    env = dict(os.environ)
+    env.pop("C2G_PRUNE_GPU", None)
+    subprocess.run([prog, host], check=True, env=env, stdout=subprocess.PIPE, stderr=subprocess.PIPE)
+    env["C2G_PRUNE_GPU"] = "0"
+    subprocess.run([prog, dev], check=True, env=env, stdout=subprocess.PIPE, stderr=subprocess.PIPE)
+    _same(host, dev)
