@@ -559,6 +559,61 @@ def run_adsorption(args):
     print(json.dumps(line), flush=True)
 
 
+def run_prune(args):
+    """purn-ppr on the GPU (c2g_prune_ppr_device) against the sequential pass: one step is
+    one pruning of the whole R-MAT graph (origin/ files in, ppr/ files out).  `value` is
+    input edges per second of kernel time; `e2e` the same through the C ABI call with the
+    files read and written; the CPU baseline is the oracle's sequential pass (oracle/ingest.c
+    orc_prune_ppr, one core); the library's own host pass (prune.cpp) is timed beside it,
+    and every step's files are compared with it byte for byte."""
+    import filecmp
+    import shutil
+
+    import c2g
+    import oracle
+
+    files = ("vlist", "elist", "wlist", "hvlist", "helist", "hwlist")
+    with tempfile.TemporaryDirectory(dir=args.workdir) as base:
+        host, dev, orc = (os.path.join(base, x) for x in ("host", "dev", "orc"))
+        c2g.rmat_write(host, args.scale, args.edge_factor, args.seed, 1, 1000, gpu=True)
+        shutil.copytree(host, dev)
+        shutil.copytree(host, orc)
+        E = len(c2g.read_array(os.path.join(host, "origin", "elist.bin")))
+        t0 = time.time()
+        c2g.prune_ppr(host, ALPHA)
+        host_s = time.time() - t0
+        t0 = time.time()
+        oracle.prune_ppr(orc, ALPHA)
+        orc_s = time.time() - t0
+        kern, call, same = [], [], True
+        for i in range(args.warmup + args.steps):
+            t0 = time.time()
+            ms, rounds, ph = c2g.prune_ppr_device(dev, ALPHA, phases=True)
+            dt = time.time() - t0
+            same = same and all(filecmp.cmp(os.path.join(host, "ppr", f + ".bin"), os.path.join(dev, "ppr", f + ".bin"),
+                                            shallow=False) for f in files)
+            if i >= args.warmup:
+                kern.append(ms / 1000.0)
+                call.append(dt)
+        same = same and all(filecmp.cmp(os.path.join(host, "ppr", f + ".bin"), os.path.join(orc, "ppr", f + ".bin"),
+                                        shallow=False) for f in files)
+        V = len(c2g.read_array(os.path.join(host, "origin", "vlist.bin"))) - 1
+    ks, cs = float(np.mean(kern)), float(np.mean(call))
+    line = {"mode": "prune", "metric": "purn-ppr input edges pruned per second", "value": E / ks, "unit": "edges/s",
+            "ms_per_step": ks * 1000.0, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+            "n_gpus": 1, "dtype": "int32 / f32 rows, f64 folds", "data": "synthetic R-MAT (seeded); no public dataset",
+            "config": {"workload": "rmat-s%d-ef%d, %d vertices, %d edges, alpha %g" % (args.scale, args.edge_factor, V, E,
+                                                                                      ALPHA)},
+            "e2e": {"value": E / cs, "unit": "edges/s", "s_per_step": cs,
+                    "includes": "reading origin/, building the rows, the kernel, writing ppr/"},
+            "cpu_baseline": {"value": E / orc_s, "unit": "edges/s", "cores": 1, "kind": "port",
+                             "sample": "the whole graph, oracle/ingest.c orc_prune_ppr"},
+            "detail": {"host_pass_s": host_s, "oracle_s": orc_s, "device_call_s": cs, "kernel_s": ks, "rounds": rounds,
+                       "phase_ms": dict(zip(("plan", "check", "disturb", "commit", "copy"), ph)),
+                       "identical_to_host_pass_and_oracle": bool(same)}}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -577,9 +632,10 @@ def main():
                     help="queries per kind in the CPU-baseline leg (0: one per host thread)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workdir", default=None)
-    ap.add_argument("--mode", default="step", choices=["step", "serve", "adjoint", "adsorption"],
+    ap.add_argument("--mode", default="step", choices=["step", "serve", "adjoint", "adsorption", "prune"],
                     help="step: the batched multi-tenant step (headline); serve: the serving loop; "
-                         "adjoint: PPR adjoint throughput; adsorption: label propagation throughput")
+                         "adjoint: PPR adjoint throughput; adsorption: label propagation throughput; "
+                         "prune: purn-ppr on the GPU against the sequential pass")
     ap.add_argument("--serve-scale", type=int, default=24)
     ap.add_argument("--serve-requests", type=int, default=200)
     ap.add_argument("--serve-rate", type=float, default=5000.0)
@@ -594,7 +650,8 @@ def main():
         __graft_entry__.build()
     if args.mode != "step":
         if rank == 0:
-            {"serve": run_serve, "adjoint": run_adjoint, "adsorption": run_adsorption}[args.mode](args)
+            {"serve": run_serve, "adjoint": run_adjoint, "adsorption": run_adsorption,
+             "prune": run_prune}[args.mode](args)
         return
     if args.impl == "reference":
         run_reference(args, rank, world)
