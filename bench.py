@@ -565,7 +565,8 @@ def run_prune(args):
     input edges per second of kernel time; `e2e` the same through the C ABI call with the
     files read and written; the CPU baseline is the oracle's sequential pass (oracle/ingest.c
     orc_prune_ppr, one core); the library's own host pass (prune.cpp) is timed beside it,
-    and every step's files are compared with it byte for byte."""
+    and every step's files are compared with it byte for byte.  purn-sssp on the GPU
+    (c2g_prune_sssp_device) is timed the same way into `detail.sssp`."""
     import filecmp
     import shutil
 
@@ -597,6 +598,26 @@ def run_prune(args):
                 call.append(dt)
         same = same and all(filecmp.cmp(os.path.join(host, "ppr", f + ".bin"), os.path.join(orc, "ppr", f + ".bin"),
                                         shallow=False) for f in files)
+        # purn-sssp the same way (seven files: the record->vertex sidecar too)
+        sfiles = files + ("hvmap",)
+        t0 = time.time()
+        c2g.prune_sssp(host)
+        s_host = time.time() - t0
+        t0 = time.time()
+        oracle.prune_sssp(orc)
+        s_orc = time.time() - t0
+        s_kern, s_call, s_same = [], [], True
+        for i in range(args.warmup + args.steps):
+            t0 = time.time()
+            s_ms, s_rounds, s_ph = c2g.prune_sssp_device(dev, phases=True)
+            dt = time.time() - t0
+            s_same = s_same and all(filecmp.cmp(os.path.join(host, "sssp", f + ".bin"),
+                                                os.path.join(dev, "sssp", f + ".bin"), shallow=False) for f in sfiles)
+            if i >= args.warmup:
+                s_kern.append(s_ms / 1000.0)
+                s_call.append(dt)
+        s_same = s_same and all(filecmp.cmp(os.path.join(host, "sssp", f + ".bin"), os.path.join(orc, "sssp", f + ".bin"),
+                                            shallow=False) for f in sfiles)
         V = len(c2g.read_array(os.path.join(host, "origin", "vlist.bin"))) - 1
     ks, cs = float(np.mean(kern)), float(np.mean(call))
     line = {"mode": "prune", "metric": "purn-ppr input edges pruned per second", "value": E / ks, "unit": "edges/s",
@@ -610,7 +631,11 @@ def run_prune(args):
                              "sample": "the whole graph, oracle/ingest.c orc_prune_ppr"},
             "detail": {"host_pass_s": host_s, "oracle_s": orc_s, "device_call_s": cs, "kernel_s": ks, "rounds": rounds,
                        "phase_ms": dict(zip(("plan", "check", "disturb", "commit", "copy"), ph)),
-                       "identical_to_host_pass_and_oracle": bool(same)}}
+                       "identical_to_host_pass_and_oracle": bool(same),
+                       "sssp": {"kernel_s": float(np.mean(s_kern)), "device_call_s": float(np.mean(s_call)),
+                                "host_pass_s": s_host, "oracle_s": s_orc, "rounds": s_rounds,
+                                "phase_ms": dict(zip(("plan", "check", "disturb", "commit", "copy"), s_ph)),
+                                "identical_to_host_pass_and_oracle": bool(s_same)}}}
     print(json.dumps(line), flush=True)
 
 

@@ -157,6 +157,8 @@ SIGNATURES = {
     "c2g_prune_ppr_device": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_double, ctypes.c_int,
                                             ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_int32),
                                             ctypes.c_void_p]),
+    "c2g_prune_sssp_device": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, ctypes.POINTER(ctypes.c_float),
+                                             ctypes.POINTER(ctypes.c_int32), ctypes.c_void_p]),
 }
 
 
@@ -222,6 +224,19 @@ def prune_ppr_device(dir, alpha=0.2, device=0, phases=False):
     ph = np.zeros(5, np.int64)
     _check(lib().c2g_prune_ppr_device(os.fsencode(dir), float(alpha), int(device), ctypes.byref(ms),
                                       ctypes.byref(rounds), ph.ctypes.data))
+    if phases:
+        return float(ms.value), int(rounds.value), [float(x) / 1e6 for x in ph]
+    return float(ms.value), int(rounds.value)
+
+
+def prune_sssp_device(dir, device=0, phases=False):
+    """purn-sssp on the GPU (same files as prune_sssp(dir), hvmap.bin included).  Returns
+    (kernel ms, rounds), and with phases=True also the phases' kernel ms."""
+    ms = ctypes.c_float(0.0)
+    rounds = ctypes.c_int32(0)
+    ph = np.zeros(5, np.int64)
+    _check(lib().c2g_prune_sssp_device(os.fsencode(dir), int(device), ctypes.byref(ms), ctypes.byref(rounds),
+                                       ph.ctypes.data))
     if phases:
         return float(ms.value), int(rounds.value), [float(x) / 1e6 for x in ph]
     return float(ms.value), int(rounds.value)

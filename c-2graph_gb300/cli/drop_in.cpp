@@ -24,8 +24,9 @@
 // as CUDA_ERROR's exit(-1) does (core/Util.cuh:17-24).
 //
 // Environment: C2G_SEEDS=exact makes sssp-purn use the record->vertex sidecar instead
-// of the reference's vertex-indexed hvlist read.  C2G_PRUNE_GPU=<device> makes purn-ppr
-// run its visits on that GPU (c2g_prune_ppr_device: the same files, byte for byte).
+// of the reference's vertex-indexed hvlist read.  C2G_PRUNE_GPU=<device> makes purn-ppr and
+// purn-sssp run their visits on that GPU (c2g_prune_ppr_device, c2g_prune_sssp_device: the
+// same files, byte for byte).
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
@@ -164,6 +165,8 @@ static int run_prune(const char* dir, bool ppr) {
     int rc;
     if (ppr && gpu && *gpu)  // alpha 0.2: the reference's baked factor 0.8 (1 - 0.2 is the same double)
         rc = c2g_prune_ppr_device(dir, 0.2, atoi(gpu), nullptr, nullptr, nullptr);
+    else if (gpu && *gpu)
+        rc = c2g_prune_sssp_device(dir, atoi(gpu), nullptr, nullptr, nullptr);
     else
         rc = ppr ? c2g_prune_ppr(dir) : c2g_prune_sssp(dir);
     if (rc) die(rc);

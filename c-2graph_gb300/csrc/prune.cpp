@@ -17,6 +17,7 @@
 #include <cstdint>
 #include <memory>
 #include <string>
+#include <type_traits>
 #include <utility>
 #include <vector>
 
@@ -237,24 +238,27 @@ void flatten(const Adj<W>& out, int32_t V, std::vector<int32_t>& vlist, std::vec
 
 }  // namespace
 
-// The rows purn-ppr starts from, flat, for the device pruner (prune_gpu.cu): the rows
+// The rows a pruner starts from, flat, for the device pruners (prune_gpu.cu): the rows
 // build_out and build_in make (out-rows: the (target, weight) pairs without self-loops,
-// sorted as pair<int32, float> and without repeated pairs; in-rows: the distinct sources of
+// sorted as pair<int32, W> and without repeated pairs; in-rows: the distinct sources of
 // each vertex, ascending), built without one allocation per row.  Input rows that are
 // already strictly increasing and free of self-loops (the R-MAT writer's) are the out-rows
 // as they are; other rows are sorted in parallel.  The in-rows are a stable counting sort
 // of the out-rows by target, each thread filling its own range of sources.  orow / irow are
-// row pointers over V + 1 entries.
-int prune_ppr_initial_rows(const std::string& dir, int32_t& V, std::vector<int32_t>& orow, std::vector<int32_t>& ot,
-                           std::vector<float>& ow, std::vector<int32_t>& irow, std::vector<int32_t>& is) {
+// row pointers over V + 1 entries.  W is float (purn-ppr: origin/flist.bin) or int32
+// (purn-sssp: origin/wlist.bin).
+template <typename W>
+int prune_initial_rows(const std::string& dir, int32_t& V, std::vector<int32_t>& orow, std::vector<int32_t>& ot,
+                       std::vector<W>& ow, std::vector<int32_t>& irow, std::vector<int32_t>& is) {
+    constexpr bool kFloat = std::is_same<W, float>::value;
     std::vector<int32_t> vlist, elist;
-    std::vector<float> flist;
+    std::vector<W> flist;
     int rc;
     if ((rc = read_array4(dir + "/origin/vlist.bin", vlist))) return rc;
     if ((rc = read_array4(dir + "/origin/elist.bin", elist))) return rc;
-    if ((rc = read_array4(dir + "/origin/flist.bin", flist))) return rc;
+    if ((rc = read_array4(dir + (kFloat ? "/origin/flist.bin" : "/origin/wlist.bin"), flist))) return rc;
     if ((rc = check_csr(vlist, elist))) return rc;
-    if (flist.size() < elist.size()) return fail(C2G_ERR_FORMAT, "flist shorter than elist");
+    if (flist.size() < elist.size()) return fail(C2G_ERR_FORMAT, kFloat ? "flist shorter than elist" : "wlist shorter than elist");
     V = (int32_t)vlist.size() - 1;
     int plain = 1;
 #pragma omp parallel for schedule(dynamic, 4096) reduction(& : plain)
@@ -267,7 +271,7 @@ int prune_ppr_initial_rows(const std::string& dir, int32_t& V, std::vector<int32
         ot = std::move(elist);
         ow = std::move(flist);
     } else {
-        std::vector<std::pair<int32_t, float>> pr(elist.size());
+        std::vector<std::pair<int32_t, W>> pr(elist.size());
         std::vector<int32_t> cnt((size_t)V, 0);
 #pragma omp parallel for schedule(dynamic, 4096)
         for (int32_t v = 0; v < V; ++v) {
@@ -331,6 +335,11 @@ int prune_ppr_initial_rows(const std::string& dir, int32_t& V, std::vector<int32
     }
     return C2G_OK;
 }
+
+template int prune_initial_rows<float>(const std::string&, int32_t&, std::vector<int32_t>&, std::vector<int32_t>&,
+                                      std::vector<float>&, std::vector<int32_t>&, std::vector<int32_t>&);
+template int prune_initial_rows<int32_t>(const std::string&, int32_t&, std::vector<int32_t>&, std::vector<int32_t>&,
+                                        std::vector<int32_t>&, std::vector<int32_t>&, std::vector<int32_t>&);
 
 int prune_sssp_dir(const std::string& dir) {
     std::vector<int32_t> vlist, elist, wlist;

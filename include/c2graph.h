@@ -454,6 +454,11 @@ int c2g_prune_ppr_alpha(const char* dir, double alpha);
  * row pool runs out (nothing is written). */
 int c2g_prune_ppr_device(const char* dir, double alpha, int device, float* ms, int32_t* rounds,
                          int64_t* phase_ns);
+/* purn-sssp on a GPU: the visits of c2g_prune_sssp (rounds k = 1..29 over the vertices in
+ * id order, src/purn-sssp.cpp:139-294) in rounds of the same speculative schedule, writing
+ * the same seven files (sssp/ with the record->vertex sidecar hvmap.bin) byte for byte.
+ * ms, rounds and phase_ns as for c2g_prune_ppr_device. */
+int c2g_prune_sssp_device(const char* dir, int device, float* ms, int32_t* rounds, int64_t* phase_ns);
 
 #ifdef __cplusplus
 }

@@ -1,6 +1,7 @@
-"""purn-ppr on the GPU (c2g_prune_ppr_device) writes the same six ppr/ files as the
-sequential pass, byte for byte: the oracle's restatement (oracle/ingest.c orc_prune_ppr)
-and the library's host pass (c2g_prune_ppr_alpha)."""
+"""purn-ppr and purn-sssp on the GPU (c2g_prune_ppr_device, c2g_prune_sssp_device) write the
+same files as the sequential passes, byte for byte: the oracle's restatements
+(oracle/ingest.c orc_prune_ppr, orc_prune_sssp) and the library's host passes
+(c2g_prune_ppr_alpha, c2g_prune_sssp)."""
 import filecmp
 import os
 import shutil
@@ -10,13 +11,14 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 
-FILES = ("vlist", "elist", "wlist", "hvlist", "helist", "hwlist")
+FILES = {"ppr": ("vlist", "elist", "wlist", "hvlist", "helist", "hwlist"),
+         "sssp": ("vlist", "elist", "wlist", "hvlist", "helist", "hwlist", "hvmap")}
 
 
-def _same(a, b):
-    for f in FILES:
-        pa, pb = os.path.join(a, "ppr", f + ".bin"), os.path.join(b, "ppr", f + ".bin")
-        assert filecmp.cmp(pa, pb, shallow=False), f
+def _same(a, b, kind="ppr"):
+    for f in FILES[kind]:
+        pa, pb = os.path.join(a, kind, f + ".bin"), os.path.join(b, kind, f + ".bin")
+        assert filecmp.cmp(pa, pb, shallow=False), (kind, f)
 
 
 @pytest.mark.parametrize("scale,ef,seed,alpha", [(10, 8, 1, None), (14, 16, 5, 0.15), (17, 16, 2, 0.15)])
@@ -37,12 +39,32 @@ def test_prune_ppr_device_matches_sequential(gpu_available, built, tmp_path, sca
     assert 0 < rounds < V // 4 and ms > 0.0
 
 
-def _write(d, vl, el, fl):
+@pytest.mark.parametrize("scale,ef,seed", [(10, 8, 1), (14, 16, 5), (17, 16, 2)])
+def test_prune_sssp_device_matches_sequential(gpu_available, built, tmp_path, scale, ef, seed):
+    """purn-sssp's visits in rounds k = 1..29; the records in visiting order with the
+    record->vertex sidecar."""
+    import c2g
+    import oracle
+
+    ref, host, dev = str(tmp_path / "ref"), str(tmp_path / "host"), str(tmp_path / "dev")
+    oracle.rmat_write(ref, scale, ef, seed, 1, 1000)
+    shutil.copytree(ref, host)
+    shutil.copytree(ref, dev)
+    oracle.prune_sssp(ref)
+    c2g.prune_sssp(host)
+    ms, rounds = c2g.prune_sssp_device(dev)
+    _same(ref, dev, "sssp")
+    _same(host, dev, "sssp")
+    assert rounds > 0 and ms > 0.0
+
+
+def _write(d, vl, el, fl, wl=None):
     os.makedirs(os.path.join(d, "origin"))
     np.asarray(vl, np.int32).tofile(os.path.join(d, "origin", "vlist.bin"))
     np.asarray(el, np.int32).tofile(os.path.join(d, "origin", "elist.bin"))
     np.asarray(fl, np.float32).tofile(os.path.join(d, "origin", "flist.bin"))
-    np.ones(len(el), np.int32).tofile(os.path.join(d, "origin", "wlist.bin"))
+    (np.ones(len(el), np.int32) if wl is None else np.asarray(wl, np.int32)).tofile(
+        os.path.join(d, "origin", "wlist.bin"))
 
 
 def test_prune_ppr_device_edge_cases(gpu_available, built, tmp_path):
@@ -86,11 +108,45 @@ def test_prune_ppr_device_edge_cases(gpu_available, built, tmp_path):
                          np.concatenate(rows_f))
     for name, (vl, el, fl) in cases.items():
         ref, dev = str(tmp_path / (name + "_ref")), str(tmp_path / (name + "_dev"))
-        _write(ref, vl, el, fl)
+        # int weights with repeats, so that purn-sssp's rows also hold repeated targets
+        _write(ref, vl, el, fl, rng.integers(1, 6, len(el)))
         shutil.copytree(ref, dev)
         oracle.prune_ppr(ref, 0.15)
         c2g.prune_ppr_device(dev, 0.15)
-        _same(ref, dev)
+        _same(ref, dev, "ppr")
+        try:
+            oracle.prune_sssp(ref)
+        except RuntimeError:  # the pass stops ("something error2"): so does the device
+            with pytest.raises(c2g.C2GError) as e:
+                c2g.prune_sssp_device(dev)
+            assert e.value.code == c2g.ERR_FORMAT
+            continue
+        c2g.prune_sssp_device(dev)
+        _same(ref, dev, "sssp")
+
+
+def test_prune_device_stops_where_the_pass_stops(gpu_available, built, tmp_path):
+    """Two pairs 1 -> 2 with different weights each kill 1's entry in 2's in-row, so 2's
+    live in-degree (1) falls below its live roots (0 and 3): both pruners stop at 2's visit
+    ("something error2", src/purn-sssp.cpp:151-166), the host passes and the device alike,
+    and nothing is written."""
+    import c2g
+    import oracle
+
+    vl, el = [0, 1, 3, 4, 5, 5], [1, 2, 2, 4, 2]
+    d = str(tmp_path / "g")
+    _write(d, vl, el, [0.5, 0.25, 0.75, 0.5, 0.5], [1, 1, 2, 1, 1])
+    for kind in ("ppr", "sssp"):
+        with pytest.raises(RuntimeError):
+            oracle.prune_ppr(d, 0.15) if kind == "ppr" else oracle.prune_sssp(d)
+        with pytest.raises(c2g.C2GError) as e:
+            c2g.prune_ppr(d, 0.15) if kind == "ppr" else c2g.prune_sssp(d)
+        assert e.value.code == c2g.ERR_FORMAT
+        shutil.rmtree(os.path.join(d, kind), ignore_errors=True)
+        with pytest.raises(c2g.C2GError) as e:
+            c2g.prune_ppr_device(d, 0.15) if kind == "ppr" else c2g.prune_sssp_device(d)
+        assert e.value.code == c2g.ERR_FORMAT
+        assert not os.path.exists(os.path.join(d, kind))
 
 
 def test_prune_ppr_device_bad_alpha(gpu_available, built, tmp_path):
@@ -104,9 +160,9 @@ def test_prune_ppr_device_bad_alpha(gpu_available, built, tmp_path):
     assert e.value.code == c2g.ERR_IO
 
 
-def test_purn_ppr_program_on_the_gpu(gpu_available, built, tmp_path):
-    """The drop-in purn-ppr with C2G_PRUNE_GPU=0 writes the reference factor's files (0.8),
-    the same bytes as the program's host pass."""
+def test_prune_programs_on_the_gpu(gpu_available, built, tmp_path):
+    """The drop-in purn-ppr and purn-sssp with C2G_PRUNE_GPU=0 write the same bytes as the
+    programs' host passes (purn-ppr with the reference factor 0.8)."""
     import subprocess
 
     import oracle
@@ -115,10 +171,12 @@ def test_purn_ppr_program_on_the_gpu(gpu_available, built, tmp_path):
     host, dev = str(tmp_path / "host"), str(tmp_path / "dev")
     oracle.rmat_write(host, 13, 16, 9, 1, 1000)
     shutil.copytree(host, dev)
-    prog = os.path.join(PKG, "bin", "purn-ppr")
     env = dict(os.environ)
-    env.pop("C2G_PRUNE_GPU", None)
-    subprocess.run([prog, host], check=True, env=env, stdout=subprocess.PIPE, stderr=subprocess.PIPE)
-    env["C2G_PRUNE_GPU"] = "0"
-    subprocess.run([prog, dev], check=True, env=env, stdout=subprocess.PIPE, stderr=subprocess.PIPE)
-    _same(host, dev)
+    for name in ("purn-ppr", "purn-sssp"):
+        prog = os.path.join(PKG, "bin", name)
+        env.pop("C2G_PRUNE_GPU", None)
+        subprocess.run([prog, host], check=True, env=env, stdout=subprocess.PIPE, stderr=subprocess.PIPE)
+        env["C2G_PRUNE_GPU"] = "0"
+        subprocess.run([prog, dev], check=True, env=env, stdout=subprocess.PIPE, stderr=subprocess.PIPE)
+    _same(host, dev, "ppr")
+    _same(host, dev, "sssp")
