@@ -115,16 +115,25 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def make_dataset(tools, d, scale, ef, seed):
+def make_dataset(tools, d, scale, ef, seed, device=None):
     """The step's inputs in <d>: the R-MAT graph (int32 weights in [1, 1000], flist),
     pruned by purn-sssp and by purn-ppr for the step's alpha (folded edges carry
     1 - alpha).  `tools` is the library (c2g) for our arm and the oracle's restatement for
-    the reference arm; both write the same bytes (tests/test_oracle_golden.py)."""
+    the reference arm; both write the same bytes (tests/test_oracle_golden.py).  With a
+    device, the library generates and prunes on that GPU (the same bytes again:
+    tests/test_gpu_ingest.py, tests/test_gpu_prune.py)."""
     t0 = time.time()
-    tools.rmat_write(d, scale, ef, seed, 1, 1000)
+    if device is None:
+        tools.rmat_write(d, scale, ef, seed, 1, 1000)
+    else:
+        tools.rmat_write(d, scale, ef, seed, 1, 1000, gpu=True, device=device)
     t1 = time.time()
-    tools.prune_sssp(d)
-    tools.prune_ppr(d, alpha=ALPHA)
+    if device is None:
+        tools.prune_sssp(d)
+        tools.prune_ppr(d, alpha=ALPHA)
+    else:
+        tools.prune_sssp_device(d, device=device)
+        tools.prune_ppr_device(d, ALPHA, device=device)
     return t1 - t0, time.time() - t1
 
 
@@ -235,7 +244,7 @@ def run_ours(args, rank, world, local_rank):
 
         tdist.init_process_group("nccl", device_id=torch.device("cuda", dev))
     work = tempfile.mkdtemp(dir=args.workdir)
-    gen_s, prune_s = make_dataset(c2g, work, args.scale, args.edge_factor, args.seed)
+    gen_s, prune_s = make_dataset(c2g, work, args.scale, args.edge_factor, args.seed, device=dev)
     so = {"vlist": c2g.read_array(os.path.join(work, "sssp", "vlist.bin"))}
     po = {"vlist": c2g.read_array(os.path.join(work, "ppr", "vlist.bin"))}
     V = len(so["vlist"]) - 1
