@@ -53,6 +53,7 @@ constexpr int kPgThreads = 256;
 constexpr int kPgWarps = kPgThreads / 32;
 constexpr int kPgSlotR = 32;   // rows a position reads: its in-row, its out-row, its roots' out-rows
 constexpr int kPgG = 6;        // roots searched in lockstep
+constexpr int kPgU = 2;        // merge items per lane searched in lockstep
 constexpr int kPgTask = 1024;  // entries per copy task
 constexpr unsigned kPgMoved = 0x80000000u;  // plan code of an out-edge that moves (| the roots lacking it)
 
@@ -445,18 +446,7 @@ __device__ __forceinline__ void pg_visit(const PgParams& p, int i, int k, int c,
         if (lane == 0) atomicOr(&p.ctl->flags, kPgErrRows);
         return;
     }
-    if (lane < j) {  // the weight of root -> i: the root's first pair with target i
-        const long long off = S.off[lane];
-        const int n = S.n[lane];
-        const int q = pg_search(p.ot, off, 0, n, i, false);
-        if (q < n && ldcg(p.ot + off + q) == i) {
-            S.dis[lane] = ldcg(p.ow + off + q);
-        } else {
-            S.dis[lane] = 0u;
-            atomicOr(&p.ctl->flags, kPgErrRows);
-        }
-        S.nnew[lane] = 0;
-    }
+    if (lane < j) S.nnew[lane] = 0;
     const long long ooff = ldl(p.out_off + i);
     const int on = ldcg(p.out_n + i);
     const long long woff = ldl(p.slot_woff + c);
@@ -543,26 +533,77 @@ __device__ __forceinline__ void pg_visit(const PgParams& p, int i, int k, int c,
         if (valid) kbs[b] = b - rs;
     }
     __syncwarp();
+    // Pass 1 with the weights of root -> i (each root's first pair with target i, looked up
+    // by lane q0 for root q0): kPgU items per lane and the lookups searched in lockstep.
     const int items = j * nrm;
-    for (int i0 = 0; i0 < items; i0 += 32) {
-        const int it = i0 + lane;
-        if (it >= items) break;
-        const int q0 = it / nrm;
-        const int b = it - q0 * nrm;
-        const long long aoff = S.off[q0];
-        const int an = S.n[q0];
-        const int tb = ldcg(p.rt + rb + b);
-        const int lb = pg_search(p.ot, aoff, 0, an, tb, false);
-        const int q = lb + ldcg(kbs + b);
-        int ins = -1;
-        if (q < an && ldcg(p.ot + aoff + q) == tb) {
-            p.ow[aoff + q] = Rule::fold_hit(ldcg(p.ow + aoff + q), ldcg(p.rw + rb + b), S.dis[q0], p.keep);
-        } else {  // after the row's pairs with this target (fewer than this pair's rank)
-            ins = lb;
-            while (ins < an && ldcg(p.ot + aoff + ins) == tb) ++ins;
-            atomicAdd(&S.nnew[q0], 1);
+    for (int i0 = 0; i0 == 0 || i0 < items; i0 += 32 * kPgU) {
+        int lo[kPgU + 1], hi[kPgU + 1], key[kPgU + 1], bb[kPgU], qq[kPgU];
+        long long off[kPgU + 1];
+#pragma unroll
+        for (int u = 0; u < kPgU; ++u) {
+            const int it = i0 + u * 32 + lane;
+            const bool valid = it < items;
+            qq[u] = valid ? it / nrm : 0;
+            bb[u] = valid ? it - qq[u] * nrm : 0;
+            off[u] = S.off[qq[u]];
+            lo[u] = 0;
+            hi[u] = valid ? S.n[qq[u]] : 0;
+            key[u] = valid ? ldcg(p.rt + rb + bb[u]) : 0;
         }
-        insp[it] = ins;
+        const bool wd = i0 == 0 && lane < j;
+        off[kPgU] = wd ? S.off[lane] : 0;
+        lo[kPgU] = 0;
+        hi[kPgU] = wd ? S.n[lane] : 0;
+        key[kPgU] = i;
+        for (;;) {
+            int t[kPgU + 1];
+            bool any = false;
+#pragma unroll
+            for (int u = 0; u <= kPgU; ++u) {
+                t[u] = 0;
+                if (lo[u] < hi[u]) {
+                    t[u] = ldcg(p.ot + off[u] + ((lo[u] + hi[u]) >> 1));
+                    any = true;
+                }
+            }
+            if (!any) break;
+#pragma unroll
+            for (int u = 0; u <= kPgU; ++u)
+                if (lo[u] < hi[u]) {
+                    const int mid = (lo[u] + hi[u]) >> 1;
+                    if (t[u] < key[u])
+                        lo[u] = mid + 1;
+                    else
+                        hi[u] = mid;
+                }
+        }
+        if (wd) {
+            const int q = lo[kPgU];
+            if (q < S.n[lane] && ldcg(p.ot + off[kPgU] + q) == i) {
+                S.dis[lane] = ldcg(p.ow + off[kPgU] + q);
+            } else {  // the reference stops on this (something error2)
+                S.dis[lane] = 0u;
+                atomicOr(&p.ctl->flags, kPgErrRows);
+            }
+        }
+        __syncwarp();  // the weights before the folds
+#pragma unroll
+        for (int u = 0; u < kPgU; ++u) {
+            const int it = i0 + u * 32 + lane;
+            if (it >= items) continue;
+            const int q0 = qq[u], b = bb[u], an = S.n[q0], tb = key[u], lb = lo[u];
+            const long long aoff = off[u];
+            const int q = lb + ldcg(kbs + b);
+            int ins = -1;
+            if (q < an && ldcg(p.ot + aoff + q) == tb) {
+                p.ow[aoff + q] = Rule::fold_hit(ldcg(p.ow + aoff + q), ldcg(p.rw + rb + b), S.dis[q0], p.keep);
+            } else {  // after the row's pairs with this target (fewer than this pair's rank)
+                ins = lb;
+                while (ins < an && ldcg(p.ot + aoff + ins) == tb) ++ins;
+                atomicAdd(&S.nnew[q0], 1);
+            }
+            insp[it] = ins;
+        }
     }
     __syncwarp();
     for (int q0 = 0; q0 < j && nrm > 0; ++q0) {
