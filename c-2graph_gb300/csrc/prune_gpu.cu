@@ -913,9 +913,12 @@ static int prune_device_dir(const std::string& dir, double keep, int device, flo
     C2G_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, prune_rounds<Rule>, kPgThreads, 0));
     if (per_sm < 1) return fail(C2G_ERR_CUDA, "pruner kernel cannot be resident");
     const size_t E0 = ot.size(), I0 = is.size();
-    // purn-sssp's positions are mostly decisions (a vertex whose in-degree exceeds the
-    // round's bound), so its window is wider
-    const int span = std::max(1, std::min(V, kSssp ? 32768 : 8192));
+    // Window (measured at R-MAT scale 22): a wider one takes fewer rounds but more plan and
+    // check work per round.  purn-ppr: 3,072 positions, 759 ms (1,024: 844; 2,048: 773;
+    // 4,096: 802; 8,192: 914; 16,384: 1,042).  purn-sssp's positions are mostly decisions (a
+    // vertex whose in-degree exceeds the round's bound), so its window is wider: 32,768,
+    // 1,454 ms (16,384: 1,542; 24,576: 1,470; 65,536: 1,571).
+    const int span = std::max(1, std::min(V, kSssp ? 32768 : 3072));
     // Pools: a row that gains entries takes a fresh block, so a pool holds every version of
     // its rows.  At R-MAT scale 20 / 22 purn-ppr's blocks add up to about 21 / 29 times the
     // original out-pairs and 22 / 33 times the original in-entries; give each 64 times,
