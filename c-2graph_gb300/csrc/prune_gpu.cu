@@ -725,47 +725,95 @@ __global__ void __launch_bounds__(kPgThreads, 3) prune_rounds(const PgParams p) 
         const unsigned pos = ldcg(&ctl->pos);
         const int round = ldcg(&ctl->round);
         const int par = round & 1;
+        // Warp w owns the window's positions w, w + nwarps, ...; its lanes take up to 32 of
+        // them at once.  A lane handles a position that only decides (reads its in-row and
+        // out-row, writes nothing) by itself; the warp handles the ones that prune, one at a
+        // time.
         // plan and reserve
-        for (int c = gwarp; c < p.span; c += nwarps) {
+        for (int b0 = 0; gwarp + b0 * nwarps < p.span; b0 += 32) {
+            const int c = gwarp + (b0 + lane) * nwarps;
             const unsigned q = pos + (unsigned)c;
-            if (q >= p.npos) break;
-            int k, i;
-            pg_at(p, q, k, i);
-            if (ldcg(p.pk + i) >= k) {
-                if (lane == 0) p.slot_rn[c] = -1;
-                continue;
+            const bool act = c < p.span && q < p.npos;
+            int k = 0, i = 0;
+            if (act) pg_at(p, q, k, i);
+            const bool done = act && ldcg(p.pk + i) >= k;
+            const bool heavy = act && !done && pg_prunes(p, i, k);
+            if (done) p.slot_rn[c] = -1;
+            if (act && !done && !heavy) {
+                int* Rw = p.slot_r + (size_t)c * kPgSlotR;
+                Rw[0] = p.V + i;
+                Rw[1] = i;
+                p.slot_rn[c] = 2;
+                p.slot_woff[c] = 0;
+                p.slot_wn[c] = 0;
+                const unsigned long long key = pg_key(round, q);
+                atomicMax(p.resA + p.V + i, key);
+                atomicMax(p.resA + i, key);
             }
-            pg_plan<Rule>(p, q, i, k, c, round, lane, S);
+            unsigned hm = __ballot_sync(kFull, heavy);
+            while (hm) {
+                const int l = __ffs(hm) - 1;
+                hm &= hm - 1u;
+                const unsigned ql = __shfl_sync(kFull, q, l);
+                const int il = __shfl_sync(kFull, i, l), kl = __shfl_sync(kFull, k, l);
+                pg_plan<Rule>(p, ql, il, kl, gwarp + (b0 + l) * nwarps, round, lane, S);
+            }
         }
         if (!grid_sync(bar, flags, p.barrier_ns)) return;
         phase_mark(ctl->phase_ns, tmark, 0);
         // check: the passers mark the rows they write
-        for (int c = gwarp; c < p.span; c += nwarps) {
+        for (int b0 = 0; gwarp + b0 * nwarps < p.span; b0 += 32) {
+            const int c = gwarp + (b0 + lane) * nwarps;
             const unsigned q = pos + (unsigned)c;
-            if (q >= p.npos) break;
-            const int rn = ldcg(p.slot_rn + c);
-            if (rn < 0) continue;
-            const unsigned long long key = pg_key(round, q);
-            const long long woff = ldl(p.slot_woff + c);
-            const int wn = ldcg(p.slot_wn + c);
-            bool ok = true;
-            for (int x = lane; x < wn; x += 32) ok = ok && ldcg(p.resA + ldcg(p.wscr + woff + x)) == key;
-            if (lane < rn) ok = ok && ldcg(p.resW + ldcg(p.slot_r + (size_t)c * kPgSlotR + lane)) <= key;
-            ok = __all_sync(kFull, ok);
-            if (lane == 0) p.slot_pass[c] = ok ? 1 : 0;
-            if (ok)
-                for (int x = lane; x < wn; x += 32) p.wmark[ldcg(p.wscr + woff + x)] = round;
+            const bool act = c < p.span && q < p.npos;
+            const int rn = act ? ldcg(p.slot_rn + c) : -1;
+            const int wn = rn >= 0 ? ldcg(p.slot_wn + c) : 0;
+            const bool light = rn == 2 && wn == 0;  // a decision: rows V + i and i read
+            if (light) {
+                int k, i;
+                pg_at(p, q, k, i);
+                const unsigned long long key = pg_key(round, q);
+                p.slot_pass[c] = (ldcg(p.resW + p.V + i) <= key && ldcg(p.resW + i) <= key) ? 1 : 0;
+            }
+            unsigned hm = __ballot_sync(kFull, rn >= 0 && !light);
+            while (hm) {
+                const int l = __ffs(hm) - 1;
+                hm &= hm - 1u;
+                const int cl = gwarp + (b0 + l) * nwarps;
+                const unsigned long long key = pg_key(round, pos + (unsigned)cl);
+                const int rnl = __shfl_sync(kFull, rn, l), wnl = __shfl_sync(kFull, wn, l);
+                const long long woff = ldl(p.slot_woff + cl);
+                bool ok = true;
+                for (int x = lane; x < wnl; x += 32) ok = ok && ldcg(p.resA + ldcg(p.wscr + woff + x)) == key;
+                if (lane < rnl) ok = ok && ldcg(p.resW + ldcg(p.slot_r + (size_t)cl * kPgSlotR + lane)) <= key;
+                ok = __all_sync(kFull, ok);
+                if (lane == 0) p.slot_pass[cl] = ok ? 1 : 0;
+                if (ok)
+                    for (int x = lane; x < wnl; x += 32) p.wmark[ldcg(p.wscr + woff + x)] = round;
+            }
         }
         if (!grid_sync(bar, flags, p.barrier_ns)) return;
         phase_mark(ctl->phase_ns, tmark, 1);
         // a failed position whose reads a passer writes holds back the ones after it
-        for (int c = gwarp; c < p.span; c += nwarps) {
+        for (int b0 = 0; gwarp + b0 * nwarps < p.span; b0 += 32) {
+            const int c = gwarp + (b0 + lane) * nwarps;
             const unsigned q = pos + (unsigned)c;
-            if (q >= p.npos) break;
-            const int rn = ldcg(p.slot_rn + c);
-            if (rn < 0 || ldb(p.slot_pass + c)) continue;
-            const bool hit = lane < rn && ldcg(p.wmark + ldcg(p.slot_r + (size_t)c * kPgSlotR + lane)) == round;
-            if (__any_sync(kFull, hit) && lane == 0) atomicMin(&ctl->dmin, q);
+            const int rn = (c < p.span && q < p.npos) ? ldcg(p.slot_rn + c) : -1;
+            const bool failed = rn >= 0 && !ldb(p.slot_pass + c);
+            if (failed && rn == 2) {  // a decision: rows V + i and i
+                int k, i;
+                pg_at(p, q, k, i);
+                if (ldcg(p.wmark + p.V + i) == round || ldcg(p.wmark + i) == round) atomicMin(&ctl->dmin, q);
+            }
+            unsigned hm = __ballot_sync(kFull, failed && rn > 2);
+            while (hm) {
+                const int l = __ffs(hm) - 1;
+                hm &= hm - 1u;
+                const int cl = gwarp + (b0 + l) * nwarps;
+                const int rnl = __shfl_sync(kFull, rn, l);
+                const bool hit = lane < rnl && ldcg(p.wmark + ldcg(p.slot_r + (size_t)cl * kPgSlotR + lane)) == round;
+                if (__any_sync(kFull, hit) && lane == 0) atomicMin(&ctl->dmin, pos + (unsigned)cl);
+            }
         }
         if (!grid_sync(bar, flags, p.barrier_ns)) return;
         phase_mark(ctl->phase_ns, tmark, 2);
@@ -773,26 +821,38 @@ __global__ void __launch_bounds__(kPgThreads, 3) prune_rounds(const PgParams p) 
         const unsigned dmin = ldcg(&ctl->dmin);
         if (gtid == 0 && dmin < p.npos) atomicMin(&ctl->nextpos, dmin);
         if (!(ldcg(flags) & (kPgErrPool | kPgErrRows))) {
-            for (int c = gwarp; c < p.span; c += nwarps) {
+            for (int b0 = 0; gwarp + b0 * nwarps < p.span; b0 += 32) {
+                const int c = gwarp + (b0 + lane) * nwarps;
                 const unsigned q = pos + (unsigned)c;
-                if (q >= p.npos || q > dmin) break;
-                if (ldcg(p.slot_rn + c) < 0) continue;
-                if (!ldb(p.slot_pass + c)) {
-                    if (lane == 0) atomicMin(&ctl->nextpos, q);
-                    continue;
+                const int rn = (c < p.span && q < p.npos && q <= dmin) ? ldcg(p.slot_rn + c) : -1;
+                bool heavy = false;
+                int k = 0, i = 0;
+                if (rn >= 0) {
+                    if (!ldb(p.slot_pass + c)) {
+                        atomicMin(&ctl->nextpos, q);
+                    } else {
+                        pg_at(p, q, k, i);
+                        // purn-sssp skips a vertex whose live in-degree is 0 or above k and
+                        // visits the rest (src/purn-sssp.cpp:142-150), so one that went negative
+                        // (two pairs with one target each kill i's in-entry) is visited and never
+                        // pruned
+                        const int d = ldcg(p.indeg + i);
+                        const bool visit = d != 0 && d <= k;
+                        heavy = visit && d > 0 && ldcg(p.out_n + i) > 0;
+                        if (!heavy) p.pk[i] = visit ? p.klast : k;
+                    }
                 }
-                int k, i;
-                pg_at(p, q, k, i);
-                // purn-sssp skips a vertex whose live in-degree is 0 or above k and visits the
-                // rest (src/purn-sssp.cpp:142-150), so one that went negative (two pairs with one
-                // target each kill i's in-entry) is visited and never pruned
-                const int d = ldcg(p.indeg + i);
-                const bool visit = d != 0 && d <= k;
-                if (visit && d > 0 && ldcg(p.out_n + i) > 0) {
-                    pg_visit<Rule>(p, i, k, c, par, lane, S);
-                    if (lane == 0) p.vk[i] = k;
+                unsigned hm = __ballot_sync(kFull, heavy);
+                while (hm) {
+                    const int l = __ffs(hm) - 1;
+                    hm &= hm - 1u;
+                    const int il = __shfl_sync(kFull, i, l), kl = __shfl_sync(kFull, k, l);
+                    pg_visit<Rule>(p, il, kl, gwarp + (b0 + l) * nwarps, par, lane, S);
+                    if (lane == 0) {
+                        p.vk[il] = kl;
+                        p.pk[il] = p.klast;
+                    }
                 }
-                if (lane == 0) p.pk[i] = visit ? p.klast : k;
             }
         }
         if (!grid_sync(bar, flags, p.barrier_ns)) return;
