@@ -25,7 +25,7 @@ NVCC_FLAGS = ARCH + ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-fopenmp", "-ffp-contract=off", "-Wall",
              "-I", os.path.join(CUDA_HOME, "include")]
 PROGRAMS = ("sssp-base", "sssp-purn", "ppr-base", "ppr-purn", "adsorption-base", "purn-sssp",
-            "purn-ppr")
+            "purn-ppr", "convert2binary")
 
 
 def _sources():

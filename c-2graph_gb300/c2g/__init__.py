@@ -152,6 +152,8 @@ SIGNATURES = {
                                           ctypes.c_int32, ctypes.c_int32, ctypes.c_double, ctypes.c_double,
                                           ctypes.c_double, ctypes.c_int]),
     "c2g_prune_sssp": (ctypes.c_int, [ctypes.c_char_p]),
+    "c2g_convert_text": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(ctypes.c_int64),
+                                        ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64)]),
     "c2g_prune_ppr": (ctypes.c_int, [ctypes.c_char_p]),
     "c2g_prune_ppr_alpha": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_double]),
     "c2g_prune_ppr_device": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_double, ctypes.c_int,
@@ -201,6 +203,14 @@ def rmat_write(dir, scale, edge_factor, seed, wmin=1, wmax=100, a=0.57, b=0.19, 
         _check(lib().c2g_rmat_write_gpu(os.fsencode(dir), scale, edge_factor, seed, wmin, wmax, a, b, c, device))
     else:
         _check(lib().c2g_rmat_write(os.fsencode(dir), scale, edge_factor, seed, wmin, wmax, a, b, c))
+
+
+def convert_text(text_path, dir):
+    """convert2binary: a text edge list into dir/origin/.  Returns (max vertex, V, E)."""
+    mv, v, e = ctypes.c_int64(0), ctypes.c_int64(0), ctypes.c_int64(0)
+    _check(lib().c2g_convert_text(os.fsencode(text_path), os.fsencode(dir), ctypes.byref(mv), ctypes.byref(v),
+                                  ctypes.byref(e)))
+    return int(mv.value), int(v.value), int(e.value)
 
 
 def prune_sssp(dir):

@@ -8,6 +8,7 @@
 //   adsorption-base <dir> <source>  src/adsorption/w-base/Main.cu (origin/ flist)
 //   purn-sssp <dir>            src/purn-sssp.cpp:61-352
 //   purn-ppr  <dir>            src/purn-ppr.cpp:63-344
+//   convert2binary <text> <dir>  utils/convert2binary.cpp:10-137 (text edge list -> origin/)
 //
 // Standard output follows the reference programs line for line: the dataset path
 // (sssp-*, ppr-purn), the Graph constructor's three lines, the device line (sssp-*),
@@ -27,6 +28,8 @@
 // of the reference's vertex-indexed hvlist read.  C2G_PRUNE_GPU=<device> makes purn-ppr and
 // purn-sssp run their visits on that GPU (c2g_prune_ppr_device, c2g_prune_sssp_device: the
 // same files, byte for byte).
+#include <unistd.h>
+
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
@@ -159,6 +162,24 @@ static int run_ppr(const char* dir, int32_t source, bool pruned, bool adsorption
     return 0;
 }
 
+// convert2binary <text> <dir> (utils/convert2binary.cpp:10-137): the reference's four lines
+// on stdout; an unreadable input prints the reference's message and exits 0 (the reference
+// then writes an empty graph; nothing is written here).
+static int run_convert(const char* text, const char* dir) {
+    printf("Reading graph from %s\n", text);
+    int64_t mv = 0, V = 0, E = 0;
+    const int rc = c2g_convert_text(text, dir, &mv, &V, &E);
+    if (rc == C2G_ERR_IO && access(text, R_OK) != 0) {
+        fprintf(stderr, "Error opening file: %s\n", text);
+        return 0;
+    }
+    if (rc) die(rc);
+    printf("Max Vertex Number: %lld\n", (long long)mv);
+    printf("Vertex Number: %lld\n", (long long)V);
+    printf("Edge Number: %lld\n", (long long)E);
+    return 0;
+}
+
 static int run_prune(const char* dir, bool ppr) {
     auto t0 = std::chrono::steady_clock::now();
     const char* gpu = getenv("C2G_PRUNE_GPU");
@@ -179,6 +200,13 @@ int main(int argc, char** argv) {
     std::string prog = argv[0];
     const size_t slash = prog.find_last_of('/');
     if (slash != std::string::npos) prog = prog.substr(slash + 1);
+    if (prog == "convert2binary") {
+        if (argc != 3) {
+            fprintf(stderr, "Usage: %s <edge_list.txt> <dataset_dir>\n", prog.c_str());
+            return 0;
+        }
+        return run_convert(argv[1], argv[2]);
+    }
     if (prog == "purn-sssp" || prog == "purn-ppr") {
         if (argc != 2) {
             fprintf(stderr, "Usage: %s <dataset_dir>\n", prog.c_str());

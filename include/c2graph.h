@@ -433,6 +433,17 @@ int c2g_rmat_write(const char* dir, int scale, int edge_factor, uint64_t seed,
 int c2g_rmat_write_gpu(const char* dir, int scale, int edge_factor, uint64_t seed, int32_t wmin, int32_t wmax,
                        double a, double b, double c, int device);
 
+/* Text edge list -> <dir>/origin/{vlist,elist,wlist,flist}.bin, the bytes the reference's
+ * convert2binary writes (utils/convert2binary.cpp:10-137): lines "src dst:dst:...", self-loops
+ * dropped, rows sorted and deduplicated, V = largest id + 1, weights rand() % 100 + 1 from
+ * glibc's unseeded rand() and flist = w / row sum.  Where the reference would stop with an
+ * uncaught exception (a destination stoi rejects) or index out of range (a negative id),
+ * returns C2G_ERR_FORMAT and writes nothing; a missing file is C2G_ERR_IO.  The three
+ * outputs (may be NULL) are the reference's printed "Max Vertex Number", "Vertex Number"
+ * and "Edge Number". */
+int c2g_convert_text(const char* text_path, const char* dir, int64_t* max_vertex, int64_t* vertices,
+                     int64_t* edges);
+
 /* C^2graph-P pruners.  Byte-identical outputs to purn-sssp (src/purn-sssp.cpp:61-352)
  * and purn-ppr (src/purn-ppr.cpp:63-344); purn-sssp additionally writes the
  * record->vertex sidecar <dir>/sssp/hvmap.bin. */

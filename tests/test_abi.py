@@ -58,6 +58,7 @@ def test_bad_variant_and_args(built, tmp_path):
     assert c2g.lib().c2g_prune_sssp(None) == c2g.ERR_ARG
     assert c2g.lib().c2g_prune_ppr_device(None, 0.15, 0, None, None, None) == c2g.ERR_ARG
     assert c2g.lib().c2g_prune_sssp_device(None, 0, None, None, None) == c2g.ERR_ARG
+    assert c2g.lib().c2g_convert_text(None, b"/tmp/x", None, None, None) == c2g.ERR_ARG
     assert c2g.lib().c2g_rmat_write(b"/tmp/x", 0, 8, 1, 1, 10, 0.57, 0.19, 0.19) == c2g.ERR_ARG
     # batched-query tuning entry points: a NULL handle or batch is a status, never a crash
     assert c2g.lib().c2g_ppr_batch_set_pull(None, 8.0) == c2g.ERR_ARG
