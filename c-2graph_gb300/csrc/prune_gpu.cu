@@ -155,20 +155,6 @@ __device__ __forceinline__ unsigned long long pg_key(int round, unsigned pos) {
     return ((unsigned long long)(unsigned)round << 32) | (unsigned long long)(~pos);
 }
 
-// first index of [lo, n) of row `off` of `t` with t > key (upper) or t >= key (lower), or n
-__device__ __forceinline__ int pg_search(const int* t, long long off, int lo, int n, int key, bool upper) {
-    int hi = n;
-    while (lo < hi) {
-        const int mid = (lo + hi) >> 1;
-        const int x = ldcg(t + off + mid);
-        if (x < key || (upper && x == key))
-            lo = mid + 1;
-        else
-            hi = mid;
-    }
-    return lo;
-}
-
 // A vertex's live roots in in-row order with their out-rows, per warp in shared memory.
 struct PgRoots {
     int j;
