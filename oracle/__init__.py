@@ -53,6 +53,9 @@ def lib():
         L.orc_prune_depth.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_double, _P]
         L.orc_prune_ppr_speculative.restype = ctypes.c_int
         L.orc_prune_ppr_speculative.argtypes = [ctypes.c_char_p, ctypes.c_double, ctypes.c_int32, ctypes.c_char_p, _P]
+        L.orc_prune_speculative.restype = ctypes.c_int
+        L.orc_prune_speculative.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_double, ctypes.c_int32,
+                                            ctypes.c_char_p, _P]
         _lib = L
     return _lib
 
@@ -242,6 +245,21 @@ def prune_depth(dir, kind, alpha=None):
     keys = ("visits", "removing", "decisions", "depth", "visit_depth", "widest", "in_levels_ge32",
             "in_levels_ge1024")
     return {k: int(x) for k, x in zip(keys, st)}
+
+
+def prune_speculative(dir, kind, alpha=None, window=1024, sub=None):
+    """Either pruner's steps (kind "sssp" or "ppr") in rounds of the device pruners'
+    reservation-based schedule over a window of `window` positions (oracle/ingest.c
+    orc_prune_speculative); outputs in dir/<sub>/ (default <kind>_spec) in the sssp/ or ppr/
+    layout.  Returns the rounds, the committed positions and the largest round."""
+    st = np.zeros(3, np.int64)
+    keep = 0.8 if alpha is None else 1.0 - alpha
+    sub = sub or kind + "_spec"
+    rc = lib().orc_prune_speculative(os.fsencode(dir), 1 if kind == "ppr" else 0, keep, int(window), sub.encode(),
+                                     st.ctypes.data)
+    if rc:
+        raise RuntimeError("orc_prune_speculative failed: %d" % rc)
+    return {"rounds": int(st[0]), "visits": int(st[1]), "widest": int(st[2])}
 
 
 def prune_ppr_speculative(dir, alpha=None, window=1024, sub="ppr_spec"):

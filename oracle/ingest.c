@@ -31,10 +31,10 @@
  *   orc_prune_depth    either pruner with a dependency analysis of its visiting order
  *                      (not a restatement: an analysis of the sequential algorithm, for
  *                      the question whether a parallel pruner could reproduce its bytes).
- *   orc_prune_ppr_speculative
- *                      purn-ppr's visits in rounds of a reservation-based parallel
- *                      schedule, run on the CPU, to check that schedule against the
- *                      sequential pass's bytes.
+ *   orc_prune_speculative, orc_prune_ppr_speculative
+ *                      either pruner's steps in rounds of the reservation-based parallel
+ *                      schedule the device pruners run, on the CPU, to check that schedule
+ *                      against the sequential pass's bytes.
  *
  * The pruners keep the reference's per-vertex state: the out-rows as sorted
  * (target, weight) lists built from each row's distinct pairs without self-loops
@@ -650,19 +650,22 @@ int orc_prune_depth(const char* dir, int ppr, double keep, int64_t* st) {
     return rc;
 }
 
-/* ---- a parallel schedule of purn-ppr, checked on the CPU ------------------------------
- * purn-ppr visits every vertex once in id order.  orc_prune_ppr_speculative runs the same
- * visits (prune_one, unchanged) in rounds over a window of the next `window` unvisited
- * vertices, the schedule a parallel pruner would use (deterministic reservations): each
- * candidate computes, on the current state, the rows it reads (its in-row, its out-row,
- * its live roots' out-rows) and the rows it would write (its out-row and its roots'
- * out-rows when it moves edges, the in-rows of the targets it moves); it reserves them
- * under its id; it commits when no earlier candidate of the window writes a row it reads
- * and none touches a row it writes, unless an earlier candidate that failed had a row it
- * reads written in this round (its plan, and so the rows it will touch, may change):
- * candidates past the first such one wait.  Records are gathered per vertex and written
- * in id order.  The outputs go to dir/<sub>/ in the ppr/ layout, so a test compares them
- * byte by byte with orc_prune_ppr's.  st[3]: rounds, committed visits, the largest round. */
+/* ---- a parallel schedule of the pruners, checked on the CPU ----------------------------
+ * The pruners visit positions (k, i) in order: purn-ppr one per vertex (bound 5), purn-sssp
+ * one per round k = 1..29 and vertex (a vertex is visited at the first k that covers its live
+ * in-degree).  orc_prune_speculative runs the same steps (prune_one, unchanged) in rounds over
+ * a window of `window` positions from the first pending one, the schedule of the device
+ * pruners (deterministic reservations): each pending position computes, on the current
+ * state, the rows it reads (its in-row, its out-row, its live roots' out-rows) and the rows it
+ * would write (its out-row and its roots' out-rows when it moves edges, the in-rows of the
+ * targets it moves); it reserves them under its index; it commits when no earlier position
+ * of the window writes a row it reads and none touches a row it writes, unless an earlier
+ * position that failed had a row it reads written in this round (its plan, and so the rows
+ * it will touch, may change): positions past the first such one wait.  Records are
+ * gathered per vertex and written in visiting order (purn-ppr: id order; purn-sssp: (k, id),
+ * with the record->vertex sidecar).  The outputs go to dir/<sub>/ in the ppr/ or sssp/
+ * layout, so a test compares them byte by byte with orc_prune_ppr's / orc_prune_sssp's.
+ * st[3]: rounds, committed positions, the largest round. */
 typedef struct {
     int32_t* a;
     int32_t n, cap;
@@ -676,32 +679,31 @@ static void rs_push(rowset* v, int32_t x) {
     v->a[v->n++] = x;
 }
 
-/* rows of visit i on the current state: out-row x is x, in-row x is V + x */
-static void ppr_visit_rows(int32_t i, int32_t V, const orow* out, const irow* in, const int32_t* indeg, rowset* R,
-                           rowset* W) {
-    const int32_t dmax = 5;
+/* rows of position (k, i) on the current state: out-row x is x, in-row x is V + x */
+static void visit_rows(int32_t i, int32_t k, int32_t V, const orow* out, const irow* in, const int32_t* indeg,
+                       rowset* R, rowset* W) {
     R->n = W->n = 0;
     rs_push(R, V + i);
     rs_push(R, i);
-    if (!(out[i].n > 0 && indeg[i] > 0 && indeg[i] <= dmax)) return;
-    int32_t root[8], nr = 0, cur[8] = {0};
-    for (int32_t k = 0; k < in[i].n; ++k)
-        if (in[i].alive[k] && nr < 8) root[nr++] = in[i].s[k];
+    if (!(out[i].n > 0 && indeg[i] > 0 && indeg[i] <= k)) return;
+    int32_t root[32], nr = 0, cur[32] = {0};
+    for (int32_t q = 0; q < in[i].n; ++q)
+        if (in[i].alive[q] && nr < 32) root[nr++] = in[i].s[q];
     const int32_t j = indeg[i] < nr ? indeg[i] : nr;
-    for (int32_t k = 0; k < nr; ++k) rs_push(R, root[k]);
+    for (int32_t q = 0; q < nr; ++q) rs_push(R, root[q]);
     int moves = 0;
     const orow* oi = &out[i];
     for (int32_t e = 0; e < oi->n; ++e) { /* the decisions of prune_one, without its writes */
         const int32_t v = oi->t[e];
         int is_root = 0;
-        for (int32_t k = 0; k < j; ++k)
-            if (root[k] == v) is_root = 1;
+        for (int32_t q = 0; q < j; ++q)
+            if (root[q] == v) is_root = 1;
         if (is_root) continue;
         int32_t cnt = 0;
-        for (int32_t k = 0; k < j; ++k) {
-            const orow* o = &out[root[k]];
-            if (cur[k] + 1 < o->n && o->t[cur[k]] < v) cur[k] = lower_i32(o->t, cur[k], o->n - 1, v);
-            if (o->t[cur[k]] == v) ++cnt;
+        for (int32_t q = 0; q < j; ++q) {
+            const orow* o = &out[root[q]];
+            if (cur[q] + 1 < o->n && o->t[cur[q]] < v) cur[q] = lower_i32(o->t, cur[q], o->n - 1, v);
+            if (o->t[cur[q]] == v) ++cnt;
         }
         if (cnt + 2 > j) {
             rs_push(W, V + v);
@@ -710,35 +712,40 @@ static void ppr_visit_rows(int32_t i, int32_t V, const orow* out, const irow* in
     }
     if (moves) {
         rs_push(W, i);
-        for (int32_t k = 0; k < nr; ++k) rs_push(W, root[k]);
+        for (int32_t q = 0; q < nr; ++q) rs_push(W, root[q]);
     }
 }
 
-int orc_prune_ppr_speculative(const char* dir, double keep, int32_t window, const char* sub, int64_t* st) {
+int orc_prune_speculative(const char* dir, int ppr, double keep, int32_t window, const char* sub, int64_t* st) {
     if (!dir || !sub || !st || window < 1) return -1;
     size_t nv = 0, ne = 0, nw = 0;
     int32_t* vl = orc_read4(dir, "origin", "vlist", &nv);
     int32_t* el = orc_read4(dir, "origin", "elist", &ne);
-    uint32_t* wl = (uint32_t*)orc_read4(dir, "origin", "flist", &nw);
+    uint32_t* wl = (uint32_t*)orc_read4(dir, "origin", ppr ? "flist" : "wlist", &nw);
     if (!vl || !el || !wl || nv < 1 || nw < ne || (size_t)vl[nv - 1] != ne) {
         free(vl), free(el), free(wl);
         return -2;
     }
     const int32_t V = (int32_t)nv - 1;
+    const int32_t kfirst = ppr ? 5 : 1, klast = ppr ? 5 : 29;
+    const int64_t npos = (int64_t)(klast - kfirst + 1) * V;
+    if (window > V) window = V ? V : 1; /* no vertex twice in a window */
     orow* out = (orow*)calloc((size_t)(V ? V : 1), sizeof(orow));
     irow* in = (irow*)calloc((size_t)(V ? V : 1), sizeof(irow));
     int32_t* indeg = (int32_t*)malloc(sizeof(int32_t) * (size_t)(V ? V : 1));
-    prune_rows(V, vl, el, wl, 1, out, in, indeg);
+    prune_rows(V, vl, el, wl, ppr, out, in, indeg);
     free(el);
     free(wl);
-    const prune_rule rule = {1, keep};
-    unsigned char* done = (unsigned char*)calloc((size_t)(V ? V : 1), 1);
-    int64_t* resA = (int64_t*)calloc(2 * (size_t)(V ? V : 1), sizeof(int64_t)); /* (round << 32) | ~id: max wins */
+    const prune_rule rule = {ppr, keep};
+    int32_t* pk = (int32_t*)malloc(sizeof(int32_t) * (size_t)(V ? V : 1)); /* last round done per vertex */
+    int32_t* vk = (int32_t*)calloc((size_t)(V ? V : 1), sizeof(int32_t));  /* round of the pruning visit */
+    for (int32_t v = 0; v < V; ++v) pk[v] = kfirst - 1;
+    int64_t* resA = (int64_t*)calloc(2 * (size_t)(V ? V : 1), sizeof(int64_t)); /* (round << 32) | ~pos: max wins */
     int64_t* resW = (int64_t*)calloc(2 * (size_t)(V ? V : 1), sizeof(int64_t));
     int32_t* wmark = (int32_t*)calloc(2 * (size_t)(V ? V : 1), sizeof(int32_t));
     rowset* R = (rowset*)calloc((size_t)window, sizeof(rowset));
     rowset* W = (rowset*)calloc((size_t)window, sizeof(rowset));
-    int32_t* cand = (int32_t*)malloc(sizeof(int32_t) * (size_t)window);
+    int64_t* cand = (int64_t*)malloc(sizeof(int64_t) * (size_t)window);
     unsigned char* pass = (unsigned char*)malloc((size_t)window);
     int64_t* rec_off = (int64_t*)calloc((size_t)V + 1, sizeof(int64_t)); /* per-vertex records, in commit order */
     int32_t* rec_n = (int32_t*)calloc((size_t)(V ? V : 1), sizeof(int32_t));
@@ -747,78 +754,91 @@ int orc_prune_ppr_speculative(const char* dir, double keep, int32_t window, cons
     memset(&pool_w, 0, sizeof(pool_w));
     records one;
     memset(&one, 0, sizeof(one));
-    int32_t pos = 0, rounds = 0, widest = 0;
-    int64_t commits = 0;
+    int64_t pos = 0, commits = 0;
+    int32_t rounds = 0, widest = 0;
     int rc = 0;
-    while (pos < V && !rc) {
+#define POS_K(p) (kfirst + (int32_t)((p) / V))
+#define POS_I(p) ((int32_t)((p) % V))
+    while (pos < npos && !rc) {
         ++rounds;
         int32_t n = 0;
-        for (int32_t v = pos; v < V && n < window; ++v)
-            if (!done[v]) cand[n++] = v;
+        for (int64_t p = pos; p < npos && p < pos + window; ++p)
+            if (pk[POS_I(p)] < POS_K(p)) cand[n++] = p;
         const int64_t tag = (int64_t)rounds << 32;
         for (int32_t c = 0; c < n; ++c) { /* plan and reserve */
-            ppr_visit_rows(cand[c], V, out, in, indeg, &R[c], &W[c]);
+            visit_rows(POS_I(cand[c]), POS_K(cand[c]), V, out, in, indeg, &R[c], &W[c]);
             const int64_t key = tag | (int64_t)(uint32_t)~(uint32_t)cand[c];
-            for (int32_t k = 0; k < R[c].n; ++k)
-                if (resA[R[c].a[k]] < key) resA[R[c].a[k]] = key;
-            for (int32_t k = 0; k < W[c].n; ++k) {
-                if (resA[W[c].a[k]] < key) resA[W[c].a[k]] = key;
-                if (resW[W[c].a[k]] < key) resW[W[c].a[k]] = key;
+            for (int32_t q = 0; q < R[c].n; ++q)
+                if (resA[R[c].a[q]] < key) resA[R[c].a[q]] = key;
+            for (int32_t q = 0; q < W[c].n; ++q) {
+                if (resA[W[c].a[q]] < key) resA[W[c].a[q]] = key;
+                if (resW[W[c].a[q]] < key) resW[W[c].a[q]] = key;
             }
         }
         for (int32_t c = 0; c < n; ++c) { /* check; the passers mark the rows they write */
             const int64_t key = tag | (int64_t)(uint32_t)~(uint32_t)cand[c];
             int ok = 1;
-            for (int32_t k = 0; k < W[c].n && ok; ++k)
-                if (resA[W[c].a[k]] != key) ok = 0;
-            for (int32_t k = 0; k < R[c].n && ok; ++k)
-                if (resW[R[c].a[k]] > key) ok = 0; /* an earlier writer this round */
+            for (int32_t q = 0; q < W[c].n && ok; ++q)
+                if (resA[W[c].a[q]] != key) ok = 0;
+            for (int32_t q = 0; q < R[c].n && ok; ++q)
+                if (resW[R[c].a[q]] > key) ok = 0; /* an earlier writer this round */
             pass[c] = (unsigned char)ok;
             if (ok)
-                for (int32_t k = 0; k < W[c].n; ++k) wmark[W[c].a[k]] = rounds;
+                for (int32_t q = 0; q < W[c].n; ++q) wmark[W[c].a[q]] = rounds;
         }
-        int32_t dmin = V; /* the first failed candidate whose reads a passer writes */
-        for (int32_t c = 0; c < n && dmin == V; ++c) {
+        int64_t dmin = npos; /* the first failed position whose reads a passer writes */
+        for (int32_t c = 0; c < n && dmin == npos; ++c) {
             if (pass[c]) continue;
-            for (int32_t k = 0; k < R[c].n; ++k)
-                if (wmark[R[c].a[k]] == rounds) {
+            for (int32_t q = 0; q < R[c].n; ++q)
+                if (wmark[R[c].a[q]] == rounds) {
                     dmin = cand[c];
                     break;
                 }
         }
         int32_t nc = 0;
         for (int32_t c = 0; c < n && !rc; ++c) { /* commit */
-            const int32_t i = cand[c];
-            if (!pass[c] || i > dmin) continue;
-            if (out[i].n > 0 && indeg[i] > 0 && indeg[i] <= 5) {
+            if (!pass[c] || cand[c] > dmin) continue;
+            const int32_t i = POS_I(cand[c]), k = POS_K(cand[c]);
+            /* a vertex whose live in-degree is 0 or above k is skipped; the rest are
+             * visited, and pruned when the in-degree is positive and out-edges remain */
+            const int visit = indeg[i] != 0 && indeg[i] <= k;
+            if (visit && indeg[i] > 0 && out[i].n > 0) {
                 one.he.n = one.hw.n = one.hv.n = one.owner.n = 0;
                 il_push(&one.hv, 0);
                 if (prune_one(&rule, i, out, in, indeg, &one, NULL)) rc = -3;
                 rec_off[i] = pool_t.n;
                 rec_n[i] = (int32_t)one.he.n;
-                for (int64_t k = 0; k < one.he.n; ++k) {
-                    il_push(&pool_t, one.he.a[k]);
-                    il_push(&pool_w, one.hw.a[k]);
+                vk[i] = k;
+                for (int64_t q = 0; q < one.he.n; ++q) {
+                    il_push(&pool_t, one.he.a[q]);
+                    il_push(&pool_w, one.hw.a[q]);
                 }
             }
-            done[i] = 1;
+            pk[i] = visit ? klast : k;
             ++nc;
         }
         commits += nc;
         if (nc > widest) widest = nc;
-        while (pos < V && done[pos]) ++pos;
+        while (pos < npos && pk[POS_I(pos)] >= POS_K(pos)) ++pos;
     }
+#undef POS_K
+#undef POS_I
     if (!rc) {
+        /* records in visiting order: purn-ppr one per vertex, purn-sssp one per pruned vertex
+         * in (round, id) order with the sidecar */
         records rec;
         memset(&rec, 0, sizeof(rec));
         il_push(&rec.hv, 0);
-        for (int32_t v = 0; v < V; ++v) {
-            for (int32_t k = 0; k < rec_n[v]; ++k) {
-                il_push(&rec.he, pool_t.a[rec_off[v] + k]);
-                il_push(&rec.hw, pool_w.a[rec_off[v] + k]);
+        for (int32_t k = ppr ? 0 : 1; k <= (ppr ? 0 : klast); ++k)
+            for (int32_t v = 0; v < V; ++v) {
+                if (!ppr && vk[v] != k) continue;
+                for (int32_t q = 0; q < rec_n[v]; ++q) {
+                    il_push(&rec.he, pool_t.a[rec_off[v] + q]);
+                    il_push(&rec.hw, pool_w.a[rec_off[v] + q]);
+                }
+                il_push(&rec.hv, (uint32_t)rec.he.n);
+                il_push(&rec.owner, (uint32_t)v);
             }
-            il_push(&rec.hv, (uint32_t)rec.he.n);
-        }
         int64_t E = 0;
         for (int32_t v = 0; v < V; ++v) E += out[v].n;
         int32_t* pe = (int32_t*)malloc(sizeof(int32_t) * (size_t)(E ? E : 1));
@@ -837,10 +857,11 @@ int orc_prune_ppr_speculative(const char* dir, double keep, int32_t window, cons
         if (!rc) rc = orc_write4(dir, sub, "hvlist", rec.hv.a, (size_t)rec.hv.n);
         if (!rc) rc = orc_write4(dir, sub, "helist", rec.he.a, (size_t)rec.he.n);
         if (!rc) rc = orc_write4(dir, sub, "hwlist", rec.hw.a, (size_t)rec.hw.n);
+        if (!rc && !ppr) rc = orc_write4(dir, sub, "hvmap", rec.owner.a, (size_t)rec.owner.n);
         if (!rc) rc = orc_write4(dir, sub, "vlist", vl, (size_t)V + 1);
         if (!rc) rc = orc_write4(dir, sub, "elist", pe, (size_t)E);
         if (!rc) rc = orc_write4(dir, sub, "wlist", pw, (size_t)E);
-        free(pe), free(pw), free(rec.hv.a), free(rec.he.a), free(rec.hw.a);
+        free(pe), free(pw), free(rec.hv.a), free(rec.he.a), free(rec.hw.a), free(rec.owner.a);
     }
     st[0] = rounds, st[1] = commits, st[2] = widest;
     for (int32_t v = 0; v < V; ++v) {
@@ -848,8 +869,13 @@ int orc_prune_ppr_speculative(const char* dir, double keep, int32_t window, cons
         free(in[v].s), free(in[v].alive);
     }
     for (int32_t c = 0; c < window; ++c) free(R[c].a), free(W[c].a);
-    free(out), free(in), free(indeg), free(vl), free(done), free(resA), free(resW), free(wmark), free(R), free(W);
+    free(out), free(in), free(indeg), free(vl), free(pk), free(vk), free(resA), free(resW), free(wmark), free(R), free(W);
     free(cand), free(pass), free(rec_off), free(rec_n), free(pool_t.a), free(pool_w.a);
     free(one.hv.a), free(one.he.a), free(one.hw.a), free(one.owner.a);
     return rc;
+}
+
+/* purn-ppr's schedule check (the first user of orc_prune_speculative) */
+int orc_prune_ppr_speculative(const char* dir, double keep, int32_t window, const char* sub, int64_t* st) {
+    return orc_prune_speculative(dir, 1, keep, window, sub, st);
 }

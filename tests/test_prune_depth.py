@@ -80,3 +80,25 @@ def test_prune_ppr_speculative_schedule_reproduces_the_bytes(tmp_path, alpha, wi
     V = 1 << 14
     assert st["visits"] == V
     assert st["rounds"] * 8 < V and st["widest"] > 32
+
+
+@pytest.mark.parametrize("kind,window", [("sssp", 4096), ("sssp", 64), ("ppr", 3072)])
+def test_prune_speculative_schedule_reproduces_the_bytes(tmp_path, kind, window):
+    """Both pruners' steps in rounds of the device pruners' schedule (a window of positions
+    from the first pending one; purn-sssp's positions are (round k, vertex)) write the same
+    bytes as the sequential passes, the record->vertex sidecar included."""
+    import oracle
+
+    d = str(tmp_path / "g")
+    oracle.rmat_write(d, 14, 16, 6, 1, 1000)
+    if kind == "ppr":
+        oracle.prune_ppr(d, 0.15)
+    else:
+        oracle.prune_sssp(d)
+    st = oracle.prune_speculative(d, kind, 0.15 if kind == "ppr" else None, window)
+    names = ("vlist", "elist", "wlist", "hvlist", "helist", "hwlist") + (("hvmap",) if kind == "sssp" else ())
+    for f in names:
+        assert filecmp.cmp(os.path.join(d, kind, f + ".bin"), os.path.join(d, kind + "_spec", f + ".bin"),
+                           shallow=False), f
+    positions = (1 if kind == "ppr" else 29) << 14
+    assert st["rounds"] < positions // window + 4096 and st["widest"] > 32
