@@ -19,7 +19,9 @@
 // it reads written in this round (its plan may change), past which nothing commits.  The
 // first pending position always commits, so every round makes progress.  A window holds at
 // most V positions, so no vertex appears in it twice.  The schedule is the one
-// orc_prune_ppr_speculative checks on the CPU.
+// orc_prune_speculative runs on the CPU (the same rounds, the same bytes).  A position that
+// only decides (its vertex is not pruned at its turn) is handled by one lane; a position
+// that prunes by a warp.
 //
 // Committed visits touch disjoint rows and run in parallel, one warp each, with the
 // reference's steps: roots in in-row order; the out-row split into kept pairs (compacted
