@@ -128,3 +128,22 @@ def test_no_device_is_reported(built):
     with pytest.raises(c2g.C2GError) as e:
         c2g.Graph.create(g["origin_vlist"], g["origin_elist"], g["origin_wlist"])
     assert e.value.code == c2g.ERR_NODEVICE
+
+
+def test_device_pruners_fail_loudly_without_a_gpu(built, tmp_path):
+    """Without a usable GPU the device pruners return a CUDA error and write nothing: no
+    silent fallback to a host pass."""
+    import torch
+
+    import c2g
+    import oracle
+
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    d = str(tmp_path)
+    oracle.rmat_write(d, 10, 8, 1, 1, 100)
+    for kind, fn in (("ppr", lambda: c2g.prune_ppr_device(d, 0.15)), ("sssp", lambda: c2g.prune_sssp_device(d))):
+        with pytest.raises(c2g.C2GError) as e:
+            fn()
+        assert e.value.code == c2g.ERR_CUDA
+        assert not os.path.exists(os.path.join(d, kind, "vlist.bin"))
