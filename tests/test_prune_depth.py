@@ -102,3 +102,50 @@ def test_prune_speculative_schedule_reproduces_the_bytes(tmp_path, kind, window)
                            shallow=False), f
     positions = (1 if kind == "ppr" else 29) << 14
     assert st["rounds"] < positions // window + 4096 and st["widest"] > 32
+
+
+def test_speculative_schedule_on_small_random_graphs(tmp_path):
+    """60 seeded random graphs of 20-300 vertices with self-loops, half of them with repeated
+    targets of different weights, windows of 1 to 64 positions: the schedule writes the
+    sequential pass's bytes for both pruners, or stops where the sequential pass stops
+    ("something error2", which repeated targets cause)."""
+    import numpy as np
+
+    import oracle
+
+    rng = np.random.default_rng(17)
+    stops, done = 0, {"ppr": 0, "sssp": 0}
+    for case in range(60):
+        V = int(rng.integers(20, 300))
+        m = int(rng.integers(V, 6 * V))
+        src = np.sort(rng.integers(0, V, m))
+        hub = rng.integers(0, max(2, V // 10), m)
+        dst = np.where(rng.random(m) < 0.5, hub, rng.integers(0, V, m))
+        order = np.lexsort((dst, src))
+        src, dst = src[order], dst[order]
+        if case % 2 == 0:  # distinct targets per row: no pair repeats a target
+            keep = np.concatenate([[True], (src[1:] != src[:-1]) | (dst[1:] != dst[:-1])])
+            src, dst = src[keep], dst[keep]
+            m = len(src)
+        d = str(tmp_path / ("g%d" % case))
+        os.makedirs(os.path.join(d, "origin"))
+        np.searchsorted(src, np.arange(V + 1)).astype(np.int32).tofile(os.path.join(d, "origin", "vlist.bin"))
+        dst.astype(np.int32).tofile(os.path.join(d, "origin", "elist.bin"))
+        rng.integers(1, 4, m).astype(np.int32).tofile(os.path.join(d, "origin", "wlist.bin"))
+        rng.choice(np.array([0.25, 0.5, 0.75], np.float32), m).tofile(os.path.join(d, "origin", "flist.bin"))
+        window = int(rng.choice([1, 3, 16, 64]))
+        for kind in ("ppr", "sssp"):
+            try:
+                oracle.prune_ppr(d, 0.15) if kind == "ppr" else oracle.prune_sssp(d)
+            except RuntimeError:
+                with pytest.raises(RuntimeError):
+                    oracle.prune_speculative(d, kind, 0.15 if kind == "ppr" else None, window)
+                stops += 1
+                continue
+            oracle.prune_speculative(d, kind, 0.15 if kind == "ppr" else None, window)
+            names = ("vlist", "elist", "wlist", "hvlist", "helist", "hwlist") + (("hvmap",) if kind == "sssp" else ())
+            for f in names:
+                assert filecmp.cmp(os.path.join(d, kind, f + ".bin"), os.path.join(d, kind + "_spec", f + ".bin"),
+                                   shallow=False), (case, kind, f)
+            done[kind] += 1
+    assert done["ppr"] >= 20 and done["sssp"] >= 20 and stops > 0, (done, stops)
