@@ -639,11 +639,11 @@ def run_prune(args):
             "cpu_baseline": {"value": E / orc_s, "unit": "edges/s", "cores": 1, "kind": "port",
                              "sample": "the whole graph, oracle/ingest.c orc_prune_ppr"},
             "detail": {"host_pass_s": host_s, "oracle_s": orc_s, "device_call_s": cs, "kernel_s": ks, "rounds": rounds,
-                       "phase_ms": dict(zip(("plan", "check", "disturb", "commit", "copy"), ph)),
+                       "phase_ms": dict(zip(("plan", "check", "commit", "copy"), ph)),
                        "identical_to_host_pass_and_oracle": bool(same),
                        "sssp": {"kernel_s": float(np.mean(s_kern)), "device_call_s": float(np.mean(s_call)),
                                 "host_pass_s": s_host, "oracle_s": s_orc, "rounds": s_rounds,
-                                "phase_ms": dict(zip(("plan", "check", "disturb", "commit", "copy"), s_ph)),
+                                "phase_ms": dict(zip(("plan", "check", "commit", "copy"), s_ph)),
                                 "identical_to_host_pass_and_oracle": bool(s_same)}}}
     print(json.dumps(line), flush=True)
 

@@ -227,11 +227,11 @@ def prune_ppr(dir, alpha=None):
 
 def prune_ppr_device(dir, alpha=0.2, device=0, phases=False):
     """purn-ppr on the GPU (same files as prune_ppr(dir, alpha)).  Returns (kernel ms, rounds),
-    and with phases=True also the kernel ms of the rounds' plan, check, disturb, commit and copy
+    and with phases=True also the kernel ms of the rounds' plan, check, commit and copy
     phases."""
     ms = ctypes.c_float(0.0)
     rounds = ctypes.c_int32(0)
-    ph = np.zeros(5, np.int64)
+    ph = np.zeros(4, np.int64)
     _check(lib().c2g_prune_ppr_device(os.fsencode(dir), float(alpha), int(device), ctypes.byref(ms),
                                       ctypes.byref(rounds), ph.ctypes.data))
     if phases:
@@ -244,7 +244,7 @@ def prune_sssp_device(dir, device=0, phases=False):
     (kernel ms, rounds), and with phases=True also the phases' kernel ms."""
     ms = ctypes.c_float(0.0)
     rounds = ctypes.c_int32(0)
-    ph = np.zeros(5, np.int64)
+    ph = np.zeros(4, np.int64)
     _check(lib().c2g_prune_sssp_device(os.fsencode(dir), int(device), ctypes.byref(ms), ctypes.byref(rounds),
                                        ph.ctypes.data))
     if phases:

@@ -15,9 +15,10 @@
 // reservations).  Every round, every pending position of a window plans its step on the
 // current state (the rows it reads and would write, and which out-edges move) and reserves
 // those rows under its index.  It commits when no earlier position of the window writes a
-// row it reads or touches a row it writes, unless an earlier position that failed had a row
-// it reads written in this round (its plan may change), past which nothing commits.  The
-// first pending position always commits, so every round makes progress.  A window holds at
+// row it reads or touches a row it writes.  A position with an earlier writer of a row it
+// reads may see its plan change before it commits, and so may the rows it will touch, so
+// nothing past the first such position commits in the round.  The first pending position
+// always commits, so every round makes progress.  A window holds at
 // most V positions, so no vertex appears in it twice.  The schedule is the one
 // orc_prune_speculative runs on the CPU (the same rounds, the same bytes).  A position that
 // only decides (its vertex is not pruned at its turn) is handled by one lane; a position
@@ -87,13 +88,13 @@ struct PgCtl {
     unsigned bar_count, bar_gen;  // GridBarrier
     int flags;
     unsigned pos;      // the window's first position
-    unsigned dmin;     // this round: the first failed position whose reads a committer writes
+    unsigned dmin;     // this round: the first position with an earlier writer of a row it reads
     unsigned nextpos;  // this round: the first position left pending
     int round;
     int finished;
     unsigned long long out_top, in_top, rec_top, wscr_top, mscr_top;  // pool bump pointers
     unsigned long long task_top[2];                                   // copy tasks, by round parity
-    unsigned long long phase_ns[5];  // block 0's time in plan, check, disturb, commit, copy (waits included)
+    unsigned long long phase_ns[4];  // block 0's time in plan, check, commit, copy (waits included)
 };
 
 struct PgTask {
@@ -128,7 +129,6 @@ struct PgParams {
     unsigned long long rec_cap;
     unsigned long long* resA;  // [2V] (round << 32) | ~position, the earliest position touching the row
     unsigned long long* resW;  // [2V] the same for writers
-    int* wmark;                // [2V] round in which a committer writes the row
     int* slot_r;               // [span][kPgSlotR] rows read (out-row x is x, in-row x is V + x)
     int* slot_rn;              // rows read, -1: the position was done before the round
     long long* slot_woff;      // plan block in wscr: rows written, then one code per out-edge
@@ -749,7 +749,11 @@ __global__ void __launch_bounds__(kPgThreads, 3) prune_rounds(const PgParams p) 
         }
         if (!grid_sync(bar, flags, p.barrier_ns)) return;
         phase_mark(ctl->phase_ns, tmark, 0);
-        // check: the passers mark the rows they write
+        // check: a position passes when no earlier position touches a row it writes or
+        // writes a row it reads.  A position with an earlier writer of a row it reads may see
+        // its plan change before it commits (whether that writer commits in this round or a
+        // later one), and so may the rows it will touch: nothing after the first such position
+        // commits in this round.
         for (int b0 = 0; gwarp + b0 * nwarps < p.span; b0 += 32) {
             const int c = gwarp + (b0 + lane) * nwarps;
             const unsigned q = pos + (unsigned)c;
@@ -761,7 +765,9 @@ __global__ void __launch_bounds__(kPgThreads, 3) prune_rounds(const PgParams p) 
                 int k, i;
                 pg_at(p, q, k, i);
                 const unsigned long long key = pg_key(round, q);
-                p.slot_pass[c] = (ldcg(p.resW + p.V + i) <= key && ldcg(p.resW + i) <= key) ? 1 : 0;
+                const bool rok = ldcg(p.resW + p.V + i) <= key && ldcg(p.resW + i) <= key;
+                p.slot_pass[c] = rok ? 1 : 0;
+                if (!rok) atomicMin(&ctl->dmin, q);
             }
             unsigned hm = __ballot_sync(kFull, rn >= 0 && !light);
             while (hm) {
@@ -771,40 +777,19 @@ __global__ void __launch_bounds__(kPgThreads, 3) prune_rounds(const PgParams p) 
                 const unsigned long long key = pg_key(round, pos + (unsigned)cl);
                 const int rnl = __shfl_sync(kFull, rn, l), wnl = __shfl_sync(kFull, wn, l);
                 const long long woff = ldl(p.slot_woff + cl);
-                bool ok = true;
-                for (int x = lane; x < wnl; x += 32) ok = ok && ldcg(p.resA + ldcg(p.wscr + woff + x)) == key;
-                if (lane < rnl) ok = ok && ldcg(p.resW + ldcg(p.slot_r + (size_t)cl * kPgSlotR + lane)) <= key;
-                ok = __all_sync(kFull, ok);
-                if (lane == 0) p.slot_pass[cl] = ok ? 1 : 0;
-                if (ok)
-                    for (int x = lane; x < wnl; x += 32) p.wmark[ldcg(p.wscr + woff + x)] = round;
+                bool wok = true, rok = true;
+                for (int x = lane; x < wnl; x += 32) wok = wok && ldcg(p.resA + ldcg(p.wscr + woff + x)) == key;
+                if (lane < rnl) rok = ldcg(p.resW + ldcg(p.slot_r + (size_t)cl * kPgSlotR + lane)) <= key;
+                wok = __all_sync(kFull, wok);
+                rok = __all_sync(kFull, rok);
+                if (lane == 0) {
+                    p.slot_pass[cl] = (wok && rok) ? 1 : 0;
+                    if (!rok) atomicMin(&ctl->dmin, pos + (unsigned)cl);
+                }
             }
         }
         if (!grid_sync(bar, flags, p.barrier_ns)) return;
         phase_mark(ctl->phase_ns, tmark, 1);
-        // a failed position whose reads a passer writes holds back the ones after it
-        for (int b0 = 0; gwarp + b0 * nwarps < p.span; b0 += 32) {
-            const int c = gwarp + (b0 + lane) * nwarps;
-            const unsigned q = pos + (unsigned)c;
-            const int rn = (c < p.span && q < p.npos) ? ldcg(p.slot_rn + c) : -1;
-            const bool failed = rn >= 0 && !ldb(p.slot_pass + c);
-            if (failed && rn == 2) {  // a decision: rows V + i and i
-                int k, i;
-                pg_at(p, q, k, i);
-                if (ldcg(p.wmark + p.V + i) == round || ldcg(p.wmark + i) == round) atomicMin(&ctl->dmin, q);
-            }
-            unsigned hm = __ballot_sync(kFull, failed && rn > 2);
-            while (hm) {
-                const int l = __ffs(hm) - 1;
-                hm &= hm - 1u;
-                const int cl = gwarp + (b0 + l) * nwarps;
-                const int rnl = __shfl_sync(kFull, rn, l);
-                const bool hit = lane < rnl && ldcg(p.wmark + ldcg(p.slot_r + (size_t)cl * kPgSlotR + lane)) == round;
-                if (__any_sync(kFull, hit) && lane == 0) atomicMin(&ctl->dmin, pos + (unsigned)cl);
-            }
-        }
-        if (!grid_sync(bar, flags, p.barrier_ns)) return;
-        phase_mark(ctl->phase_ns, tmark, 2);
         // commit; the first position left pending starts the next window
         const unsigned dmin = ldcg(&ctl->dmin);
         if (gtid == 0 && dmin < p.npos) atomicMin(&ctl->nextpos, dmin);
@@ -844,7 +829,7 @@ __global__ void __launch_bounds__(kPgThreads, 3) prune_rounds(const PgParams p) 
             }
         }
         if (!grid_sync(bar, flags, p.barrier_ns)) return;
-        phase_mark(ctl->phase_ns, tmark, 3);
+        phase_mark(ctl->phase_ns, tmark, 2);
         // the queued copies; the next window from the first pending position, past the
         // positions already done behind it (a bounded look)
         pg_copy(p, par, gwarp, nwarps, lane);
@@ -878,7 +863,7 @@ __global__ void __launch_bounds__(kPgThreads, 3) prune_rounds(const PgParams p) 
             }
         }
         if (!grid_sync(bar, flags, p.barrier_ns)) return;
-        phase_mark(ctl->phase_ns, tmark, 4);
+        phase_mark(ctl->phase_ns, tmark, 3);
         if (ldcg(&ctl->finished) || (ldcg(flags) & (kPgErrPool | kPgErrRows))) return;
     }
     if (gtid == 0) atomicOr(flags, C2G_FLAG_ITER_CAP);
@@ -1012,7 +997,6 @@ static int prune_device_dir(const std::string& dir, double keep, int device, flo
     if (e == cudaSuccess) e = db.get(&p.rmiss, rec_cap);
     if (e == cudaSuccess) e = db.get(&p.resA, 2 * (size_t)V);
     if (e == cudaSuccess) e = db.get(&p.resW, 2 * (size_t)V);
-    if (e == cudaSuccess) e = db.get(&p.wmark, 2 * (size_t)V);
     if (e == cudaSuccess) e = db.get(&p.slot_r, (size_t)span * kPgSlotR);
     if (e == cudaSuccess) e = db.get(&p.slot_rn, (size_t)span);
     if (e == cudaSuccess) e = db.get(&p.slot_woff, (size_t)span);
@@ -1070,7 +1054,6 @@ static int prune_device_dir(const std::string& dir, double keep, int device, flo
         C2G_CUDA(cudaMemset(p.rec_off, 0, sizeof(long long) * (size_t)V));
         C2G_CUDA(cudaMemset(p.resA, 0, sizeof(unsigned long long) * 2 * (size_t)V));
         C2G_CUDA(cudaMemset(p.resW, 0, sizeof(unsigned long long) * 2 * (size_t)V));
-        C2G_CUDA(cudaMemset(p.wmark, 0, sizeof(int) * 2 * (size_t)V));
         C2G_CUDA(cudaMemcpy(p.ctl, &c, sizeof(c), cudaMemcpyHostToDevice));
     }
     std::vector<int32_t>().swap(ot);
@@ -1096,7 +1079,7 @@ static int prune_device_dir(const std::string& dir, double keep, int device, flo
     if (ms) *ms = t;
     if (rounds) *rounds = c.round - 1;
     if (phase_ns)
-        for (int k = 0; k < 5; ++k) phase_ns[k] = (int64_t)c.phase_ns[k];
+        for (int k = 0; k < 4; ++k) phase_ns[k] = (int64_t)c.phase_ns[k];
     if (c.flags & kPgErrPool) return fail(C2G_ERR_OVERFLOW, "pruner: a row pool ran out");
     if (c.flags & kPgErrRows) return fail(C2G_ERR_FORMAT, "pruner: in-row and out-rows disagree");
     if (c.flags & (C2G_FLAG_BARRIER_TIMEOUT | C2G_FLAG_ITER_CAP) || (V > 0 && !c.finished))

@@ -459,9 +459,9 @@ int c2g_prune_ppr_alpha(const char* dir, double alpha);
  * reads and writes; the visits that no earlier planned visit conflicts with run in
  * parallel, one warp each), writing the same six files byte for byte.  Replaces the
  * sequential pass of purn-ppr (src/purn-ppr.cpp:146-283) on `device`.  *ms (may be NULL)
- * gets the kernel time, *rounds (may be NULL) the number of rounds, phase_ns[5] (may be
- * NULL) the kernel time spent in the rounds' five phases: plan, check, disturb, commit,
- * copy (each with the grid barrier that ends it).  Returns C2G_ERR_OVERFLOW when a device
+ * gets the kernel time, *rounds (may be NULL) the number of rounds, phase_ns[4] (may be
+ * NULL) the kernel time spent in the rounds' four phases: plan, check, commit, copy (each
+ * with the grid barrier that ends it).  Returns C2G_ERR_OVERFLOW when a device
  * row pool runs out (nothing is written). */
 int c2g_prune_ppr_device(const char* dir, double alpha, int device, float* ms, int32_t* rounds,
                          int64_t* phase_ns);

@@ -659,9 +659,10 @@ int orc_prune_depth(const char* dir, int ppr, double keep, int64_t* st) {
  * state, the rows it reads (its in-row, its out-row, its live roots' out-rows) and the rows it
  * would write (its out-row and its roots' out-rows when it moves edges, the in-rows of the
  * targets it moves); it reserves them under its index; it commits when no earlier position
- * of the window writes a row it reads and none touches a row it writes, unless an earlier
- * position that failed had a row it reads written in this round (its plan, and so the rows
- * it will touch, may change): positions past the first such one wait.  Records are
+ * of the window writes a row it reads and none touches a row it writes.  A position with an
+ * earlier writer of a row it reads has a plan that may change before it commits (whether
+ * that writer commits in this round or a later one), and so may the rows it will touch:
+ * positions past the first such one wait.  Records are
  * gathered per vertex and written in visiting order (purn-ppr: id order; purn-sssp: (k, id),
  * with the record->vertex sidecar).  The outputs go to dir/<sub>/ in the ppr/ or sssp/
  * layout, so a test compares them byte by byte with orc_prune_ppr's / orc_prune_sssp's.
@@ -742,7 +743,6 @@ int orc_prune_speculative(const char* dir, int ppr, double keep, int32_t window,
     for (int32_t v = 0; v < V; ++v) pk[v] = kfirst - 1;
     int64_t* resA = (int64_t*)calloc(2 * (size_t)(V ? V : 1), sizeof(int64_t)); /* (round << 32) | ~pos: max wins */
     int64_t* resW = (int64_t*)calloc(2 * (size_t)(V ? V : 1), sizeof(int64_t));
-    int32_t* wmark = (int32_t*)calloc(2 * (size_t)(V ? V : 1), sizeof(int32_t));
     rowset* R = (rowset*)calloc((size_t)window, sizeof(rowset));
     rowset* W = (rowset*)calloc((size_t)window, sizeof(rowset));
     int64_t* cand = (int64_t*)malloc(sizeof(int64_t) * (size_t)window);
@@ -775,25 +775,16 @@ int orc_prune_speculative(const char* dir, int ppr, double keep, int32_t window,
                 if (resW[W[c].a[q]] < key) resW[W[c].a[q]] = key;
             }
         }
-        for (int32_t c = 0; c < n; ++c) { /* check; the passers mark the rows they write */
+        int64_t dmin = npos; /* the first position with an earlier writer of a row it reads */
+        for (int32_t c = 0; c < n; ++c) { /* check */
             const int64_t key = tag | (int64_t)(uint32_t)~(uint32_t)cand[c];
-            int ok = 1;
-            for (int32_t q = 0; q < W[c].n && ok; ++q)
-                if (resA[W[c].a[q]] != key) ok = 0;
-            for (int32_t q = 0; q < R[c].n && ok; ++q)
-                if (resW[R[c].a[q]] > key) ok = 0; /* an earlier writer this round */
-            pass[c] = (unsigned char)ok;
-            if (ok)
-                for (int32_t q = 0; q < W[c].n; ++q) wmark[W[c].a[q]] = rounds;
-        }
-        int64_t dmin = npos; /* the first failed position whose reads a passer writes */
-        for (int32_t c = 0; c < n && dmin == npos; ++c) {
-            if (pass[c]) continue;
-            for (int32_t q = 0; q < R[c].n; ++q)
-                if (wmark[R[c].a[q]] == rounds) {
-                    dmin = cand[c];
-                    break;
-                }
+            int wok = 1, rok = 1;
+            for (int32_t q = 0; q < W[c].n && wok; ++q)
+                if (resA[W[c].a[q]] != key) wok = 0; /* an earlier position touches a row it writes */
+            for (int32_t q = 0; q < R[c].n && rok; ++q)
+                if (resW[R[c].a[q]] > key) rok = 0; /* an earlier position writes a row it reads */
+            pass[c] = (unsigned char)(wok && rok);
+            if (!rok && cand[c] < dmin) dmin = cand[c];
         }
         int32_t nc = 0;
         for (int32_t c = 0; c < n && !rc; ++c) { /* commit */
@@ -869,7 +860,7 @@ int orc_prune_speculative(const char* dir, int ppr, double keep, int32_t window,
         free(in[v].s), free(in[v].alive);
     }
     for (int32_t c = 0; c < window; ++c) free(R[c].a), free(W[c].a);
-    free(out), free(in), free(indeg), free(vl), free(pk), free(vk), free(resA), free(resW), free(wmark), free(R), free(W);
+    free(out), free(in), free(indeg), free(vl), free(pk), free(vk), free(resA), free(resW), free(R), free(W);
     free(cand), free(pass), free(rec_off), free(rec_n), free(pool_t.a), free(pool_w.a);
     free(one.hv.a), free(one.he.a), free(one.hw.a), free(one.owner.a);
     return rc;

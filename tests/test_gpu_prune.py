@@ -180,3 +180,42 @@ def test_prune_programs_on_the_gpu(gpu_available, built, tmp_path):
         subprocess.run([prog, dev], check=True, env=env, stdout=subprocess.PIPE, stderr=subprocess.PIPE)
     _same(host, dev, "ppr")
     _same(host, dev, "sssp")
+
+
+def test_prune_device_on_small_random_graphs(gpu_available, built, tmp_path):
+    """40 seeded random graphs of 20-300 vertices with self-loops, half of them with repeated
+    targets of different weights: both device pruners write the oracle's bytes, or stop with
+    a format error where the sequential pass stops, writing nothing."""
+    import c2g
+    import oracle
+
+    rng = np.random.default_rng(23)
+    done, stops = 0, 0
+    for case in range(40):
+        V = int(rng.integers(20, 300))
+        m = int(rng.integers(V, 6 * V))
+        src = np.sort(rng.integers(0, V, m))
+        dst = np.where(rng.random(m) < 0.5, rng.integers(0, max(2, V // 10), m), rng.integers(0, V, m))
+        order = np.lexsort((dst, src))
+        src, dst = src[order], dst[order]
+        if case % 2 == 0:
+            keep = np.concatenate([[True], (src[1:] != src[:-1]) | (dst[1:] != dst[:-1])])
+            src, dst = src[keep], dst[keep]
+        ref, dev = str(tmp_path / ("r%d" % case)), str(tmp_path / ("d%d" % case))
+        _write(ref, np.searchsorted(src, np.arange(V + 1)), dst,
+               rng.choice(np.array([0.25, 0.5, 0.75], np.float32), len(dst)), rng.integers(1, 4, len(dst)))
+        shutil.copytree(ref, dev)
+        for kind in ("ppr", "sssp"):
+            try:
+                oracle.prune_ppr(ref, 0.15) if kind == "ppr" else oracle.prune_sssp(ref)
+            except RuntimeError:
+                with pytest.raises(c2g.C2GError) as e:
+                    c2g.prune_ppr_device(dev, 0.15) if kind == "ppr" else c2g.prune_sssp_device(dev)
+                assert e.value.code == c2g.ERR_FORMAT
+                assert not os.path.exists(os.path.join(dev, kind, "vlist.bin"))
+                stops += 1
+                continue
+            c2g.prune_ppr_device(dev, 0.15) if kind == "ppr" else c2g.prune_sssp_device(dev)
+            _same(ref, dev, kind)
+            done += 1
+    assert done >= 40 and stops > 0, (done, stops)

@@ -106,7 +106,7 @@ def test_prune_speculative_schedule_reproduces_the_bytes(tmp_path, kind, window)
 
 def test_speculative_schedule_on_small_random_graphs(tmp_path):
     """60 seeded random graphs of 20-300 vertices with self-loops, half of them with repeated
-    targets of different weights, windows of 1 to 64 positions: the schedule writes the
+    targets of different weights, windows of 1 to V positions: the schedule writes the
     sequential pass's bytes for both pruners, or stops where the sequential pass stops
     ("something error2", which repeated targets cause)."""
     import numpy as np
@@ -133,7 +133,7 @@ def test_speculative_schedule_on_small_random_graphs(tmp_path):
         dst.astype(np.int32).tofile(os.path.join(d, "origin", "elist.bin"))
         rng.integers(1, 4, m).astype(np.int32).tofile(os.path.join(d, "origin", "wlist.bin"))
         rng.choice(np.array([0.25, 0.5, 0.75], np.float32), m).tofile(os.path.join(d, "origin", "flist.bin"))
-        window = int(rng.choice([1, 3, 16, 64]))
+        window = int(rng.choice([1, 3, 16, 64, V]))  # V: every position of the graph in one window
         for kind in ("ppr", "sssp"):
             try:
                 oracle.prune_ppr(d, 0.15) if kind == "ppr" else oracle.prune_sssp(d)
