@@ -34,36 +34,6 @@ template <typename W>
 using Adj = std::vector<std::vector<std::pair<int32_t, W>>>;
 using InAdj = std::vector<std::vector<std::pair<int32_t, bool>>>;
 
-// Out-adjacency: per row the sorted set of distinct (dst, weight) pairs without
-// self-loops (the reference builds it through std::set, core/util.hpp:94-110).
-template <typename W>
-void build_out(const std::vector<int32_t>& vlist, const std::vector<int32_t>& elist,
-               const std::vector<W>& wl, int32_t V, Adj<W>& out) {
-    out.assign(V, {});
-    for (int32_t v = 0; v < V; ++v) {
-        auto& row = out[v];
-        for (int32_t e = vlist[v]; e < vlist[v + 1]; ++e)
-            if (elist[e] != v) row.emplace_back(elist[e], wl[e]);
-        std::sort(row.begin(), row.end());
-        row.erase(std::unique(row.begin(), row.end()), row.end());
-    }
-}
-
-// In-adjacency: for each v (ascending) its distinct out-neighbours d get (v, alive).
-void build_in(const std::vector<int32_t>& vlist, const std::vector<int32_t>& elist, int32_t V,
-              InAdj& in) {
-    in.assign(V, {});
-    std::vector<int32_t> tmp;
-    for (int32_t v = 0; v < V; ++v) {
-        tmp.clear();
-        for (int32_t e = vlist[v]; e < vlist[v + 1]; ++e)
-            if (elist[e] != v) tmp.push_back(elist[e]);
-        std::sort(tmp.begin(), tmp.end());
-        tmp.erase(std::unique(tmp.begin(), tmp.end()), tmp.end());
-        for (int32_t d : tmp) in[d].emplace_back(v, true);
-    }
-}
-
 std::vector<std::pair<int32_t, bool>>::iterator in_find(std::vector<std::pair<int32_t, bool>>& row,
                                                          int32_t key) {
     return std::lower_bound(row.begin(), row.end(), key,
@@ -238,10 +208,11 @@ void flatten(const Adj<W>& out, int32_t V, std::vector<int32_t>& vlist, std::vec
 
 }  // namespace
 
-// The rows a pruner starts from, flat, for the device pruners (prune_gpu.cu): the rows
-// build_out and build_in make (out-rows: the (target, weight) pairs without self-loops,
-// sorted as pair<int32, W> and without repeated pairs; in-rows: the distinct sources of
-// each vertex, ascending), built without one allocation per row.  Input rows that are
+// The rows a pruner starts from, flat, for the device pruners (prune_gpu.cu) and the host
+// passes: out-rows of the (target, weight) pairs without self-loops, sorted as
+// pair<int32, W> and without repeated pairs (the reference builds them through std::set,
+// core/util.hpp:94-110); in-rows of the distinct sources of each vertex, ascending.  Built
+// without one allocation per row.  Input rows that are
 // already strictly increasing and free of self-loops (the R-MAT writer's) are the out-rows
 // as they are; other rows are sorted in parallel.  The in-rows are a stable counting sort
 // of the out-rows by target, each thread filling its own range of sources.  orow / irow are
@@ -341,24 +312,40 @@ template int prune_initial_rows<float>(const std::string&, int32_t&, std::vector
 template int prune_initial_rows<int32_t>(const std::string&, int32_t&, std::vector<int32_t>&, std::vector<int32_t>&,
                                         std::vector<int32_t>&, std::vector<int32_t>&, std::vector<int32_t>&);
 
-int prune_sssp_dir(const std::string& dir) {
-    std::vector<int32_t> vlist, elist, wlist;
-    int rc;
-    if ((rc = read_array4(dir + "/origin/vlist.bin", vlist))) return rc;
-    if ((rc = read_array4(dir + "/origin/elist.bin", elist))) return rc;
-    if ((rc = read_array4(dir + "/origin/wlist.bin", wlist))) return rc;
-    if ((rc = check_csr(vlist, elist))) return rc;
-    if (wlist.size() < elist.size()) return fail(C2G_ERR_FORMAT, "wlist shorter than elist");
-    const int32_t V = (int32_t)vlist.size() - 1;
+namespace {
 
+// The host passes' per-vertex rows (every in-entry alive), filled from the flat initial rows.
+template <typename W>
+int host_rows(const std::string& dir, int32_t& V, Adj<W>& out, InAdj& in, std::vector<int32_t>& indeg) {
+    std::vector<int32_t> orow, ot, irow, is;
+    std::vector<W> ow;
+    const int rc = prune_initial_rows<W>(dir, V, orow, ot, ow, irow, is);
+    if (rc) return rc;
+    out.assign((size_t)V, {});
+    in.assign((size_t)V, {});
+    indeg.assign((size_t)V, 0);
+#pragma omp parallel for schedule(dynamic, 4096)
+    for (int32_t v = 0; v < V; ++v) {
+        auto& o = out[v];
+        o.reserve((size_t)(orow[v + 1] - orow[v]));
+        for (int32_t x = orow[v]; x < orow[v + 1]; ++x) o.emplace_back(ot[x], ow[x]);
+        auto& r = in[v];
+        r.reserve((size_t)(irow[v + 1] - irow[v]));
+        for (int32_t x = irow[v]; x < irow[v + 1]; ++x) r.emplace_back(is[x], true);
+        indeg[v] = irow[v + 1] - irow[v];
+    }
+    return C2G_OK;
+}
+
+}  // namespace
+
+int prune_sssp_dir(const std::string& dir) {
+    int32_t V = 0;
     Adj<int32_t> out;
     InAdj in;
-    build_out(vlist, elist, wlist, V, out);
-    build_in(vlist, elist, V, in);
-    std::vector<int32_t>().swap(elist);
-    std::vector<int32_t>().swap(wlist);
-    std::vector<int32_t> indeg(V);
-    for (int32_t v = 0; v < V; ++v) indeg[v] = (int32_t)in[v].size();
+    std::vector<int32_t> indeg;
+    int rc = host_rows<int32_t>(dir, V, out, in, indeg);
+    if (rc) return rc;
 
     // Rounds k = 0..29; a vertex is visited once, in the first round whose bound
     // covers its live in-degree (src/purn-sssp.cpp:139-150).
@@ -390,24 +377,12 @@ int prune_sssp_dir(const std::string& dir) {
 
 int prune_ppr_dir(const std::string& dir, double keep) {
     g_ppr_keep = keep;
-    std::vector<int32_t> vlist, elist;
-    std::vector<float> flist;
-    int rc;
-    if ((rc = read_array4(dir + "/origin/vlist.bin", vlist))) return rc;
-    if ((rc = read_array4(dir + "/origin/elist.bin", elist))) return rc;
-    if ((rc = read_array4(dir + "/origin/flist.bin", flist))) return rc;
-    if ((rc = check_csr(vlist, elist))) return rc;
-    if (flist.size() < elist.size()) return fail(C2G_ERR_FORMAT, "flist shorter than elist");
-    const int32_t V = (int32_t)vlist.size() - 1;
-
+    int32_t V = 0;
     Adj<float> out;
     InAdj in;
-    build_out(vlist, elist, flist, V, out);
-    build_in(vlist, elist, V, in);
-    std::vector<int32_t>().swap(elist);
-    std::vector<float>().swap(flist);
-    std::vector<int32_t> indeg(V);
-    for (int32_t v = 0; v < V; ++v) indeg[v] = (int32_t)in[v].size();
+    std::vector<int32_t> indeg;
+    int rc = host_rows<float>(dir, V, out, in, indeg);
+    if (rc) return rc;
 
     // One pass in vertex order with in-degree bound 5; every vertex gets a record,
     // empty when it is not pruned (src/purn-ppr.cpp:146-152,281-283).
